@@ -1,0 +1,1017 @@
+// gt_assembly.cu -- sparsity construction, per-cell integration and the
+// deterministic CSR scatter.
+//
+// Pipeline of one assemble_matrix call (reference: src/problems.jl:319-350
+// -> allocate_matrix counting pass src/assembly.jl:119-153, the generated
+// cell loop src/compiler.jl:1865-1917 with contribute! src/assembly.jl:
+// 189-208, and the COO->CSC compress src/assembly.jl:571-575):
+//   1. incidence: block row (free node dof) -> sorted list of (cell, local
+//      node) that touch it  [k_inc_count, scan, k_inc_fill, k_inc_sort]
+//   2. pattern: per block row, the sorted union of the free node dofs of its
+//      cells  [k_pattern<count>, scan, k_pattern<fill>]  == the reference's
+//      sorted, duplicate-free CSC (the forms are symmetric, CSR == CSC)
+//   3. element matrices: FP64 Jacobian / inverse / determinant per
+//      quadrature point, element matrix in T (FP64 or FP32)  [k_elements]
+//   4. scatter: each block row is owned by one thread group that sums the
+//      contributions of its cells in ascending cell order -- the order in
+//      which the reference's COO->CSC conversion sums duplicates -- and
+//      writes the row once.  No atomics on values: bitwise deterministic.
+#include <climits>
+#include <cstring>
+#include <type_traits>
+
+#include "gt_internal.cuh"
+#include "gt_refcell.cuh"
+
+namespace gt {
+
+static inline Ctx* ctx_of(const Space* sp) { return sp->mesh->ctx; }
+
+// ---------------------------------------------------------------------------
+// reference tabulation (quadrature + shape functions), built on the device
+// quadrature: tensor Gauss-Legendre, ceil((deg+1)/2) points per direction,
+// first index fastest (src/quadrature.jl:78-106); tetrahedron: 4-point Strang
+// rule (src/quadrature.jl:512-529).  Shape functions: tensor-product Lagrange
+// on equispaced nodes (the reference builds the same basis from monomials
+// and a Vandermonde inverse, src/space.jl:942-970).
+// ---------------------------------------------------------------------------
+struct TabLayout {
+  int D, nlv, nn, nq;
+  int off_w, off_gg, off_sv, off_sg, total;
+};
+inline TabLayout tab_layout(int ctype, int order) {
+  TabLayout L{};
+  L.D = ctype == GT_QUAD4 ? 2 : 3;
+  L.nlv = ctype == GT_QUAD4 ? 4 : (ctype == GT_HEX8 ? 8 : 4);
+  L.nn = space_nodes(ctype, order);
+  int n1 = ctype == GT_TET4 ? 0 : order + 1;  // Gauss points per direction for degree 2*order
+  L.nq = ctype == GT_TET4 ? 4 : (L.D == 2 ? n1 * n1 : n1 * n1 * n1);
+  L.off_w = 0;
+  L.off_gg = L.nq;
+  L.off_sv = L.off_gg + L.nq * L.nlv * L.D;
+  L.off_sg = L.off_sv + L.nq * L.nn;
+  L.total = L.off_sg + L.nq * L.nn * L.D;
+  return L;
+}
+
+__device__ void lagrange1d(int order, double x, double* v, double* dv) {
+  if (order == 1) {
+    v[0] = 1.0 - x; v[1] = x; dv[0] = -1.0; dv[1] = 1.0;
+  } else {
+    v[0] = 2.0 * (x - 0.5) * (x - 1.0);
+    v[1] = -4.0 * x * (x - 1.0);
+    v[2] = 2.0 * x * (x - 0.5);
+    dv[0] = 4.0 * x - 3.0; dv[1] = -8.0 * x + 4.0; dv[2] = 4.0 * x - 1.0;
+  }
+}
+
+__global__ void k_tabulate(int ctype, int order, TabLayout L, double* tab) {
+  int q = threadIdx.x;
+  if (q >= L.nq) return;
+  double x[3] = {0, 0, 0}, w;
+  if (ctype == GT_TET4) {
+    const double a = 0.5854101966249685, b = 0.1381966011250105;
+    x[0] = x[1] = x[2] = b;
+    if (q > 0) x[q - 1] = a;
+    w = 1.0 / 24.0;
+  } else {
+    int n1 = order + 1;
+    double g[3], gw[3];
+    if (n1 == 2) {
+      double s = 0.5 / sqrt(3.0);
+      g[0] = 0.5 - s; g[1] = 0.5 + s; gw[0] = gw[1] = 0.5;
+    } else {
+      double s = 0.5 * sqrt(0.6);
+      g[0] = 0.5 - s; g[1] = 0.5; g[2] = 0.5 + s;
+      gw[0] = 5.0 / 18.0; gw[1] = 8.0 / 18.0; gw[2] = 5.0 / 18.0;
+    }
+    int i[3] = {q % n1, (q / n1) % n1, q / (n1 * n1)};
+    w = 1.0;
+    for (int d = 0; d < L.D; d++) { x[d] = g[i[d]]; w *= gw[i[d]]; }
+  }
+  tab[L.off_w + q] = w;
+  // geometry map gradients (P1 / Q1)
+  if (ctype == GT_TET4) {
+    const double gr[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int n = 0; n < 4; n++)
+      for (int d = 0; d < 3; d++) {
+        tab[L.off_gg + (q * 4 + n) * 3 + d] = gr[n][d];
+        tab[L.off_sg + (q * 4 + n) * 3 + d] = gr[n][d];
+      }
+    double v[4] = {1.0 - x[0] - x[1] - x[2], x[0], x[1], x[2]};
+    for (int n = 0; n < 4; n++) tab[L.off_sv + q * 4 + n] = v[n];
+    return;
+  }
+  double v1[3][3], d1[3][3];
+  for (int d = 0; d < L.D; d++) lagrange1d(1, x[d], v1[d], d1[d]);
+  for (int n = 0; n < L.nlv; n++)
+    for (int d = 0; d < L.D; d++) {
+      double g = 1.0;
+      for (int e = 0; e < L.D; e++) {
+        int bit = (n >> e) & 1;
+        g *= (e == d) ? d1[e][bit] : v1[e][bit];
+      }
+      tab[L.off_gg + (q * L.nlv + n) * L.D + d] = g;
+    }
+  double vk[3][3], dk[3][3];
+  for (int d = 0; d < L.D; d++) lagrange1d(order, x[d], vk[d], dk[d]);
+  int m = order + 1;
+  for (int n = 0; n < L.nn; n++) {
+    int e[3] = {n % m, (n / m) % m, n / (m * m)};
+    double p = 1.0;
+    for (int d = 0; d < L.D; d++) p *= vk[d][e[d]];
+    tab[L.off_sv + q * L.nn + n] = p;
+    for (int d = 0; d < L.D; d++) {
+      double g = 1.0;
+      for (int d2 = 0; d2 < L.D; d2++) g *= (d2 == d) ? dk[d2][e[d2]] : vk[d2][e[d2]];
+      tab[L.off_sg + (q * L.nn + n) * L.D + d] = g;
+    }
+  }
+}
+
+static int get_tab(Ctx* ctx, int ctype, int order, double** tab, TabLayout* L) {
+  *L = tab_layout(ctype, order);
+  GT_TRY(dalloc(ctx, tab, L->total));
+  k_tabulate<<<1, 32, 0, ctx->stream>>>(ctype, order, *L, *tab);
+  GT_LAUNCH(ctx, "k_tabulate");
+  return GT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// 1. incidence
+// ---------------------------------------------------------------------------
+__global__ void k_inc_count(const int32_t* cnd, int64_t n, int32_t* cnt) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t d = cnd[i];
+    if (d > 0) atomicAdd(&cnt[d - 1], 1);
+  }
+}
+__global__ void k_inc_fill(const int32_t* cnd, int64_t n, const int64_t* ptr, int32_t* cursor, int32_t* inc) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t d = cnd[i];
+    if (d > 0) {
+      int32_t p = atomicAdd(&cursor[d - 1], 1);
+      inc[ptr[d - 1] + p] = (int32_t)i;  // cell * nn + local node
+    }
+  }
+}
+// sort each row's incidences ascending (= by cell); rows are short
+__global__ void k_inc_sort(const int64_t* ptr, int32_t* inc, int64_t nrows, int32_t* maxlen) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  int64_t b = ptr[r], e = ptr[r + 1];
+  for (int64_t i = b + 1; i < e; i++) {
+    int32_t v = inc[i];
+    int64_t j = i - 1;
+    while (j >= b && inc[j] > v) { inc[j + 1] = inc[j]; j--; }
+    inc[j + 1] = v;
+  }
+  atomicMax(maxlen, (int32_t)(e - b));
+}
+
+int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc) {
+  cudaStream_t st = ctx->stream;
+  int64_t nrows = sp->nfree_nodes, n = sp->mesh->ncells * sp->nn;
+  int32_t *cnt = nullptr, *cursor = nullptr, *dmax = nullptr;
+  GT_TRY(dalloc(ctx, &cnt, nrows + 1));
+  GT_TRY(dalloc(ctx, &cursor, nrows + 1));
+  GT_TRY(dalloc(ctx, &dmax, 1));
+  GT_TRY(dalloc(ctx, inc_ptr, nrows + 1));
+  GT_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), st));
+  GT_CUDA(ctx, cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (nrows + 1), st));
+  GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
+  k_inc_count<<<grid_for(n, 256), 256, 0, st>>>(sp->cell_ndofs, n, cnt);
+  GT_LAUNCH(ctx, "k_inc_count");
+  GT_TRY(exclusive_scan_i64(ctx, cnt, *inc_ptr, nrows));
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], *inc_ptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GT_CUDA(ctx, cudaStreamSynchronize(st));
+  *ninc = ctx->h_scratch[0];
+  GT_TRY(dalloc(ctx, inc, *ninc));
+  k_inc_fill<<<grid_for(n, 256), 256, 0, st>>>(sp->cell_ndofs, n, *inc_ptr, cursor, *inc);
+  k_inc_sort<<<grid_for(nrows, 128), 128, 0, st>>>(*inc_ptr, *inc, nrows, dmax);
+  GT_LAUNCH(ctx, "k_inc_fill/sort");
+  dfree(ctx, cnt);
+  dfree(ctx, cursor);
+  dfree(ctx, dmax);
+  return GT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// 2. pattern: one warp per block row, bitonic sort of the candidate columns
+// in shared memory, duplicates dropped
+// ---------------------------------------------------------------------------
+template <bool FILL>
+__global__ void k_pattern(const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                          const int32_t* __restrict__ cnd, int nn, int64_t nrows, int cap, int32_t* __restrict__ rowcnt,
+                          const int64_t* __restrict__ rowptr, int32_t* __restrict__ colind, uint32_t* err) {
+  extern __shared__ int32_t s_buf[];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t* buf = s_buf + w * cap;
+  int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
+  if (r >= nrows) return;
+  int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+  int ncand = (int)(ie - ib) * nn;
+  if (ncand > cap) {
+    if (lane == 0) { atomicOr(err, DEV_ERR_ROW_CAP); if (!FILL) rowcnt[r] = 0; }
+    return;
+  }
+  int P = 32;
+  while (P < ncand) P <<= 1;
+  for (int i = lane; i < P; i += 32) {
+    int32_t v = INT_MAX;
+    if (i < ncand) {
+      int k = i / nn, b = i - k * nn;
+      int32_t cb = inc[ib + k];
+      int32_t c = cb / nn;
+      int32_t d = cnd[(int64_t)c * nn + b];
+      v = d > 0 ? d - 1 : INT_MAX;
+    }
+    buf[i] = v;
+  }
+  __syncwarp();
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = lane; i < P; i += 32) {
+        int ixj = i ^ j;
+        if (ixj > i) {
+          int32_t a = buf[i], b = buf[ixj];
+          bool up = (i & k) == 0;
+          if ((a > b) == up) { buf[i] = b; buf[ixj] = a; }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  int count = 0;
+  for (int base = 0; base < P; base += 32) {
+    int i = base + lane;
+    int32_t v = buf[i];
+    bool keep = v != INT_MAX && (i == 0 || buf[i - 1] != v);
+    unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (FILL && keep) colind[rowptr[r] + count + __popc(m & ((1u << lane) - 1))] = v;
+    count += __popc(m);
+  }
+  if (!FILL && lane == 0) rowcnt[r] = count;
+}
+
+__global__ void k_max_diff(const int64_t* ptr, int64_t n, int32_t* out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int32_t v = 0;
+  if (i < n) v = (int32_t)(ptr[i + 1] - ptr[i]);
+  for (int o = 16; o; o >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, v);
+}
+
+static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out) {
+  int32_t* d = nullptr;
+  GT_TRY(dalloc(ctx, &d, 1));
+  GT_CUDA(ctx, cudaMemsetAsync(d, 0, sizeof(int32_t), ctx->stream));
+  if (n > 0) k_max_diff<<<grid_for(n, 256), 256, 0, ctx->stream>>>(ptr, n, d);
+  GT_LAUNCH(ctx, "k_max_diff");
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[8], d, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  memcpy(out, &ctx->h_scratch[8], sizeof(int32_t));
+  dfree(ctx, d);
+  return GT_OK;
+}
+
+int build_pattern(Matrix* A) {
+  const Space* sp = A->space;
+  Ctx* ctx = sp->mesh->ctx;
+  cudaStream_t st = ctx->stream;
+  int64_t nrows = sp->nfree_nodes;
+  A->nbrows = nrows;
+  int32_t maxinc = 0;
+  GT_TRY(max_diff(ctx, A->inc_ptr, nrows, &maxinc));
+  int cap = 32;
+  while (cap < maxinc * sp->nn) cap <<= 1;
+  if (cap > 4096) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells for the sparsity kernel");
+  int warps = cap >= 2048 ? 2 : (cap >= 1024 ? 4 : 8);
+  size_t smem = (size_t)warps * cap * sizeof(int32_t);
+  if (smem > 48 * 1024) {
+    cudaFuncSetAttribute(k_pattern<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_pattern<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
+  int32_t* rowcnt = nullptr;
+  GT_TRY(dalloc(ctx, &rowcnt, nrows + 1));
+  GT_TRY(dalloc(ctx, &A->rowptr, nrows + 1));
+  int grid = grid_for(nrows, warps);
+  k_pattern<false><<<grid, warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, sp->nn, nrows, cap, rowcnt,
+                                                  nullptr, nullptr, ctx->d_err);
+  GT_LAUNCH(ctx, "k_pattern<count>");
+  GT_TRY(exclusive_scan_i64(ctx, rowcnt, A->rowptr, nrows));
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], A->rowptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  uint32_t bits = 0;
+  GT_TRY(take_device_error(ctx, &bits));  // synchronises
+  if (bits) return set_error(ctx, GT_ERR_INVALID, "sparsity: row capacity exceeded");
+  A->bnnz = ctx->h_scratch[0];
+  GT_TRY(dalloc(ctx, &A->colind, A->bnnz));
+  k_pattern<true><<<grid, warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, sp->nn, nrows, cap, nullptr,
+                                                 A->rowptr, A->colind, ctx->d_err);
+  GT_LAUNCH(ctx, "k_pattern<fill>");
+  dfree(ctx, rowcnt);
+  int32_t mr = 0;
+  GT_TRY(max_diff(ctx, A->rowptr, nrows, &mr));
+  A->max_row = mr;
+  return GT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// 3. element matrices / vectors
+// One CTA integrates CPB cells.  Phase 1: per (cell, quadrature point) the
+// FP64 Jacobian J = sum_n x_n (x) grad m_n (src/accessors.jl:941-968), its
+// inverse and determinant, dV = |det J| w (src/quadrature.jl:4-6) and the
+// physical gradients J^-T grad_ref phi (src/accessors.jl:1365-1368), stored
+// in shared memory in T.  Phase 2: per (cell, node pair n <= m) the BSxBS
+// block of the element matrix, accumulated over quadrature points in T and
+// written with its transpose.  Affine cells (TET4) compute J once per cell.
+// ---------------------------------------------------------------------------
+template <int D, int NLV, int NN, int NQ, int BS, int FORM, class T, int CPB, bool AFFINE>
+__global__ void __launch_bounds__(128) k_elements(const double* __restrict__ coords, const int32_t* __restrict__ cell_nodes,
+                                                  const double* __restrict__ coef, double nu,
+                                                  const double* __restrict__ tab, TabLayout L, int64_t ncells,
+                                                  T* __restrict__ Ke, double* __restrict__ be, const double* __restrict__ fsrc,
+                                                  const double* __restrict__ scoef, int want_matrix, uint32_t* err) {
+  constexpr int NLOC = NN * BS;
+  constexpr int NQG = AFFINE ? 1 : NQ;  // quadrature points that carry gradients
+  constexpr int NPAIR = NN * (NN + 1) / 2;
+  __shared__ double s_x[CPB][NLV][D];
+  __shared__ T s_g[CPB][NQG][NN][D];
+  __shared__ T s_dv[CPB][NQ];
+  __shared__ double s_tab[NQ * (1 + NLV * D + NN + NN * D)];
+  const int tid = threadIdx.x;
+  const int64_t c0 = (int64_t)blockIdx.x * CPB;
+  for (int i = tid; i < L.total; i += blockDim.x) s_tab[i] = tab[i];
+  for (int i = tid; i < CPB * NLV * D; i += blockDim.x) {
+    int cl = i / (NLV * D), r = i - cl * NLV * D, n = r / D, d = r - n * D;
+    int64_t c = c0 + cl;
+    double v = 0.0;
+    if (c < ncells) v = coords[(int64_t)cell_nodes[c * NLV + n] * D + d];
+    s_x[cl][n][d] = v;
+  }
+  __syncthreads();
+  const double* w = s_tab + L.off_w;
+  const double* gg = s_tab + L.off_gg;
+  const double* sv = s_tab + L.off_sv;
+  const double* sg = s_tab + L.off_sg;
+  // phase 1
+  for (int item = tid; item < CPB * NQG; item += blockDim.x) {
+    int cl = item / NQG, q = item - cl * NQG;
+    double J[D][D];
+#pragma unroll
+    for (int i = 0; i < D; i++)
+#pragma unroll
+      for (int j = 0; j < D; j++) J[i][j] = 0.0;
+#pragma unroll
+    for (int n = 0; n < NLV; n++)
+#pragma unroll
+      for (int i = 0; i < D; i++)
+#pragma unroll
+        for (int j = 0; j < D; j++) J[i][j] = fma(s_x[cl][n][i], gg[(q * NLV + n) * D + j], J[i][j]);
+    double inv[D][D], det;
+    if (D == 2) {
+      det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      double r = 1.0 / det;
+      inv[0][0] = J[1][1] * r; inv[0][1] = -J[0][1] * r;
+      inv[1][0] = -J[1][0] * r; inv[1][1] = J[0][0] * r;
+    } else {
+      double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+      double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+      double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+      det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+      double r = 1.0 / det;
+      inv[0][0] = c00 * r; inv[1][0] = c01 * r; inv[2][0] = c02 * r;
+      inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+      inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+      inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+      inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+      inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+      inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+    }
+    if (c0 + cl < ncells && !(det != 0.0)) atomicOr(err, DEV_ERR_DEGENERATE);
+    double adet = fabs(det);
+    if (AFFINE) {
+#pragma unroll
+      for (int qq = 0; qq < NQ; qq++) s_dv[cl][qq] = (T)(adet * w[qq]);
+    } else {
+      s_dv[cl][q] = (T)(adet * w[q]);
+    }
+#pragma unroll 1
+    for (int n = 0; n < NN; n++)
+#pragma unroll
+      for (int d = 0; d < D; d++) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < D; k++) s = fma(inv[k][d], sg[(q * NN + n) * D + k], s);
+        s_g[cl][q][n][d] = (T)s;
+      }
+  }
+  __syncthreads();
+  // phase 2: element matrix blocks
+  if (want_matrix) {
+    const T lamf = (T)(nu / ((1.0 + nu) * (1.0 - 2.0 * nu))), muf = (T)(1.0 / (2.0 * (1.0 + nu)));
+    for (int item = tid; item < CPB * NPAIR; item += blockDim.x) {
+      int cl = item / NPAIR, p = item - cl * NPAIR;
+      int64_t c = c0 + cl;
+      if (c >= ncells) continue;
+      // pair index -> (n, m) with n <= m
+      int n = 0, rem = p;
+      while (rem >= NN - n) { rem -= NN - n; n++; }
+      int m = n + rem;
+      T cf = (T)(coef ? coef[c] : 1.0);
+      T blk[BS][BS];
+      if (FORM == GT_ELASTICITY) {
+        T A[D][D], sdot = 0;
+#pragma unroll
+        for (int a = 0; a < D; a++)
+#pragma unroll
+          for (int b = 0; b < D; b++) A[a][b] = 0;
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+          const int qg = AFFINE ? 0 : q;
+          T dv = s_dv[cl][q];
+          T gn[D], gm[D];
+#pragma unroll
+          for (int d = 0; d < D; d++) { gn[d] = s_g[cl][qg][n][d] * dv; gm[d] = s_g[cl][qg][m][d]; }
+#pragma unroll
+          for (int a = 0; a < D; a++) {
+            sdot += gn[a] * gm[a];
+#pragma unroll
+            for (int b = 0; b < D; b++) A[a][b] += gn[a] * gm[b];
+          }
+        }
+        T lam = cf * lamf, mu = cf * muf;
+#pragma unroll
+        for (int a = 0; a < BS; a++)
+#pragma unroll
+          for (int b = 0; b < BS; b++) blk[a][b] = lam * A[a][b] + mu * A[b][a] + (a == b ? mu * sdot : (T)0);
+      } else {
+        T acc = 0;
+        if (FORM == GT_LAPLACE) {
+          if (AFFINE) {
+            T dvs = 0, dot = 0;
+#pragma unroll
+            for (int q = 0; q < NQ; q++) dvs += s_dv[cl][q];
+#pragma unroll
+            for (int d = 0; d < D; d++) dot += s_g[cl][0][n][d] * s_g[cl][0][m][d];
+            acc = dot * dvs;
+          } else {
+#pragma unroll
+            for (int q = 0; q < NQ; q++) {
+              T dot = 0;
+#pragma unroll
+              for (int d = 0; d < D; d++) dot += s_g[cl][q][n][d] * s_g[cl][q][m][d];
+              acc += dot * s_dv[cl][q];
+            }
+          }
+        } else {
+#pragma unroll
+          for (int q = 0; q < NQ; q++) acc += (T)(sv[q * NN + n] * sv[q * NN + m]) * s_dv[cl][q];
+        }
+        acc *= cf;
+#pragma unroll
+        for (int a = 0; a < BS; a++)
+#pragma unroll
+          for (int b = 0; b < BS; b++) blk[a][b] = a == b ? acc : (T)0;
+      }
+      T* K = Ke + c * (NLOC * NLOC);
+#pragma unroll
+      for (int a = 0; a < BS; a++)
+#pragma unroll
+        for (int b = 0; b < BS; b++) {
+          K[(n * BS + a) * NLOC + m * BS + b] = blk[a][b];
+          K[(m * BS + b) * NLOC + n * BS + a] = blk[a][b];
+        }
+    }
+  }
+  // element vector: int coef f . v dOmega
+  if (be) {
+    for (int item = tid; item < CPB * NN; item += blockDim.x) {
+      int cl = item / NN, n = item - cl * NN;
+      int64_t c = c0 + cl;
+      if (c >= ncells) continue;
+      double cf = scoef ? scoef[c] : 1.0;
+      double s = 0.0;
+      for (int q = 0; q < NQ; q++) s += sv[q * NN + n] * (double)s_dv[cl][q];
+#pragma unroll
+      for (int k = 0; k < BS; k++) be[c * NLOC + n * BS + k] = cf * fsrc[k] * s;
+    }
+  }
+}
+
+template <int D, int NLV, int NN, int NQ, int BS, int FORM, class T, int CPB, bool AFFINE>
+static int launch_elements(const Space* sp, const double* coef, double nu, const double* tab, const TabLayout& L, T* Ke,
+                           double* be, const double* f, const double* scoef, int want_matrix) {
+  Ctx* ctx = sp->mesh->ctx;
+  int64_t nc = sp->mesh->ncells;
+  int64_t grid = (nc + CPB - 1) / CPB;
+  k_elements<D, NLV, NN, NQ, BS, FORM, T, CPB, AFFINE><<<(unsigned)grid, 128, 0, ctx->stream>>>(
+      sp->mesh->coords, sp->mesh->cell_nodes, coef, nu, tab, L, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
+  GT_LAUNCH(ctx, "k_elements");
+  return GT_OK;
+}
+
+template <int D, int NLV, int NN, int NQ, int CPB, bool AFFINE, class T>
+static int dispatch_form(const Space* sp, int form, const double* coef, double nu, const double* tab, const TabLayout& L,
+                         T* Ke, double* be, const double* f, const double* scoef, int want_matrix) {
+  int bs = sp->ncomp;
+  if (bs == 1) {
+    if (form == GT_LAPLACE)
+      return launch_elements<D, NLV, NN, NQ, 1, GT_LAPLACE, T, CPB, AFFINE>(sp, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
+    if (form == GT_MASS)
+      return launch_elements<D, NLV, NN, NQ, 1, GT_MASS, T, CPB, AFFINE>(sp, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
+  } else {
+    if (form == GT_LAPLACE)
+      return launch_elements<D, NLV, NN, NQ, D, GT_LAPLACE, T, CPB, AFFINE>(sp, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
+    if (form == GT_MASS)
+      return launch_elements<D, NLV, NN, NQ, D, GT_MASS, T, CPB, AFFINE>(sp, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
+    if (form == GT_ELASTICITY)
+      return launch_elements<D, NLV, NN, NQ, D, GT_ELASTICITY, T, CPB, AFFINE>(sp, coef, nu, tab, L, Ke, be, f,
+                                                                               scoef, want_matrix);
+  }
+  return set_error(ctx_of(sp), GT_ERR_UNSUPPORTED, "weak form not supported on this space");
+}
+
+
+// element kernels per cell type / order; returns GT_OK or an error
+template <class T>
+static int elements_T(const Space* sp, int form, const double* coef, double nu, const double* tab, const TabLayout& L,
+                      T* Ke, double* be, const double* f, const double* scoef, int want_matrix) {
+  int ct = sp->mesh->ctype, o = sp->order;
+  if (ct == GT_TET4) return dispatch_form<3, 4, 4, 4, 128, true, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
+  if (ct == GT_QUAD4 && o == 1) return dispatch_form<2, 4, 4, 4, 32, false, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
+  if (ct == GT_QUAD4 && o == 2) return dispatch_form<2, 4, 9, 9, 8, false, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
+  if (ct == GT_HEX8 && o == 1) return dispatch_form<3, 8, 8, 8, 8, false, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
+  if (ct == GT_HEX8 && o == 2) return dispatch_form<3, 8, 27, 27, 1, false, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
+  return set_error(ctx_of(sp), GT_ERR_UNSUPPORTED, "element not supported");
+}
+
+int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision, const double* f,
+                     const double* d_scoef, void* Ke, double* be, int want_matrix) {
+  Ctx* ctx = ctx_of(sp);
+  if (form != GT_LAPLACE && form != GT_MASS && form != GT_ELASTICITY)
+    return set_error(ctx, GT_ERR_UNSUPPORTED, "weak form not supported (Laplacian, mass, linear elasticity only)");
+  if (form == GT_ELASTICITY && sp->ncomp != sp->mesh->D)
+    return set_error(ctx, GT_ERR_UNSUPPORTED, "linear elasticity needs a vector space (tensor_size = (D,))");
+  double* tab = nullptr;
+  TabLayout L;
+  GT_TRY(get_tab(ctx, sp->mesh->ctype, sp->order, &tab, &L));
+  int s;
+  if (precision == GT_FP32)
+    s = elements_T<float>(sp, form, d_coef, nu, tab, L, (float*)Ke, be, f, d_scoef, want_matrix);
+  else
+    s = elements_T<double>(sp, form, d_coef, nu, tab, L, (double*)Ke, be, f, d_scoef, want_matrix);
+  dfree(ctx, tab);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// 4. scatter: G lanes own one block row; the row's column indices and
+// accumulators live in shared memory; incidences are visited in ascending
+// cell order with a group barrier between cells, so every entry is summed in
+// the same order on every run.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int find_col(const int32_t* cols, int L, int32_t j) {
+  int lo = 0, hi = L - 1;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (cols[mid] < j) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+template <int BS, int G, class TK, class TA>
+__global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                          const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                          const int32_t* __restrict__ cnd, int nn, int64_t nrows, int lmax,
+                          const TK* __restrict__ Ke, double* __restrict__ v64, float* __restrict__ v32) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  constexpr int RPW = 32 / G;  // rows per warp
+  const int nloc = nn * BS;
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int sub = lane / G, gl = lane - sub * G;
+  int slot = w * RPW + sub;
+  TA* acc = (TA*)s_raw + (size_t)slot * lmax * BS * BS;
+  int32_t* cols = (int32_t*)((TA*)s_raw + (size_t)(blockDim.x / G) * lmax * BS * BS) + (size_t)slot * lmax;
+  int64_t r = ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * RPW + sub;
+  bool active = r < nrows;
+  unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
+  int64_t rb = 0;
+  int L = 0;
+  if (active) {
+    rb = rowptr[r];
+    L = (int)(rowptr[r + 1] - rb);
+    for (int i = gl; i < L; i += G) cols[i] = colind[rb + i];
+    for (int i = gl; i < L * BS * BS; i += G) acc[i] = (TA)0;
+  }
+  __syncwarp(gmask);
+  if (active) {
+    int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+    for (int64_t k = ib; k < ie; k++) {
+      int32_t cb = inc[k];
+      int32_t c = cb / nn, a = cb - c * nn;
+      const TK* Krow = Ke + (int64_t)c * nloc * nloc + (int64_t)(a * BS) * nloc;
+      for (int b = gl; b < nn; b += G) {
+        int32_t j = cnd[(int64_t)c * nn + b];
+        if (j > 0) {
+          int p = find_col(cols, L, j - 1);
+#pragma unroll
+          for (int cc = 0; cc < BS; cc++)
+#pragma unroll
+            for (int dd = 0; dd < BS; dd++) acc[(p * BS + cc) * BS + dd] += (TA)Krow[cc * nloc + b * BS + dd];
+        }
+      }
+      __syncwarp(gmask);
+    }
+    int64_t ob = rb * BS * BS;
+    for (int i = gl; i < L * BS * BS; i += G) {
+      TA v = acc[i];
+      if (v64) v64[ob + i] = (double)v;
+      if (v32) v32[ob + i] = (float)v;
+    }
+  }
+}
+
+template <int BS, class TK, class TA>
+static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32) {
+  const Space* sp = A->space;
+  Ctx* ctx = ctx_of(sp);
+  int nn = sp->nn;
+  int lmax = A->max_row > 0 ? A->max_row : 1;
+  auto go = [&](auto Gtag) -> int {
+    constexpr int G = decltype(Gtag)::value;
+    constexpr int RPW = 32 / G;
+    int warps = 4;
+    size_t per_row = (size_t)lmax * (BS * BS * sizeof(TA) + sizeof(int32_t));
+    while (warps > 1 && (size_t)warps * RPW * per_row > 96 * 1024) warps >>= 1;
+    size_t smem = (size_t)warps * RPW * per_row;
+    if (smem > 200 * 1024) return set_error(ctx, GT_ERR_UNSUPPORTED, "sparsity row too wide for the scatter kernel");
+    cudaFuncSetAttribute(k_scatter<BS, G, TK, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int64_t rows_per_block = (int64_t)warps * RPW;
+    int64_t grid = (A->nbrows + rows_per_block - 1) / rows_per_block;
+    k_scatter<BS, G, TK, TA><<<(unsigned)(grid > 0 ? grid : 1), warps * 32, smem, ctx->stream>>>(
+        A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, A->nbrows, lmax, Ke, v64, v32);
+    GT_LAUNCH(ctx, "k_scatter");
+    return GT_OK;
+  };
+  if (nn <= 4) return go(std::integral_constant<int, 4>());
+  if (nn <= 8) return go(std::integral_constant<int, 8>());
+  if (nn <= 16) return go(std::integral_constant<int, 16>());
+  return go(std::integral_constant<int, 32>());
+}
+
+int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision) {
+  double* v64 = (out_precision == GT_FP64 || out_precision == GT_MIXED) ? A->val64 : nullptr;
+  float* v32 = (out_precision == GT_FP32 || out_precision == GT_MIXED) ? A->val32 : nullptr;
+  int bs = A->bs;
+  if (ke_precision == GT_FP32) {
+    const float* K = (const float*)Ke;
+    if (bs == 1) return launch_scatter<1, float, float>(A, K, v64, v32);
+    if (bs == 2) return launch_scatter<2, float, float>(A, K, v64, v32);
+    return launch_scatter<3, float, float>(A, K, v64, v32);
+  }
+  const double* K = (const double*)Ke;
+  if (bs == 1) return launch_scatter<1, double, double>(A, K, v64, v32);
+  if (bs == 2) return launch_scatter<2, double, double>(A, K, v64, v32);
+  return launch_scatter<3, double, double>(A, K, v64, v32);
+}
+
+// vector scatter: each (row, component) sums its cells in ascending order
+__global__ void k_scatter_vec(const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, int nn, int bs,
+                              int64_t nrows, const double* __restrict__ be, double* __restrict__ b) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nrows * bs) return;
+  int64_t r = t / bs;
+  int k = (int)(t - r * bs);
+  int nloc = nn * bs;
+  double s = 0.0;
+  for (int64_t i = inc_ptr[r]; i < inc_ptr[r + 1]; i++) {
+    int32_t cb = inc[i];
+    int32_t c = cb / nn, a = cb - c * nn;
+    s += be[(int64_t)c * nloc + a * bs + k];
+  }
+  b[t] = s;
+}
+
+int scatter_vector(const Space* sp, const int64_t* inc_ptr, const int32_t* inc, const double* be, double* b) {
+  Ctx* ctx = ctx_of(sp);
+  int64_t n = sp->nfree_nodes * sp->ncomp;
+  k_scatter_vec<<<grid_for(n, 256), 256, 0, ctx->stream>>>(inc_ptr, inc, sp->nn, sp->ncomp, sp->nfree_nodes, be, b);
+  GT_LAUNCH(ctx, "k_scatter_vec");
+  return GT_OK;
+}
+
+__global__ void k_find_diag(const int64_t* rowptr, const int32_t* colind, int64_t n, int32_t* pos, uint32_t* err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  int64_t b = rowptr[r], e = rowptr[r + 1];
+  int32_t p = -1;
+  int64_t lo = b, hi = e - 1;
+  while (lo <= hi) {
+    int64_t mid = (lo + hi) >> 1;
+    int32_t c = colind[mid];
+    if (c == r) { p = (int32_t)(mid - b); break; }
+    if (c < r) lo = mid + 1; else hi = mid - 1;
+  }
+  if (p < 0) atomicOr(err, DEV_ERR_LOOKUP);
+  pos[r] = p < 0 ? 0 : p;
+}
+
+int find_diag(Matrix* A) {
+  Ctx* ctx = ctx_of(A->space);
+  if (A->diag_pos) return GT_OK;
+  GT_TRY(dalloc(ctx, &A->diag_pos, A->nbrows + 1));
+  k_find_diag<<<grid_for(A->nbrows, 256), 256, 0, ctx->stream>>>(A->rowptr, A->colind, A->nbrows, A->diag_pos, ctx->d_err);
+  GT_LAUNCH(ctx, "k_find_diag");
+  return GT_OK;
+}
+
+// scalar CSR expansion of a block CSR matrix (download path)
+__global__ void k_expand_rowptr(const int64_t* rowptr, int64_t nbrows, int bs, int64_t* out) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t > nbrows * bs) return;
+  if (t == nbrows * bs) { out[t] = rowptr[nbrows] * bs * bs; return; }
+  int64_t i = t / bs;
+  int c = (int)(t - i * bs);
+  int64_t len = rowptr[i + 1] - rowptr[i];
+  out[t] = rowptr[i] * bs * bs + (int64_t)c * bs * len;
+}
+template <class V>
+__global__ void k_expand_entries(const int64_t* rowptr, const int32_t* colind, const V* vals, int64_t nbrows, int bs,
+                                 int32_t* ocol, V* oval) {
+  int64_t i = blockIdx.x;  // block row
+  if (i >= nbrows) return;
+  int64_t b = rowptr[i];
+  int64_t len = rowptr[i + 1] - b;
+  for (int64_t t = threadIdx.x; t < len * bs * bs; t += blockDim.x) {
+    int64_t c = t / (len * bs);
+    int64_t r = t - c * len * bs;
+    int64_t k = r / bs;
+    int d = (int)(r - k * bs);
+    int64_t o = b * bs * bs + t;
+    if (ocol) ocol[o] = colind[b + k] * bs + d;
+    if (oval) oval[o] = vals[(b + k) * bs * bs + c * bs + d];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------
+// a pointer the kernels can read: device pointers pass through, host data is
+// staged into a pooled device buffer
+template <class T>
+struct DevIn {
+  Ctx* ctx;
+  const T* p = nullptr;
+  T* owned = nullptr;
+  int init(Ctx* c, const T* src, int64_t n) {
+    ctx = c;
+    if (!src) return GT_OK;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, src) == cudaSuccess &&
+        (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)) {
+      p = src;
+      return GT_OK;
+    }
+    cudaGetLastError();
+    GT_TRY(dalloc(c, &owned, n));
+    GT_TRY(copy_in(c, owned, src, n));
+    p = owned;
+    return GT_OK;
+  }
+  ~DevIn() {
+    if (owned) dfree(ctx, owned);
+  }
+};
+
+static bool is_device_ptr(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+static int alloc_values(Matrix* A) {
+  Ctx* ctx = ctx_of(A->space);
+  int64_t nv = A->bnnz * A->bs * A->bs;
+  if (A->precision != GT_FP32 && !A->val64) GT_TRY(dalloc(ctx, &A->val64, nv));
+  if (A->precision != GT_FP64 && !A->val32) GT_TRY(dalloc(ctx, &A->val32, nv));
+  return GT_OK;
+}
+
+// element matrices + scatter on the existing pattern (and optionally b)
+static int numeric(Matrix* A, int form, const double* coef_in, double nu, const double* f_in, const double* scoef_in,
+                   double* b_out) {
+  const Space* sp = A->space;
+  Ctx* ctx = ctx_of(sp);
+  int64_t nc = sp->mesh->ncells;
+  DevIn<double> coef, f, scoef;
+  GT_TRY(coef.init(ctx, coef_in, nc));
+  GT_TRY(f.init(ctx, f_in, sp->ncomp));
+  GT_TRY(scoef.init(ctx, scoef_in, nc));
+  int kprec = A->precision == GT_FP32 ? GT_FP32 : GT_FP64;
+  size_t esz = kprec == GT_FP32 ? sizeof(float) : sizeof(double);
+  void* Ke = nullptr;
+  double* be = nullptr;
+  GT_TRY(dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz)));
+  if (b_out) GT_TRY(dalloc(ctx, &be, nc * sp->nloc));
+  int s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
+  if (s == GT_OK) s = alloc_values(A);
+  if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision);
+  if (s == GT_OK && b_out) {
+    bool dev = is_device_ptr(b_out);
+    double* bd = b_out;
+    int64_t nb = sp->nfree_nodes * sp->ncomp;
+    if (!dev) s = dalloc(ctx, &bd, nb);
+    if (s == GT_OK) s = scatter_vector(sp, A->inc_ptr, A->inc, be, bd);
+    if (s == GT_OK && !dev) {
+      s = copy_out(ctx, b_out, bd, nb);
+      if (s == GT_OK) {
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) s = check_cuda(ctx, e, "assemble_vector");
+      }
+      dfree(ctx, bd);
+    }
+  }
+  pool_free(ctx, Ke);
+  if (be) dfree(ctx, be);
+  return s;
+}
+
+static int device_status(Ctx* ctx, const char* where) {
+  uint32_t bits = 0;
+  GT_TRY(take_device_error(ctx, &bits));
+  if (!bits) return GT_OK;
+  if (bits & DEV_ERR_DEGENERATE) return set_error(ctx, GT_ERR_INVALID, std::string(where) + ": degenerate cell (det J = 0)");
+  return set_error(ctx, GT_ERR_INVALID, std::string(where) + ": device-side check failed");
+}
+
+}  // namespace gt
+
+using namespace gt;
+
+static void matrix_release(gt_matrix* A) {
+  Ctx* c = A->space->mesh->ctx;
+  dfree(c, A->rowptr);
+  dfree(c, A->colind);
+  dfree(c, A->val64);
+  dfree(c, A->val32);
+  dfree(c, A->inc_ptr);
+  dfree(c, A->inc);
+  dfree(c, A->diag_pos);
+}
+
+extern "C" {
+
+int gt_assemble_matrix_and_vector(gt_space* sp, int form, const double* cell_coef, double nu, int precision,
+                                  const double* f, const double* source_coef, double* b, gt_matrix** out) {
+  if (!sp || !out) return GT_ERR_INVALID;
+  *out = nullptr;
+  Ctx* ctx = sp->mesh->ctx;
+  if (precision != GT_FP64 && precision != GT_FP32 && precision != GT_MIXED)
+    return set_error(ctx, GT_ERR_INVALID, "precision must be GT_FP64, GT_FP32 or GT_MIXED");
+  if (form != GT_LAPLACE && form != GT_MASS && form != GT_ELASTICITY)
+    return set_error(ctx, GT_ERR_UNSUPPORTED, "weak form not supported (Laplacian, mass, linear elasticity only)");
+  if (form == GT_ELASTICITY && sp->ncomp != sp->mesh->D)
+    return set_error(ctx, GT_ERR_UNSUPPORTED, "linear elasticity needs a vector space (tensor_size = (D,))");
+  if (b && !f) return set_error(ctx, GT_ERR_INVALID, "vector assembly needs a source f");
+  cudaSetDevice(ctx->device);
+  gt_matrix* A = new gt_matrix();
+  A->space = sp;
+  A->bs = sp->ncomp;
+  A->precision = precision;
+  int s = build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc);
+  if (s == GT_OK) s = build_pattern(A);
+  if (s == GT_OK) s = numeric(A, form, cell_coef, nu, f, source_coef, b);
+  if (s == GT_OK) s = device_status(ctx, "assemble_matrix");
+  if (s != GT_OK) {
+    matrix_release(A);
+    delete A;
+    return s;
+  }
+  *out = A;
+  return GT_OK;
+}
+
+int gt_assemble_matrix(gt_space* sp, int form, const double* cell_coef, double nu, int precision, gt_matrix** out) {
+  return gt_assemble_matrix_and_vector(sp, form, cell_coef, nu, precision, nullptr, nullptr, nullptr, out);
+}
+
+int gt_update_matrix(gt_matrix* A, int form, const double* cell_coef, double nu) {
+  if (!A) return GT_ERR_INVALID;
+  Ctx* ctx = A->space->mesh->ctx;
+  GT_TRY(numeric(A, form, cell_coef, nu, nullptr, nullptr, nullptr));
+  return device_status(ctx, "update_matrix");
+}
+
+int gt_update_matrix_and_vector(gt_matrix* A, int form, const double* cell_coef, double nu, const double* f,
+                                const double* source_coef, double* b) {
+  if (!A) return GT_ERR_INVALID;
+  Ctx* ctx = A->space->mesh->ctx;
+  if (b && !f) return set_error(ctx, GT_ERR_INVALID, "vector assembly needs a source f");
+  GT_TRY(numeric(A, form, cell_coef, nu, f, source_coef, b));
+  return device_status(ctx, "update_matrix");
+}
+
+int gt_assemble_vector(gt_space* sp, const double* f, const double* cell_coef, double* b) {
+  if (!sp || !f || !b) return GT_ERR_INVALID;
+  Ctx* ctx = sp->mesh->ctx;
+  cudaSetDevice(ctx->device);
+  if (!sp->inc) GT_TRY(build_incidence(ctx, sp, &sp->inc_ptr, &sp->inc, &sp->ninc));
+  int64_t nc = sp->mesh->ncells;
+  DevIn<double> coef, fd;
+  GT_TRY(coef.init(ctx, cell_coef, nc));
+  GT_TRY(fd.init(ctx, f, sp->ncomp));
+  double* be = nullptr;
+  GT_TRY(dalloc(ctx, &be, nc * sp->nloc));
+  int s = compute_elements(sp, GT_MASS, nullptr, 0.0, GT_FP64, fd.p, coef.p, nullptr, be, 0);
+  int64_t nb = sp->nfree_nodes * sp->ncomp;
+  bool dev = is_device_ptr(b);
+  double* bd = b;
+  if (s == GT_OK && !dev) s = dalloc(ctx, &bd, nb);
+  if (s == GT_OK) s = scatter_vector(sp, sp->inc_ptr, sp->inc, be, bd);
+  if (s == GT_OK && !dev) s = copy_out(ctx, b, bd, nb);
+  if (s == GT_OK) s = device_status(ctx, "assemble_vector");
+  if (!dev && bd) dfree(ctx, bd);
+  dfree(ctx, be);
+  return s;
+}
+
+int gt_matrix_info(const gt_matrix* A, int64_t* info) {
+  if (!A || !info) return GT_ERR_INVALID;
+  info[0] = A->nbrows * A->bs;
+  info[1] = A->bnnz * A->bs * A->bs;
+  info[2] = A->bs;
+  info[3] = A->precision;
+  info[4] = A->nbrows;
+  info[5] = A->bnnz;
+  return GT_OK;
+}
+
+int gt_matrix_download_csr(gt_matrix* A, int64_t* rowptr, int32_t* colind, double* v64, float* v32) {
+  if (!A) return GT_ERR_INVALID;
+  Ctx* ctx = A->space->mesh->ctx;
+  cudaSetDevice(ctx->device);
+  int bs = A->bs;
+  int64_t n = A->nbrows * bs, nnz = A->bnnz * bs * bs;
+  int s = GT_OK;
+  if (bs == 1) {
+    if (rowptr) s = copy_out(ctx, rowptr, A->rowptr, n + 1);
+    if (s == GT_OK && colind) s = copy_out(ctx, colind, A->colind, nnz);
+    if (s == GT_OK && v64 && A->val64) s = copy_out(ctx, v64, A->val64, nnz);
+    if (s == GT_OK && v32 && A->val32) s = copy_out(ctx, v32, A->val32, nnz);
+  } else {
+    int64_t* rp = nullptr;
+    int32_t* ci = nullptr;
+    double* d64 = nullptr;
+    float* d32 = nullptr;
+    if (rowptr) {
+      s = dalloc(ctx, &rp, n + 1);
+      if (s == GT_OK) {
+        k_expand_rowptr<<<grid_for(n + 1, 256), 256, 0, ctx->stream>>>(A->rowptr, A->nbrows, bs, rp);
+        s = copy_out(ctx, rowptr, rp, n + 1);
+      }
+    }
+    if (s == GT_OK && (colind || (v64 && A->val64))) {
+      if (colind) s = dalloc(ctx, &ci, nnz);
+      if (s == GT_OK && v64 && A->val64) s = dalloc(ctx, &d64, nnz);
+      if (s == GT_OK) {
+        k_expand_entries<double><<<(unsigned)A->nbrows, 128, 0, ctx->stream>>>(A->rowptr, A->colind, A->val64, A->nbrows,
+                                                                             bs, ci, d64);
+        if (colind) s = copy_out(ctx, colind, ci, nnz);
+        if (s == GT_OK && d64) s = copy_out(ctx, v64, d64, nnz);
+      }
+    }
+    if (s == GT_OK && v32 && A->val32) {
+      s = dalloc(ctx, &d32, nnz);
+      if (s == GT_OK) {
+        k_expand_entries<float><<<(unsigned)A->nbrows, 128, 0, ctx->stream>>>(A->rowptr, A->colind, A->val32, A->nbrows,
+                                                                            bs, nullptr, d32);
+        s = copy_out(ctx, v32, d32, nnz);
+      }
+    }
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (s == GT_OK && e != cudaSuccess) s = check_cuda(ctx, e, "gt_matrix_download_csr");
+    dfree(ctx, rp);
+    dfree(ctx, ci);
+    dfree(ctx, d64);
+    dfree(ctx, d32);
+    return s;
+  }
+  if (s == GT_OK) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) s = check_cuda(ctx, e, "gt_matrix_download_csr");
+  }
+  return s;
+}
+
+int gt_matrix_destroy(gt_matrix* A) {
+  if (!A) return GT_ERR_INVALID;
+  matrix_release(A);
+  delete A;
+  return GT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,251 @@
+// gt_context.cu -- context, device buffer pool, error plumbing, scans.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+#include "gt_internal.cuh"
+
+namespace gt {
+
+int set_error(Ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+int check_cuda(Ctx* ctx, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return set_error(ctx, GT_ERR_OOM, m);
+  return set_error(ctx, GT_ERR_CUDA, m);
+}
+
+// Blocks are pooled by exact size class (rounded up to 2 MiB above 1 MiB,
+// to 256 B below) so that repeated assemblies of the same problem reuse
+// their buffers without cudaMalloc/cudaFree, which synchronise the device.
+static size_t size_class(size_t b) {
+  if (b <= (1u << 20)) return (b + 255) & ~size_t(255);
+  size_t g = size_t(2) << 20;
+  return (b + g - 1) / g * g;
+}
+
+void* pool_alloc(Ctx* ctx, size_t bytes) {
+  size_t sc = size_class(bytes);
+  auto it = ctx->pool.lower_bound(sc);
+  if (it != ctx->pool.end() && it->first <= sc + sc / 4) {
+    void* p = it->second;
+    size_t s = it->first;
+    ctx->pool.erase(it);
+    ctx->pooled_bytes -= (int64_t)s;
+    ctx->live[p] = s;
+    ctx->live_bytes += (int64_t)s;
+    return p;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, sc);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    pool_trim(ctx);
+    e = cudaMalloc(&p, sc);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+  }
+  ctx->live[p] = sc;
+  ctx->live_bytes += (int64_t)sc;
+  return p;
+}
+
+void pool_free(Ctx* ctx, void* p) {
+  auto it = ctx->live.find(p);
+  if (it == ctx->live.end()) return;
+  size_t s = it->second;
+  ctx->live.erase(it);
+  ctx->live_bytes -= (int64_t)s;
+  ctx->pool.emplace(s, p);
+  ctx->pooled_bytes += (int64_t)s;
+}
+
+void pool_trim(Ctx* ctx) {
+  if (ctx->pool.empty()) return;
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& kv : ctx->pool) cudaFree(kv.second);
+  ctx->pool.clear();
+  ctx->pooled_bytes = 0;
+}
+
+int take_device_error(Ctx* ctx, uint32_t* bits) {
+  GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  *bits = *ctx->h_err;
+  if (*bits) GT_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream));
+  return GT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// exclusive scan: per-block sums, recursive scan of the sums, then a block
+// scan that adds the block offset.  2048 items per block of 256 threads.
+// ---------------------------------------------------------------------------
+constexpr int SCAN_T = 256, SCAN_V = 8, SCAN_B = SCAN_T * SCAN_V;
+
+template <class Tin, class Tout>
+__global__ void k_block_sums(const Tin* __restrict__ in, Tout* __restrict__ sums, int64_t n) {
+  __shared__ Tout red[SCAN_T / 32];
+  int64_t base = (int64_t)blockIdx.x * SCAN_B;
+  Tout s = 0;
+#pragma unroll
+  for (int v = 0; v < SCAN_V; v++) {
+    int64_t i = base + (int64_t)v * SCAN_T + threadIdx.x;
+    if (i < n) s += (Tout)in[i];
+  }
+  for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Tout t = 0;
+    for (int w = 0; w < SCAN_T / 32; w++) t += red[w];
+    sums[blockIdx.x] = t;
+  }
+}
+
+template <class Tin, class Tout>
+__global__ void k_block_scan(const Tin* __restrict__ in, Tout* __restrict__ out, const Tout* __restrict__ offs,
+                             int64_t n) {
+  __shared__ Tout warp_tot[SCAN_T / 32];
+  int64_t base = (int64_t)blockIdx.x * SCAN_B + (int64_t)threadIdx.x * SCAN_V;
+  Tout v[SCAN_V];
+  Tout t = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_V; k++) {
+    int64_t i = base + k;
+    v[k] = i < n ? (Tout)in[i] : (Tout)0;
+    t += v[k];
+  }
+  // inclusive warp scan of thread totals
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  Tout x = t;
+  for (int o = 1; o < 32; o <<= 1) {
+    Tout y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_tot[w] = x;
+  __syncthreads();
+  Tout wo = 0;
+  for (int k = 0; k < w; k++) wo += warp_tot[k];
+  Tout run = (offs ? offs[blockIdx.x] : (Tout)0) + wo + x - t;
+#pragma unroll
+  for (int k = 0; k < SCAN_V; k++) {
+    int64_t i = base + k;
+    if (i < n) out[i] = run;
+    run += v[k];
+  }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == SCAN_T - 1) out[n] = run;
+}
+
+template <class Tin, class Tout>
+static int scan_impl(Ctx* ctx, const Tin* in, Tout* out, int64_t n) {
+  if (n <= 0) {
+    GT_CUDA(ctx, cudaMemsetAsync(out, 0, sizeof(Tout), ctx->stream));
+    return GT_OK;
+  }
+  int64_t nb = (n + SCAN_B - 1) / SCAN_B;
+  if (nb == 1) {
+    k_block_scan<Tin, Tout><<<1, SCAN_T, 0, ctx->stream>>>(in, out, nullptr, n);
+    GT_LAUNCH(ctx, "k_block_scan");
+    return GT_OK;
+  }
+  Tout* sums = nullptr;
+  Tout* soff = nullptr;
+  GT_TRY(dalloc(ctx, &sums, nb));
+  GT_TRY(dalloc(ctx, &soff, nb + 1));
+  k_block_sums<Tin, Tout><<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(in, sums, n);
+  GT_LAUNCH(ctx, "k_block_sums");
+  int s = scan_impl<Tout, Tout>(ctx, sums, soff, nb);
+  if (s == GT_OK) {
+    k_block_scan<Tin, Tout><<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(in, out, soff, n);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) s = check_cuda(ctx, e, "k_block_scan");
+  }
+  dfree(ctx, sums);
+  dfree(ctx, soff);
+  return s;
+}
+
+int exclusive_scan_i64(Ctx* ctx, const int32_t* in, int64_t* out, int64_t n) {
+  return scan_impl<int32_t, int64_t>(ctx, in, out, n);
+}
+int exclusive_scan_i32(Ctx* ctx, const int32_t* in, int32_t* out, int64_t n) {
+  return scan_impl<int32_t, int32_t>(ctx, in, out, n);
+}
+
+}  // namespace gt
+
+using namespace gt;
+
+extern "C" {
+
+int gt_ctx_create(int device, gt_ctx** out) {
+  if (!out) return GT_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return GT_ERR_CUDA;
+  }
+  if (device < 0 || device >= ndev) return GT_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return GT_ERR_CUDA;
+  gt_ctx* c = new gt_ctx();
+  c->device = device;
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->d_err, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMallocHost(&c->h_err, sizeof(uint32_t)) != cudaSuccess ||
+      cudaMallocHost(&c->h_scratch, 64 * sizeof(int64_t)) != cudaSuccess ||
+      cudaMallocHost(&c->h_dscratch, 64 * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return GT_ERR_CUDA;
+  }
+  c->stream = c->own_stream;
+  cudaMemset(c->d_err, 0, sizeof(uint32_t));
+  cudaDeviceSynchronize();
+  *out = c;
+  return GT_OK;
+}
+
+int gt_ctx_destroy(gt_ctx* c) {
+  if (!c) return GT_ERR_INVALID;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  for (auto& kv : c->live) cudaFree(kv.first);
+  for (auto& kv : c->pool) cudaFree(kv.second);
+  cudaFree(c->d_err);
+  cudaFreeHost(c->h_err);
+  cudaFreeHost(c->h_scratch);
+  cudaFreeHost(c->h_dscratch);
+  cudaStreamDestroy(c->own_stream);
+  delete c;
+  return GT_OK;
+}
+
+const char* gt_last_error(const gt_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int gt_ctx_synchronize(gt_ctx* c) {
+  if (!c) return GT_ERR_INVALID;
+  GT_CUDA(c, cudaStreamSynchronize(c->stream));
+  return GT_OK;
+}
+
+int gt_ctx_set_stream(gt_ctx* c, void* stream) {
+  if (!c) return GT_ERR_INVALID;
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return GT_OK;
+}
+
+int gt_ctx_memory(gt_ctx* c, int64_t* live, int64_t* pooled) {
+  if (!c) return GT_ERR_INVALID;
+  if (live) *live = c->live_bytes;
+  if (pooled) *pooled = c->pooled_bytes;
+  return GT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,204 @@
+// gt_internal.cuh -- shared definitions of the GB300 assembly/solve library.
+//
+// Object model (all device state lives in HBM and is owned by a context):
+//   gt_ctx    stream, buffer pool, error flag, last error message
+//   gt_mesh   coords (node-major FP64), cell->nodes (0-based), parent faces
+//   gt_space  node-level DOF ids per cell (1-based free, negative Dirichlet);
+//             a vector space with ncomp components numbers DOF (node, comp)
+//             as (node_dof-1)*ncomp + comp + 1, which is the reference's
+//             component-major numbering when Dirichlet tags whole nodes
+//   gt_matrix block CSR (block size = ncomp) sparsity plus FP64 and/or FP32
+//             values; the incidence lists (block row -> (cell, local node))
+//             drive the deterministic row-owner scatter
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/gtgpu.h"
+
+namespace gt {
+
+constexpr int kMaxNodesPerCell = 27;  // Q2 hexahedron
+constexpr int kMaxLocal = 81;         // Q2 hexahedron, 3 components
+
+struct Ctx;
+
+// ---------------------------------------------------------------------------
+// error plumbing
+// ---------------------------------------------------------------------------
+int set_error(Ctx* ctx, int code, const std::string& msg);
+int check_cuda(Ctx* ctx, cudaError_t e, const char* what);
+#define GT_CUDA(ctx, call)                                   \
+  do {                                                       \
+    cudaError_t e__ = (call);                                \
+    if (e__ != cudaSuccess) return check_cuda(ctx, e__, #call); \
+  } while (0)
+#define GT_LAUNCH(ctx, what)                                         \
+  do {                                                               \
+    cudaError_t e__ = cudaGetLastError();                            \
+    if (e__ != cudaSuccess) return check_cuda(ctx, e__, what);       \
+  } while (0)
+#define GT_TRY(expr)          \
+  do {                        \
+    int s__ = (expr);         \
+    if (s__ != GT_OK) return s__; \
+  } while (0)
+
+// device-side error word bits (written with atomicOr, read by the host)
+enum : uint32_t {
+  DEV_ERR_NODE_RANGE = 1u,
+  DEV_ERR_ROW_CAP = 2u,
+  DEV_ERR_HASH_FULL = 4u,
+  DEV_ERR_LOOKUP = 8u,
+  DEV_ERR_DEGENERATE = 16u,
+  DEV_ERR_KEY_RANGE = 32u,
+};
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct Ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // size-bucketed pool of device blocks (no cudaMalloc in steady state)
+  std::multimap<size_t, void*> pool;
+  std::unordered_map<void*, size_t> live;
+  int64_t live_bytes = 0, pooled_bytes = 0;
+  uint32_t* d_err = nullptr;       // device error word
+  uint32_t* h_err = nullptr;       // pinned mirror
+  int64_t* h_scratch = nullptr;    // pinned small readbacks (64 words)
+  double* h_dscratch = nullptr;    // pinned small FP64 readbacks (64 words)
+};
+
+void* pool_alloc(Ctx* ctx, size_t bytes);
+void pool_free(Ctx* ctx, void* p);
+void pool_trim(Ctx* ctx);
+
+template <class T>
+int dalloc(Ctx* ctx, T** out, int64_t n) {
+  size_t bytes = (size_t)(n > 0 ? n : 1) * sizeof(T);
+  void* p = pool_alloc(ctx, bytes);
+  if (!p) {
+    *out = nullptr;
+    return set_error(ctx, GT_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+  }
+  *out = (T*)p;
+  return GT_OK;
+}
+template <class T>
+void dfree(Ctx* ctx, T*& p) {
+  if (p) pool_free(ctx, (void*)p);
+  p = nullptr;
+}
+
+// reads the device error word (synchronises the stream) and clears it
+int take_device_error(Ctx* ctx, uint32_t* bits);
+
+// copy n elements from a host or device pointer (unified addressing)
+template <class T>
+int copy_in(Ctx* ctx, T* dst, const T* src, int64_t n) {
+  if (n <= 0) return GT_OK;
+  GT_CUDA(ctx, cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyDefault, ctx->stream));
+  return GT_OK;
+}
+template <class T>
+int copy_out(Ctx* ctx, T* dst, const T* src, int64_t n) {
+  if (n <= 0) return GT_OK;
+  GT_CUDA(ctx, cudaMemcpyAsync(dst, src, sizeof(T) * n, cudaMemcpyDefault, ctx->stream));
+  return GT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// mesh / space / matrix
+// ---------------------------------------------------------------------------
+struct Mesh {
+  Ctx* ctx = nullptr;
+  int ctype = 0, D = 0, nv = 0;  // cell type, dimension, nodes per cell
+  int64_t nnodes = 0, ncells = 0;
+  double* coords = nullptr;      // nnodes * D
+  int32_t* cell_nodes = nullptr; // ncells * nv, 0-based
+  int64_t ncorners = 0;
+  int32_t* corners = nullptr;    // 0-based
+  int64_t nbfaces = 0;
+  int nbfv = 0;                  // nodes per boundary face
+  int32_t* bfaces = nullptr;     // 0-based
+  int32_t* bgroup = nullptr;
+  int64_t nbedges = 0;
+  int32_t* bedges = nullptr;     // 3-D parent 1-faces, 0-based
+};
+
+struct Space {
+  Mesh* mesh = nullptr;
+  int order = 1, ncomp = 1, nn = 0, nloc = 0;
+  int64_t nfree_nodes = 0, ndiri_nodes = 0;
+  int32_t* cell_ndofs = nullptr;  // ncells * nn: node-level dof, >0 free (1-based), <0 Dirichlet
+  // incidence cache used by stand-alone vector assembly
+  int64_t* inc_ptr = nullptr;
+  int32_t* inc = nullptr;
+  int64_t ninc = 0;
+};
+
+struct Matrix {
+  Space* space = nullptr;
+  int bs = 1, precision = GT_FP64;
+  int64_t nbrows = 0, bnnz = 0;
+  int max_row = 0;                 // longest block row
+  int64_t* rowptr = nullptr;       // nbrows + 1
+  int32_t* colind = nullptr;       // bnnz, 0-based block columns
+  double* val64 = nullptr;         // bnnz * bs * bs (row-major blocks)
+  float* val32 = nullptr;
+  int64_t* inc_ptr = nullptr;      // block row -> incidences
+  int32_t* inc = nullptr;          // cell * nn + local node
+  int64_t ninc = 0;
+  int32_t* diag_pos = nullptr;     // position of the diagonal block in each row
+};
+
+// ---------------------------------------------------------------------------
+// library-internal entry points (implemented across the .cu files)
+// ---------------------------------------------------------------------------
+int number_dofs(Space* sp, int ngroups, const int32_t* groups);
+int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc);
+int build_pattern(Matrix* A);
+int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision,
+                     const double* f, const double* d_scoef, void* Ke, double* be, int want_matrix);
+int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision);
+int scatter_vector(const Space* sp, const int64_t* inc_ptr, const int32_t* inc, const double* be,
+                   double* b);
+int find_diag(Matrix* A);
+int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mode, gt_solve_info* info);
+int spmv64(Matrix* A, const double* x, double* y);
+
+// device scans (exclusive prefix sum; out has n+1 entries, out[n] = total)
+int exclusive_scan_i64(Ctx* ctx, const int32_t* in, int64_t* out, int64_t n);
+int exclusive_scan_i32(Ctx* ctx, const int32_t* in, int32_t* out, int64_t n);
+
+inline int grid_for(int64_t n, int block) {
+  int64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > 2147483647LL) g = 2147483647LL;
+  return (int)g;
+}
+
+inline int space_nodes(int ctype, int order) {
+  if (ctype == GT_TET4) return 4;
+  int D = ctype == GT_QUAD4 ? 2 : 3;
+  int m = order + 1;
+  return D == 2 ? m * m : m * m * m;
+}
+
+}  // namespace gt
+
+// opaque ABI handles are the internal structs
+struct gt_ctx : gt::Ctx {};
+struct gt_mesh : gt::Mesh {};
+struct gt_space : gt::Space {};
+struct gt_matrix : gt::Matrix {};

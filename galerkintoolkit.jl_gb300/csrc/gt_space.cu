@@ -1,0 +1,668 @@
+// gt_space.cu -- mesh upload and device DOF numbering.
+//
+// Restates on the device what GalerkinToolkit computes sequentially:
+//  * vertex ids (create_vertices!, src/topology.jl:1034-1097): nodes of the
+//    parent 0-faces first in parent order, then every other node in node
+//    order -- a flag + exclusive scan;
+//  * edge and face ids for Q2 (generate_face_boundary, src/topology.jl:
+//    1594-1704): parent faces keep ids 1..npar, every other face gets the
+//    next id in the order in which the scan over the higher-dimensional
+//    faces first meets it.  On the device: a hash table keyed by the face's
+//    sorted vertices collects, per face, the minimum scan rank of its
+//    instances (atomicMin); a flag at that rank + exclusive scan gives the
+//    new ids in first-encounter order -- the sequential order, recovered
+//    without a sequential scan;
+//  * DOF offsets per d-face (generate_dof_ids_step_1, src/space.jl:327-466)
+//    and the free-first / negative-Dirichlet renumbering of step_2
+//    (src/space.jl:477-535, partition_from_mask :910-920) -- flags + scans.
+#include <climits>
+#include <cstring>
+
+#include "gt_internal.cuh"
+#include "gt_refcell.cuh"
+
+namespace gt {
+
+constexpr unsigned long long EMPTY_KEY = ~0ull;
+
+__device__ __forceinline__ void sort3(int32_t& a, int32_t& b, int32_t& c) {
+  int32_t t;
+  if (a > b) { t = a; a = b; b = t; }
+  if (b > c) { t = b; b = c; c = t; }
+  if (a > b) { t = a; a = b; b = t; }
+}
+
+// Key of a face given its vertex ids: 2 vertices -> (min, max) in 32-bit
+// halves; 3 or 4 vertices -> the 3 smallest ids in 21-bit fields (three
+// vertices determine a triangle or a quadrilateral of a conforming mesh).
+__device__ __forceinline__ unsigned long long face_key(const int32_t* v, int n, uint32_t* err) {
+  if (n == 2) {
+    int32_t a = v[0] < v[1] ? v[0] : v[1], b = v[0] < v[1] ? v[1] : v[0];
+    return ((unsigned long long)(uint32_t)a << 32) | (uint32_t)b;
+  }
+  int32_t a = v[0], b = v[1], c = v[2];
+  sort3(a, b, c);
+  if (n == 4) {
+    int32_t d = v[3];
+    if (d < c) { c = d; sort3(a, b, c); }
+  }
+  if (c >= (1 << 21)) { atomicOr(err, DEV_ERR_KEY_RANGE); return EMPTY_KEY - 1; }
+  return ((unsigned long long)a << 42) | ((unsigned long long)b << 21) | (unsigned long long)c;
+}
+
+struct Hash {
+  unsigned long long* keys;
+  int32_t* vals;
+  int32_t* rank;
+  int64_t cap;  // power of two
+};
+
+__device__ __forceinline__ uint64_t mix64(unsigned long long x) {
+  x ^= x >> 33; x *= 0xff51afd7ed558ccdULL; x ^= x >> 33; x *= 0xc4ceb9fe1a85ec53ULL; x ^= x >> 33;
+  return x;
+}
+
+__device__ int64_t hash_insert(Hash h, unsigned long long key, uint32_t* err) {
+  uint64_t s = mix64(key) & (uint64_t)(h.cap - 1);
+  for (int64_t probe = 0; probe < h.cap; probe++) {
+    unsigned long long prev = atomicCAS(&h.keys[s], EMPTY_KEY, key);
+    if (prev == EMPTY_KEY || prev == key) return (int64_t)s;
+    s = (s + 1) & (uint64_t)(h.cap - 1);
+  }
+  atomicOr(err, DEV_ERR_HASH_FULL);
+  return -1;
+}
+
+__device__ int64_t hash_find(Hash h, unsigned long long key) {
+  uint64_t s = mix64(key) & (uint64_t)(h.cap - 1);
+  for (int64_t probe = 0; probe < h.cap; probe++) {
+    unsigned long long k = h.keys[s];
+    if (k == key) return (int64_t)s;
+    if (k == EMPTY_KEY) return -1;
+    s = (s + 1) & (uint64_t)(h.cap - 1);
+  }
+  return -1;
+}
+
+// ---------------------------------------------------------------------------
+// mesh validation / index conversion
+// ---------------------------------------------------------------------------
+__global__ void k_to_zero_based(int32_t* a, int64_t n, int64_t nmax, uint32_t* err) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t v = a[i] - 1;
+    if (v < 0 || v >= nmax) { atomicOr(err, DEV_ERR_NODE_RANGE); v = 0; }
+    a[i] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// vertices
+// ---------------------------------------------------------------------------
+__global__ void k_fill_i32(int32_t* a, int64_t n, int32_t v) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) a[i] = v;
+}
+__global__ void k_corner_first(const int32_t* corners, int64_t nc, int32_t* first) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < nc) atomicMin(&first[corners[i]], (int32_t)i);
+}
+__global__ void k_corner_flags(const int32_t* corners, int64_t nc, const int32_t* first, int32_t* flag) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < nc) flag[i] = first[corners[i]] == (int32_t)i;
+}
+__global__ void k_noncorner_flags(const int32_t* first, int64_t nnodes, int32_t* flag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnodes; i += (int64_t)gridDim.x * blockDim.x)
+    flag[i] = first[i] == INT_MAX;
+}
+__global__ void k_vertex_ids(const int32_t* corners, int64_t nc, const int32_t* first, const int32_t* cpos,
+                             const int32_t* npos, int32_t ncu, int64_t nnodes, int32_t* node_vertex) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < nnodes; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t f = first[i];
+    node_vertex[i] = f == INT_MAX ? ncu + npos[i] : cpos[f];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// first-encounter face numbering
+// ---------------------------------------------------------------------------
+// instances: nf higher-dim faces, each with nlv vertices (fverts), nld local
+// d-faces with ndv vertices given by ld (local vertex indices)
+__global__ void k_insert_parents(Hash h, const int32_t* pverts, int64_t npar, int ndv, uint32_t* err) {
+  int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= npar) return;
+  int32_t v[4];
+  for (int i = 0; i < ndv; i++) v[i] = pverts[p * ndv + i];
+  int64_t s = hash_insert(h, face_key(v, ndv, err), err);
+  if (s >= 0) h.vals[s] = (int32_t)(p + 1);
+}
+struct LocalFaces {
+  int8_t v[12][4];
+};
+__global__ void k_insert_instances(Hash h, const int32_t* fverts, int64_t nf, int nlv, int nld, int ndv, LocalFaces ld,
+                                   int64_t* inst_slot, uint32_t* err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nf * nld) return;
+  int64_t f = r / nld;
+  int l = (int)(r - f * nld);
+  int32_t v[4];
+  for (int i = 0; i < ndv; i++) v[i] = fverts[f * nlv + ld.v[l][i]];
+  int64_t s = hash_insert(h, face_key(v, ndv, err), err);
+  inst_slot[r] = s;
+  if (s >= 0) atomicMin(&h.rank[s], (int32_t)r);
+}
+__global__ void k_first_flags(Hash h, int32_t* flag) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < h.cap; s += (int64_t)gridDim.x * blockDim.x)
+    if (h.keys[s] != EMPTY_KEY && h.vals[s] == 0 && h.rank[s] != INT_MAX) flag[h.rank[s]] = 1;
+}
+__global__ void k_assign_new(Hash h, const int32_t* pos, int32_t npar) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < h.cap; s += (int64_t)gridDim.x * blockDim.x)
+    if (h.keys[s] != EMPTY_KEY && h.vals[s] == 0 && h.rank[s] != INT_MAX) h.vals[s] = npar + pos[h.rank[s]] + 1;
+}
+__global__ void k_instance_ids(Hash h, const int64_t* inst_slot, int64_t n, int32_t* out, uint32_t* err) {
+  for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t s = inst_slot[r];
+    out[r] = s >= 0 ? h.vals[s] : 0;
+    if (s < 0) atomicOr(err, DEV_ERR_LOOKUP);
+  }
+}
+// vertices of every d-face: parents from their own list, new ones from the
+// instance that first met them (generate_face_vertices, topology.jl:1468-1540)
+__global__ void k_face_verts_parent(const int32_t* pverts, int64_t npar, int ndv, int32_t* dverts) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < npar * ndv) dverts[i] = pverts[i];
+}
+__global__ void k_face_verts_new(Hash h, int32_t npar, const int32_t* fverts, int nlv, int nld, int ndv,
+                                 LocalFaces ld, int32_t* dverts) {
+  for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < h.cap; s += (int64_t)gridDim.x * blockDim.x) {
+    if (h.keys[s] == EMPTY_KEY) continue;
+    int32_t id = h.vals[s];
+    if (id <= npar) continue;
+    int64_t r = h.rank[s];
+    int64_t f = r / nld;
+    int l = (int)(r - f * nld);
+    for (int i = 0; i < ndv; i++) dverts[(int64_t)(id - 1) * ndv + i] = fverts[f * nlv + ld.v[l][i]];
+  }
+}
+__global__ void k_lookup_instances(Hash h, const int32_t* fverts, int64_t nf, int nlv, int nld, int ndv, LocalFaces ld,
+                                   int32_t* out, uint32_t* err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nf * nld) return;
+  int64_t f = r / nld;
+  int l = (int)(r - f * nld);
+  int32_t v[4];
+  for (int i = 0; i < ndv; i++) v[i] = fverts[f * nlv + ld.v[l][i]];
+  int64_t s = hash_find(h, face_key(v, ndv, err));
+  if (s < 0) { atomicOr(err, DEV_ERR_LOOKUP); out[r] = 0; } else out[r] = h.vals[s];
+}
+
+struct HashBuf {
+  Hash h{};
+  int alloc(Ctx* ctx, int64_t nkeys) {
+    int64_t cap = 1024;
+    while (cap < 2 * nkeys) cap <<= 1;
+    h.cap = cap;
+    GT_TRY(dalloc(ctx, &h.keys, cap));
+    GT_TRY(dalloc(ctx, &h.vals, cap));
+    GT_TRY(dalloc(ctx, &h.rank, cap));
+    GT_CUDA(ctx, cudaMemsetAsync(h.keys, 0xFF, sizeof(unsigned long long) * cap, ctx->stream));
+    GT_CUDA(ctx, cudaMemsetAsync(h.vals, 0, sizeof(int32_t) * cap, ctx->stream));
+    k_fill_i32<<<grid_for(cap, 256), 256, 0, ctx->stream>>>(h.rank, cap, INT_MAX);
+    GT_LAUNCH(ctx, "k_fill_i32");
+    return GT_OK;
+  }
+  void release(Ctx* ctx) {
+    dfree(ctx, h.keys);
+    dfree(ctx, h.vals);
+    dfree(ctx, h.rank);
+  }
+};
+
+// Numbers the d-faces of nf higher-dimensional faces (see file header).
+// Outputs inst_ids[nf*nld] (1-based) and, if dverts != NULL, the vertices of
+// every d-face (capacity npar + nf*nld faces).  Returns the count in *nd.
+static int number_faces(Ctx* ctx, const int32_t* fverts, int64_t nf, int nlv, int nld, int ndv, const LocalFaces& ld,
+                        const int32_t* pverts, int64_t npar, int32_t* inst_ids, int32_t** dverts_out, int64_t* nd) {
+  HashBuf hb;
+  int64_t ninst = nf * nld;
+  int s = hb.alloc(ctx, npar + ninst);
+  int64_t* inst_slot = nullptr;
+  int32_t *flag = nullptr, *pos = nullptr;
+  if (s == GT_OK) s = dalloc(ctx, &inst_slot, ninst);
+  if (s == GT_OK) s = dalloc(ctx, &flag, ninst);
+  if (s == GT_OK) s = dalloc(ctx, &pos, ninst + 1);
+  if (s == GT_OK) {
+    cudaStream_t st = ctx->stream;
+    cudaMemsetAsync(flag, 0, sizeof(int32_t) * ninst, st);
+    if (npar > 0) k_insert_parents<<<grid_for(npar, 256), 256, 0, st>>>(hb.h, pverts, npar, ndv, ctx->d_err);
+    k_insert_instances<<<grid_for(ninst, 256), 256, 0, st>>>(hb.h, fverts, nf, nlv, nld, ndv, ld, inst_slot, ctx->d_err);
+    k_first_flags<<<grid_for(hb.h.cap, 256), 256, 0, st>>>(hb.h, flag);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) s = check_cuda(ctx, e, "face numbering");
+  }
+  if (s == GT_OK) s = exclusive_scan_i32(ctx, flag, pos, ninst);
+  if (s == GT_OK) {
+    cudaStream_t st = ctx->stream;
+    k_assign_new<<<grid_for(hb.h.cap, 256), 256, 0, st>>>(hb.h, pos, (int32_t)npar);
+    k_instance_ids<<<grid_for(ninst, 256), 256, 0, st>>>(hb.h, inst_slot, ninst, inst_ids, ctx->d_err);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) s = check_cuda(ctx, e, "face ids");
+  }
+  if (s == GT_OK) {
+    int32_t nnew = 0;
+    cudaMemcpyAsync(&ctx->h_scratch[0], pos + ninst, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    memcpy(&nnew, &ctx->h_scratch[0], sizeof(int32_t));
+    *nd = npar + nnew;
+    if (dverts_out) {
+      int32_t* dv = nullptr;
+      s = dalloc(ctx, &dv, (*nd) * ndv);
+      if (s == GT_OK) {
+        cudaStream_t st = ctx->stream;
+        if (npar > 0) k_face_verts_parent<<<grid_for(npar * ndv, 256), 256, 0, st>>>(pverts, npar, ndv, dv);
+        k_face_verts_new<<<grid_for(hb.h.cap, 256), 256, 0, st>>>(hb.h, (int32_t)npar, fverts, nlv, nld, ndv, ld, dv);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) s = check_cuda(ctx, e, "face vertices");
+        *dverts_out = dv;
+      }
+    }
+  }
+  dfree(ctx, inst_slot);
+  dfree(ctx, flag);
+  dfree(ctx, pos);
+  hb.release(ctx);
+  return s;
+}
+
+// lookup of existing d-faces (fill_face_boundary_mesh_topology!,
+// src/topology.jl:515-591)
+static int lookup_faces(Ctx* ctx, const int32_t* dverts, int64_t nd, int ndv, const int32_t* fverts, int64_t nf,
+                        int nlv, int nld, const LocalFaces& ld, int32_t* out) {
+  HashBuf hb;
+  GT_TRY(hb.alloc(ctx, nd));
+  cudaStream_t st = ctx->stream;
+  k_insert_parents<<<grid_for(nd, 256), 256, 0, st>>>(hb.h, dverts, nd, ndv, ctx->d_err);
+  k_lookup_instances<<<grid_for(nf * nld, 256), 256, 0, st>>>(hb.h, fverts, nf, nlv, nld, ndv, ld, out, ctx->d_err);
+  cudaError_t e = cudaGetLastError();
+  hb.release(ctx);
+  if (e != cudaSuccess) return check_cuda(ctx, e, "face lookup");
+  return GT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// DOF ids
+// ---------------------------------------------------------------------------
+__global__ void k_gather_cell_vertices(const int32_t* cell_nodes, int64_t n, const int32_t* node_vertex, int32_t* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = node_vertex[cell_nodes[i]] + 1;  // 1-based vertex ids
+}
+
+// global node-level dof (1-based, before the free/Dirichlet split):
+// vertices, then edges, faces, cells (generate_dof_ids_step_1)
+__global__ void k_cell_node_dofs(RefTables t, int order, int64_t nc, const int32_t* cverts, const int32_t* cedges,
+                                 const int32_t* cfaces, int64_t nverts, int64_t nedges, int64_t nfaces,
+                                 int32_t* cnd) {
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  int32_t* o = cnd + c * t.nn;
+  for (int v = 0; v < t.nlv; v++) o[t.vnode[v]] = cverts[c * t.nlv + v];
+  if (order == 2) {
+    for (int e = 0; e < t.nle; e++) o[t.enode[e]] = (int32_t)(nverts + cedges[c * t.nle + e]);
+    if (t.D == 3)
+      for (int f = 0; f < 6; f++) o[t.fnode[f]] = (int32_t)(nverts + nedges + cfaces[c * 6 + f]);
+    o[t.cnode] = (int32_t)(nverts + nedges + nfaces + c + 1);
+  }
+}
+
+// tag the closure nodes of tagged local (D-1)-faces (step_2, src/space.jl:487-508)
+__global__ void k_tag_dirichlet(Hash tagged, RefTables t, int64_t nc, const int32_t* cverts, const int32_t* cnd,
+                                int32_t* tag, uint32_t* err) {
+  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nc * t.nlf) return;
+  int64_t c = r / t.nlf;
+  int f = (int)(r - c * t.nlf);
+  int32_t v[4];
+  for (int i = 0; i < t.nlfv; i++) v[i] = cverts[c * t.nlv + t.lf_verts[f][i]];
+  if (hash_find(tagged, face_key(v, t.nlfv, err)) < 0) return;
+  for (int i = 0; i < t.nclosure; i++) tag[cnd[c * t.nn + t.closure[f][i]] - 1] = 1;
+}
+__global__ void k_free_flags(const int32_t* tag, int64_t n, int32_t* freef) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    freef[i] = 1 - tag[i];
+}
+__global__ void k_renumber(int32_t* cnd, int64_t n, const int32_t* tag, const int32_t* fpos, const int32_t* dpos) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    int32_t g = cnd[i] - 1;
+    cnd[i] = tag[g] ? -(dpos[g] + 1) : fpos[g] + 1;
+  }
+}
+__global__ void k_select_faces(const int32_t* bfaces, const int32_t* bgroup, int64_t nb, int nbfv, const int32_t* node_vertex,
+                               const int32_t* groups, int ngroups, int32_t* out_verts, int32_t* keep) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  int k = 1;
+  if (ngroups > 0) {
+    k = 0;
+    for (int g = 0; g < ngroups; g++) k |= bgroup[i] == groups[g];
+  }
+  keep[i] = k;
+  for (int j = 0; j < nbfv; j++) out_verts[i * nbfv + j] = k ? node_vertex[bfaces[i * nbfv + j]] + 1 : 0;
+}
+__global__ void k_insert_tagged(Hash h, const int32_t* verts, const int32_t* keep, int64_t nb, int ndv, uint32_t* err) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nb || !keep[i]) return;
+  hash_insert(h, face_key(verts + i * ndv, ndv, err), err);
+}
+__global__ void k_tag_vertices(const int32_t* sel, int64_t n, int32_t* tag) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (sel[i] > 0) tag[sel[i] - 1] = 1;
+}
+__global__ void k_map_vertices(const int32_t* nodes, int64_t n, const int32_t* node_vertex, int32_t* out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = node_vertex[nodes[i]] + 1;
+}
+
+static int device_error_status(Ctx* ctx, const char* where) {
+  uint32_t bits = 0;
+  GT_TRY(take_device_error(ctx, &bits));
+  if (!bits) return GT_OK;
+  std::string m = std::string(where) + ": ";
+  if (bits & DEV_ERR_NODE_RANGE) m += "node id out of range; ";
+  if (bits & DEV_ERR_KEY_RANGE) return set_error(ctx, GT_ERR_UNSUPPORTED, m + "more than 2^21-1 vertices for face keys");
+  if (bits & DEV_ERR_HASH_FULL) m += "hash table full; ";
+  if (bits & DEV_ERR_LOOKUP) m += "face not found (mesh is not a face complex); ";
+  if (bits & DEV_ERR_ROW_CAP) m += "sparsity row above the supported width; ";
+  return set_error(ctx, GT_ERR_INVALID, m);
+}
+
+int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
+  Mesh* M = sp->mesh;
+  Ctx* ctx = M->ctx;
+  cudaStream_t st = ctx->stream;
+  RefTables t = make_ref_tables(M->ctype, sp->order);
+  int64_t nc = M->ncells, nn_ = M->nnodes;
+  int s = GT_OK;
+  // ---- vertices
+  int32_t *first = nullptr, *cflag = nullptr, *cpos = nullptr, *nflag = nullptr, *npos = nullptr, *node_vertex = nullptr;
+  GT_TRY(dalloc(ctx, &first, nn_));
+  GT_TRY(dalloc(ctx, &cflag, M->ncorners + 1));
+  GT_TRY(dalloc(ctx, &cpos, M->ncorners + 1));
+  GT_TRY(dalloc(ctx, &nflag, nn_));
+  GT_TRY(dalloc(ctx, &npos, nn_ + 1));
+  GT_TRY(dalloc(ctx, &node_vertex, nn_));
+  k_fill_i32<<<grid_for(nn_, 256), 256, 0, st>>>(first, nn_, INT_MAX);
+  if (M->ncorners > 0) {
+    k_corner_first<<<grid_for(M->ncorners, 256), 256, 0, st>>>(M->corners, M->ncorners, first);
+    k_corner_flags<<<grid_for(M->ncorners, 256), 256, 0, st>>>(M->corners, M->ncorners, first, cflag);
+  }
+  k_noncorner_flags<<<grid_for(nn_, 256), 256, 0, st>>>(first, nn_, nflag);
+  GT_LAUNCH(ctx, "vertex flags");
+  GT_TRY(exclusive_scan_i32(ctx, cflag, cpos, M->ncorners));
+  GT_TRY(exclusive_scan_i32(ctx, nflag, npos, nn_));
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], cpos + M->ncorners, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GT_CUDA(ctx, cudaStreamSynchronize(st));
+  int32_t ncu = 0;
+  memcpy(&ncu, &ctx->h_scratch[0], sizeof(int32_t));
+  k_vertex_ids<<<grid_for(nn_, 256), 256, 0, st>>>(M->corners, M->ncorners, first, cpos, npos, ncu, nn_, node_vertex);
+  GT_LAUNCH(ctx, "k_vertex_ids");
+  int64_t nverts = nn_;
+  dfree(ctx, first);
+  dfree(ctx, cflag);
+  dfree(ctx, cpos);
+  dfree(ctx, nflag);
+  dfree(ctx, npos);
+  // cell vertices (1-based vertex ids)
+  int32_t* cverts = nullptr;
+  GT_TRY(dalloc(ctx, &cverts, nc * M->nv));
+  k_gather_cell_vertices<<<grid_for(nc * M->nv, 256), 256, 0, st>>>(M->cell_nodes, nc * M->nv, node_vertex, cverts);
+  GT_LAUNCH(ctx, "k_gather_cell_vertices");
+  // ---- edges / faces (Q2)
+  int32_t *cedges = nullptr, *cfaces = nullptr;
+  int64_t nedges = 0, nfaces = 0;
+  if (sp->order == 2) {
+    LocalFaces lq{}, lh{}, le{};
+    if (t.D == 2) {
+      for (int e = 0; e < 4; e++) { lq.v[e][0] = t.le_verts[e][0]; lq.v[e][1] = t.le_verts[e][1]; }
+      int32_t* pv = nullptr;
+      GT_TRY(dalloc(ctx, &pv, M->nbfaces * 2));
+      k_map_vertices<<<grid_for(M->nbfaces * 2, 256), 256, 0, st>>>(M->bfaces, M->nbfaces * 2, node_vertex, pv);
+      GT_LAUNCH(ctx, "k_map_vertices");
+      GT_TRY(dalloc(ctx, &cedges, nc * 4));
+      s = number_faces(ctx, cverts, nc, 4, 4, 2, lq, pv, M->nbfaces, cedges, nullptr, &nedges);
+      dfree(ctx, pv);
+      GT_TRY(s);
+    } else {
+      for (int f = 0; f < 6; f++)
+        for (int i = 0; i < 4; i++) lh.v[f][i] = t.lf_verts[f][i];
+      static const int QE[4][2] = {{0, 1}, {2, 3}, {0, 2}, {1, 3}};
+      for (int e = 0; e < 4; e++) { lq.v[e][0] = QE[e][0]; lq.v[e][1] = QE[e][1]; }
+      for (int e = 0; e < 12; e++) { le.v[e][0] = t.le_verts[e][0]; le.v[e][1] = t.le_verts[e][1]; }
+      int32_t *pf = nullptr, *pe = nullptr, *fverts = nullptr, *fedges = nullptr, *everts = nullptr;
+      GT_TRY(dalloc(ctx, &pf, M->nbfaces * 4));
+      GT_TRY(dalloc(ctx, &pe, M->nbedges * 2 + 1));
+      k_map_vertices<<<grid_for(M->nbfaces * 4, 256), 256, 0, st>>>(M->bfaces, M->nbfaces * 4, node_vertex, pf);
+      if (M->nbedges > 0)
+        k_map_vertices<<<grid_for(M->nbedges * 2, 256), 256, 0, st>>>(M->bedges, M->nbedges * 2, node_vertex, pe);
+      GT_LAUNCH(ctx, "k_map_vertices");
+      GT_TRY(dalloc(ctx, &cfaces, nc * 6));
+      GT_TRY(number_faces(ctx, cverts, nc, 8, 6, 4, lh, pf, M->nbfaces, cfaces, &fverts, &nfaces));
+      GT_TRY(dalloc(ctx, &fedges, nfaces * 4));
+      GT_TRY(number_faces(ctx, fverts, nfaces, 4, 4, 2, lq, pe, M->nbedges, fedges, &everts, &nedges));
+      GT_TRY(dalloc(ctx, &cedges, nc * 12));
+      GT_TRY(lookup_faces(ctx, everts, nedges, 2, cverts, nc, 8, 12, le, cedges));
+      dfree(ctx, pf);
+      dfree(ctx, pe);
+      dfree(ctx, fverts);
+      dfree(ctx, fedges);
+      dfree(ctx, everts);
+    }
+  }
+  // ---- node dofs before the split
+  int64_t nnodes_sp = nverts + (sp->order == 2 ? nedges + nfaces + nc : 0);
+  GT_TRY(dalloc(ctx, &sp->cell_ndofs, nc * t.nn));
+  k_cell_node_dofs<<<grid_for(nc, 128), 128, 0, st>>>(t, sp->order, nc, cverts, cedges, cfaces, nverts, nedges, nfaces,
+                                                       sp->cell_ndofs);
+  GT_LAUNCH(ctx, "k_cell_node_dofs");
+  // ---- Dirichlet tags
+  int32_t *tag = nullptr, *freef = nullptr, *fpos = nullptr, *dpos = nullptr;
+  GT_TRY(dalloc(ctx, &tag, nnodes_sp));
+  GT_CUDA(ctx, cudaMemsetAsync(tag, 0, sizeof(int32_t) * nnodes_sp, st));
+  if (ngroups != 0 && M->nbfaces > 0) {
+    int32_t *sel = nullptr, *keep = nullptr, *dgroups = nullptr;
+    int ng = ngroups > 0 ? ngroups : 0;
+    GT_TRY(dalloc(ctx, &sel, M->nbfaces * M->nbfv));
+    GT_TRY(dalloc(ctx, &keep, M->nbfaces));
+    GT_TRY(dalloc(ctx, &dgroups, ng + 1));
+    if (ng > 0) GT_TRY(copy_in(ctx, dgroups, groups_host, ng));
+    k_select_faces<<<grid_for(M->nbfaces, 256), 256, 0, st>>>(M->bfaces, M->bgroup, M->nbfaces, M->nbfv, node_vertex,
+                                                               dgroups, ng, sel, keep);
+    GT_LAUNCH(ctx, "k_select_faces");
+    if (sp->order == 1) {
+      // the closure of a tagged face holds only its vertices, whose
+      // pre-split node dof is the vertex id
+      k_tag_vertices<<<grid_for(M->nbfaces * M->nbfv, 256), 256, 0, st>>>(sel, M->nbfaces * M->nbfv, tag);
+      GT_LAUNCH(ctx, "k_tag_vertices");
+    } else {
+      HashBuf hb;
+      GT_TRY(hb.alloc(ctx, M->nbfaces));
+      k_insert_tagged<<<grid_for(M->nbfaces, 256), 256, 0, st>>>(hb.h, sel, keep, M->nbfaces, M->nbfv, ctx->d_err);
+      k_tag_dirichlet<<<grid_for(nc * t.nlf, 256), 256, 0, st>>>(hb.h, t, nc, cverts, sp->cell_ndofs, tag, ctx->d_err);
+      GT_LAUNCH(ctx, "k_tag_dirichlet");
+      hb.release(ctx);
+    }
+    dfree(ctx, sel);
+    dfree(ctx, keep);
+    dfree(ctx, dgroups);
+  }
+  GT_TRY(dalloc(ctx, &freef, nnodes_sp));
+  GT_TRY(dalloc(ctx, &fpos, nnodes_sp + 1));
+  GT_TRY(dalloc(ctx, &dpos, nnodes_sp + 1));
+  k_free_flags<<<grid_for(nnodes_sp, 256), 256, 0, st>>>(tag, nnodes_sp, freef);
+  GT_LAUNCH(ctx, "k_free_flags");
+  GT_TRY(exclusive_scan_i32(ctx, freef, fpos, nnodes_sp));
+  GT_TRY(exclusive_scan_i32(ctx, tag, dpos, nnodes_sp));
+  k_renumber<<<grid_for(nc * t.nn, 256), 256, 0, st>>>(sp->cell_ndofs, nc * t.nn, tag, fpos, dpos);
+  GT_LAUNCH(ctx, "k_renumber");
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], fpos + nnodes_sp, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[1], dpos + nnodes_sp, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GT_TRY(device_error_status(ctx, "lagrange_space"));  // synchronises
+  int32_t nf = 0, ndr = 0;
+  memcpy(&nf, &ctx->h_scratch[0], sizeof(int32_t));
+  memcpy(&ndr, &ctx->h_scratch[1], sizeof(int32_t));
+  sp->nfree_nodes = nf;
+  sp->ndiri_nodes = ndr;
+  dfree(ctx, tag);
+  dfree(ctx, freef);
+  dfree(ctx, fpos);
+  dfree(ctx, dpos);
+  dfree(ctx, cverts);
+  dfree(ctx, cedges);
+  dfree(ctx, cfaces);
+  dfree(ctx, node_vertex);
+  return GT_OK;
+}
+
+__global__ void k_expand_cell_dofs(const int32_t* cnd, int64_t nc, int nn, int ncomp, int32_t* out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nc * nn * ncomp) return;
+  int64_t c = i / (nn * ncomp);
+  int r = (int)(i - c * nn * ncomp);
+  int a = r / ncomp, k = r - a * ncomp;
+  int32_t d = cnd[c * nn + a];
+  out[i] = d > 0 ? (d - 1) * ncomp + k + 1 : -((-d - 1) * ncomp + k + 1);
+}
+
+}  // namespace gt
+
+using namespace gt;
+
+extern "C" {
+
+int gt_mesh_create(gt_ctx* ctx, int cell_type, int64_t nnodes, const double* coords, int64_t ncells,
+                   const int32_t* cell_nodes, int64_t ncorners, const int32_t* corner_nodes, int64_t nbfaces,
+                   const int32_t* bface_nodes, const int32_t* bface_group, int64_t nbedges, const int32_t* bedge_nodes,
+                   gt_mesh** out) {
+  if (!ctx || !out) return GT_ERR_INVALID;
+  *out = nullptr;
+  if (cell_type != GT_QUAD4 && cell_type != GT_HEX8 && cell_type != GT_TET4)
+    return set_error(ctx, GT_ERR_UNSUPPORTED, "cell type must be QUAD4, HEX8 or TET4");
+  if (nnodes <= 0 || ncells <= 0 || !coords || !cell_nodes) return set_error(ctx, GT_ERR_INVALID, "empty mesh");
+  if (nnodes >= INT_MAX || ncells >= INT_MAX / 8) return set_error(ctx, GT_ERR_UNSUPPORTED, "mesh too large for Int32 ids");
+  cudaSetDevice(ctx->device);
+  gt_mesh* M = new gt_mesh();
+  M->ctx = ctx;
+  M->ctype = cell_type;
+  M->D = cell_type == GT_QUAD4 ? 2 : 3;
+  M->nv = cell_type == GT_QUAD4 ? 4 : (cell_type == GT_HEX8 ? 8 : 4);
+  M->nbfv = cell_type == GT_QUAD4 ? 2 : (cell_type == GT_HEX8 ? 4 : 3);
+  M->nnodes = nnodes;
+  M->ncells = ncells;
+  M->ncorners = ncorners;
+  M->nbfaces = nbfaces;
+  M->nbedges = M->D == 3 ? nbedges : 0;
+  int s = GT_OK;
+  auto up = [&](int32_t** dst, const int32_t* src, int64_t n, int64_t nmax) {
+    if (s != GT_OK) return;
+    s = dalloc(ctx, dst, n > 0 ? n : 1);
+    if (s != GT_OK || n <= 0) return;
+    s = copy_in(ctx, *dst, src, n);
+    if (s != GT_OK) return;
+    if (nmax > 0) k_to_zero_based<<<grid_for(n, 256), 256, 0, ctx->stream>>>(*dst, n, nmax, ctx->d_err);
+  };
+  s = dalloc(ctx, &M->coords, nnodes * M->D);
+  if (s == GT_OK) s = copy_in(ctx, M->coords, coords, nnodes * M->D);
+  up(&M->cell_nodes, cell_nodes, ncells * M->nv, nnodes);
+  up(&M->corners, corner_nodes, ncorners, nnodes);
+  up(&M->bfaces, bface_nodes, nbfaces * M->nbfv, nnodes);
+  up(&M->bgroup, bface_group, bface_group ? nbfaces : 0, 0);
+  up(&M->bedges, bedge_nodes, M->nbedges * 2, nnodes);
+  if (s == GT_OK) s = device_error_status(ctx, "gt_mesh_create");
+  if (s != GT_OK) {
+    gt_mesh_destroy(M);
+    return s;
+  }
+  *out = M;
+  return GT_OK;
+}
+
+int gt_mesh_set_coords(gt_mesh* M, const double* coords) {
+  if (!M || !coords) return GT_ERR_INVALID;
+  return copy_in(M->ctx, M->coords, coords, M->nnodes * M->D);
+}
+
+int gt_mesh_destroy(gt_mesh* M) {
+  if (!M) return GT_ERR_INVALID;
+  Ctx* c = M->ctx;
+  dfree(c, M->coords);
+  dfree(c, M->cell_nodes);
+  dfree(c, M->corners);
+  dfree(c, M->bfaces);
+  dfree(c, M->bgroup);
+  dfree(c, M->bedges);
+  delete M;
+  return GT_OK;
+}
+
+int gt_space_create(gt_mesh* M, int order, int ncomp, int ngroups, const int32_t* groups, gt_space** out) {
+  if (!M || !out) return GT_ERR_INVALID;
+  *out = nullptr;
+  Ctx* ctx = M->ctx;
+  if (order != 1 && order != 2) return set_error(ctx, GT_ERR_UNSUPPORTED, "order must be 1 or 2");
+  if (M->ctype == GT_TET4 && order != 1) return set_error(ctx, GT_ERR_UNSUPPORTED, "TET4 supports P1 only");
+  if (ncomp != 1 && ncomp != M->D) return set_error(ctx, GT_ERR_UNSUPPORTED, "ncomp must be 1 or the dimension");
+  if (ngroups > 0 && !groups) return set_error(ctx, GT_ERR_INVALID, "groups is NULL");
+  if (ngroups != 0 && M->nbfaces > 0 && M->ctype == GT_QUAD4 && !M->bgroup && ngroups > 0)
+    return set_error(ctx, GT_ERR_INVALID, "mesh has no boundary groups");
+  cudaSetDevice(ctx->device);
+  gt_space* sp = new gt_space();
+  sp->mesh = M;
+  sp->order = order;
+  sp->ncomp = ncomp;
+  sp->nn = space_nodes(M->ctype, order);
+  sp->nloc = sp->nn * ncomp;
+  int s = number_dofs(sp, ngroups, groups);
+  if (s != GT_OK) {
+    gt_space_destroy(sp);
+    return s;
+  }
+  *out = sp;
+  return GT_OK;
+}
+
+int gt_space_info(const gt_space* sp, int64_t* info) {
+  if (!sp || !info) return GT_ERR_INVALID;
+  info[0] = sp->nfree_nodes * sp->ncomp;
+  info[1] = sp->ndiri_nodes * sp->ncomp;
+  info[2] = sp->nloc;
+  info[3] = sp->mesh->ncells;
+  info[4] = sp->nfree_nodes;
+  info[5] = sp->ncomp;
+  return GT_OK;
+}
+
+int gt_space_cell_dofs(const gt_space* sp, int32_t* out) {
+  if (!sp || !out) return GT_ERR_INVALID;
+  Ctx* ctx = sp->mesh->ctx;
+  int64_t n = sp->mesh->ncells * sp->nloc;
+  int32_t* tmp = nullptr;
+  GT_TRY(dalloc(ctx, &tmp, n));
+  k_expand_cell_dofs<<<grid_for(n, 256), 256, 0, ctx->stream>>>(sp->cell_ndofs, sp->mesh->ncells, sp->nn, sp->ncomp, tmp);
+  GT_LAUNCH(ctx, "k_expand_cell_dofs");
+  int s = copy_out(ctx, out, tmp, n);
+  if (s == GT_OK) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) s = check_cuda(ctx, e, "gt_space_cell_dofs");
+  }
+  dfree(ctx, tmp);
+  return s;
+}
+
+int gt_space_destroy(gt_space* sp) {
+  if (!sp) return GT_ERR_INVALID;
+  Ctx* c = sp->mesh->ctx;
+  dfree(c, sp->cell_ndofs);
+  dfree(c, sp->inc_ptr);
+  dfree(c, sp->inc);
+  delete sp;
+  return GT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,394 @@
+"""GT-style host API over the C ABI (the drop-in for the assembly + solve path).
+
+Mirrors the problem-level entry points of GalerkinToolkit.jl v0.6.3:
+
+  GT.interior / GT.boundary            src/mesh.jl:223-271
+  GT.lagrange_space                    src/space.jl:1702-1735
+  GT.assemble_matrix / update_matrix!  src/problems.jl:319-361
+  GT.assemble_vector                   src/problems.jl:244-274
+  GT.assemble_matrix_and_vector        src/problems.jl:391-414
+  GT.PartitionedSolvers_linear_problem src/problems.jl:439-462 (+ PS.solve)
+
+Weak forms are passed as explicit tags (``laplacian``, ``mass``,
+``elasticity``, ``source``) instead of closures; any other form raises
+``NotImplementedError`` -- the GB300 kernels implement only these integrands.
+Every computation runs in libgtgpu.so on the GPU; there is no CPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import GTError, check
+from .mesh import Mesh
+
+_default_ctx = None
+
+
+class Context:
+    """Owns a CUDA stream and the device buffer pool (gt_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        h = C.c_void_p()
+        st = self.lib.gt_ctx_create(device, C.byref(h))
+        if st != 0:
+            raise GTError(st, f"gt_ctx_create(device={device}) failed (is a CUDA GPU present?)")
+        self.h = h
+        self.device = device
+
+    def synchronize(self):
+        check(self.h, self.lib.gt_ctx_synchronize(self.h))
+
+    def set_stream(self, stream_ptr):
+        check(self.h, self.lib.gt_ctx_set_stream(self.h, stream_ptr))
+
+    def memory(self):
+        a, b = C.c_int64(), C.c_int64()
+        check(self.h, self.lib.gt_ctx_memory(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def close(self):
+        if self.h:
+            self.lib.gt_ctx_destroy(self.h)
+            self.h = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+def _ptr(a):
+    """Pointer of a numpy array or a torch tensor (host or device)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return C.c_void_p(a.ctypes.data)
+    if hasattr(a, "data_ptr"):
+        return C.c_void_p(a.data_ptr())
+    raise TypeError(f"unsupported buffer type {type(a)}")
+
+
+# ---------------------------------------------------------------------------
+# mesh on the device
+# ---------------------------------------------------------------------------
+class DeviceMesh:
+    def __init__(self, mesh: Mesh, ctx: Context):
+        self.ctx, self.mesh = ctx, mesh
+        h = C.c_void_p()
+        m = mesh
+        check(ctx.h, ctx.lib.gt_mesh_create(
+            ctx.h, m.cell_type, m.num_nodes, _ptr(m.coords), m.num_cells, _ptr(m.cell_nodes),
+            m.corners.size, _ptr(m.corners), m.bfaces.shape[0], _ptr(m.bfaces), _ptr(m.bface_group),
+            m.bedges.shape[0], _ptr(m.bedges), C.byref(h)))
+        self.h = h
+
+    def set_coords(self, coords):
+        check(self.ctx.h, self.ctx.lib.gt_mesh_set_coords(self.h, _ptr(coords)))
+
+    def __del__(self):
+        try:
+            if self.h and self.ctx.h:
+                self.ctx.lib.gt_mesh_destroy(self.h)
+        except Exception:
+            pass
+
+
+def device_mesh(mesh: Mesh, ctx: Context | None = None) -> DeviceMesh:
+    ctx = ctx or default_context()
+    dm = mesh._device.get(id(ctx))
+    if dm is None:
+        dm = DeviceMesh(mesh, ctx)
+        mesh._device[id(ctx)] = dm
+    return dm
+
+
+# ---------------------------------------------------------------------------
+# domains and spaces
+# ---------------------------------------------------------------------------
+@dataclass
+class Domain:
+    mesh: Mesh
+    dim: int
+    group_names: tuple | None = None  # None = every boundary face
+
+    def groups(self):
+        """-1 (all boundary faces) or the list of k of "(D-1)-face-k"."""
+        if self.group_names is None or "boundary" in self.group_names:
+            return -1, None
+        ks = []
+        for name in self.group_names:
+            d, sep, k = name.partition("-face-")
+            if not sep or int(d) != self.mesh.D - 1:
+                raise ValueError(f"unknown boundary group {name!r}")
+            ks.append(int(k))
+        return len(ks), np.asarray(ks, np.int32)
+
+
+def interior(mesh: Mesh) -> Domain:
+    return Domain(mesh, mesh.D)
+
+
+def boundary(mesh: Mesh, group_names=None) -> Domain:
+    return Domain(mesh, mesh.D - 1, tuple(group_names) if group_names else None)
+
+
+class Space:
+    """A Lagrange space with device DOF numbering (gt_space)."""
+
+    def __init__(self, domain: Domain, order: int, tensor_size=None, dirichlet_boundary: Domain | None = None,
+                 ctx: Context | None = None):
+        if domain.dim != domain.mesh.D:
+            raise NotImplementedError("spaces live on the interior of the mesh")
+        self.ctx = ctx or default_context()
+        self.mesh = domain.mesh
+        self.dmesh = device_mesh(self.mesh, self.ctx)
+        ncomp = 1
+        if tensor_size is not None:
+            ts = tuple(tensor_size) if not isinstance(tensor_size, int) else (tensor_size,)
+            if len(ts) != 1:
+                raise NotImplementedError("only scalar and vector spaces are supported")
+            ncomp = ts[0]
+        if dirichlet_boundary is None:
+            ng, groups = 0, None
+        else:
+            ng, groups = dirichlet_boundary.groups()
+        h = C.c_void_p()
+        check(self.ctx.h, self.ctx.lib.gt_space_create(self.dmesh.h, order, ncomp, ng, _ptr(groups), C.byref(h)))
+        self.h = h
+        self.order, self.ncomp = order, ncomp
+        info = np.zeros(6, np.int64)
+        check(self.ctx.h, self.ctx.lib.gt_space_info(h, _ptr(info)))
+        self.num_free_dofs = int(info[0])
+        self.num_dirichlet_dofs = int(info[1])
+        self.num_local_dofs = int(info[2])
+
+    def face_dofs(self) -> np.ndarray:
+        """GT.face_dofs(V): (ncells, nloc) int32, free > 0, Dirichlet < 0."""
+        out = np.zeros((self.mesh.num_cells, self.num_local_dofs), np.int32)
+        check(self.ctx.h, self.ctx.lib.gt_space_cell_dofs(self.h, _ptr(out)))
+        return out
+
+    def __del__(self):
+        try:
+            if self.h and self.ctx.h:
+                self.ctx.lib.gt_space_destroy(self.h)
+        except Exception:
+            pass
+
+
+def lagrange_space(domain: Domain, order: int, tensor_size=None, dirichlet_boundary=None, ctx=None) -> Space:
+    return Space(domain, order, tensor_size, dirichlet_boundary, ctx)
+
+
+def num_free_dofs(V: Space) -> int:
+    return V.num_free_dofs
+
+
+def num_dirichlet_dofs(V: Space) -> int:
+    return V.num_dirichlet_dofs
+
+
+# ---------------------------------------------------------------------------
+# weak forms (the supported set)
+# ---------------------------------------------------------------------------
+@dataclass
+class Form:
+    kind: int
+    coef: object = None    # None, scalar, or per-cell array (host/device)
+    nu: float = 0.3
+
+    def cell_coef(self, ncells):
+        if self.coef is None:
+            return None
+        if np.isscalar(self.coef):
+            return np.full(ncells, float(self.coef))
+        return self.coef
+
+
+def laplacian(coef=None) -> Form:
+    """a(u,v) = int coef grad(u).grad(v) dOmega (per-cell coef)."""
+    return Form(_lib.GT_LAPLACE, coef)
+
+
+def mass(coef=None) -> Form:
+    """a(u,v) = int coef u v dOmega."""
+    return Form(_lib.GT_MASS, coef)
+
+
+def elasticity(E=None, nu=0.3) -> Form:
+    """a(u,v) = int sigma(eps(u)):eps(v), sigma = lam tr(eps) I + 2 mu eps."""
+    return Form(_lib.GT_ELASTICITY, E, float(nu))
+
+
+@dataclass
+class Source:
+    f: object = 1.0        # scalar or ncomp vector
+    coef: object = None    # optional per-cell factor
+
+    def fvec(self, ncomp):
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(self.f, np.float64), (ncomp,)))
+
+
+def source(f=1.0, coef=None) -> Source:
+    """l(v) = int coef f . v dOmega."""
+    return Source(f, coef)
+
+
+def _check_form(a):
+    if not isinstance(a, Form):
+        raise NotImplementedError("only the Laplacian, mass and linear-elasticity forms are supported "
+                                  "on the GPU path (use gtgpu.laplacian / mass / elasticity)")
+
+
+def _precision(T):
+    if T in (np.float64, float, "float64", "fp64"):
+        return _lib.GT_FP64
+    if T in (np.float32, "float32", "fp32"):
+        return _lib.GT_FP32
+    if T in ("mixed",):
+        return _lib.GT_MIXED
+    raise ValueError(f"unsupported value type {T!r}")
+
+
+# ---------------------------------------------------------------------------
+# matrices
+# ---------------------------------------------------------------------------
+class Matrix:
+    """Free x free matrix on the device (block CSR, block = ncomp)."""
+
+    def __init__(self, space: Space, handle, form: Form):
+        self.space, self.h, self.form = space, handle, form
+        self.ctx = space.ctx
+        info = np.zeros(6, np.int64)
+        check(self.ctx.h, self.ctx.lib.gt_matrix_info(handle, _ptr(info)))
+        self.shape = (int(info[0]), int(info[0]))
+        self.nnz = int(info[1])
+        self.block_size = int(info[2])
+        self.precision = int(info[3])
+
+    def csr(self, dtype=np.float64):
+        """(rowptr int64, colind int32, values) of the scalar CSR matrix."""
+        n, nnz = self.shape[0], self.nnz
+        rp = np.zeros(n + 1, np.int64)
+        ci = np.zeros(nnz, np.int32)
+        v64 = np.zeros(nnz, np.float64) if dtype == np.float64 and self.precision != _lib.GT_FP32 else None
+        v32 = np.zeros(nnz, np.float32) if v64 is None else None
+        check(self.ctx.h, self.ctx.lib.gt_matrix_download_csr(self.h, _ptr(rp), _ptr(ci), _ptr(v64), _ptr(v32)))
+        return rp, ci, (v64 if v64 is not None else v32)
+
+    def values32(self):
+        nnz = self.nnz
+        v32 = np.zeros(nnz, np.float32)
+        check(self.ctx.h, self.ctx.lib.gt_matrix_download_csr(self.h, None, None, None, _ptr(v32)))
+        return v32
+
+    def tocsr(self):
+        import scipy.sparse as sp
+        rp, ci, v = self.csr()
+        return sp.csr_matrix((v, ci, rp), shape=self.shape)
+
+    def __matmul__(self, x):
+        y = np.zeros(self.shape[0], np.float64)
+        x = np.ascontiguousarray(x, np.float64)
+        check(self.ctx.h, self.ctx.lib.gt_spmv(self.h, _ptr(x), _ptr(y)))
+        return y
+
+    def __del__(self):
+        try:
+            if self.h and self.ctx.h:
+                self.ctx.lib.gt_matrix_destroy(self.h)
+        except Exception:
+            pass
+
+
+def assemble_matrix(a: Form, T, U: Space, V: Space | None = None, reuse=False):
+    """GT.assemble_matrix(a, T, U, V): sparsity + values on the GPU."""
+    _check_form(a)
+    V = V or U
+    if V is not U:
+        raise NotImplementedError("trial and test spaces must be the same space")
+    h = C.c_void_p()
+    coef = a.cell_coef(U.mesh.num_cells)
+    check(U.ctx.h, U.ctx.lib.gt_assemble_matrix(U.h, a.kind, _ptr(coef), a.nu, _precision(T), C.byref(h)))
+    A = Matrix(U, h, a)
+    return (A, A) if reuse else A
+
+
+def update_matrix(A: Matrix, a: Form | None = None):
+    """GT.update_matrix!(A, cache): new values on the same sparsity."""
+    a = a or A.form
+    _check_form(a)
+    coef = a.cell_coef(A.space.mesh.num_cells)
+    check(A.ctx.h, A.ctx.lib.gt_update_matrix(A.h, a.kind, _ptr(coef), a.nu))
+    A.form = a
+    return A
+
+
+def assemble_vector(l: Source, T, V: Space, out=None):
+    """GT.assemble_vector(l, T, V) for l(v) = int coef f . v."""
+    if not isinstance(l, Source):
+        raise NotImplementedError("only source terms int coef*f*v are supported (use gtgpu.source)")
+    b = out if out is not None else np.zeros(V.num_free_dofs, np.float64)
+    coef = None if l.coef is None else (np.full(V.mesh.num_cells, float(l.coef)) if np.isscalar(l.coef) else l.coef)
+    check(V.ctx.h, V.ctx.lib.gt_assemble_vector(V.h, _ptr(l.fvec(V.ncomp)), _ptr(coef), _ptr(b)))
+    return b
+
+
+def assemble_matrix_and_vector(a: Form, l: Source, T, U: Space, V: Space | None = None, out=None):
+    """GT.assemble_matrix_and_vector(a, l, T, U, V) -> (A, b)."""
+    _check_form(a)
+    if not isinstance(l, Source):
+        raise NotImplementedError("only source terms int coef*f*v are supported")
+    V = V or U
+    if V is not U:
+        raise NotImplementedError("trial and test spaces must be the same space")
+    h = C.c_void_p()
+    b = out if out is not None else np.zeros(U.num_free_dofs, np.float64)
+    coef = a.cell_coef(U.mesh.num_cells)
+    scoef = None if l.coef is None else (np.full(U.mesh.num_cells, float(l.coef)) if np.isscalar(l.coef) else l.coef)
+    check(U.ctx.h, U.ctx.lib.gt_assemble_matrix_and_vector(U.h, a.kind, _ptr(coef), a.nu, _precision(T),
+                                                           _ptr(l.fvec(U.ncomp)), _ptr(scoef), _ptr(b), C.byref(h)))
+    return Matrix(U, h, a), b
+
+
+# ---------------------------------------------------------------------------
+# linear problems and the solve
+# ---------------------------------------------------------------------------
+@dataclass
+class LinearProblem:
+    A: Matrix
+    b: np.ndarray
+    x: np.ndarray
+
+
+def linear_problem(U: Space, a: Form, l: Source, T=np.float64, V=None) -> LinearProblem:
+    """GT.PartitionedSolvers_linear_problem(T, U, a, l) with homogeneous
+    Dirichlet data: A, b assembled on the GPU, x = 0."""
+    A, b = assemble_matrix_and_vector(a, l, T, U, V)
+    return LinearProblem(A, b, np.zeros_like(b))
+
+
+_MODES = {"fp64": _lib.GT_SOLVE_FP64, "ir": _lib.GT_SOLVE_IR, "mixed": _lib.GT_SOLVE_IR, "fp32": _lib.GT_SOLVE_FP32}
+
+
+def solve(p: LinearProblem | Matrix, b=None, x=None, rtol=1e-10, maxit=20000, mode="fp64", raise_on_fail=True):
+    """Jacobi-PCG (mode "fp64"), FP64 refinement around FP32 PCG ("ir"), or
+    FP32 PCG ("fp32").  Returns (x, info dict)."""
+    if isinstance(p, LinearProblem):
+        A, b, x = p.A, p.b, p.x if x is None else x
+    else:
+        A = p
+        x = np.zeros(A.shape[0]) if x is None else x
+    info = _lib.SolveInfo()
+    st = A.ctx.lib.gt_solve(A.h, _ptr(b), _ptr(x), float(rtol), int(maxit), _MODES[mode], C.byref(info))
+    if st != 0 and (raise_on_fail or st != _lib.GT_ERR_NOT_CONVERGED):
+        check(A.ctx.h, st)
+    return x, dict(iterations=info.iterations, outer_iterations=info.outer_iterations,
+                   rel_residual=info.rel_residual, converged=st == 0)

@@ -1,0 +1,169 @@
+/*
+ * gtgpu.h -- C ABI of the GB300 finite-element assembly + solve library.
+ *
+ * The entry points replace the problem-level seam of GalerkinToolkit.jl
+ * (v0.6.3).  Each declaration names the reference interface it stands in
+ * for (paths are inside the GalerkinToolkit.jl source tree).
+ *
+ * Conventions
+ *  - Every function returns an int status: GT_OK (0) or a negative GT_ERR_*.
+ *    Nothing aborts; gt_last_error(ctx) gives the message of the last error.
+ *  - Pointer arguments may be host (pageable or pinned) or device pointers;
+ *    the library copies through unified addressing.  Output pointers that
+ *    refer to host memory are complete when the call returns.
+ *  - Ids follow GalerkinToolkit (src/helpers.jl:47-61): node ids in
+ *    cell_nodes and boundary-face arrays are 1-based Int32; DOF ids returned
+ *    by gt_space_cell_dofs are 1-based for free DOFs and negative for
+ *    Dirichlet DOFs (src/space.jl:515-524).  CSR arrays are 0-based
+ *    (rowptr int64, colind int32); a Julia caller adds 1 when it wraps them
+ *    as SparseMatrixCSC (the matrix is symmetric, so CSR == CSC).
+ *  - One context per host thread (or serialise calls).  All work of a
+ *    context runs on its CUDA stream, in call order.
+ */
+#ifndef GTGPU_H
+#define GTGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define GT_OK 0
+#define GT_ERR_INVALID (-1)       /* bad argument or malformed mesh */
+#define GT_ERR_CUDA (-2)          /* CUDA runtime error */
+#define GT_ERR_OOM (-3)           /* device allocation failed */
+#define GT_ERR_UNSUPPORTED (-4)   /* weak form / element outside the supported set */
+#define GT_ERR_NOT_CONVERGED (-5) /* iterative solve hit maxit */
+#define GT_ERR_TIMEOUT (-6)       /* a bounded device-side wait gave up */
+#define GT_ERR_BUDGET (-7)        /* request refused by the HBM admission budget */
+
+/* cell types (geometry) */
+#define GT_QUAD4 1
+#define GT_HEX8 2
+#define GT_TET4 3
+
+/* weak forms (the only ones supported; anything else is GT_ERR_UNSUPPORTED) */
+#define GT_LAPLACE 1    /* int coef * grad(u) . grad(v) */
+#define GT_MASS 2       /* int coef * u v */
+#define GT_ELASTICITY 3 /* int sigma(eps(u)) : eps(v), E = coef, Poisson ratio nu */
+
+/* precision of the assembled values */
+#define GT_FP64 0  /* FP64 integration, FP64 values */
+#define GT_FP32 1  /* FP64 Jacobian inverse/determinant, FP32 element matrix and values */
+#define GT_MIXED 2 /* FP64 integration, FP64 values plus an FP32 copy sharing the index arrays */
+
+/* solve modes */
+#define GT_SOLVE_FP64 0 /* Jacobi-PCG in FP64 */
+#define GT_SOLVE_IR 1   /* FP64 iterative refinement around an FP32 Jacobi-PCG */
+#define GT_SOLVE_FP32 2 /* Jacobi-PCG in FP32 (needs FP32 values) */
+
+typedef struct gt_ctx gt_ctx;
+typedef struct gt_mesh gt_mesh;
+typedef struct gt_space gt_space;
+typedef struct gt_matrix gt_matrix;
+
+typedef struct gt_solve_info {
+  int32_t iterations;       /* total inner (PCG) iterations */
+  int32_t outer_iterations; /* refinement steps (GT_SOLVE_IR), else 0 */
+  double rel_residual;      /* final ||b - A x|| / ||b|| in FP64 */
+} gt_solve_info;
+
+/* ---- context ------------------------------------------------------------ */
+/* No reference counterpart (the reference is a single-process CPU library);
+ * owns the CUDA stream, the buffer pool and the last error message. */
+int gt_ctx_create(int device, gt_ctx** ctx);
+int gt_ctx_destroy(gt_ctx* ctx);
+const char* gt_last_error(const gt_ctx* ctx);
+int gt_ctx_synchronize(gt_ctx* ctx);
+/* Use an external stream (cudaStream_t passed as void*); NULL restores the
+ * context's own stream. */
+int gt_ctx_set_stream(gt_ctx* ctx, void* stream);
+/* Bytes of device memory currently held by the context (live + pooled). */
+int gt_ctx_memory(gt_ctx* ctx, int64_t* live_bytes, int64_t* pooled_bytes);
+
+/* ---- mesh --------------------------------------------------------------- */
+/* Replaces GT.mesh(...) of a cartesian_mesh (src/mesh.jl:573-650,
+ * src/cartesian_mesh.jl:16-54): node coordinates (node-major, nnodes*D),
+ * cell->nodes (1-based, local node order of the reference cell), the parent
+ * 0-faces (corner nodes), the parent (D-1)-faces with their group index k
+ * (group "(D-1)-face-k"), and in 3-D the parent 1-faces (box-edge
+ * segments).  Parent faces fix the topology numbering of complexify
+ * (src/topology.jl:1034-1125). */
+int gt_mesh_create(gt_ctx* ctx, int cell_type, int64_t nnodes, const double* coords,
+                   int64_t ncells, const int32_t* cell_nodes, int64_t ncorners,
+                   const int32_t* corner_nodes, int64_t nbfaces, const int32_t* bface_nodes,
+                   const int32_t* bface_group, int64_t nbedges, const int32_t* bedge_nodes,
+                   gt_mesh** mesh);
+/* Replaces GT.replace_node_coordinates (src/mesh.jl:698-713) in place. */
+int gt_mesh_set_coords(gt_mesh* mesh, const double* coords);
+int gt_mesh_destroy(gt_mesh* mesh);
+
+/* ---- space / DOF numbering ---------------------------------------------- */
+/* Replaces GT.lagrange_space(Omega, order; tensor_size, dirichlet_boundary)
+ * (src/space.jl:1702-1735) and its generate_dof_ids (src/space.jl:299-535),
+ * computed on the device.  order 1 or 2 (P1 on TET4), ncomp 1 or D.
+ * ngroups: -1 = Dirichlet on all boundary faces (GT.boundary(mesh)),
+ * 0 = no Dirichlet, >0 = the groups listed in `groups` (values k of
+ * "(D-1)-face-k").  Vector spaces are clamped on all components. */
+int gt_space_create(gt_mesh* mesh, int order, int ncomp, int ngroups, const int32_t* groups,
+                    gt_space** space);
+/* info[0]=num_free_dofs info[1]=num_dirichlet_dofs info[2]=local dofs per
+ * cell info[3]=ncells info[4]=free nodes (block rows) info[5]=ncomp */
+int gt_space_info(const gt_space* space, int64_t* info);
+/* GT.face_dofs(V) (src/space.jl:1820-1853): ncells*nloc, GT convention. */
+int gt_space_cell_dofs(const gt_space* space, int32_t* cell_dofs);
+int gt_space_destroy(gt_space* space);
+
+/* ---- matrix assembly ---------------------------------------------------- */
+/* Replaces GT.assemble_matrix(a, T, V, V; reuse=Val(true))
+ * (src/problems.jl:319-350): sparsity (allocate_matrix counting pass and
+ * COO->CSC compress, src/assembly.jl:75-153,571-575) plus values of the
+ * form, in one call.  cell_coef: per-cell coefficient (ncells) or NULL
+ * (= 1); nu: Poisson ratio (GT_ELASTICITY only).  The returned matrix keeps
+ * the sparsity so gt_update_matrix can refill values. */
+int gt_assemble_matrix(gt_space* space, int form, const double* cell_coef, double nu, int precision,
+                       gt_matrix** matrix);
+/* Replaces GT.assemble_matrix_and_vector(a, l, T, U, V; reuse=Val(true))
+ * (src/problems.jl:391-407): the matrix as gt_assemble_matrix plus the
+ * vector of int source_coef*f.v (f: ncomp values; source_coef per cell or
+ * NULL = 1) into b (num_free_dofs FP64), sharing one sparsity construction. */
+int gt_assemble_matrix_and_vector(gt_space* space, int form, const double* cell_coef, double nu,
+                                  int precision, const double* f, const double* source_coef, double* b,
+                                  gt_matrix** matrix);
+/* Replaces GT.update_matrix!(A, cache) (src/problems.jl:352-361): new values
+ * on the existing sparsity. */
+int gt_update_matrix(gt_matrix* matrix, int form, const double* cell_coef, double nu);
+/* Replaces GT.update_matrix_and_vector! (src/problems.jl:409-414). */
+int gt_update_matrix_and_vector(gt_matrix* matrix, int form, const double* cell_coef, double nu,
+                                const double* f, const double* source_coef, double* b);
+/* info[0]=rows info[1]=nnz (scalar) info[2]=block size info[3]=precision
+ * info[4]=block rows info[5]=block nnz */
+int gt_matrix_info(const gt_matrix* matrix, int64_t* info);
+/* Scalar CSR of the free x free matrix.  Any output may be NULL; the
+ * values arrays are filled only if the matrix holds that precision. */
+int gt_matrix_download_csr(gt_matrix* matrix, int64_t* rowptr, int32_t* colind, double* values_f64,
+                           float* values_f32);
+int gt_matrix_destroy(gt_matrix* matrix);
+
+/* ---- vector assembly ---------------------------------------------------- */
+/* Replaces GT.assemble_vector(v -> int f*v dOmega, T, V) (src/problems.jl:
+ * 244-274, src/assembly.jl:27-73,558-569) with a constant source f (ncomp
+ * values) times an optional per-cell coefficient.  b: num_free_dofs FP64. */
+int gt_assemble_vector(gt_space* space, const double* f, const double* cell_coef, double* b);
+
+/* ---- solve -------------------------------------------------------------- */
+/* Replaces PS.solve(PS.LinearAlgebra_lu(GT.PartitionedSolvers_linear_problem
+ * (...))) (src/problems.jl:439-462) with a Jacobi-preconditioned CG (the
+ * reference has no CG of its own).  b, x: num_free_dofs FP64; x holds the
+ * initial guess on entry.  rtol on ||b - A x|| / ||b||. */
+int gt_solve(gt_matrix* matrix, const double* b, double* x, double rtol, int maxit, int mode,
+             gt_solve_info* info);
+/* y = A x in the matrix's FP64 values (or FP32 when it has no FP64). */
+int gt_spmv(gt_matrix* matrix, const double* x, double* y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GTGPU_H */

@@ -1,0 +1,161 @@
+"""GPU path (through the C ABI) against the CPU oracle on the same seeded
+inputs: DOF ids and sparsity bit-exact, FP64 values within 1e-12 (normwise,
+relative to the largest entry), FP32 values within 2e-6, vectors, solves."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as sla
+
+import gtgpu as GT
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12   # plain FP64 path vs FP64 oracle
+TOL32 = 2e-6    # FP32 element integration / values vs FP64 oracle
+
+
+def _oracle_mesh(m):
+    return dict(D=m.D, ctype=m.cell_type, coords=m.coords, cell_nodes=m.cell_nodes, pf0=m.corners,
+                pf1=m.bedges if m.D == 3 else m.bfaces, pf1g=m.bface_group if m.D == 2 else None,
+                pf2=m.bfaces if m.D == 3 else None, pf2g=m.bface_group if m.D == 3 else None,
+                cells=m.cells_per_dir, box=m.domain)
+
+
+def _oracle_space(m, order, ncomp, groups):
+    om = _oracle_mesh(m)
+    if m.D == 2:
+        om["pf1"], om["pf1g"] = m.bfaces, m.bface_group
+    return O.lagrange_space(om, order, ncomp=ncomp, dirichlet=groups), om
+
+
+CASES = [
+    # (id, cells, simplex, order, ncomp, dirichlet groups, form, jitter, coef sigma)
+    ("q1quad_64x64", (64, 64), False, 1, 1, "boundary", O.LAPLACE, 0.0, 0.0),
+    ("p1tet_6x5x4_jitter", (6, 5, 4), True, 1, 1, "boundary", O.LAPLACE, 0.2, 1.0),
+    ("p1tet_4_mass", (4, 4, 4), True, 1, 1, None, O.MASS, 0.2, 0.5),
+    ("q1hex_5x4x3_x0", (5, 4, 3), False, 1, 1, ["2-face-5"], O.LAPLACE, 0.15, 1.0),
+    ("q1hex_elast", (4, 3, 3), False, 1, 3, ["2-face-5"], O.ELASTICITY, 0.1, 0.5),
+    ("q2quad_5x7", (5, 7), False, 2, 1, "boundary", O.LAPLACE, 0.2, 1.0),
+    ("q2quad_mass_vec", (3, 4), False, 2, 2, ["1-face-1", "1-face-3"], O.MASS, 0.0, 0.0),
+    ("q2hex_elast_x0", (3, 4, 5), False, 2, 3, ["2-face-5"], O.ELASTICITY, 0.1, 0.5),
+    ("q2hex_lap_free", (3, 3, 3), False, 2, 1, None, O.LAPLACE, 0.0, 0.0),
+    ("q1quad_1x1_alldiri", (1, 1), False, 1, 1, "boundary", O.LAPLACE, 0.0, 0.0),
+    ("q2quad_1x1", (1, 1), False, 2, 1, "boundary", O.LAPLACE, 0.0, 0.0),
+]
+
+_KIND = {O.LAPLACE: GT.laplacian, O.MASS: GT.mass, O.ELASTICITY: GT.elasticity}
+
+
+def _build(case):
+    cid, cells, simplex, order, ncomp, groups, form, jit, sig = case
+    D = len(cells)
+    m = GT.cartesian_mesh(tuple(x for _ in cells for x in (0.0, 1.0)), cells, simplexify=simplex)
+    if jit:
+        GT.jitter_interior_nodes(m, jit, 7)
+    coef = GT.lognormal_cells(m.num_cells, sig, 11) if sig else None
+    Om = GT.interior(m)
+    diri = None if groups is None else GT.boundary(m, None if groups == "boundary" else groups)
+    V = GT.lagrange_space(Om, order, tensor_size=(ncomp,) if ncomp > 1 else None, dirichlet_boundary=diri)
+    ref, om = _oracle_space(m, order, ncomp, None if groups is None else groups)
+    a = _KIND[form](coef) if form != O.ELASTICITY else GT.elasticity(coef, 0.3)
+    return m, V, ref, a, coef, form, order
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_dof_numbering_bit_exact(case):
+    m, V, ref, *_ = _build(case)
+    assert V.num_free_dofs == ref["nfree"] and V.num_dirichlet_dofs == ref["ndiri"]
+    assert np.array_equal(V.face_dofs(), ref["cell_dofs"])
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_matrix_pattern_and_fp64_values(case):
+    m, V, ref, a, coef, form, order = _build(case)
+    A = GT.assemble_matrix(a, np.float64, V, V)
+    rp, ci, v = A.csr()
+    cp, rv, nz = O.assemble_matrix(ref, form, 2 * order, coef=coef, nu=0.3)
+    orp, oci, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    if ov.size:
+        scale = np.abs(ov).max()
+        assert np.abs(v - ov).max() <= TOL64 * scale
+
+
+@pytest.mark.parametrize("case", CASES[:8], ids=[c[0] for c in CASES[:8]])
+def test_fp32_and_mixed_values(case):
+    m, V, ref, a, coef, form, order = _build(case)
+    cp, rv, nz = O.assemble_matrix(ref, form, 2 * order, coef=coef, nu=0.3)
+    _, _, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
+    A32 = GT.assemble_matrix(a, np.float32, V, V)
+    v32 = A32.values32()
+    scale = np.abs(ov).max()
+    assert np.abs(v32 - ov).max() <= TOL32 * scale
+    Am = GT.assemble_matrix(a, "mixed", V, V)
+    _, _, v64 = Am.csr()
+    assert np.abs(v64 - ov).max() <= TOL64 * scale
+    assert np.array_equal(Am.values32(), v64.astype(np.float32))
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_vector(case):
+    m, V, ref, a, coef, form, order = _build(case)
+    ncomp = V.ncomp
+    f = np.array([0.0, 0.0, -1.0])[-ncomp:] if ncomp > 1 else 1.0
+    b = GT.assemble_vector(GT.source(f, coef), np.float64, V)
+    ob = O.assemble_vector(ref, 2 * order, f, coef=coef)
+    if ob.size:
+        assert np.abs(b - ob).max() <= TOL64 * np.abs(ob).max()
+    # combined entry point: same matrix and vector
+    A2, b2 = GT.assemble_matrix_and_vector(a, GT.source(f, coef), np.float64, V)
+    assert np.array_equal(b2, b)
+
+
+def test_assembly_is_deterministic():
+    m, V, ref, a, coef, form, order = _build(CASES[1])
+    A1 = GT.assemble_matrix(a, np.float64, V, V)
+    A2 = GT.assemble_matrix(a, np.float64, V, V)
+    assert np.array_equal(A1.csr()[2], A2.csr()[2])
+
+
+def test_update_matrix_equals_fresh_assembly():
+    m, V, ref, a, coef, form, order = _build(CASES[1])
+    A = GT.assemble_matrix(a, np.float64, V, V)
+    k2 = GT.lognormal_cells(m.num_cells, 1.0, 99)
+    GT.update_matrix(A, GT.laplacian(k2))
+    B = GT.assemble_matrix(GT.laplacian(k2), np.float64, V, V)
+    assert np.array_equal(A.csr()[2], B.csr()[2])
+
+
+def test_unsupported_forms_raise():
+    m = GT.cartesian_mesh((0, 1, 0, 1), (4, 4))
+    V = GT.lagrange_space(GT.interior(m), 1)
+    with pytest.raises(NotImplementedError):
+        GT.assemble_matrix(lambda u, v: None, np.float64, V, V)
+    with pytest.raises(GT.GTError):
+        GT.assemble_matrix(GT.elasticity(None, 0.3), np.float64, V, V)  # scalar space
+
+
+@pytest.mark.parametrize("mode", ["fp64", "ir"])
+def test_solve_cfg1_poisson(mode):
+    """2-D Poisson -lap u = 1, 64x64 Q1, CG to 1e-10 (plain) / IR to 1e-10."""
+    m = GT.cartesian_mesh((0, 1, 0, 1), (64, 64))
+    V = GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m))
+    T = np.float64 if mode == "fp64" else "mixed"
+    A, b = GT.assemble_matrix_and_vector(GT.laplacian(), GT.source(1.0), T, V)
+    x, info = GT.solve(A, b, rtol=1e-10, mode=mode)
+    assert info["converged"] and info["rel_residual"] <= 1e-10
+    ref, _ = _oracle_space(m, 1, 1, "boundary")
+    cp, rv, nz = O.assemble_matrix(ref, O.LAPLACE, 2)
+    xd = sla.spsolve(sp.csc_matrix((nz, rv, cp), shape=(ref["nfree"],) * 2), O.assemble_vector(ref, 2, 1.0))
+    assert np.abs(x - xd).max() / np.abs(xd).max() < 1e-8
+
+
+def test_solve_q2_elasticity_ir():
+    m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (4, 4, 4))
+    V = GT.lagrange_space(GT.interior(m), 2, tensor_size=(3,), dirichlet_boundary=GT.boundary(m, ["2-face-5"]))
+    A, b = GT.assemble_matrix_and_vector(GT.elasticity(1.0, 0.3), GT.source([0, 0, -1.0]), "mixed", V)
+    x, info = GT.solve(A, b, rtol=1e-10, mode="ir")
+    assert info["converged"]
+    xd = sla.spsolve(A.tocsr().tocsc(), b)
+    assert np.abs(x - xd).max() / np.abs(xd).max() < 1e-8
