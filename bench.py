@@ -1,0 +1,348 @@
+#!/usr/bin/env python
+"""Benchmark of the finite-element assembly + solve path on GB300.
+
+Workload (default): 3-D Poisson on jittered tetrahedra -- unit cube, 96^3
+cubes split into 6 tets (5,308,416 cells, 857,375 free DOFs), interior nodes
+jittered U(-0.2h, 0.2h) (seed 202), P1, 4-point Strang quadrature, per-cell
+coefficient lognormal(0,1) (seed 202), homogeneous Dirichlet on the whole
+boundary, plain FP64.  One step = GT.assemble_matrix + GT.assemble_vector from
+the device-resident space: sparsity (incidence + pattern), FP64 integration,
+deterministic scatter and the load vector.  Metric: nnz assembled per second.
+
+`e2e` measures the same step through the C ABI with host buffers: the node
+coordinates and the coefficient are copied in from pinned host memory and
+the CSR arrays and the vector are read back into pinned host memory, every
+step.  The JSON line also carries the roofline of the dominant kernel, the
+CPU baseline (the oracle restatement of the reference algorithm on the
+host's cores), the solve rates (plain FP64 PCG vs FP64-refined FP32 PCG) and
+the SM clocks sampled during the timed region.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+N > 1 runs N independent replicas (the path is assembled per mesh; there is
+no data-path exchange), launched by torch.distributed.run.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "galerkintoolkit.jl_gb300"))
+
+METRIC = "nnz/s assembled (assemble_matrix + assemble_vector, plain FP64)"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    p.add_argument("--cells", type=int, default=96, help="cubes per direction (96 = the benchmark workload)")
+    p.add_argument("--no-solve", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def workload(n):
+    import gtgpu as GT
+    m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (n, n, n), simplexify=True)
+    GT.jitter_interior_nodes(m, 0.2, 202)
+    kappa = GT.lognormal_cells(m.num_cells, 1.0, 202)
+    return m, kappa
+
+
+def wl_config(n, extra=None):
+    c = {"workload": f"3-D Poisson, unit cube {n}^3 cubes x 6 P1 tets ({6 * n ** 3} cells), jittered +-0.2h, "
+                     f"kappa lognormal(0,1), Dirichlet on the boundary, plain FP64",
+         "cells": 6 * n ** 3, "order": 1, "quadrature": "Strang 4-point", "seed": 202,
+         "l2": "flushed between timed steps (256 MiB write)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+def load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except Exception:
+        return dict(PEAKS_FALLBACK), "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join("/tmp", f"gt_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device),
+                 "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 8 and f[0].replace(".", "").isdigit():
+                    rows.append(f)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[0]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][1]), "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle restatement of the reference algorithm
+# ---------------------------------------------------------------------------
+def cpu_assembly(m, kappa, reps=1, threads=None):
+    """Times count pass + COO + COO->CSC + assemble_vector of the oracle."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    import oracle as O
+    om = dict(D=3, ctype=O.TET4, coords=m.coords, cell_nodes=m.cell_nodes, pf0=m.corners, pf1=m.bedges,
+              pf2=m.bfaces, pf2g=m.bface_group)
+    V = O.lagrange_space(om, 1, dirichlet="boundary")
+    times, nnz = [], 0
+    for _ in range(reps):
+        t = time.perf_counter()
+        cp, rv, nz = O.assemble_matrix(V, O.LAPLACE, 2, coef=kappa)
+        O.assemble_vector(V, 2, 1.0)
+        times.append(time.perf_counter() - t)
+        nnz = rv.size
+    return nnz, times, O.num_threads()
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n = args.cells
+    m, kappa = workload(n)
+    ncores = os.cpu_count()
+    nnz, times, used = cpu_assembly(m, kappa, reps=max(1, args.warmup + args.steps if args.steps <= 2 else 2),
+                                    threads=ncores)
+    t = min(times)
+    v = nnz / t
+    line = {"metric": METRIC, "value": v, "unit": "nnz/s", "impl": "reference", "n_gpus": args.gpus,
+            "steps": len(times), "warmup": 0, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": wl_config(n, {"nnz": int(nnz)}),
+            "cpu_baseline": {"value": v, "unit": "nnz/s", "cores": used, "kind": "port",
+                             "sample": f"full workload, best of {len(times)} (OpenMP {used} threads)"},
+            "e2e": {"value": v, "unit": "nnz/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "C restatement of GalerkinToolkit's assembly (counting pass, COO append, COO->CSC); "
+                    "the Julia reference cannot be installed offline"}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    import gtgpu as GT
+
+    n = args.cells
+    m, kappa = workload(n)
+    ctx = GT.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.set_stream(stream.cuda_stream)
+    V = GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m), ctx=ctx)
+    kd = torch.from_numpy(kappa).cuda()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    a, l = GT.laplacian(kd), GT.source(1.0)
+
+    def step(T=np.float64):
+        A, b = GT.assemble_matrix_and_vector(a, l, T, V, out=bdev)
+        return A
+
+    bdev = torch.empty(V.num_free_dofs, dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup):
+        A = step()
+        del A
+    torch.cuda.synchronize()
+    nnz = None
+    times = []
+    launches0 = ctx.launches()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t_wall = time.perf_counter()
+        for _ in range(args.steps):
+            flush.fill_(1)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            A = step()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            nnz = A.nnz
+            del A
+        torch.cuda.synchronize()
+        t_wall = time.perf_counter() - t_wall
+    if world > 1:
+        dist.barrier()
+    launches = ctx.launches() - launches0
+    ms = sum(times) / len(times)
+    tmax = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    ms_max = float(tmax.item())
+    value = world * nnz / (ms_max * 1e-3)
+
+    # ---- phase profile of one extra step (dominant kernel + roofline)
+    flush.fill_(1)
+    ctx.profile_begin()
+    A = step()
+    phases = ctx.profile_end()
+    del A
+    peaks, peaks_kind = load_peaks()
+    fp64_tf = ctx.fma_rate(fp64=True)
+    nc, nn = m.num_cells, 4
+    nfree = V.num_free_dofs
+    ph = {k: v for k, v in phases}
+    # algorithmic bytes per launch of the phases (stated in the design doc)
+    alg = {
+        "elements": nc * (4 * 4 + 8) + m.num_nodes * 24 + nc * 16 * 8 + nc * 4 * 8,  # reads + Ke/be writes
+        "scatter": nc * 16 * 8 + nc * 4 * 4 + nfree * 8 + nnz * (4 + 8),               # Ke, inc, rowptr, colind+values
+    }
+    flops_el = nc * 130.0  # FP64 flops per P1 tetrahedron (geometry + 10 entries)
+    dom = max((k for k in ph if k in ("elements", "scatter", "pattern_count", "pattern_fill", "incidence")),
+              key=lambda k: ph[k])
+    if dom == "elements":
+        achieved = flops_el / (ph[dom] * 1e-3) / 1e12
+        roof = {"bound": "fp64", "kernel": "k_elements<P1 tet, Laplacian, FP64>", "achieved": achieved,
+                "peak": fp64_tf, "unit": "TFLOP/s", "frac": achieved / fp64_tf,
+                "peak_source": "measured FP64 FMA rate of this device (gt_ctx_fma_rate)", "traffic": None}
+    else:
+        bytes_dom = alg.get(dom, nnz * 12)
+        achieved = bytes_dom / (ph[dom] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks_kind, "traffic": None}
+    b_asm = nnz * 8 + nc * 4 * 4 + m.num_nodes * 24 + nc * 8
+    step_roof = {"algorithmic_bytes": b_asm, "GB/s": b_asm / (ms * 1e-3) / 1e9,
+                 "frac_of_hbm": b_asm / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}
+
+    # ---- e2e through the C ABI with host buffers
+    coords_h = torch.from_numpy(m.coords).pin_memory()
+    kappa_h = torch.from_numpy(kappa).pin_memory()
+    rp_h = torch.empty(nfree + 1, dtype=torch.int64).pin_memory()
+    ci_h = torch.empty(nnz, dtype=torch.int32).pin_memory()
+    v_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    b_h = torch.empty(nfree, dtype=torch.float64).pin_memory()
+    from gtgpu.api import _ptr
+    import ctypes as C
+    lib = ctx.lib
+    f_one = np.ones(1)
+    e2e_times = []
+    for it in range(args.warmup + max(3, args.steps // 2)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        V.dmesh.set_coords(coords_h)
+        h = C.c_void_p()
+        GT.api.check(ctx.h, lib.gt_assemble_matrix_and_vector(V.h, GT.api._lib.GT_LAPLACE, _ptr(kappa_h), 0.3,
+                                                              GT.api._lib.GT_FP64, _ptr(f_one), None,
+                                                              _ptr(b_h), C.byref(h)))
+        GT.api.check(ctx.h, lib.gt_matrix_download_csr(h, _ptr(rp_h), _ptr(ci_h), _ptr(v_h), None))
+        lib.gt_matrix_destroy(h)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            e2e_times.append(dt)
+    e2e_ms = 1e3 * sum(e2e_times) / len(e2e_times)
+    h2d = m.coords.nbytes + kappa.nbytes
+    d2h = rp_h.numel() * 8 + nnz * 4 + nnz * 8 + nfree * 8
+
+    # ---- solve: plain FP64 PCG vs FP64 refinement around FP32 PCG
+    solve = None
+    if not args.no_solve:
+        Am, bm = GT.assemble_matrix_and_vector(a, l, "mixed", V)
+        res = {}
+        xs = {}
+        for mode in ("fp64", "ir"):
+            lat = []
+            for r in range(3):
+                t0 = time.perf_counter()
+                x, info = GT.solve(Am, bm, rtol=1e-10, mode=mode)
+                lat.append(time.perf_counter() - t0)
+            xs[mode] = x
+            lat.sort()
+            res[mode] = {"solves_per_s": 1.0 / statistics.mean(lat), "p50_ms": 1e3 * lat[len(lat) // 2],
+                         "p99_ms": 1e3 * lat[-1], "iterations": info["iterations"],
+                         "outer": info["outer_iterations"], "rel_residual": info["rel_residual"]}
+        res["ir_vs_fp64_rel_err"] = float(np.abs(xs["ir"] - xs["fp64"]).max() / np.abs(xs["fp64"]).max())
+        res["rtol"] = 1e-10
+        solve = res
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        ncores = os.cpu_count()
+        cnnz, ctimes, used = cpu_assembly(m, kappa, reps=1, threads=ncores)
+        cpu = {"value": cnnz / min(ctimes), "unit": "nnz/s", "cores": used, "kind": "port",
+               "sample": "full workload, 1 repetition (C restatement of the reference, OpenMP)"}
+
+    line = {"metric": METRIC, "value": value, "unit": "nnz/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": wl_config(n, {"nnz": int(nnz), "free_dofs": int(nfree), "parallelism": f"replicas x{world}"}),
+            "e2e": {"value": world * nnz / (e2e_ms * 1e-3), "unit": "nnz/s", "ms_per_step": e2e_ms,
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "roofline": roof, "step_roofline": step_roof,
+            "phases_ms": {k: round(v, 4) for k, v in phases},
+            "cpu_baseline": cpu, "solve": solve, "clocks": clocks.summary(),
+            "gpu_launches": int(launches), "wall_s_timed": t_wall}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -7,6 +7,7 @@
 // 189-208, and the COO->CSC compress src/assembly.jl:571-575):
 //   1. incidence: block row (free node dof) -> sorted list of (cell, local
 //      node) that touch it  [k_inc_count, scan, k_inc_fill, k_inc_sort]
+//      (k_inc_sort: one warp per row, bitonic sort in shared memory)
 //   2. pattern: per block row, the sorted union of the free node dofs of its
 //      cells  [k_pattern<count>, scan, k_pattern<fill>]  == the reference's
 //      sorted, duplicate-free CSC (the forms are symmetric, CSR == CSC)
@@ -132,7 +133,7 @@ __global__ void k_tabulate(int ctype, int order, TabLayout L, double* tab) {
 static int get_tab(Ctx* ctx, int ctype, int order, double** tab, TabLayout* L) {
   *L = tab_layout(ctype, order);
   GT_TRY(dalloc(ctx, tab, L->total));
-  k_tabulate<<<1, 32, 0, ctx->stream>>>(ctype, order, *L, *tab);
+  k_tabulate<<<GT_KC(ctx, 1), 32, 0, ctx->stream>>>(ctype, order, *L, *tab);
   GT_LAUNCH(ctx, "k_tabulate");
   return GT_OK;
 }
@@ -155,80 +156,10 @@ __global__ void k_inc_fill(const int32_t* cnd, int64_t n, const int64_t* ptr, in
     }
   }
 }
-// sort each row's incidences ascending (= by cell); rows are short
-__global__ void k_inc_sort(const int64_t* ptr, int32_t* inc, int64_t nrows, int32_t* maxlen) {
-  int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (r >= nrows) return;
-  int64_t b = ptr[r], e = ptr[r + 1];
-  for (int64_t i = b + 1; i < e; i++) {
-    int32_t v = inc[i];
-    int64_t j = i - 1;
-    while (j >= b && inc[j] > v) { inc[j + 1] = inc[j]; j--; }
-    inc[j + 1] = v;
-  }
-  atomicMax(maxlen, (int32_t)(e - b));
-}
-
-int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc) {
-  cudaStream_t st = ctx->stream;
-  int64_t nrows = sp->nfree_nodes, n = sp->mesh->ncells * sp->nn;
-  int32_t *cnt = nullptr, *cursor = nullptr, *dmax = nullptr;
-  GT_TRY(dalloc(ctx, &cnt, nrows + 1));
-  GT_TRY(dalloc(ctx, &cursor, nrows + 1));
-  GT_TRY(dalloc(ctx, &dmax, 1));
-  GT_TRY(dalloc(ctx, inc_ptr, nrows + 1));
-  GT_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), st));
-  GT_CUDA(ctx, cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (nrows + 1), st));
-  GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
-  k_inc_count<<<grid_for(n, 256), 256, 0, st>>>(sp->cell_ndofs, n, cnt);
-  GT_LAUNCH(ctx, "k_inc_count");
-  GT_TRY(exclusive_scan_i64(ctx, cnt, *inc_ptr, nrows));
-  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], *inc_ptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  GT_CUDA(ctx, cudaStreamSynchronize(st));
-  *ninc = ctx->h_scratch[0];
-  GT_TRY(dalloc(ctx, inc, *ninc));
-  k_inc_fill<<<grid_for(n, 256), 256, 0, st>>>(sp->cell_ndofs, n, *inc_ptr, cursor, *inc);
-  k_inc_sort<<<grid_for(nrows, 128), 128, 0, st>>>(*inc_ptr, *inc, nrows, dmax);
-  GT_LAUNCH(ctx, "k_inc_fill/sort");
-  dfree(ctx, cnt);
-  dfree(ctx, cursor);
-  dfree(ctx, dmax);
-  return GT_OK;
-}
-
-// ---------------------------------------------------------------------------
-// 2. pattern: one warp per block row, bitonic sort of the candidate columns
-// in shared memory, duplicates dropped
-// ---------------------------------------------------------------------------
-template <bool FILL>
-__global__ void k_pattern(const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
-                          const int32_t* __restrict__ cnd, int nn, int64_t nrows, int cap, int32_t* __restrict__ rowcnt,
-                          const int64_t* __restrict__ rowptr, int32_t* __restrict__ colind, uint32_t* err) {
-  extern __shared__ int32_t s_buf[];
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int32_t* buf = s_buf + w * cap;
-  int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
-  if (r >= nrows) return;
-  int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
-  int ncand = (int)(ie - ib) * nn;
-  if (ncand > cap) {
-    if (lane == 0) { atomicOr(err, DEV_ERR_ROW_CAP); if (!FILL) rowcnt[r] = 0; }
-    return;
-  }
-  int P = 32;
-  while (P < ncand) P <<= 1;
-  for (int i = lane; i < P; i += 32) {
-    int32_t v = INT_MAX;
-    if (i < ncand) {
-      int k = i / nn, b = i - k * nn;
-      int32_t cb = inc[ib + k];
-      int32_t c = cb / nn;
-      int32_t d = cnd[(int64_t)c * nn + b];
-      v = d > 0 ? d - 1 : INT_MAX;
-    }
-    buf[i] = v;
-  }
-  __syncwarp();
+// sort each row's incidences ascending (= by cell): one warp per row,
+// bitonic sort in shared memory (icap slots per warp)
+// ascending bitonic sort of buf[0..P) (P a power of two >= 32) by one warp
+__device__ __forceinline__ void warp_bitonic_sort(int32_t* buf, int P, int lane) {
   for (int k = 2; k <= P; k <<= 1) {
     for (int j = k >> 1; j > 0; j >>= 1) {
       for (int i = lane; i < P; i += 32) {
@@ -242,6 +173,101 @@ __global__ void k_pattern(const int64_t* __restrict__ inc_ptr, const int32_t* __
       __syncwarp();
     }
   }
+}
+
+__global__ void k_inc_sort(const int64_t* __restrict__ ptr, int32_t* __restrict__ inc, int64_t nrows, int icap) {
+  extern __shared__ int32_t s_ibuf[];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t* buf = s_ibuf + w * icap;
+  int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
+  if (r >= nrows) return;
+  int64_t b = ptr[r];
+  int n = (int)(ptr[r + 1] - b);
+  int P = 32;
+  while (P < n) P <<= 1;
+  for (int i = lane; i < P; i += 32) buf[i] = i < n ? inc[b + i] : INT_MAX;
+  __syncwarp();
+  warp_bitonic_sort(buf, P, lane);
+  for (int i = lane; i < n; i += 32) inc[b + i] = buf[i];
+}
+
+static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out);
+
+int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc) {
+  cudaStream_t st = ctx->stream;
+  int64_t nrows = sp->nfree_nodes, n = sp->mesh->ncells * sp->nn;
+  int32_t *cnt = nullptr, *cursor = nullptr, *dmax = nullptr;
+  GT_TRY(dalloc(ctx, &cnt, nrows + 1));
+  GT_TRY(dalloc(ctx, &cursor, nrows + 1));
+  GT_TRY(dalloc(ctx, &dmax, 1));
+  GT_TRY(dalloc(ctx, inc_ptr, nrows + 1));
+  GT_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), st));
+  GT_CUDA(ctx, cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (nrows + 1), st));
+  GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
+  k_inc_count<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, cnt);
+  GT_LAUNCH(ctx, "k_inc_count");
+  GT_TRY(exclusive_scan_i64(ctx, cnt, *inc_ptr, nrows));
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], *inc_ptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GT_CUDA(ctx, cudaStreamSynchronize(st));
+  *ninc = ctx->h_scratch[0];
+  GT_TRY(dalloc(ctx, inc, *ninc));
+  k_inc_fill<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, *inc_ptr, cursor, *inc);
+  GT_LAUNCH(ctx, "k_inc_fill");
+  int32_t maxinc = 0;
+  GT_TRY(max_diff(ctx, *inc_ptr, nrows, &maxinc));
+  int icap = 32;
+  while (icap < maxinc) icap <<= 1;
+  if (icap > 4096) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells");
+  int warps = 8;
+  size_t smem = (size_t)warps * icap * sizeof(int32_t);
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_inc_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (nrows > 0)
+    k_inc_sort<<<GT_KC(ctx, grid_for(nrows, warps)), warps * 32, smem, st>>>(*inc_ptr, *inc, nrows, icap);
+  GT_LAUNCH(ctx, "k_inc_sort");
+  dfree(ctx, cnt);
+  dfree(ctx, cursor);
+  dfree(ctx, dmax);
+  return GT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// 2. pattern: one warp per block row, bitonic sort of the candidate columns
+// in shared memory, duplicates dropped
+// ---------------------------------------------------------------------------
+template <bool FILL>
+__global__ void k_pattern(const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                          const int32_t* __restrict__ cnd, int nn, int64_t nrows, int cap, int icap,
+                          int32_t* __restrict__ rowcnt, const int64_t* __restrict__ rowptr,
+                          int32_t* __restrict__ colind, uint32_t* err) {
+  extern __shared__ int32_t s_buf[];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t* buf = s_buf + w * (cap + icap);  // candidate columns
+  int32_t* ibuf = buf + cap;                // the row's incidences
+  int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
+  if (r >= nrows) return;
+  int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+  int ninc = (int)(ie - ib);
+  int ncand = ninc * nn;
+  if (ncand > cap || ninc > icap) {
+    if (lane == 0) { atomicOr(err, DEV_ERR_ROW_CAP); if (!FILL) rowcnt[r] = 0; }
+    return;
+  }
+  for (int i = lane; i < ninc; i += 32) ibuf[i] = inc[ib + i];
+  __syncwarp();
+  int P = 32;
+  while (P < ncand) P <<= 1;
+  for (int i = lane; i < P; i += 32) {
+    int32_t v = INT_MAX;
+    if (i < ncand) {
+      int k = i / nn, b = i - k * nn;
+      int32_t c = ibuf[k] / nn;
+      int32_t d = cnd[(int64_t)c * nn + b];
+      v = d > 0 ? d - 1 : INT_MAX;
+    }
+    buf[i] = v;
+  }
+  __syncwarp();
+  warp_bitonic_sort(buf, P, lane);
   int count = 0;
   for (int base = 0; base < P; base += 32) {
     int i = base + lane;
@@ -266,7 +292,7 @@ static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out) {
   int32_t* d = nullptr;
   GT_TRY(dalloc(ctx, &d, 1));
   GT_CUDA(ctx, cudaMemsetAsync(d, 0, sizeof(int32_t), ctx->stream));
-  if (n > 0) k_max_diff<<<grid_for(n, 256), 256, 0, ctx->stream>>>(ptr, n, d);
+  if (n > 0) k_max_diff<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, ctx->stream>>>(ptr, n, d);
   GT_LAUNCH(ctx, "k_max_diff");
   GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[8], d, sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
   GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -283,11 +309,12 @@ int build_pattern(Matrix* A) {
   A->nbrows = nrows;
   int32_t maxinc = 0;
   GT_TRY(max_diff(ctx, A->inc_ptr, nrows, &maxinc));
-  int cap = 32;
+  int cap = 32, icap = 32;
   while (cap < maxinc * sp->nn) cap <<= 1;
+  while (icap < maxinc) icap <<= 1;
   if (cap > 4096) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells for the sparsity kernel");
   int warps = cap >= 2048 ? 2 : (cap >= 1024 ? 4 : 8);
-  size_t smem = (size_t)warps * cap * sizeof(int32_t);
+  size_t smem = (size_t)warps * (cap + icap) * sizeof(int32_t);
   if (smem > 48 * 1024) {
     cudaFuncSetAttribute(k_pattern<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_pattern<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -296,19 +323,21 @@ int build_pattern(Matrix* A) {
   GT_TRY(dalloc(ctx, &rowcnt, nrows + 1));
   GT_TRY(dalloc(ctx, &A->rowptr, nrows + 1));
   int grid = grid_for(nrows, warps);
-  k_pattern<false><<<grid, warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, sp->nn, nrows, cap, rowcnt,
-                                                  nullptr, nullptr, ctx->d_err);
+  k_pattern<false><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, sp->nn, nrows, cap, icap,
+                                                                rowcnt, nullptr, nullptr, ctx->d_err);
   GT_LAUNCH(ctx, "k_pattern<count>");
   GT_TRY(exclusive_scan_i64(ctx, rowcnt, A->rowptr, nrows));
+  mark(ctx, "pattern_count");
   GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], A->rowptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   uint32_t bits = 0;
   GT_TRY(take_device_error(ctx, &bits));  // synchronises
   if (bits) return set_error(ctx, GT_ERR_INVALID, "sparsity: row capacity exceeded");
   A->bnnz = ctx->h_scratch[0];
   GT_TRY(dalloc(ctx, &A->colind, A->bnnz));
-  k_pattern<true><<<grid, warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, sp->nn, nrows, cap, nullptr,
-                                                 A->rowptr, A->colind, ctx->d_err);
+  k_pattern<true><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, sp->nn, nrows, cap, icap,
+                                                               nullptr, A->rowptr, A->colind, ctx->d_err);
   GT_LAUNCH(ctx, "k_pattern<fill>");
+  mark(ctx, "pattern_fill");
   dfree(ctx, rowcnt);
   int32_t mr = 0;
   GT_TRY(max_diff(ctx, A->rowptr, nrows, &mr));
@@ -505,7 +534,7 @@ static int launch_elements(const Space* sp, const double* coef, double nu, const
   Ctx* ctx = sp->mesh->ctx;
   int64_t nc = sp->mesh->ncells;
   int64_t grid = (nc + CPB - 1) / CPB;
-  k_elements<D, NLV, NN, NQ, BS, FORM, T, CPB, AFFINE><<<(unsigned)grid, 128, 0, ctx->stream>>>(
+  k_elements<D, NLV, NN, NQ, BS, FORM, T, CPB, AFFINE><<<GT_KC(ctx, (unsigned)grid), 128, 0, ctx->stream>>>(
       sp->mesh->coords, sp->mesh->cell_nodes, coef, nu, tab, L, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
   GT_LAUNCH(ctx, "k_elements");
   return GT_OK;
@@ -649,7 +678,7 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32) {
     cudaFuncSetAttribute(k_scatter<BS, G, TK, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int64_t rows_per_block = (int64_t)warps * RPW;
     int64_t grid = (A->nbrows + rows_per_block - 1) / rows_per_block;
-    k_scatter<BS, G, TK, TA><<<(unsigned)(grid > 0 ? grid : 1), warps * 32, smem, ctx->stream>>>(
+    k_scatter<BS, G, TK, TA><<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
         A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, A->nbrows, lmax, Ke, v64, v32);
     GT_LAUNCH(ctx, "k_scatter");
     return GT_OK;
@@ -696,7 +725,7 @@ __global__ void k_scatter_vec(const int64_t* __restrict__ inc_ptr, const int32_t
 int scatter_vector(const Space* sp, const int64_t* inc_ptr, const int32_t* inc, const double* be, double* b) {
   Ctx* ctx = ctx_of(sp);
   int64_t n = sp->nfree_nodes * sp->ncomp;
-  k_scatter_vec<<<grid_for(n, 256), 256, 0, ctx->stream>>>(inc_ptr, inc, sp->nn, sp->ncomp, sp->nfree_nodes, be, b);
+  k_scatter_vec<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, ctx->stream>>>(inc_ptr, inc, sp->nn, sp->ncomp, sp->nfree_nodes, be, b);
   GT_LAUNCH(ctx, "k_scatter_vec");
   return GT_OK;
 }
@@ -721,7 +750,7 @@ int find_diag(Matrix* A) {
   Ctx* ctx = ctx_of(A->space);
   if (A->diag_pos) return GT_OK;
   GT_TRY(dalloc(ctx, &A->diag_pos, A->nbrows + 1));
-  k_find_diag<<<grid_for(A->nbrows, 256), 256, 0, ctx->stream>>>(A->rowptr, A->colind, A->nbrows, A->diag_pos, ctx->d_err);
+  k_find_diag<<<GT_KC(ctx, grid_for(A->nbrows, 256)), 256, 0, ctx->stream>>>(A->rowptr, A->colind, A->nbrows, A->diag_pos, ctx->d_err);
   GT_LAUNCH(ctx, "k_find_diag");
   return GT_OK;
 }
@@ -818,14 +847,17 @@ static int numeric(Matrix* A, int form, const double* coef_in, double nu, const 
   GT_TRY(dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz)));
   if (b_out) GT_TRY(dalloc(ctx, &be, nc * sp->nloc));
   int s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
+  mark(ctx, "elements");
   if (s == GT_OK) s = alloc_values(A);
   if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision);
+  mark(ctx, "scatter");
   if (s == GT_OK && b_out) {
     bool dev = is_device_ptr(b_out);
     double* bd = b_out;
     int64_t nb = sp->nfree_nodes * sp->ncomp;
     if (!dev) s = dalloc(ctx, &bd, nb);
     if (s == GT_OK) s = scatter_vector(sp, A->inc_ptr, A->inc, be, bd);
+    mark(ctx, "scatter_vector");
     if (s == GT_OK && !dev) {
       s = copy_out(ctx, b_out, bd, nb);
       if (s == GT_OK) {
@@ -853,7 +885,7 @@ static int device_status(Ctx* ctx, const char* where) {
 using namespace gt;
 
 static void matrix_release(gt_matrix* A) {
-  Ctx* c = A->space->mesh->ctx;
+  Ctx* c = A->ctx;
   dfree(c, A->rowptr);
   dfree(c, A->colind);
   dfree(c, A->val64);
@@ -879,10 +911,13 @@ int gt_assemble_matrix_and_vector(gt_space* sp, int form, const double* cell_coe
   if (b && !f) return set_error(ctx, GT_ERR_INVALID, "vector assembly needs a source f");
   cudaSetDevice(ctx->device);
   gt_matrix* A = new gt_matrix();
+  A->ctx = ctx;
   A->space = sp;
   A->bs = sp->ncomp;
   A->precision = precision;
+  mark(ctx, "setup");
   int s = build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc);
+  mark(ctx, "incidence");
   if (s == GT_OK) s = build_pattern(A);
   if (s == GT_OK) s = numeric(A, form, cell_coef, nu, f, source_coef, b);
   if (s == GT_OK) s = device_status(ctx, "assemble_matrix");
@@ -970,7 +1005,7 @@ int gt_matrix_download_csr(gt_matrix* A, int64_t* rowptr, int32_t* colind, doubl
     if (rowptr) {
       s = dalloc(ctx, &rp, n + 1);
       if (s == GT_OK) {
-        k_expand_rowptr<<<grid_for(n + 1, 256), 256, 0, ctx->stream>>>(A->rowptr, A->nbrows, bs, rp);
+        k_expand_rowptr<<<GT_KC(ctx, grid_for(n + 1, 256)), 256, 0, ctx->stream>>>(A->rowptr, A->nbrows, bs, rp);
         s = copy_out(ctx, rowptr, rp, n + 1);
       }
     }
@@ -978,7 +1013,7 @@ int gt_matrix_download_csr(gt_matrix* A, int64_t* rowptr, int32_t* colind, doubl
       if (colind) s = dalloc(ctx, &ci, nnz);
       if (s == GT_OK && v64 && A->val64) s = dalloc(ctx, &d64, nnz);
       if (s == GT_OK) {
-        k_expand_entries<double><<<(unsigned)A->nbrows, 128, 0, ctx->stream>>>(A->rowptr, A->colind, A->val64, A->nbrows,
+        k_expand_entries<double><<<GT_KC(ctx, (unsigned)A->nbrows), 128, 0, ctx->stream>>>(A->rowptr, A->colind, A->val64, A->nbrows,
                                                                              bs, ci, d64);
         if (colind) s = copy_out(ctx, colind, ci, nnz);
         if (s == GT_OK && d64) s = copy_out(ctx, v64, d64, nnz);
@@ -987,7 +1022,7 @@ int gt_matrix_download_csr(gt_matrix* A, int64_t* rowptr, int32_t* colind, doubl
     if (s == GT_OK && v32 && A->val32) {
       s = dalloc(ctx, &d32, nnz);
       if (s == GT_OK) {
-        k_expand_entries<float><<<(unsigned)A->nbrows, 128, 0, ctx->stream>>>(A->rowptr, A->colind, A->val32, A->nbrows,
+        k_expand_entries<float><<<GT_KC(ctx, (unsigned)A->nbrows), 128, 0, ctx->stream>>>(A->rowptr, A->colind, A->val32, A->nbrows,
                                                                             bs, nullptr, d32);
         s = copy_out(ctx, v32, d32, nnz);
       }

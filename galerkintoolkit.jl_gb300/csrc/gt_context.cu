@@ -73,6 +73,20 @@ void pool_trim(Ctx* ctx) {
   ctx->pooled_bytes = 0;
 }
 
+void mark(Ctx* ctx, const char* name) {
+  if (!ctx->prof) return;
+  cudaEvent_t e;
+  if (!ctx->spare_events.empty()) {
+    e = ctx->spare_events.back();
+    ctx->spare_events.pop_back();
+  } else if (cudaEventCreate(&e) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  cudaEventRecord(e, ctx->stream);
+  ctx->marks.emplace_back(name, e);
+}
+
 int take_device_error(Ctx* ctx, uint32_t* bits) {
   GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -149,7 +163,7 @@ static int scan_impl(Ctx* ctx, const Tin* in, Tout* out, int64_t n) {
   }
   int64_t nb = (n + SCAN_B - 1) / SCAN_B;
   if (nb == 1) {
-    k_block_scan<Tin, Tout><<<1, SCAN_T, 0, ctx->stream>>>(in, out, nullptr, n);
+    k_block_scan<Tin, Tout><<<GT_KC(ctx, 1), SCAN_T, 0, ctx->stream>>>(in, out, nullptr, n);
     GT_LAUNCH(ctx, "k_block_scan");
     return GT_OK;
   }
@@ -157,11 +171,11 @@ static int scan_impl(Ctx* ctx, const Tin* in, Tout* out, int64_t n) {
   Tout* soff = nullptr;
   GT_TRY(dalloc(ctx, &sums, nb));
   GT_TRY(dalloc(ctx, &soff, nb + 1));
-  k_block_sums<Tin, Tout><<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(in, sums, n);
+  k_block_sums<Tin, Tout><<<GT_KC(ctx, (unsigned)nb), SCAN_T, 0, ctx->stream>>>(in, sums, n);
   GT_LAUNCH(ctx, "k_block_sums");
   int s = scan_impl<Tout, Tout>(ctx, sums, soff, nb);
   if (s == GT_OK) {
-    k_block_scan<Tin, Tout><<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(in, out, soff, n);
+    k_block_scan<Tin, Tout><<<GT_KC(ctx, (unsigned)nb), SCAN_T, 0, ctx->stream>>>(in, out, soff, n);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) s = check_cuda(ctx, e, "k_block_scan");
   }
@@ -175,6 +189,42 @@ int exclusive_scan_i64(Ctx* ctx, const int32_t* in, int64_t* out, int64_t n) {
 }
 int exclusive_scan_i32(Ctx* ctx, const int32_t* in, int32_t* out, int64_t n) {
   return scan_impl<int32_t, int32_t>(ctx, in, out, n);
+}
+
+// FMA throughput probe: 8 independent FMA chains per thread, a full wave of
+// CTAs on every SM; used to state the FP32/FP64 pipe roofline of the
+// integration kernels on the running device.
+template <class T>
+__global__ void k_fma_rate(T* out, int iters, T a, T b) {
+  T x0 = (T)threadIdx.x, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; i++) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b); x3 = fma(x3, a, b);
+    x4 = fma(x4, a, b); x5 = fma(x5, a, b); x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+template <class T>
+static int fma_rate(Ctx* ctx, int iters, double* tflops) {
+  int blocks = ctx->num_sms * 8, threads = 256;
+  T* out = nullptr;
+  GT_TRY(dalloc(ctx, &out, (int64_t)blocks * threads));
+  cudaEvent_t e0, e1;
+  GT_CUDA(ctx, cudaEventCreate(&e0));
+  GT_CUDA(ctx, cudaEventCreate(&e1));
+  k_fma_rate<T><<<GT_KC(ctx, blocks), threads, 0, ctx->stream>>>(out, iters / 4, (T)0.999, (T)0.001);
+  cudaEventRecord(e0, ctx->stream);
+  k_fma_rate<T><<<GT_KC(ctx, blocks), threads, 0, ctx->stream>>>(out, iters, (T)0.999, (T)0.001);
+  cudaEventRecord(e1, ctx->stream);
+  cudaError_t e = cudaEventSynchronize(e1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  dfree(ctx, out);
+  if (e != cudaSuccess) return check_cuda(ctx, e, "k_fma_rate");
+  *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3) / 1e12;
+  return GT_OK;
 }
 
 }  // namespace gt
@@ -222,6 +272,8 @@ int gt_ctx_destroy(gt_ctx* c) {
   cudaFreeHost(c->h_err);
   cudaFreeHost(c->h_scratch);
   cudaFreeHost(c->h_dscratch);
+  for (auto& m : c->marks) cudaEventDestroy(m.second);
+  for (auto e : c->spare_events) cudaEventDestroy(e);
   cudaStreamDestroy(c->own_stream);
   delete c;
   return GT_OK;
@@ -238,6 +290,48 @@ int gt_ctx_synchronize(gt_ctx* c) {
 int gt_ctx_set_stream(gt_ctx* c, void* stream) {
   if (!c) return GT_ERR_INVALID;
   c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  return GT_OK;
+}
+
+int gt_ctx_fma_rate(gt_ctx* c, int precision, double* tflops) {
+  if (!c || !tflops) return GT_ERR_INVALID;
+  cudaSetDevice(c->device);
+  if (precision == GT_FP64) return fma_rate<double>(c, 1 << 11, tflops);
+  if (precision == GT_FP32) return fma_rate<float>(c, 1 << 14, tflops);
+  return set_error(c, GT_ERR_INVALID, "precision must be GT_FP64 or GT_FP32");
+}
+
+int gt_ctx_launch_count(gt_ctx* c, int64_t* launches) {
+  if (!c || !launches) return GT_ERR_INVALID;
+  *launches = c->launches;
+  return GT_OK;
+}
+
+int gt_ctx_profile_begin(gt_ctx* c) {
+  if (!c) return GT_ERR_INVALID;
+  for (auto& m : c->marks) c->spare_events.push_back(m.second);
+  c->marks.clear();
+  c->prof = true;
+  mark(c, "begin");
+  return GT_OK;
+}
+
+int gt_ctx_profile_end(gt_ctx* c, int max, char* names, double* ms, int* count) {
+  if (!c || !count) return GT_ERR_INVALID;
+  mark(c, "end");
+  c->prof = false;
+  GT_CUDA(c, cudaStreamSynchronize(c->stream));
+  int n = 0;
+  for (size_t i = 1; i < c->marks.size() && n < max; i++, n++) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, c->marks[i - 1].second, c->marks[i].second);
+    if (ms) ms[n] = t;
+    if (names) {
+      strncpy(names + 32 * n, c->marks[i].first.c_str(), 31);
+      names[32 * n + 31] = 0;
+    }
+  }
+  *count = n;
   return GT_OK;
 }
 

@@ -77,7 +77,18 @@ struct Ctx {
   uint32_t* h_err = nullptr;       // pinned mirror
   int64_t* h_scratch = nullptr;    // pinned small readbacks (64 words)
   double* h_dscratch = nullptr;    // pinned small FP64 readbacks (64 words)
+  int64_t launches = 0;            // kernels launched by this context
+  // phase profiling: CUDA events recorded on the stream between phases
+  bool prof = false;
+  std::vector<std::pair<std::string, cudaEvent_t>> marks;
+  std::vector<cudaEvent_t> spare_events;
 };
+
+// counts a kernel launch; used as the grid argument: k<<<GT_KC(ctx, g), ...>>>
+#define GT_KC(ctx, g) ((ctx)->launches++, (g))
+
+// records a named phase boundary when profiling is on
+void mark(Ctx* ctx, const char* name);
 
 void* pool_alloc(Ctx* ctx, size_t bytes);
 void pool_free(Ctx* ctx, void* p);
@@ -137,6 +148,7 @@ struct Mesh {
 };
 
 struct Space {
+  Ctx* ctx = nullptr;  // owning context (also reachable as mesh->ctx while the mesh lives)
   Mesh* mesh = nullptr;
   int order = 1, ncomp = 1, nn = 0, nloc = 0;
   int64_t nfree_nodes = 0, ndiri_nodes = 0;
@@ -148,6 +160,7 @@ struct Space {
 };
 
 struct Matrix {
+  Ctx* ctx = nullptr;  // owning context
   Space* space = nullptr;
   int bs = 1, precision = GT_FP64;
   int64_t nbrows = 0, bnnz = 0;

@@ -34,7 +34,8 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// CTA sum into partials[blockIdx.x]; returns true in thread 0 of the last CTA
+// CTA sum into partials[blockIdx.x]; returns (in every thread of the CTA)
+// whether this CTA finished last
 __device__ bool cta_partial(double v, double* partials, uint32_t* counter) {
   __shared__ double red[RED_T / 32];
   __shared__ bool last;
@@ -52,15 +53,26 @@ __device__ bool cta_partial(double v, double* partials, uint32_t* counter) {
   __syncthreads();
   return last;
 }
-__device__ double sum_partials(const double* partials, int n) {
-  // fixed order, executed by one thread
+// Sum of n partials by the whole CTA in a fixed order (strided per-thread
+// sums, then a fixed tree); every thread gets the total.
+__device__ double block_sum_partials(const double* partials, int n) {
+  __shared__ double tree[RED_T];
   double t = 0.0;
-  for (int i = 0; i < n; i++) t += ((volatile const double*)partials)[i];
-  return t;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) t += ((volatile const double*)partials)[i];
+  tree[threadIdx.x] = t;
+  __syncthreads();
+  for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) tree[threadIdx.x] += tree[threadIdx.x + o];
+    __syncthreads();
+  }
+  double r = tree[0];
+  __syncthreads();
+  return r;
 }
 
 // ---------------------------------------------------------------------------
-// SpMV: G lanes per block row
+// SpMV: G lanes per block row, grid-stride over rows (fixed grid, so the
+// partial sums are always formed over the same row sets)
 // ---------------------------------------------------------------------------
 template <int BS, int G, class V, class X>
 __device__ __forceinline__ void row_product(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
@@ -88,20 +100,25 @@ __device__ __forceinline__ void row_product(const int64_t* __restrict__ rowptr, 
   }
 }
 
-// y = A x   (optionally y = b - A x)
+// y = A x   (or y = bsub - A x)
 template <int BS, int G, class V, class X>
 __global__ void __launch_bounds__(RED_T) k_spmv(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                                                 const V* __restrict__ val, const X* __restrict__ x, int64_t nrows,
                                                 const X* __restrict__ bsub, X* __restrict__ y) {
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int64_t r = t / G;
-  int gl = (int)(t - r * G);
-  if (r >= nrows) r = nrows - 1;  // keep the whole group in the shuffles
-  X o[BS];
-  row_product<BS, G, V, X>(rowptr, colind, val, x, r, gl, o);
-  if (gl == 0 && t / G < nrows)
+  int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int gl = (int)(t0 % G);
+  int64_t stride = ((int64_t)gridDim.x * blockDim.x) / G;
+  int64_t nit = (nrows + stride - 1) / stride;  // uniform trip count keeps whole groups in the shuffles
+  for (int64_t it = 0; it < nit; it++) {
+    int64_t r = t0 / G + it * stride;
+    bool valid = r < nrows;
+    int64_t rr = valid ? r : nrows - 1;
+    X o[BS];
+    row_product<BS, G, V, X>(rowptr, colind, val, x, rr, gl, o);
+    if (gl == 0 && valid)
 #pragma unroll
-    for (int c = 0; c < BS; c++) y[r * BS + c] = bsub ? bsub[r * BS + c] - o[c] : o[c];
+      for (int c = 0; c < BS; c++) y[r * BS + c] = bsub ? bsub[r * BS + c] - o[c] : o[c];
+  }
 }
 
 // q = A p, partial p.q -> alpha = rz / pq in the last CTA
@@ -110,25 +127,31 @@ __global__ void __launch_bounds__(RED_T) k_cg_spmv(const int64_t* __restrict__ r
                                                    const V* __restrict__ val, const X* __restrict__ p, X* __restrict__ q,
                                                    int64_t nrows, CGState* st, double* partials) {
   if (st->done) return;
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int64_t r = t / G;
-  int gl = (int)(t - r * G);
-  bool valid = r < nrows;
-  if (!valid) r = nrows - 1;
-  X o[BS];
-  row_product<BS, G, V, X>(rowptr, colind, val, p, r, gl, o);
+  int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int gl = (int)(t0 % G);
+  int64_t stride = ((int64_t)gridDim.x * blockDim.x) / G;
+  int64_t nit = (nrows + stride - 1) / stride;
   double d = 0.0;
-  if (gl == 0 && valid) {
+  for (int64_t it = 0; it < nit; it++) {
+    int64_t r = t0 / G + it * stride;
+    bool valid = r < nrows;
+    int64_t rr = valid ? r : nrows - 1;
+    X o[BS];
+    row_product<BS, G, V, X>(rowptr, colind, val, p, rr, gl, o);
+    if (gl == 0 && valid) {
 #pragma unroll
-    for (int c = 0; c < BS; c++) {
-      q[r * BS + c] = o[c];
-      d += (double)o[c] * (double)p[r * BS + c];
+      for (int c = 0; c < BS; c++) {
+        q[r * BS + c] = o[c];
+        d += (double)o[c] * (double)p[r * BS + c];
+      }
     }
   }
   if (cta_partial(d, partials, &st->counter[0])) {
-    double pq = sum_partials(partials, gridDim.x);
-    st->pq = pq;
-    st->alpha = st->rz / pq;
+    double pq = block_sum_partials(partials, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->pq = pq;
+      st->alpha = st->rz / pq;
+    }
   }
 }
 
@@ -161,13 +184,15 @@ __global__ void __launch_bounds__(RED_T) k_cg_update(X* __restrict__ x, X* __res
     partials[gridDim.x + blockIdx.x] = t;
   }
   if (cta_partial(rz, partials, &st->counter[1])) {
-    double rzn = sum_partials(partials, gridDim.x);
-    double rrn = sum_partials(partials + gridDim.x, gridDim.x);
-    st->beta = rzn / st->rz;
-    st->rz = rzn;
-    st->rr = rrn;
-    st->iters += 1;
-    if (rrn <= st->tol2 || st->iters >= st->maxit || !(rrn == rrn)) st->done = 1;
+    double rzn = block_sum_partials(partials, gridDim.x);
+    double rrn = block_sum_partials(partials + gridDim.x, gridDim.x);
+    if (threadIdx.x == 0) {
+      st->beta = rzn / st->rz;
+      st->rz = rzn;
+      st->rr = rrn;
+      st->iters += 1;
+      if (rrn <= st->tol2 || st->iters >= st->maxit || !(rrn == rrn)) st->done = 1;
+    }
   }
 }
 
@@ -214,8 +239,9 @@ __global__ void __launch_bounds__(RED_T) k_cg_init(const X* __restrict__ r, X* _
     partials[gridDim.x + blockIdx.x] = t;
   }
   if (cta_partial(rz, partials, &st->counter[2])) {
-    double rzs = sum_partials(partials, gridDim.x);
-    double rrs = sum_partials(partials + gridDim.x, gridDim.x);
+    double rzs = block_sum_partials(partials, gridDim.x);
+    double rrs = block_sum_partials(partials + gridDim.x, gridDim.x);
+    if (threadIdx.x != 0) return;
     st->rz = rzs;
     st->rr = rrs;
     double ref = bb_dev ? *bb_dev : rrs;
@@ -234,7 +260,10 @@ __global__ void __launch_bounds__(RED_T) k_norm2(const X* __restrict__ v, int64_
   double s = 0.0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     s += (double)v[i] * (double)v[i];
-  if (cta_partial(s, partials, counter)) *out = sum_partials(partials, gridDim.x);
+  if (cta_partial(s, partials, counter)) {
+    double t = block_sum_partials(partials, gridDim.x);
+    if (threadIdx.x == 0) *out = t;
+  }
 }
 
 // mixed precision helpers
@@ -261,15 +290,28 @@ static int pick_group(const Matrix* A) {
   return 32;
 }
 
+static unsigned spmv_grid(Ctx* ctx, const Matrix* A) {
+  int G = pick_group(A);
+  int64_t g = (A->nbrows * G + RED_T - 1) / RED_T;
+  int64_t cap = (int64_t)ctx->num_sms * 8;
+  if (g > cap) g = cap;
+  return (unsigned)(g > 0 ? g : 1);
+}
+static unsigned vec_grid(Ctx* ctx, int64_t n) {
+  int64_t g = (n + RED_T - 1) / RED_T;
+  int64_t cap = (int64_t)ctx->num_sms * 8;
+  if (g > cap) g = cap;
+  return (unsigned)(g > 0 ? g : 1);
+}
+
 template <class V, class X>
 struct Ops {
   static int spmv(Ctx* ctx, const Matrix* A, const V* val, const X* x, const X* bsub, X* y) {
     int G = pick_group(A);
-    int64_t threads = A->nbrows * G;
-    unsigned grid = (unsigned)((threads + RED_T - 1) / RED_T);
+    unsigned grid = spmv_grid(ctx, A);
     auto go = [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
-      k_spmv<BS, GG, V, X><<<grid, RED_T, 0, ctx->stream>>>(A->rowptr, A->colind, val, x, A->nbrows, bsub, y);
+      k_spmv<BS, GG, V, X><<<GT_KC(ctx, grid), RED_T, 0, ctx->stream>>>(A->rowptr, A->colind, val, x, A->nbrows, bsub, y);
     };
     dispatch(A->bs, G, go);
     GT_LAUNCH(ctx, "k_spmv");
@@ -277,11 +319,10 @@ struct Ops {
   }
   static int cg_spmv(Ctx* ctx, const Matrix* A, const V* val, const X* p, X* q, CGState* st, double* partials) {
     int G = pick_group(A);
-    int64_t threads = A->nbrows * G;
-    unsigned grid = (unsigned)((threads + RED_T - 1) / RED_T);
+    unsigned grid = spmv_grid(ctx, A);
     auto go = [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
-      k_cg_spmv<BS, GG, V, X><<<grid, RED_T, 0, ctx->stream>>>(A->rowptr, A->colind, val, p, q, A->nbrows, st, partials);
+      k_cg_spmv<BS, GG, V, X><<<GT_KC(ctx, grid), RED_T, 0, ctx->stream>>>(A->rowptr, A->colind, val, p, q, A->nbrows, st, partials);
     };
     dispatch(A->bs, G, go);
     GT_LAUNCH(ctx, "k_cg_spmv");
@@ -308,17 +349,6 @@ struct Ops {
   }
 };
 
-static unsigned spmv_grid(const Matrix* A) {
-  int G = pick_group(A);
-  return (unsigned)((A->nbrows * G + RED_T - 1) / RED_T);
-}
-static unsigned vec_grid(Ctx* ctx, int64_t n) {
-  int64_t g = (n + RED_T - 1) / RED_T;
-  int64_t cap = (int64_t)ctx->num_sms * 8;
-  if (g > cap) g = cap;
-  return (unsigned)(g > 0 ? g : 1);
-}
-
 // PCG on A (values val) for A x = b; x holds the start value.  Vectors in X.
 template <class V, class X>
 static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit, const double* bb_dev,
@@ -329,7 +359,7 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
   X *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
   CGState* st = nullptr;
   double* partials = nullptr;
-  unsigned gs = spmv_grid(A), gv = vec_grid(ctx, n);
+  unsigned gs = spmv_grid(ctx, A), gv = vec_grid(ctx, n);
   unsigned gmax = gs > gv ? gs : gv;
   GT_TRY(dalloc(ctx, &r, n));
   GT_TRY(dalloc(ctx, &z, n));
@@ -343,20 +373,20 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
   h0.maxit = maxit;
   GT_CUDA(ctx, cudaMemcpyAsync(&st->maxit, &h0.maxit, sizeof(int32_t), cudaMemcpyHostToDevice, s));
   GT_TRY(find_diag(A));
-  if (A->bs == 1) k_dinv<1, V, X><<<grid_for(n, 256), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
-  else if (A->bs == 2) k_dinv<2, V, X><<<grid_for(n, 256), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
-  else k_dinv<3, V, X><<<grid_for(n, 256), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
+  if (A->bs == 1) k_dinv<1, V, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
+  else if (A->bs == 2) k_dinv<2, V, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
+  else k_dinv<3, V, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
   GT_LAUNCH(ctx, "k_dinv");
   // r = b - A x
   GT_TRY((Ops<V, X>::spmv(ctx, A, val, x, b, r)));
-  k_cg_init<X><<<gv, RED_T, 0, s>>>(r, z, p, dinv, n, st, partials, rtol * rtol, bb_dev);
+  k_cg_init<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(r, z, p, dinv, n, st, partials, rtol * rtol, bb_dev);
   GT_LAUNCH(ctx, "k_cg_init");
   int status = GT_OK;
   for (int it = 0; it < maxit; it += CHUNK) {
     for (int k = 0; k < CHUNK; k++) {
       GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, partials)));
-      k_cg_update<X><<<gv, RED_T, 0, s>>>(x, r, z, p, q, dinv, n, st, partials);
-      k_cg_pupdate<X><<<gv, RED_T, 0, s>>>(p, z, n, st);
+      k_cg_update<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(x, r, z, p, q, dinv, n, st, partials);
+      k_cg_pupdate<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(p, z, n, st);
     }
     GT_LAUNCH(ctx, "cg iteration");
     GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
@@ -383,7 +413,7 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
 
 static int norm2(Ctx* ctx, const double* v, int64_t n, double* out_dev, double* partials, uint32_t* counter) {
   unsigned g = vec_grid(ctx, n);
-  k_norm2<double><<<g, RED_T, 0, ctx->stream>>>(v, n, out_dev, partials, counter);
+  k_norm2<double><<<GT_KC(ctx, g), RED_T, 0, ctx->stream>>>(v, n, out_dev, partials, counter);
   GT_LAUNCH(ctx, "k_norm2");
   return GT_OK;
 }
@@ -430,14 +460,14 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
     GT_TRY(dalloc(ctx, &xf, n));
     double* one = nullptr;
     GT_TRY(dalloc(ctx, &one, 1));
-    k_set_scalar<<<1, 1, 0, s>>>(one, 1.0);
-    k_scale_to_f32<<<vec_grid(ctx, n), RED_T, 0, s>>>(b, n, one, bf);
-    k_scale_to_f32<<<vec_grid(ctx, n), RED_T, 0, s>>>(x, n, one, xf);
+    k_set_scalar<<<GT_KC(ctx, 1), 1, 0, s>>>(one, 1.0);
+    k_scale_to_f32<<<GT_KC(ctx, vec_grid(ctx, n)), RED_T, 0, s>>>(b, n, one, bf);
+    k_scale_to_f32<<<GT_KC(ctx, vec_grid(ctx, n)), RED_T, 0, s>>>(x, n, one, xf);
     int32_t it = 0;
     double rr = 0, bb = 0;
     status = pcg<float, float>(A, A->val32, bf, xf, rtol, maxit, nullptr, &it, &rr, &bb);
     GT_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-    k_add_scaled_f32<<<vec_grid(ctx, n), RED_T, 0, s>>>(x, xf, n, one);
+    k_add_scaled_f32<<<GT_KC(ctx, vec_grid(ctx, n)), RED_T, 0, s>>>(x, xf, n, one);
     inf.iterations = it;
     dfree(ctx, bf);
     dfree(ctx, xf);
@@ -470,7 +500,7 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
       if (relres <= rtol) { status = GT_OK; break; }
       if (total_inner >= maxit) break;
       // inner: A32 d = r / ||r||, from d = 0, to inner_tol
-      k_scale_to_f32<<<g, RED_T, 0, s>>>(r, n, scal, rf);
+      k_scale_to_f32<<<GT_KC(ctx, g), RED_T, 0, s>>>(r, n, scal, rf);
       GT_CUDA(ctx, cudaMemsetAsync(df, 0, sizeof(float) * n, s));
       int32_t it = 0;
       double rr = 0, bb = 0;
@@ -479,7 +509,7 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
       int st2 = pcg<float, float>(A, A->val32, rf, df, tol_here, maxit - total_inner, nullptr, &it, &rr, &bb);
       (void)st2;  // a stalled inner solve still improves x; the outer test decides
       total_inner += it;
-      k_add_scaled_f32<<<g, RED_T, 0, s>>>(x, df, n, scal);
+      k_add_scaled_f32<<<GT_KC(ctx, g), RED_T, 0, s>>>(x, df, n, scal);
       GT_LAUNCH(ctx, "refinement update");
     }
     inf.iterations = total_inner;

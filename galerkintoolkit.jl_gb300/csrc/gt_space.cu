@@ -205,7 +205,7 @@ struct HashBuf {
     GT_TRY(dalloc(ctx, &h.rank, cap));
     GT_CUDA(ctx, cudaMemsetAsync(h.keys, 0xFF, sizeof(unsigned long long) * cap, ctx->stream));
     GT_CUDA(ctx, cudaMemsetAsync(h.vals, 0, sizeof(int32_t) * cap, ctx->stream));
-    k_fill_i32<<<grid_for(cap, 256), 256, 0, ctx->stream>>>(h.rank, cap, INT_MAX);
+    k_fill_i32<<<GT_KC(ctx, grid_for(cap, 256)), 256, 0, ctx->stream>>>(h.rank, cap, INT_MAX);
     GT_LAUNCH(ctx, "k_fill_i32");
     return GT_OK;
   }
@@ -232,17 +232,17 @@ static int number_faces(Ctx* ctx, const int32_t* fverts, int64_t nf, int nlv, in
   if (s == GT_OK) {
     cudaStream_t st = ctx->stream;
     cudaMemsetAsync(flag, 0, sizeof(int32_t) * ninst, st);
-    if (npar > 0) k_insert_parents<<<grid_for(npar, 256), 256, 0, st>>>(hb.h, pverts, npar, ndv, ctx->d_err);
-    k_insert_instances<<<grid_for(ninst, 256), 256, 0, st>>>(hb.h, fverts, nf, nlv, nld, ndv, ld, inst_slot, ctx->d_err);
-    k_first_flags<<<grid_for(hb.h.cap, 256), 256, 0, st>>>(hb.h, flag);
+    if (npar > 0) k_insert_parents<<<GT_KC(ctx, grid_for(npar, 256)), 256, 0, st>>>(hb.h, pverts, npar, ndv, ctx->d_err);
+    k_insert_instances<<<GT_KC(ctx, grid_for(ninst, 256)), 256, 0, st>>>(hb.h, fverts, nf, nlv, nld, ndv, ld, inst_slot, ctx->d_err);
+    k_first_flags<<<GT_KC(ctx, grid_for(hb.h.cap, 256)), 256, 0, st>>>(hb.h, flag);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) s = check_cuda(ctx, e, "face numbering");
   }
   if (s == GT_OK) s = exclusive_scan_i32(ctx, flag, pos, ninst);
   if (s == GT_OK) {
     cudaStream_t st = ctx->stream;
-    k_assign_new<<<grid_for(hb.h.cap, 256), 256, 0, st>>>(hb.h, pos, (int32_t)npar);
-    k_instance_ids<<<grid_for(ninst, 256), 256, 0, st>>>(hb.h, inst_slot, ninst, inst_ids, ctx->d_err);
+    k_assign_new<<<GT_KC(ctx, grid_for(hb.h.cap, 256)), 256, 0, st>>>(hb.h, pos, (int32_t)npar);
+    k_instance_ids<<<GT_KC(ctx, grid_for(ninst, 256)), 256, 0, st>>>(hb.h, inst_slot, ninst, inst_ids, ctx->d_err);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) s = check_cuda(ctx, e, "face ids");
   }
@@ -257,8 +257,8 @@ static int number_faces(Ctx* ctx, const int32_t* fverts, int64_t nf, int nlv, in
       s = dalloc(ctx, &dv, (*nd) * ndv);
       if (s == GT_OK) {
         cudaStream_t st = ctx->stream;
-        if (npar > 0) k_face_verts_parent<<<grid_for(npar * ndv, 256), 256, 0, st>>>(pverts, npar, ndv, dv);
-        k_face_verts_new<<<grid_for(hb.h.cap, 256), 256, 0, st>>>(hb.h, (int32_t)npar, fverts, nlv, nld, ndv, ld, dv);
+        if (npar > 0) k_face_verts_parent<<<GT_KC(ctx, grid_for(npar * ndv, 256)), 256, 0, st>>>(pverts, npar, ndv, dv);
+        k_face_verts_new<<<GT_KC(ctx, grid_for(hb.h.cap, 256)), 256, 0, st>>>(hb.h, (int32_t)npar, fverts, nlv, nld, ndv, ld, dv);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) s = check_cuda(ctx, e, "face vertices");
         *dverts_out = dv;
@@ -279,8 +279,8 @@ static int lookup_faces(Ctx* ctx, const int32_t* dverts, int64_t nd, int ndv, co
   HashBuf hb;
   GT_TRY(hb.alloc(ctx, nd));
   cudaStream_t st = ctx->stream;
-  k_insert_parents<<<grid_for(nd, 256), 256, 0, st>>>(hb.h, dverts, nd, ndv, ctx->d_err);
-  k_lookup_instances<<<grid_for(nf * nld, 256), 256, 0, st>>>(hb.h, fverts, nf, nlv, nld, ndv, ld, out, ctx->d_err);
+  k_insert_parents<<<GT_KC(ctx, grid_for(nd, 256)), 256, 0, st>>>(hb.h, dverts, nd, ndv, ctx->d_err);
+  k_lookup_instances<<<GT_KC(ctx, grid_for(nf * nld, 256)), 256, 0, st>>>(hb.h, fverts, nf, nlv, nld, ndv, ld, out, ctx->d_err);
   cudaError_t e = cudaGetLastError();
   hb.release(ctx);
   if (e != cudaSuccess) return check_cuda(ctx, e, "face lookup");
@@ -388,12 +388,12 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
   GT_TRY(dalloc(ctx, &nflag, nn_));
   GT_TRY(dalloc(ctx, &npos, nn_ + 1));
   GT_TRY(dalloc(ctx, &node_vertex, nn_));
-  k_fill_i32<<<grid_for(nn_, 256), 256, 0, st>>>(first, nn_, INT_MAX);
+  k_fill_i32<<<GT_KC(ctx, grid_for(nn_, 256)), 256, 0, st>>>(first, nn_, INT_MAX);
   if (M->ncorners > 0) {
-    k_corner_first<<<grid_for(M->ncorners, 256), 256, 0, st>>>(M->corners, M->ncorners, first);
-    k_corner_flags<<<grid_for(M->ncorners, 256), 256, 0, st>>>(M->corners, M->ncorners, first, cflag);
+    k_corner_first<<<GT_KC(ctx, grid_for(M->ncorners, 256)), 256, 0, st>>>(M->corners, M->ncorners, first);
+    k_corner_flags<<<GT_KC(ctx, grid_for(M->ncorners, 256)), 256, 0, st>>>(M->corners, M->ncorners, first, cflag);
   }
-  k_noncorner_flags<<<grid_for(nn_, 256), 256, 0, st>>>(first, nn_, nflag);
+  k_noncorner_flags<<<GT_KC(ctx, grid_for(nn_, 256)), 256, 0, st>>>(first, nn_, nflag);
   GT_LAUNCH(ctx, "vertex flags");
   GT_TRY(exclusive_scan_i32(ctx, cflag, cpos, M->ncorners));
   GT_TRY(exclusive_scan_i32(ctx, nflag, npos, nn_));
@@ -401,7 +401,7 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
   GT_CUDA(ctx, cudaStreamSynchronize(st));
   int32_t ncu = 0;
   memcpy(&ncu, &ctx->h_scratch[0], sizeof(int32_t));
-  k_vertex_ids<<<grid_for(nn_, 256), 256, 0, st>>>(M->corners, M->ncorners, first, cpos, npos, ncu, nn_, node_vertex);
+  k_vertex_ids<<<GT_KC(ctx, grid_for(nn_, 256)), 256, 0, st>>>(M->corners, M->ncorners, first, cpos, npos, ncu, nn_, node_vertex);
   GT_LAUNCH(ctx, "k_vertex_ids");
   int64_t nverts = nn_;
   dfree(ctx, first);
@@ -412,7 +412,7 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
   // cell vertices (1-based vertex ids)
   int32_t* cverts = nullptr;
   GT_TRY(dalloc(ctx, &cverts, nc * M->nv));
-  k_gather_cell_vertices<<<grid_for(nc * M->nv, 256), 256, 0, st>>>(M->cell_nodes, nc * M->nv, node_vertex, cverts);
+  k_gather_cell_vertices<<<GT_KC(ctx, grid_for(nc * M->nv, 256)), 256, 0, st>>>(M->cell_nodes, nc * M->nv, node_vertex, cverts);
   GT_LAUNCH(ctx, "k_gather_cell_vertices");
   // ---- edges / faces (Q2)
   int32_t *cedges = nullptr, *cfaces = nullptr;
@@ -423,7 +423,7 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
       for (int e = 0; e < 4; e++) { lq.v[e][0] = t.le_verts[e][0]; lq.v[e][1] = t.le_verts[e][1]; }
       int32_t* pv = nullptr;
       GT_TRY(dalloc(ctx, &pv, M->nbfaces * 2));
-      k_map_vertices<<<grid_for(M->nbfaces * 2, 256), 256, 0, st>>>(M->bfaces, M->nbfaces * 2, node_vertex, pv);
+      k_map_vertices<<<GT_KC(ctx, grid_for(M->nbfaces * 2, 256)), 256, 0, st>>>(M->bfaces, M->nbfaces * 2, node_vertex, pv);
       GT_LAUNCH(ctx, "k_map_vertices");
       GT_TRY(dalloc(ctx, &cedges, nc * 4));
       s = number_faces(ctx, cverts, nc, 4, 4, 2, lq, pv, M->nbfaces, cedges, nullptr, &nedges);
@@ -438,9 +438,9 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
       int32_t *pf = nullptr, *pe = nullptr, *fverts = nullptr, *fedges = nullptr, *everts = nullptr;
       GT_TRY(dalloc(ctx, &pf, M->nbfaces * 4));
       GT_TRY(dalloc(ctx, &pe, M->nbedges * 2 + 1));
-      k_map_vertices<<<grid_for(M->nbfaces * 4, 256), 256, 0, st>>>(M->bfaces, M->nbfaces * 4, node_vertex, pf);
+      k_map_vertices<<<GT_KC(ctx, grid_for(M->nbfaces * 4, 256)), 256, 0, st>>>(M->bfaces, M->nbfaces * 4, node_vertex, pf);
       if (M->nbedges > 0)
-        k_map_vertices<<<grid_for(M->nbedges * 2, 256), 256, 0, st>>>(M->bedges, M->nbedges * 2, node_vertex, pe);
+        k_map_vertices<<<GT_KC(ctx, grid_for(M->nbedges * 2, 256)), 256, 0, st>>>(M->bedges, M->nbedges * 2, node_vertex, pe);
       GT_LAUNCH(ctx, "k_map_vertices");
       GT_TRY(dalloc(ctx, &cfaces, nc * 6));
       GT_TRY(number_faces(ctx, cverts, nc, 8, 6, 4, lh, pf, M->nbfaces, cfaces, &fverts, &nfaces));
@@ -458,7 +458,7 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
   // ---- node dofs before the split
   int64_t nnodes_sp = nverts + (sp->order == 2 ? nedges + nfaces + nc : 0);
   GT_TRY(dalloc(ctx, &sp->cell_ndofs, nc * t.nn));
-  k_cell_node_dofs<<<grid_for(nc, 128), 128, 0, st>>>(t, sp->order, nc, cverts, cedges, cfaces, nverts, nedges, nfaces,
+  k_cell_node_dofs<<<GT_KC(ctx, grid_for(nc, 128)), 128, 0, st>>>(t, sp->order, nc, cverts, cedges, cfaces, nverts, nedges, nfaces,
                                                        sp->cell_ndofs);
   GT_LAUNCH(ctx, "k_cell_node_dofs");
   // ---- Dirichlet tags
@@ -472,19 +472,19 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
     GT_TRY(dalloc(ctx, &keep, M->nbfaces));
     GT_TRY(dalloc(ctx, &dgroups, ng + 1));
     if (ng > 0) GT_TRY(copy_in(ctx, dgroups, groups_host, ng));
-    k_select_faces<<<grid_for(M->nbfaces, 256), 256, 0, st>>>(M->bfaces, M->bgroup, M->nbfaces, M->nbfv, node_vertex,
+    k_select_faces<<<GT_KC(ctx, grid_for(M->nbfaces, 256)), 256, 0, st>>>(M->bfaces, M->bgroup, M->nbfaces, M->nbfv, node_vertex,
                                                                dgroups, ng, sel, keep);
     GT_LAUNCH(ctx, "k_select_faces");
     if (sp->order == 1) {
       // the closure of a tagged face holds only its vertices, whose
       // pre-split node dof is the vertex id
-      k_tag_vertices<<<grid_for(M->nbfaces * M->nbfv, 256), 256, 0, st>>>(sel, M->nbfaces * M->nbfv, tag);
+      k_tag_vertices<<<GT_KC(ctx, grid_for(M->nbfaces * M->nbfv, 256)), 256, 0, st>>>(sel, M->nbfaces * M->nbfv, tag);
       GT_LAUNCH(ctx, "k_tag_vertices");
     } else {
       HashBuf hb;
       GT_TRY(hb.alloc(ctx, M->nbfaces));
-      k_insert_tagged<<<grid_for(M->nbfaces, 256), 256, 0, st>>>(hb.h, sel, keep, M->nbfaces, M->nbfv, ctx->d_err);
-      k_tag_dirichlet<<<grid_for(nc * t.nlf, 256), 256, 0, st>>>(hb.h, t, nc, cverts, sp->cell_ndofs, tag, ctx->d_err);
+      k_insert_tagged<<<GT_KC(ctx, grid_for(M->nbfaces, 256)), 256, 0, st>>>(hb.h, sel, keep, M->nbfaces, M->nbfv, ctx->d_err);
+      k_tag_dirichlet<<<GT_KC(ctx, grid_for(nc * t.nlf, 256)), 256, 0, st>>>(hb.h, t, nc, cverts, sp->cell_ndofs, tag, ctx->d_err);
       GT_LAUNCH(ctx, "k_tag_dirichlet");
       hb.release(ctx);
     }
@@ -495,11 +495,11 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
   GT_TRY(dalloc(ctx, &freef, nnodes_sp));
   GT_TRY(dalloc(ctx, &fpos, nnodes_sp + 1));
   GT_TRY(dalloc(ctx, &dpos, nnodes_sp + 1));
-  k_free_flags<<<grid_for(nnodes_sp, 256), 256, 0, st>>>(tag, nnodes_sp, freef);
+  k_free_flags<<<GT_KC(ctx, grid_for(nnodes_sp, 256)), 256, 0, st>>>(tag, nnodes_sp, freef);
   GT_LAUNCH(ctx, "k_free_flags");
   GT_TRY(exclusive_scan_i32(ctx, freef, fpos, nnodes_sp));
   GT_TRY(exclusive_scan_i32(ctx, tag, dpos, nnodes_sp));
-  k_renumber<<<grid_for(nc * t.nn, 256), 256, 0, st>>>(sp->cell_ndofs, nc * t.nn, tag, fpos, dpos);
+  k_renumber<<<GT_KC(ctx, grid_for(nc * t.nn, 256)), 256, 0, st>>>(sp->cell_ndofs, nc * t.nn, tag, fpos, dpos);
   GT_LAUNCH(ctx, "k_renumber");
   GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], fpos + nnodes_sp, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[1], dpos + nnodes_sp, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -565,7 +565,7 @@ int gt_mesh_create(gt_ctx* ctx, int cell_type, int64_t nnodes, const double* coo
     if (s != GT_OK || n <= 0) return;
     s = copy_in(ctx, *dst, src, n);
     if (s != GT_OK) return;
-    if (nmax > 0) k_to_zero_based<<<grid_for(n, 256), 256, 0, ctx->stream>>>(*dst, n, nmax, ctx->d_err);
+    if (nmax > 0) k_to_zero_based<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, ctx->stream>>>(*dst, n, nmax, ctx->d_err);
   };
   s = dalloc(ctx, &M->coords, nnodes * M->D);
   if (s == GT_OK) s = copy_in(ctx, M->coords, coords, nnodes * M->D);
@@ -613,6 +613,7 @@ int gt_space_create(gt_mesh* M, int order, int ncomp, int ngroups, const int32_t
     return set_error(ctx, GT_ERR_INVALID, "mesh has no boundary groups");
   cudaSetDevice(ctx->device);
   gt_space* sp = new gt_space();
+  sp->ctx = ctx;
   sp->mesh = M;
   sp->order = order;
   sp->ncomp = ncomp;
@@ -644,7 +645,7 @@ int gt_space_cell_dofs(const gt_space* sp, int32_t* out) {
   int64_t n = sp->mesh->ncells * sp->nloc;
   int32_t* tmp = nullptr;
   GT_TRY(dalloc(ctx, &tmp, n));
-  k_expand_cell_dofs<<<grid_for(n, 256), 256, 0, ctx->stream>>>(sp->cell_ndofs, sp->mesh->ncells, sp->nn, sp->ncomp, tmp);
+  k_expand_cell_dofs<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, ctx->stream>>>(sp->cell_ndofs, sp->mesh->ncells, sp->nn, sp->ncomp, tmp);
   GT_LAUNCH(ctx, "k_expand_cell_dofs");
   int s = copy_out(ctx, out, tmp, n);
   if (s == GT_OK) {
@@ -657,7 +658,7 @@ int gt_space_cell_dofs(const gt_space* sp, int32_t* out) {
 
 int gt_space_destroy(gt_space* sp) {
   if (!sp) return GT_ERR_INVALID;
-  Ctx* c = sp->mesh->ctx;
+  Ctx* c = sp->ctx;
   dfree(c, sp->cell_ndofs);
   dfree(c, sp->inc_ptr);
   dfree(c, sp->inc);

@@ -55,6 +55,10 @@ SIGNATURES = [
     ("gt_ctx_synchronize", I32, [P]),
     ("gt_ctx_set_stream", I32, [P, P]),
     ("gt_ctx_memory", I32, [P, P, P]),
+    ("gt_ctx_launch_count", I32, [P, P]),
+    ("gt_ctx_fma_rate", I32, [P, I32, P]),
+    ("gt_ctx_profile_begin", I32, [P]),
+    ("gt_ctx_profile_end", I32, [P, I32, P, P, P]),
     ("gt_mesh_create", I32, [P, I32, I64, P, I64, P, I64, P, I64, P, P, I64, P, C.POINTER(P)]),
     ("gt_mesh_set_coords", I32, [P, P]),
     ("gt_mesh_destroy", I32, [P]),

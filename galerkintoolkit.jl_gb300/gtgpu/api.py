@@ -51,6 +51,28 @@ class Context:
         check(self.h, self.lib.gt_ctx_memory(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def launches(self) -> int:
+        n = C.c_int64()
+        check(self.h, self.lib.gt_ctx_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def fma_rate(self, fp64=True) -> float:
+        """Measured FMA throughput (TFLOP/s) of FP64 or FP32 on this device."""
+        t = C.c_double()
+        check(self.h, self.lib.gt_ctx_fma_rate(self.h, _lib.GT_FP64 if fp64 else _lib.GT_FP32, C.byref(t)))
+        return t.value
+
+    def profile_begin(self):
+        check(self.h, self.lib.gt_ctx_profile_begin(self.h))
+
+    def profile_end(self, max_phases=64):
+        names = C.create_string_buffer(32 * max_phases)
+        ms = np.zeros(max_phases, np.float64)
+        n = C.c_int()
+        check(self.h, self.lib.gt_ctx_profile_end(self.h, max_phases, names, _ptr(ms), C.byref(n)))
+        raw = names.raw
+        return [(raw[32 * i:32 * i + 32].split(b"\0")[0].decode(), float(ms[i])) for i in range(n.value)]
+
     def close(self):
         if self.h:
             self.lib.gt_ctx_destroy(self.h)
@@ -79,8 +101,11 @@ def _ptr(a):
 # mesh on the device
 # ---------------------------------------------------------------------------
 class DeviceMesh:
+    """gt_mesh handle.  Holds no reference back to the host Mesh (which caches
+    it), so no reference cycle decides the destruction order."""
+
     def __init__(self, mesh: Mesh, ctx: Context):
-        self.ctx, self.mesh = ctx, mesh
+        self.ctx = ctx
         h = C.c_void_p()
         m = mesh
         check(ctx.h, ctx.lib.gt_mesh_create(

@@ -82,6 +82,16 @@ int gt_ctx_synchronize(gt_ctx* ctx);
 int gt_ctx_set_stream(gt_ctx* ctx, void* stream);
 /* Bytes of device memory currently held by the context (live + pooled). */
 int gt_ctx_memory(gt_ctx* ctx, int64_t* live_bytes, int64_t* pooled_bytes);
+/* Measured FMA throughput of the device in TFLOP/s (GT_FP64 or GT_FP32);
+ * the roofline of the integration kernels.  No reference counterpart. */
+int gt_ctx_fma_rate(gt_ctx* ctx, int precision, double* tflops);
+/* Number of kernels the context has launched so far. */
+int gt_ctx_launch_count(gt_ctx* ctx, int64_t* launches);
+/* Phase timing with CUDA events on the context's stream: begin, run calls,
+ * end.  end() returns up to max phases: names (32 chars each) and device
+ * milliseconds between consecutive phase boundaries. */
+int gt_ctx_profile_begin(gt_ctx* ctx);
+int gt_ctx_profile_end(gt_ctx* ctx, int max, char* names, double* ms, int* count);
 
 /* ---- mesh --------------------------------------------------------------- */
 /* Replaces GT.mesh(...) of a cartesian_mesh (src/mesh.jl:573-650,
