@@ -594,6 +594,25 @@ int compute_elements(const Space* sp, int form, const double* d_coef, double nu,
   return s;
 }
 
+// Number of doubles of the tabulation buffer of a space's reference cell.
+int tabulation_doubles(const Space* sp) { return tab_layout(sp->mesh->ctype, sp->order).total; }
+
+// Element matrices with a caller-provided tabulation buffer (no allocation).
+int compute_elements_with_tab(const Space* sp, int form, const double* d_coef, double nu, int precision, double* tab,
+                              void* Ke) {
+  Ctx* ctx = ctx_of(sp);
+  if (form != GT_LAPLACE && form != GT_MASS && form != GT_ELASTICITY)
+    return set_error(ctx, GT_ERR_UNSUPPORTED, "weak form not supported (Laplacian, mass, linear elasticity only)");
+  if (form == GT_ELASTICITY && sp->ncomp != sp->mesh->D)
+    return set_error(ctx, GT_ERR_UNSUPPORTED, "linear elasticity needs a vector space (tensor_size = (D,))");
+  TabLayout L = tab_layout(sp->mesh->ctype, sp->order);
+  k_tabulate<<<GT_KC(ctx, 1), 32, 0, ctx->stream>>>(sp->mesh->ctype, sp->order, L, tab);
+  GT_LAUNCH(ctx, "k_tabulate");
+  if (precision == GT_FP32)
+    return elements_T<float>(sp, form, d_coef, nu, tab, L, (float*)Ke, nullptr, nullptr, nullptr, 1);
+  return elements_T<double>(sp, form, d_coef, nu, tab, L, (double*)Ke, nullptr, nullptr, nullptr, 1);
+}
+
 // ---------------------------------------------------------------------------
 // 4. scatter: G lanes own one block row; the row's column indices and
 // accumulators live in shared memory; incidences are visited in ascending

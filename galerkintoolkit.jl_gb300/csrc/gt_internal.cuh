@@ -184,6 +184,9 @@ int build_pattern(Matrix* A);
 int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision,
                      const double* f, const double* d_scoef, void* Ke, double* be, int want_matrix);
 int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision);
+int tabulation_doubles(const Space* sp);
+int compute_elements_with_tab(const Space* sp, int form, const double* d_coef, double nu, int precision,
+                              double* tab, void* Ke);
 int scatter_vector(const Space* sp, const int64_t* inc_ptr, const int32_t* inc, const double* be,
                    double* b);
 int find_diag(Matrix* A);

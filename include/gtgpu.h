@@ -145,6 +145,18 @@ int gt_assemble_matrix_and_vector(gt_space* space, int form, const double* cell_
 /* Replaces GT.update_matrix!(A, cache) (src/problems.jl:352-361): new values
  * on the existing sparsity. */
 int gt_update_matrix(gt_matrix* matrix, int form, const double* cell_coef, double nu);
+/* No counterpart in the reference.  gt_update_matrix without allocating:
+ * for callers that must not have the library allocate device memory (a
+ * process whose device memory is budgeted up front by its own admission
+ * control or memory pool, or a latency-critical refill loop where
+ * cudaMalloc/cudaFree can synchronise the device).  Refills the values of an
+ * assembled matrix using one static 128 MiB device array as scratch;
+ * cell_coef must be device memory or NULL; a refill needing more scratch
+ * than 128 MiB (tabulation + ncells*nloc^2 values) returns GT_ERR_INVALID.
+ * The first call on a device looks up the array's address (do it before any
+ * stream capture).  All calls share the array: calls that overlap on the
+ * GPU race. */
+int gt_update_matrix_noalloc(gt_matrix* matrix, int form, const double* cell_coef, double nu);
 /* Replaces GT.update_matrix_and_vector! (src/problems.jl:409-414). */
 int gt_update_matrix_and_vector(gt_matrix* matrix, int form, const double* cell_coef, double nu,
                                 const double* f, const double* source_coef, double* b);
