@@ -192,7 +192,10 @@ def main():
     n = args.cells
     m, kappa = workload(n)
     ctx = GT.Context(local)
-    stream = torch.cuda.current_stream()
+    # one stream for torch and the library: the CUDA events below bracket
+    # exactly the library's work
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     V = GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m), ctx=ctx)
     kd = torch.from_numpy(kappa).cuda()

@@ -193,91 +193,170 @@ __global__ void k_inc_sort(const int64_t* __restrict__ ptr, int32_t* __restrict_
 
 static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out);
 
-int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc) {
+int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc, bool sort) {
   cudaStream_t st = ctx->stream;
   int64_t nrows = sp->nfree_nodes, n = sp->mesh->ncells * sp->nn;
-  int32_t *cnt = nullptr, *cursor = nullptr, *dmax = nullptr;
+  int32_t *cnt = nullptr, *cursor = nullptr;
   GT_TRY(dalloc(ctx, &cnt, nrows + 1));
   GT_TRY(dalloc(ctx, &cursor, nrows + 1));
-  GT_TRY(dalloc(ctx, &dmax, 1));
   GT_TRY(dalloc(ctx, inc_ptr, nrows + 1));
+  GT_TRY(dalloc(ctx, inc, n));  // upper bound: every (cell, node) free
   GT_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), st));
   GT_CUDA(ctx, cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (nrows + 1), st));
-  GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
   k_inc_count<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, cnt);
   GT_LAUNCH(ctx, "k_inc_count");
   GT_TRY(exclusive_scan_i64(ctx, cnt, *inc_ptr, nrows));
-  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], *inc_ptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  GT_CUDA(ctx, cudaStreamSynchronize(st));
-  *ninc = ctx->h_scratch[0];
-  GT_TRY(dalloc(ctx, inc, *ninc));
   k_inc_fill<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, *inc_ptr, cursor, *inc);
   GT_LAUNCH(ctx, "k_inc_fill");
-  int32_t maxinc = 0;
-  GT_TRY(max_diff(ctx, *inc_ptr, nrows, &maxinc));
-  int icap = 32;
-  while (icap < maxinc) icap <<= 1;
-  if (icap > 4096) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells");
-  int warps = 8;
-  size_t smem = (size_t)warps * icap * sizeof(int32_t);
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_inc_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (nrows > 0)
-    k_inc_sort<<<GT_KC(ctx, grid_for(nrows, warps)), warps * 32, smem, st>>>(*inc_ptr, *inc, nrows, icap);
-  GT_LAUNCH(ctx, "k_inc_sort");
+  *ninc = -1;  // not read back: the sparsity pass knows the row extents
+  if (sort) {
+    int32_t maxinc = 0;
+    GT_TRY(max_diff(ctx, *inc_ptr, nrows, &maxinc));
+    int icap = 32;
+    while (icap < maxinc) icap <<= 1;
+    if (icap > 4096) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells");
+    int warps = 8;
+    size_t smem = (size_t)warps * icap * sizeof(int32_t);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k_inc_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (nrows > 0)
+      k_inc_sort<<<GT_KC(ctx, grid_for(nrows, warps)), warps * 32, smem, st>>>(*inc_ptr, *inc, nrows, icap);
+    GT_LAUNCH(ctx, "k_inc_sort");
+  }
   dfree(ctx, cnt);
   dfree(ctx, cursor);
-  dfree(ctx, dmax);
   return GT_OK;
 }
 
 // ---------------------------------------------------------------------------
-// 2. pattern: one warp per block row, bitonic sort of the candidate columns
-// in shared memory, duplicates dropped
+// 2. pattern
 // ---------------------------------------------------------------------------
-template <bool FILL>
-__global__ void k_pattern(const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
-                          const int32_t* __restrict__ cnd, int nn, int64_t nrows, int cap, int icap,
-                          int32_t* __restrict__ rowcnt, const int64_t* __restrict__ rowptr,
-                          int32_t* __restrict__ colind, uint32_t* err) {
+// ascending bitonic sort of 32 keys held one per lane (register shuffles)
+__device__ __forceinline__ int32_t warp_sort32(int32_t v, int lane) {
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1)
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      int32_t o = __shfl_xor_sync(0xffffffffu, v, j);
+      bool up = (lane & k) == 0, lower = (lane & j) == 0;
+      v = (lower == up) ? min(v, o) : max(v, o);
+    }
+  return v;
+}
+
+// Per block row: the sorted union of the free node DOFs of its cells.
+// One warp per row.  Candidates go into a shared-memory hash set (atomicCAS
+// on 32-bit keys, linear probing).  The count pass counts the distinct keys
+// and, for rows of at most S columns, compacts and sorts them (register
+// shuffles for <= 32 keys, shared-memory bitonic sort above) into the row's
+// slot of S entries; the fill pass copies those slots and runs the hash
+// again only for longer rows.  The count pass also sorts the row's
+// incidence list in place (ascending = by cell), which fixes the scatter's
+// summation order.
+template <int NN, int S, bool FILL>
+__global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc_ptr, int32_t* __restrict__ inc,
+                                                 const int32_t* __restrict__ cnd, int64_t nrows, int hcap, int icap,
+                                                 int32_t* __restrict__ rowcnt, const int64_t* __restrict__ rowptr,
+                                                 int32_t* __restrict__ colind, int32_t* __restrict__ slots,
+                                                 uint8_t* __restrict__ small, int32_t* maxrow, uint32_t* err) {
   extern __shared__ int32_t s_buf[];
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int32_t* buf = s_buf + w * (cap + icap);  // candidate columns
-  int32_t* ibuf = buf + cap;                // the row's incidences
+  int32_t* tab = s_buf + w * (hcap + icap);  // hash set
+  int32_t* ibuf = tab + hcap;                 // the row's incidences, later the compacted keys
   int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
   if (r >= nrows) return;
-  int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
-  int ninc = (int)(ie - ib);
-  int ncand = ninc * nn;
-  if (ncand > cap || ninc > icap) {
-    if (lane == 0) { atomicOr(err, DEV_ERR_ROW_CAP); if (!FILL) rowcnt[r] = 0; }
+  if (FILL && small[r]) {
+    // the count pass already wrote this row's sorted columns to its slot
+    int64_t o = rowptr[r];
+    int n = (int)(rowptr[r + 1] - o);
+    for (int i = lane; i < n; i += 32) colind[o + i] = slots[r * S + i];
     return;
   }
-  for (int i = lane; i < ninc; i += 32) ibuf[i] = inc[ib + i];
-  __syncwarp();
-  int P = 32;
-  while (P < ncand) P <<= 1;
-  for (int i = lane; i < P; i += 32) {
-    int32_t v = INT_MAX;
-    if (i < ncand) {
-      int k = i / nn, b = i - k * nn;
-      int32_t c = ibuf[k] / nn;
-      int32_t d = cnd[(int64_t)c * nn + b];
-      v = d > 0 ? d - 1 : INT_MAX;
+  int64_t ib = inc_ptr[r];
+  int ninc = (int)(inc_ptr[r + 1] - ib);
+  int ncand = ninc * NN;
+  if (2 * ncand > hcap || ninc > icap) {
+    if (lane == 0) { atomicOr(err, DEV_ERR_ROW_CAP); if (!FILL) { rowcnt[r] = 0; small[r] = 1; } }
+    return;
+  }
+  for (int i = lane; i < hcap; i += 32) tab[i] = -1;
+  if (!FILL) {
+    if (ninc <= 32) {
+      int32_t v = warp_sort32(lane < ninc ? inc[ib + lane] : INT_MAX, lane);
+      if (lane < ninc) {
+        inc[ib + lane] = v;
+        ibuf[lane] = v;
+      }
+    } else {
+      int P2 = 32;
+      while (P2 < ninc) P2 <<= 1;
+      for (int i = lane; i < P2; i += 32) ibuf[i] = i < ninc ? inc[ib + i] : INT_MAX;
+      __syncwarp();
+      warp_bitonic_sort(ibuf, P2, lane);
+      for (int i = lane; i < ninc; i += 32) inc[ib + i] = ibuf[i];
     }
-    buf[i] = v;
+  } else {
+    for (int i = lane; i < ninc; i += 32) ibuf[i] = inc[ib + i];
   }
   __syncwarp();
-  warp_bitonic_sort(buf, P, lane);
-  int count = 0;
-  for (int base = 0; base < P; base += 32) {
-    int i = base + lane;
-    int32_t v = buf[i];
-    bool keep = v != INT_MAX && (i == 0 || buf[i - 1] != v);
-    unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (FILL && keep) colind[rowptr[r] + count + __popc(m & ((1u << lane) - 1))] = v;
-    count += __popc(m);
+  int mine = 0;  // distinct keys this lane inserted
+  const unsigned hmask = (unsigned)hcap - 1u;
+  for (int i = lane; i < ncand; i += 32) {
+    int k = i / NN, b = i - k * NN;
+    int32_t c = ibuf[k] / NN;
+    int32_t d = cnd[(int64_t)c * NN + b];
+    if (d <= 0) continue;
+    int32_t key = d - 1;
+    unsigned h = ((unsigned)key * 2654435761u) & hmask;
+    for (;;) {
+      int32_t old = atomicCAS(&tab[h], -1, key);
+      if (old == -1) { mine++; break; }
+      if (old == key) break;
+      h = (h + 1) & hmask;
+    }
   }
-  if (!FILL && lane == 0) rowcnt[r] = count;
+  __syncwarp();
+  int total = mine;
+  for (int o = 16; o; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
+  if (!FILL) {
+    if (lane == 0) {
+      rowcnt[r] = total;
+      atomicMax(maxrow, total);
+      small[r] = total <= S;
+    }
+    if (total > S) return;
+  }
+  // compact the distinct keys (icap >= P: the host keeps icap >= hcap / 2 >=
+  // ncand >= total), sort them, and write them to the row's slot (count
+  // pass, rows of at most S columns) or to colind (fill pass)
+  int P = 32;
+  while (P < total) P <<= 1;
+  int32_t* keys = ibuf;
+  int base = 0;
+  for (int s0 = 0; s0 < hcap; s0 += 32) {
+    int32_t v = tab[s0 + lane];
+    bool keep = v >= 0;
+    unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) keys[base + __popc(m & ((1u << lane) - 1u))] = v;
+    base += __popc(m);
+  }
+  __syncwarp();
+  if (P == 32) {
+    int32_t v = warp_sort32(lane < total ? keys[lane] : INT_MAX, lane);
+    if (lane < total) {
+      if (FILL) colind[rowptr[r] + lane] = v;
+      else slots[r * S + lane] = v;
+    }
+    return;
+  }
+  for (int i = total + lane; i < P; i += 32) keys[i] = INT_MAX;
+  __syncwarp();
+  warp_bitonic_sort(keys, P, lane);
+  if (FILL) {
+    int64_t o = rowptr[r];
+    for (int i = lane; i < total; i += 32) colind[o + i] = keys[i];
+  } else {
+    for (int i = lane; i < total; i += 32) slots[r * S + i] = keys[i];
+  }
 }
 
 __global__ void k_max_diff(const int64_t* ptr, int64_t n, int32_t* out) {
@@ -301,48 +380,76 @@ static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out) {
   return GT_OK;
 }
 
-int build_pattern(Matrix* A) {
+template <int NN>
+static int launch_pattern(Matrix* A, int maxinc) {
+  // slot width of the count pass: P1/Q1/Q2-quad rows have <= 27 columns,
+  // Q2-hex rows up to 125
+  constexpr int S = NN == 27 ? 128 : 32;
   const Space* sp = A->space;
   Ctx* ctx = sp->mesh->ctx;
   cudaStream_t st = ctx->stream;
-  int64_t nrows = sp->nfree_nodes;
-  A->nbrows = nrows;
-  int32_t maxinc = 0;
-  GT_TRY(max_diff(ctx, A->inc_ptr, nrows, &maxinc));
-  int cap = 32, icap = 32;
-  while (cap < maxinc * sp->nn) cap <<= 1;
+  int64_t nrows = A->nbrows;
+  int hcap = 64, icap = 32;
+  while (hcap < 2 * maxinc * NN) hcap <<= 1;
   while (icap < maxinc) icap <<= 1;
-  if (cap > 4096) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells for the sparsity kernel");
-  int warps = cap >= 2048 ? 2 : (cap >= 1024 ? 4 : 8);
-  size_t smem = (size_t)warps * (cap + icap) * sizeof(int32_t);
-  if (smem > 48 * 1024) {
-    cudaFuncSetAttribute(k_pattern<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_pattern<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  }
-  int32_t* rowcnt = nullptr;
+  if (icap < hcap / 2) icap = hcap / 2;  // room for the compacted keys (<= candidates)
+  if (hcap > 8192) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells for the sparsity kernel");
+  int warps = hcap >= 4096 ? 2 : (hcap >= 2048 ? 4 : 8);
+  size_t smem = (size_t)warps * (hcap + icap) * sizeof(int32_t);
+  cudaFuncSetAttribute(k_pattern<NN, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_pattern<NN, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int32_t *rowcnt = nullptr, *dmax = nullptr, *slots = nullptr;
+  uint8_t* small = nullptr;
   GT_TRY(dalloc(ctx, &rowcnt, nrows + 1));
+  GT_TRY(dalloc(ctx, &dmax, 1));
+  GT_TRY(dalloc(ctx, &slots, nrows * S));
+  GT_TRY(dalloc(ctx, &small, nrows + 1));
   GT_TRY(dalloc(ctx, &A->rowptr, nrows + 1));
+  GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
   int grid = grid_for(nrows, warps);
-  k_pattern<false><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, sp->nn, nrows, cap, icap,
-                                                                rowcnt, nullptr, nullptr, ctx->d_err);
+  if (nrows > 0)
+    k_pattern<NN, S, false><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, nrows,
+                                                                        hcap, icap, rowcnt, nullptr, nullptr, slots,
+                                                                        small, dmax, ctx->d_err);
   GT_LAUNCH(ctx, "k_pattern<count>");
   GT_TRY(exclusive_scan_i64(ctx, rowcnt, A->rowptr, nrows));
   mark(ctx, "pattern_count");
   GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], A->rowptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[1], dmax, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   uint32_t bits = 0;
   GT_TRY(take_device_error(ctx, &bits));  // synchronises
   if (bits) return set_error(ctx, GT_ERR_INVALID, "sparsity: row capacity exceeded");
   A->bnnz = ctx->h_scratch[0];
+  int32_t mr = 0;
+  memcpy(&mr, &ctx->h_scratch[1], sizeof(int32_t));
+  A->max_row = mr;
   GT_TRY(dalloc(ctx, &A->colind, A->bnnz));
-  k_pattern<true><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, sp->nn, nrows, cap, icap,
-                                                               nullptr, A->rowptr, A->colind, ctx->d_err);
+  if (nrows > 0)
+    k_pattern<NN, S, true><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, nrows,
+                                                                       hcap, icap, nullptr, A->rowptr, A->colind,
+                                                                       slots, small, dmax, ctx->d_err);
   GT_LAUNCH(ctx, "k_pattern<fill>");
   mark(ctx, "pattern_fill");
   dfree(ctx, rowcnt);
-  int32_t mr = 0;
-  GT_TRY(max_diff(ctx, A->rowptr, nrows, &mr));
-  A->max_row = mr;
+  dfree(ctx, dmax);
+  dfree(ctx, slots);
+  dfree(ctx, small);
   return GT_OK;
+}
+
+int build_pattern(Matrix* A) {
+  const Space* sp = A->space;
+  Ctx* ctx = sp->mesh->ctx;
+  A->nbrows = sp->nfree_nodes;
+  int32_t maxinc = 0;
+  GT_TRY(max_diff(ctx, A->inc_ptr, A->nbrows, &maxinc));
+  switch (sp->nn) {
+    case 4: return launch_pattern<4>(A, maxinc);
+    case 8: return launch_pattern<8>(A, maxinc);
+    case 9: return launch_pattern<9>(A, maxinc);
+    case 27: return launch_pattern<27>(A, maxinc);
+  }
+  return set_error(ctx, GT_ERR_UNSUPPORTED, "element not supported");
 }
 
 // ---------------------------------------------------------------------------
@@ -562,11 +669,115 @@ static int dispatch_form(const Space* sp, int form, const double* coef, double n
 }
 
 
+// P1 tetrahedra, scalar Laplacian / mass: one thread per cell.  The map is
+// affine, so J = [x1-x0, x2-x0, x3-x0] is constant over the cell and the
+// physical gradients are the columns c_j of the cofactor matrix of J divided
+// by det J (J^-T = cof(J) / det J), with c_0 = -(c_1 + c_2 + c_3).  Then
+//   Laplacian  K_nm = coef * (sum_q w_q) / |det J| * (c_n . c_m)
+//   mass       K_nm = coef * |det J| * sum_q w_q phi_n(q) phi_m(q)
+// -- the quadrature sums of the reference loop (src/compiler.jl:1865-1917
+// with dV = |det J| w, src/quadrature.jl:4-6) with the constant factors
+// taken out: one FP64 division and ~90 FP64 operations per cell.  J, its
+// cofactors and det stay FP64 in every precision; in FP32 mode the cofactor
+// columns are rounded to FP32 for the entries.
+template <int FORM, class T>
+__global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ coords,
+                                                     const int32_t* __restrict__ cell_nodes,
+                                                     const double* __restrict__ coef, const double* __restrict__ tab,
+                                                     TabLayout L, int64_t ncells, T* __restrict__ Ke,
+                                                     double* __restrict__ be, const double* __restrict__ fsrc,
+                                                     const double* __restrict__ scoef, int want_matrix, uint32_t* err) {
+  __shared__ double s_mass[16], s_load[4], s_wsum;
+  if (threadIdx.x < 16) {
+    int n = threadIdx.x >> 2, m = threadIdx.x & 3;
+    double s = 0.0;
+    for (int q = 0; q < 4; q++) s += tab[L.off_w + q] * tab[L.off_sv + q * 4 + n] * tab[L.off_sv + q * 4 + m];
+    s_mass[threadIdx.x] = s;
+  }
+  if (threadIdx.x < 4) {
+    double s = 0.0;
+    for (int q = 0; q < 4; q++) s += tab[L.off_w + q] * tab[L.off_sv + q * 4 + threadIdx.x];
+    s_load[threadIdx.x] = s;
+  }
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < 4; q++) s += tab[L.off_w + q];
+    s_wsum = s;
+  }
+  __syncthreads();
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  int4 nd = *reinterpret_cast<const int4*>(cell_nodes + 4 * c);
+  const double* p0 = coords + 3 * (int64_t)nd.x;
+  const double* p1 = coords + 3 * (int64_t)nd.y;
+  const double* p2 = coords + 3 * (int64_t)nd.z;
+  const double* p3 = coords + 3 * (int64_t)nd.w;
+  double x0 = p0[0], y0 = p0[1], z0 = p0[2];
+  // J columns
+  double a0 = p1[0] - x0, a1 = p1[1] - y0, a2 = p1[2] - z0;
+  double b0 = p2[0] - x0, b1 = p2[1] - y0, b2 = p2[2] - z0;
+  double d0 = p3[0] - x0, d1 = p3[1] - y0, d2 = p3[2] - z0;
+  // J = [[a0 b0 d0],[a1 b1 d1],[a2 b2 d2]]; cofactor columns C[:,j]
+  double c10 = b1 * d2 - b2 * d1, c11 = b2 * d0 - b0 * d2, c12 = b0 * d1 - b1 * d0;  // column 0 (row of J^-1 #0)
+  double c20 = d1 * a2 - d2 * a1, c21 = d2 * a0 - d0 * a2, c22 = d0 * a1 - d1 * a0;  // column 1
+  double c30 = a1 * b2 - a2 * b1, c31 = a2 * b0 - a0 * b2, c32 = a0 * b1 - a1 * b0;  // column 2
+  double det = a0 * c10 + a1 * c11 + a2 * c12;
+  if (!(det != 0.0)) atomicOr(err, DEV_ERR_DEGENERATE);
+  double adet = fabs(det);
+  double cf = coef ? coef[c] : 1.0;
+  if (want_matrix) {
+    T k[10];
+    if (FORM == GT_LAPLACE) {
+      T g[4][3];
+      g[1][0] = (T)c10; g[1][1] = (T)c11; g[1][2] = (T)c12;
+      g[2][0] = (T)c20; g[2][1] = (T)c21; g[2][2] = (T)c22;
+      g[3][0] = (T)c30; g[3][1] = (T)c31; g[3][2] = (T)c32;
+      for (int d = 0; d < 3; d++) g[0][d] = -(g[1][d] + g[2][d] + g[3][d]);
+      T s = (T)(cf * s_wsum / adet);
+      int e = 0;
+#pragma unroll
+      for (int n = 0; n < 4; n++)
+#pragma unroll
+        for (int m = n; m < 4; m++) k[e++] = s * (g[n][0] * g[m][0] + g[n][1] * g[m][1] + g[n][2] * g[m][2]);
+    } else {
+      T s = (T)(cf * adet);
+      int e = 0;
+#pragma unroll
+      for (int n = 0; n < 4; n++)
+#pragma unroll
+        for (int m = n; m < 4; m++) k[e++] = s * (T)s_mass[n * 4 + m];
+    }
+    T* K = Ke + 16 * c;
+    const int up[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
+#pragma unroll
+    for (int n = 0; n < 4; n++)
+#pragma unroll
+      for (int m = 0; m < 4; m++) K[n * 4 + m] = k[up[n][m]];
+  }
+  if (be) {
+    double sc = (scoef ? scoef[c] : 1.0) * fsrc[0] * adet;
+#pragma unroll
+    for (int n = 0; n < 4; n++) be[4 * c + n] = sc * s_load[n];
+  }
+}
+
 // element kernels per cell type / order; returns GT_OK or an error
 template <class T>
 static int elements_T(const Space* sp, int form, const double* coef, double nu, const double* tab, const TabLayout& L,
                       T* Ke, double* be, const double* f, const double* scoef, int want_matrix) {
   int ct = sp->mesh->ctype, o = sp->order;
+  if (ct == GT_TET4 && sp->ncomp == 1 && (form == GT_LAPLACE || form == GT_MASS)) {
+    Ctx* ctx = ctx_of(sp);
+    int64_t nc = sp->mesh->ncells;
+    if (form == GT_LAPLACE)
+      k_elements_p1<GT_LAPLACE, T><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
+          sp->mesh->coords, sp->mesh->cell_nodes, coef, tab, L, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
+    else
+      k_elements_p1<GT_MASS, T><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
+          sp->mesh->coords, sp->mesh->cell_nodes, coef, tab, L, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
+    GT_LAUNCH(ctx, "k_elements_p1");
+    return GT_OK;
+  }
   if (ct == GT_TET4) return dispatch_form<3, 4, 4, 4, 128, true, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
   if (ct == GT_QUAD4 && o == 1) return dispatch_form<2, 4, 4, 4, 32, false, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
   if (ct == GT_QUAD4 && o == 2) return dispatch_form<2, 4, 9, 9, 8, false, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
@@ -654,22 +865,40 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
   }
   __syncwarp(gmask);
   if (active) {
+    // lane gl owns local column node b = gl (nn <= G).  Incidences are taken
+    // U at a time: the loads of all U are issued first (independent, in
+    // flight together), then the U contributions are added in order with a
+    // group barrier between cells, which keeps the summation order fixed.
+    constexpr int U = BS == 1 ? 4 : 2;
+    const int b = gl;
     int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
-    for (int64_t k = ib; k < ie; k++) {
-      int32_t cb = inc[k];
-      int32_t c = cb / nn, a = cb - c * nn;
-      const TK* Krow = Ke + (int64_t)c * nloc * nloc + (int64_t)(a * BS) * nloc;
-      for (int b = gl; b < nn; b += G) {
-        int32_t j = cnd[(int64_t)c * nn + b];
-        if (j > 0) {
-          int p = find_col(cols, L, j - 1);
+    for (int64_t k0 = ib; k0 < ie; k0 += U) {
+      int32_t jj[U];
+      TA kv[U][BS * BS];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        jj[u] = 0;
+        int64_t k = k0 + u;
+        if (k < ie && b < nn) {
+          int32_t cb = __ldg(inc + k);
+          int32_t c = cb / nn, a = cb - c * nn;
+          jj[u] = __ldg(cnd + (int64_t)c * nn + b);
+          const TK* Krow = Ke + (int64_t)c * nloc * nloc + (int64_t)(a * BS) * nloc + b * BS;
 #pragma unroll
           for (int cc = 0; cc < BS; cc++)
 #pragma unroll
-            for (int dd = 0; dd < BS; dd++) acc[(p * BS + cc) * BS + dd] += (TA)Krow[cc * nloc + b * BS + dd];
+            for (int dd = 0; dd < BS; dd++) kv[u][cc * BS + dd] = (TA)__ldg(Krow + cc * nloc + dd);
         }
       }
-      __syncwarp(gmask);
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        if (jj[u] > 0) {
+          int p = find_col(cols, L, jj[u] - 1);
+#pragma unroll
+          for (int e = 0; e < BS * BS; e++) acc[p * BS * BS + e] += kv[u][e];
+        }
+        __syncwarp(gmask);
+      }
     }
     int64_t ob = rb * BS * BS;
     for (int i = gl; i < L * BS * BS; i += G) {
@@ -935,7 +1164,7 @@ int gt_assemble_matrix_and_vector(gt_space* sp, int form, const double* cell_coe
   A->bs = sp->ncomp;
   A->precision = precision;
   mark(ctx, "setup");
-  int s = build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc);
+  int s = build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc, false);
   mark(ctx, "incidence");
   if (s == GT_OK) s = build_pattern(A);
   if (s == GT_OK) s = numeric(A, form, cell_coef, nu, f, source_coef, b);
@@ -973,7 +1202,7 @@ int gt_assemble_vector(gt_space* sp, const double* f, const double* cell_coef, d
   if (!sp || !f || !b) return GT_ERR_INVALID;
   Ctx* ctx = sp->mesh->ctx;
   cudaSetDevice(ctx->device);
-  if (!sp->inc) GT_TRY(build_incidence(ctx, sp, &sp->inc_ptr, &sp->inc, &sp->ninc));
+  if (!sp->inc) GT_TRY(build_incidence(ctx, sp, &sp->inc_ptr, &sp->inc, &sp->ninc, true));
   int64_t nc = sp->mesh->ncells;
   DevIn<double> coef, fd;
   GT_TRY(coef.init(ctx, cell_coef, nc));

@@ -179,7 +179,8 @@ struct Matrix {
 // library-internal entry points (implemented across the .cu files)
 // ---------------------------------------------------------------------------
 int number_dofs(Space* sp, int ngroups, const int32_t* groups);
-int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc);
+// incidence lists; sort = false leaves the order to the sparsity count pass
+int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc, bool sort);
 int build_pattern(Matrix* A);
 int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision,
                      const double* f, const double* d_scoef, void* Ke, double* be, int want_matrix);

@@ -3,12 +3,16 @@
 //
 // The reference has no iterative solver (it calls an external direct solve,
 // src/problems.jl:439-462); this file is the GB300 replacement for that call.
-// Every reduction is deterministic: each CTA writes a partial sum, the last
-// CTA to finish (threadfence + counter) adds the partials in CTA order and
-// derives the CG scalars on the device, so no host round trip is needed per
-// iteration and results do not depend on scheduling or co-running work.
-// Iterations run in chunks; kernels return at once when the device-side
-// "done" flag is set, and the host polls the flag once per chunk.
+//
+// Every kernel runs one thread (vectors) or one lane group (SpMV rows) per
+// item over a full grid, so all loads of a pass are in flight at once.  Dot
+// products are reduced deterministically in two fixed levels: each CTA
+// writes its partial, the last CTA of every group of 256 CTAs (threadfence +
+// counter) sums the group in a fixed tree, and the last group sums the group
+// partials.  The CG scalars (alpha, beta, residual, iteration count, done
+// flag) live on the device, so iterations need no host round trip; the host
+// polls the done flag once per chunk of iterations.  Results are bitwise
+// reproducible and independent of co-running work.
 #include <cmath>
 #include <cstring>
 #include <type_traits>
@@ -17,15 +21,22 @@
 
 namespace gt {
 
-constexpr int RED_T = 256;      // threads per reduction CTA
-constexpr int CHUNK = 16;       // iterations between host polls
+constexpr int RED_T = 256;  // threads per CTA of the reduction kernels
+constexpr int GROUP = 256;  // CTAs per first-level reduction group
+constexpr int CHUNK = 16;   // CG iterations between host polls
 
 // device-resident CG state (one per solve)
 struct CGState {
-  double rz, rz_new, pq, rr, bb, alpha, beta;
-  double tol2;           // (rtol * ||b||)^2
+  double rz, pq, rr, bb, alpha, beta;
+  double tol2;  // (rtol * ||b||)^2
   int32_t done, iters, maxit, pad;
-  uint32_t counter[4];   // last-CTA counters
+};
+
+// reduction scratch sized for the largest grid of a solve
+struct RedBuf {
+  double* p1;     // per-CTA partials (K per CTA)
+  double* p2;     // per-group partials (K per group)
+  uint32_t* ctr;  // group counters [ngroups] + final counter; each returns to 0 after use
 };
 
 template <class T>
@@ -34,45 +45,81 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// CTA sum into partials[blockIdx.x]; returns (in every thread of the CTA)
-// whether this CTA finished last
-__device__ bool cta_partial(double v, double* partials, uint32_t* counter) {
-  __shared__ double red[RED_T / 32];
-  __shared__ bool last;
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
-    partials[blockIdx.x] = t;
-    __threadfence();
-    unsigned prev = atomicInc(counter, gridDim.x - 1);
-    last = prev == gridDim.x - 1;
+// Sums K values over the whole grid.  Returns true in every thread of the one
+// CTA that finishes last, with the totals in v; other CTAs return false.
+// A: accumulator type of the in-CTA sums (the FP32 CG sums in FP32: GB300
+// runs FP64 at 1/58 of the FP32 rate).  LEAD: only lanes that are multiples
+// of LEAD hold values, so the warp sum skips the rounds below LEAD.
+template <int K, class A = double, int LEAD = 1>
+__device__ bool reduce_last(A (&v)[K], RedBuf rb) {
+  __shared__ A sred[K][RED_T / 32];
+  __shared__ double tree[K][RED_T];
+  __shared__ int s_flag;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    A t = v[k];
+#pragma unroll
+    for (int o = 16; o >= LEAD; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) sred[k][w] = t;
   }
   __syncthreads();
-  return last;
-}
-// Sum of n partials by the whole CTA in a fixed order (strided per-thread
-// sums, then a fixed tree); every thread gets the total.
-__device__ double block_sum_partials(const double* partials, int n) {
-  __shared__ double tree[RED_T];
-  double t = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) t += ((volatile const double*)partials)[i];
-  tree[threadIdx.x] = t;
+  const unsigned nb = gridDim.x, b = blockIdx.x;
+  const unsigned ng = (nb + GROUP - 1) / GROUP, g = b / GROUP;
+  const unsigned gs = min((unsigned)GROUP, nb - g * GROUP);
+  if (tid == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      A t = (A)0;
+      for (int i = 0; i < nw; i++) t += sred[k][i];
+      rb.p1[(size_t)b * K + k] = (double)t;
+    }
+    __threadfence();
+    unsigned prev = atomicInc(&rb.ctr[g], gs - 1);
+    s_flag = prev == gs - 1;
+  }
   __syncthreads();
-  for (int o = blockDim.x >> 1; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) tree[threadIdx.x] += tree[threadIdx.x + o];
+  if (!s_flag) return false;
+#pragma unroll
+  for (int k = 0; k < K; k++) tree[k][tid] = tid < (int)gs ? __ldcg(&rb.p1[((size_t)g * GROUP + tid) * K + k]) : 0.0;
+  __syncthreads();
+  for (int o = RED_T / 2; o; o >>= 1) {
+    if (tid < o)
+#pragma unroll
+      for (int k = 0; k < K; k++) tree[k][tid] += tree[k][tid + o];
     __syncthreads();
   }
-  double r = tree[0];
+  if (tid == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) rb.p2[(size_t)g * K + k] = tree[k][0];
+    __threadfence();
+    unsigned prev = atomicInc(&rb.ctr[ng], ng - 1);
+    s_flag = prev == ng - 1;
+  }
   __syncthreads();
-  return r;
+  if (!s_flag) return false;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double t = 0.0;
+    for (unsigned i = tid; i < ng; i += RED_T) t += __ldcg(&rb.p2[(size_t)i * K + k]);
+    tree[k][tid] = t;
+  }
+  __syncthreads();
+  for (int o = RED_T / 2; o; o >>= 1) {
+    if (tid < o)
+#pragma unroll
+      for (int k = 0; k < K; k++) tree[k][tid] += tree[k][tid + o];
+    __syncthreads();
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++) v[k] = (A)tree[k][0];
+  __syncthreads();
+  return true;
 }
 
 // ---------------------------------------------------------------------------
-// SpMV: G lanes per block row, grid-stride over rows (fixed grid, so the
-// partial sums are always formed over the same row sets)
+// SpMV: G lanes per block row (whole groups stay in the shuffles; rows past
+// the end compute the last row again and write nothing)
 // ---------------------------------------------------------------------------
 template <int BS, int G, class V, class X>
 __device__ __forceinline__ void row_product(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
@@ -82,14 +129,31 @@ __device__ __forceinline__ void row_product(const int64_t* __restrict__ rowptr, 
 #pragma unroll
   for (int c = 0; c < BS; c++) acc[c] = (X)0;
   int64_t b = rowptr[r], e = rowptr[r + 1];
-  for (int64_t k = b + gl; k < e; k += G) {
-    int32_t j = colind[k];
+  // two entries per lane per trip: both index loads, then both gathers, are
+  // independent and in flight together
+  int64_t k = b + gl;
+  for (; k + G < e; k += 2 * G) {
+    int32_t j0 = __ldg(colind + k), j1 = __ldg(colind + k + G);
+    const V* b0 = val + k * BS * BS;
+    const V* b1 = val + (k + G) * BS * BS;
+#pragma unroll
+    for (int d = 0; d < BS; d++) {
+      X x0 = x[(int64_t)j0 * BS + d], x1 = x[(int64_t)j1 * BS + d];
+#pragma unroll
+      for (int c = 0; c < BS; c++) {
+        acc[c] = fma((X)__ldg(b0 + c * BS + d), x0, acc[c]);
+        acc[c] = fma((X)__ldg(b1 + c * BS + d), x1, acc[c]);
+      }
+    }
+  }
+  if (k < e) {
+    int32_t j = __ldg(colind + k);
     const V* blk = val + k * BS * BS;
 #pragma unroll
     for (int d = 0; d < BS; d++) {
       X xj = x[(int64_t)j * BS + d];
 #pragma unroll
-      for (int c = 0; c < BS; c++) acc[c] = fma((X)blk[c * BS + d], xj, acc[c]);
+      for (int c = 0; c < BS; c++) acc[c] = fma((X)__ldg(blk + c * BS + d), xj, acc[c]);
     }
   }
 #pragma unroll
@@ -105,94 +169,94 @@ template <int BS, int G, class V, class X>
 __global__ void __launch_bounds__(RED_T) k_spmv(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                                                 const V* __restrict__ val, const X* __restrict__ x, int64_t nrows,
                                                 const X* __restrict__ bsub, X* __restrict__ y) {
-  int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int gl = (int)(t0 % G);
-  int64_t stride = ((int64_t)gridDim.x * blockDim.x) / G;
-  int64_t nit = (nrows + stride - 1) / stride;  // uniform trip count keeps whole groups in the shuffles
-  for (int64_t it = 0; it < nit; it++) {
-    int64_t r = t0 / G + it * stride;
-    bool valid = r < nrows;
-    int64_t rr = valid ? r : nrows - 1;
-    X o[BS];
-    row_product<BS, G, V, X>(rowptr, colind, val, x, rr, gl, o);
-    if (gl == 0 && valid)
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t r = t / G;
+  int gl = (int)(t - r * G);
+  bool valid = r < nrows;
+  if (!valid) r = nrows - 1;
+  X o[BS];
+  row_product<BS, G, V, X>(rowptr, colind, val, x, r, gl, o);
+  if (gl == 0 && valid)
 #pragma unroll
-      for (int c = 0; c < BS; c++) y[r * BS + c] = bsub ? bsub[r * BS + c] - o[c] : o[c];
-  }
+    for (int c = 0; c < BS; c++) y[r * BS + c] = bsub ? bsub[r * BS + c] - o[c] : o[c];
 }
 
-// q = A p, partial p.q -> alpha = rz / pq in the last CTA
+// q = A p and p.q; the last CTA sets alpha = rz / pq.  Each lane group
+// handles RPG adjacent rows (independent loads in flight together; the CTA
+// reduction is amortised over more rows).
+constexpr int RPG = 2;
 template <int BS, int G, class V, class X>
 __global__ void __launch_bounds__(RED_T) k_cg_spmv(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                                                    const V* __restrict__ val, const X* __restrict__ p, X* __restrict__ q,
-                                                   int64_t nrows, CGState* st, double* partials) {
+                                                   int64_t nrows, CGState* st, RedBuf rb) {
   if (st->done) return;
-  int64_t t0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int gl = (int)(t0 % G);
-  int64_t stride = ((int64_t)gridDim.x * blockDim.x) / G;
-  int64_t nit = (nrows + stride - 1) / stride;
-  double d = 0.0;
-  for (int64_t it = 0; it < nit; it++) {
-    int64_t r = t0 / G + it * stride;
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t grp = t / G;
+  int gl = (int)(t - grp * G);
+  X v[1] = {(X)0};
+#pragma unroll
+  for (int u = 0; u < RPG; u++) {
+    int64_t r = grp * RPG + u;
     bool valid = r < nrows;
-    int64_t rr = valid ? r : nrows - 1;
+    if (!valid) r = nrows - 1;
     X o[BS];
-    row_product<BS, G, V, X>(rowptr, colind, val, p, rr, gl, o);
+    row_product<BS, G, V, X>(rowptr, colind, val, p, r, gl, o);
     if (gl == 0 && valid) {
 #pragma unroll
       for (int c = 0; c < BS; c++) {
         q[r * BS + c] = o[c];
-        d += (double)o[c] * (double)p[r * BS + c];
+        v[0] += o[c] * p[r * BS + c];
       }
     }
   }
-  if (cta_partial(d, partials, &st->counter[0])) {
-    double pq = block_sum_partials(partials, gridDim.x);
-    if (threadIdx.x == 0) {
-      st->pq = pq;
-      st->alpha = st->rz / pq;
-    }
+  if (reduce_last<1, X, G>(v, rb) && threadIdx.x == 0) {
+    st->pq = (double)v[0];
+    st->alpha = st->rz / (double)v[0];
   }
 }
 
-// x += alpha p; r -= alpha q; z = Dinv r; partial r.z and r.r
+// x += alpha p; r -= alpha q; z = Dinv r; r.z and r.r -> beta, convergence.
+// IPT elements per thread (coalesced, all loads issued before the math).
+constexpr int IPT = 4;
 template <class X>
 __global__ void __launch_bounds__(RED_T) k_cg_update(X* __restrict__ x, X* __restrict__ r, X* __restrict__ z,
                                                      const X* __restrict__ p, const X* __restrict__ q,
-                                                     const X* __restrict__ dinv, int64_t n, CGState* st,
-                                                     double* partials) {
+                                                     const X* __restrict__ dinv, int64_t n, CGState* st, RedBuf rb) {
   if (st->done) return;
-  __shared__ double red2[RED_T / 32];
-  X alpha = (X)st->alpha;
-  double rz = 0.0, rr = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    X ri = r[i] - alpha * q[i];
-    x[i] += alpha * p[i];
-    X zi = dinv[i] * ri;
-    r[i] = ri;
-    z[i] = zi;
-    rz += (double)ri * (double)zi;
-    rr += (double)ri * (double)ri;
+  const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
+  const X alpha = (X)st->alpha;
+  X rv[IPT], qv[IPT], pv[IPT], xv[IPT], dv[IPT];
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    int64_t i = base + (int64_t)j * blockDim.x;
+    bool ok = i < n;
+    rv[j] = ok ? r[i] : (X)0;
+    qv[j] = ok ? q[i] : (X)0;
+    pv[j] = ok ? p[i] : (X)0;
+    xv[j] = ok ? x[i] : (X)0;
+    dv[j] = ok ? dinv[i] : (X)0;
   }
-  // second reduction (r.r) into partials[gridDim.x + blockIdx.x]
-  rr = warp_sum(rr);
-  if ((threadIdx.x & 31) == 0) red2[threadIdx.x >> 5] = rr;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red2[w];
-    partials[gridDim.x + blockIdx.x] = t;
-  }
-  if (cta_partial(rz, partials, &st->counter[1])) {
-    double rzn = block_sum_partials(partials, gridDim.x);
-    double rrn = block_sum_partials(partials + gridDim.x, gridDim.x);
-    if (threadIdx.x == 0) {
-      st->beta = rzn / st->rz;
-      st->rz = rzn;
-      st->rr = rrn;
-      st->iters += 1;
-      if (rrn <= st->tol2 || st->iters >= st->maxit || !(rrn == rrn)) st->done = 1;
+  X v[2] = {(X)0, (X)0};
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    int64_t i = base + (int64_t)j * blockDim.x;
+    X ri = rv[j] - alpha * qv[j];
+    X zi = dv[j] * ri;
+    if (i < n) {
+      x[i] = xv[j] + alpha * pv[j];
+      r[i] = ri;
+      z[i] = zi;
     }
+    v[0] += ri * zi;
+    v[1] += ri * ri;
+  }
+  if (reduce_last<2, X>(v, rb) && threadIdx.x == 0) {
+    double rz = (double)v[0], rr = (double)v[1];
+    st->beta = rz / st->rz;
+    st->rz = rz;
+    st->rr = rr;
+    st->iters += 1;
+    if (rr <= st->tol2 || st->iters >= st->maxit || !(rr == rr)) st->done = 1;
   }
 }
 
@@ -200,9 +264,53 @@ template <class X>
 __global__ void __launch_bounds__(RED_T) k_cg_pupdate(X* __restrict__ p, const X* __restrict__ z, int64_t n,
                                                       const CGState* st) {
   if (st->done) return;
-  X beta = (X)st->beta;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    p[i] = z[i] + beta * p[i];
+  const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
+  const X beta = (X)st->beta;
+  X zv[IPT], pv[IPT];
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    int64_t i = base + (int64_t)j * blockDim.x;
+    zv[j] = i < n ? z[i] : (X)0;
+    pv[j] = i < n ? p[i] : (X)0;
+  }
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    int64_t i = base + (int64_t)j * blockDim.x;
+    if (i < n) p[i] = zv[j] + beta * pv[j];
+  }
+}
+
+// CG start: z = Dinv r; p = z; r.z and r.r; tolerance from ||b||^2 (or ||r0||^2)
+template <class X>
+__global__ void __launch_bounds__(RED_T) k_cg_init(const X* __restrict__ r, X* __restrict__ z, X* __restrict__ p,
+                                                   const X* __restrict__ dinv, int64_t n, CGState* st, RedBuf rb,
+                                                   double rtol2, const double* bb_dev) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double v[2] = {0.0, 0.0};
+  if (i < n) {
+    X zi = dinv[i] * r[i];
+    z[i] = zi;
+    p[i] = zi;
+    v[0] = (double)r[i] * (double)zi;
+    v[1] = (double)r[i] * (double)r[i];
+  }
+  if (reduce_last<2>(v, rb) && threadIdx.x == 0) {
+    st->rz = v[0];
+    st->rr = v[1];
+    double ref = bb_dev ? *bb_dev : v[1];
+    st->bb = ref;
+    st->tol2 = rtol2 * ref;
+    st->iters = 0;
+    st->beta = 0.0;
+    st->done = (v[1] <= st->tol2) || v[1] == 0.0;
+  }
+}
+
+template <class X>
+__global__ void __launch_bounds__(RED_T) k_norm2(const X* __restrict__ x, int64_t n, double* out, RedBuf rb) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  double v[1] = {i < n ? (double)x[i] * (double)x[i] : 0.0};
+  if (reduce_last<1>(v, rb) && threadIdx.x == 0) *out = v[0];
 }
 
 // Jacobi: dinv = 1 / diag(A) (per scalar row)
@@ -216,140 +324,123 @@ __global__ void k_dinv(const int64_t* rowptr, const int32_t* diag_pos, const V* 
   dinv[t] = (X)(1.0 / (double)val[k * BS * BS + c * BS + c]);
 }
 
-// CG start: z = Dinv r; p = z; partial r.z, r.r, b.b
-template <class X>
-__global__ void __launch_bounds__(RED_T) k_cg_init(const X* __restrict__ r, X* __restrict__ z, X* __restrict__ p,
-                                                   const X* __restrict__ dinv, int64_t n, CGState* st,
-                                                   double* partials, double rtol2, const double* bb_dev) {
-  __shared__ double red2[RED_T / 32];
-  double rz = 0.0, rr = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    X zi = dinv[i] * r[i];
-    z[i] = zi;
-    p[i] = zi;
-    rz += (double)r[i] * (double)zi;
-    rr += (double)r[i] * (double)r[i];
-  }
-  rr = warp_sum(rr);
-  if ((threadIdx.x & 31) == 0) red2[threadIdx.x >> 5] = rr;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red2[w];
-    partials[gridDim.x + blockIdx.x] = t;
-  }
-  if (cta_partial(rz, partials, &st->counter[2])) {
-    double rzs = block_sum_partials(partials, gridDim.x);
-    double rrs = block_sum_partials(partials + gridDim.x, gridDim.x);
-    if (threadIdx.x != 0) return;
-    st->rz = rzs;
-    st->rr = rrs;
-    double ref = bb_dev ? *bb_dev : rrs;
-    st->bb = ref;
-    st->tol2 = rtol2 * ref;
-    st->iters = 0;
-    st->beta = 0.0;
-    st->done = (rrs <= st->tol2) || rrs == 0.0;
-  }
-}
-
-// deterministic norm^2 of a vector (one launch, last CTA finalises)
-template <class X>
-__global__ void __launch_bounds__(RED_T) k_norm2(const X* __restrict__ v, int64_t n, double* out, double* partials,
-                                                 uint32_t* counter) {
-  double s = 0.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    s += (double)v[i] * (double)v[i];
-  if (cta_partial(s, partials, counter)) {
-    double t = block_sum_partials(partials, gridDim.x);
-    if (threadIdx.x == 0) *out = t;
-  }
-}
-
-// mixed precision helpers
+// mixed precision helpers: rf = r / ||r|| (FP32), x += ||r|| d
 __global__ void k_scale_to_f32(const double* r, int64_t n, const double* norm2, float* out) {
   double sc = *norm2 > 0.0 ? 1.0 / sqrt(*norm2) : 1.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = (float)(r[i] * sc);
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)(r[i] * sc);
 }
 __global__ void k_add_scaled_f32(double* x, const float* d, int64_t n, const double* norm2) {
   double sc = *norm2 > 0.0 ? sqrt(*norm2) : 1.0;
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    x[i] += sc * (double)d[i];
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) x[i] += sc * (double)d[i];
 }
-__global__ void k_set_scalar(double* d, double v) { *d = v; }
+__global__ void k_copy_f64_to_f32(const double* a, int64_t n, float* out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)a[i];
+}
+__global__ void k_copy_f32_to_f64(const float* a, int64_t n, double* out) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (double)a[i];
+}
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+// lanes per block row: about 4 entries per lane, so that many rows are in
+// flight per SM (the SpMV is latency-bound with one entry per lane)
 static int pick_group(const Matrix* A) {
   double avg = A->nbrows > 0 ? (double)A->bnnz / (double)A->nbrows : 1.0;
-  if (avg <= 6) return 4;
-  if (avg <= 12) return 8;
-  if (avg <= 24) return 16;
+  if (avg <= 16) return 4;
+  if (avg <= 32) return 8;
+  if (avg <= 64) return 16;
   return 32;
 }
-
-static unsigned spmv_grid(Ctx* ctx, const Matrix* A) {
-  int G = pick_group(A);
-  int64_t g = (A->nbrows * G + RED_T - 1) / RED_T;
-  int64_t cap = (int64_t)ctx->num_sms * 8;
-  if (g > cap) g = cap;
+static unsigned spmv_grid(const Matrix* A) {
+  int64_t g = (A->nbrows * pick_group(A) + RED_T - 1) / RED_T;
   return (unsigned)(g > 0 ? g : 1);
 }
-static unsigned vec_grid(Ctx* ctx, int64_t n) {
+static unsigned cg_spmv_grid(const Matrix* A) {
+  int64_t groups = (A->nbrows + RPG - 1) / RPG;
+  int64_t g = (groups * pick_group(A) + RED_T - 1) / RED_T;
+  return (unsigned)(g > 0 ? g : 1);
+}
+static unsigned ipt_grid(int64_t n) {
+  int64_t g = (n + (int64_t)RED_T * IPT - 1) / ((int64_t)RED_T * IPT);
+  return (unsigned)(g > 0 ? g : 1);
+}
+static unsigned vec_grid(int64_t n) {
   int64_t g = (n + RED_T - 1) / RED_T;
-  int64_t cap = (int64_t)ctx->num_sms * 8;
-  if (g > cap) g = cap;
   return (unsigned)(g > 0 ? g : 1);
 }
+
+struct Scratch {
+  Ctx* ctx = nullptr;
+  RedBuf rb{};
+  int alloc(Ctx* c, unsigned max_grid) {
+    ctx = c;
+    unsigned ng = (max_grid + GROUP - 1) / GROUP;
+    GT_TRY(dalloc(c, &rb.p1, (int64_t)max_grid * 2 + 2));
+    GT_TRY(dalloc(c, &rb.p2, (int64_t)ng * 2 + 2));
+    GT_TRY(dalloc(c, &rb.ctr, (int64_t)ng + 2));
+    GT_CUDA(c, cudaMemsetAsync(rb.ctr, 0, sizeof(uint32_t) * (ng + 2), c->stream));
+    return GT_OK;
+  }
+  ~Scratch() {
+    if (ctx) {
+      dfree(ctx, rb.p1);
+      dfree(ctx, rb.p2);
+      dfree(ctx, rb.ctr);
+    }
+  }
+};
 
 template <class V, class X>
 struct Ops {
-  static int spmv(Ctx* ctx, const Matrix* A, const V* val, const X* x, const X* bsub, X* y) {
-    int G = pick_group(A);
-    unsigned grid = spmv_grid(ctx, A);
-    auto go = [&](auto bs_t, auto g_t) {
-      constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
-      k_spmv<BS, GG, V, X><<<GT_KC(ctx, grid), RED_T, 0, ctx->stream>>>(A->rowptr, A->colind, val, x, A->nbrows, bsub, y);
-    };
-    dispatch(A->bs, G, go);
-    GT_LAUNCH(ctx, "k_spmv");
-    return GT_OK;
-  }
-  static int cg_spmv(Ctx* ctx, const Matrix* A, const V* val, const X* p, X* q, CGState* st, double* partials) {
-    int G = pick_group(A);
-    unsigned grid = spmv_grid(ctx, A);
-    auto go = [&](auto bs_t, auto g_t) {
-      constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
-      k_cg_spmv<BS, GG, V, X><<<GT_KC(ctx, grid), RED_T, 0, ctx->stream>>>(A->rowptr, A->colind, val, p, q, A->nbrows, st, partials);
-    };
-    dispatch(A->bs, G, go);
-    GT_LAUNCH(ctx, "k_cg_spmv");
-    return GT_OK;
-  }
   template <class F>
   static void dispatch(int bs, int G, F&& go) {
     using I1 = std::integral_constant<int, 1>;
     using I2 = std::integral_constant<int, 2>;
     using I3 = std::integral_constant<int, 3>;
-    using G4 = std::integral_constant<int, 4>;
-    using G8 = std::integral_constant<int, 8>;
-    using G16 = std::integral_constant<int, 16>;
-    using G32 = std::integral_constant<int, 32>;
     auto byg = [&](auto bst) {
-      if (G == 4) go(bst, G4());
-      else if (G == 8) go(bst, G8());
-      else if (G == 16) go(bst, G16());
-      else go(bst, G32());
+      if (G == 4) go(bst, std::integral_constant<int, 4>());
+      else if (G == 8) go(bst, std::integral_constant<int, 8>());
+      else if (G == 16) go(bst, std::integral_constant<int, 16>());
+      else go(bst, std::integral_constant<int, 32>());
     };
     if (bs == 1) byg(I1());
     else if (bs == 2) byg(I2());
     else byg(I3());
   }
+  static int spmv(Ctx* ctx, const Matrix* A, const V* val, const X* x, const X* bsub, X* y) {
+    unsigned grid = spmv_grid(A);
+    dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
+      constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
+      k_spmv<BS, GG, V, X><<<GT_KC(ctx, grid), RED_T, 0, ctx->stream>>>(A->rowptr, A->colind, val, x, A->nbrows, bsub, y);
+    });
+    GT_LAUNCH(ctx, "k_spmv");
+    return GT_OK;
+  }
+  static int cg_spmv(Ctx* ctx, const Matrix* A, const V* val, const X* p, X* q, CGState* st, RedBuf rb) {
+    unsigned grid = cg_spmv_grid(A);
+    dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
+      constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
+      k_cg_spmv<BS, GG, V, X><<<GT_KC(ctx, grid), RED_T, 0, ctx->stream>>>(A->rowptr, A->colind, val, p, q, A->nbrows, st, rb);
+    });
+    GT_LAUNCH(ctx, "k_cg_spmv");
+    return GT_OK;
+  }
 };
 
+template <class X>
+static int norm2(Ctx* ctx, const X* v, int64_t n, double* out_dev, RedBuf rb) {
+  k_norm2<X><<<GT_KC(ctx, vec_grid(n)), RED_T, 0, ctx->stream>>>(v, n, out_dev, rb);
+  GT_LAUNCH(ctx, "k_norm2");
+  return GT_OK;
+}
+
 // PCG on A (values val) for A x = b; x holds the start value.  Vectors in X.
+// The tolerance is relative to *bb_dev (||b||^2) or, if NULL, to ||r0||^2.
 template <class V, class X>
 static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit, const double* bb_dev,
                int32_t* iters_out, double* rr_out, double* bb_out) {
@@ -358,70 +449,77 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
   int64_t n = A->nbrows * A->bs;
   X *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
   CGState* st = nullptr;
-  double* partials = nullptr;
-  unsigned gs = spmv_grid(ctx, A), gv = vec_grid(ctx, n);
-  unsigned gmax = gs > gv ? gs : gv;
+  unsigned gs = cg_spmv_grid(A), gv = vec_grid(n), gi = ipt_grid(n);
+  Scratch sc;
+  GT_TRY(sc.alloc(ctx, gs > gv ? gs : gv));
   GT_TRY(dalloc(ctx, &r, n));
   GT_TRY(dalloc(ctx, &z, n));
   GT_TRY(dalloc(ctx, &p, n));
   GT_TRY(dalloc(ctx, &q, n));
   GT_TRY(dalloc(ctx, &dinv, n));
   GT_TRY(dalloc(ctx, (unsigned char**)&st, sizeof(CGState)));
-  GT_TRY(dalloc(ctx, &partials, 2 * (int64_t)gmax + 2));
-  GT_CUDA(ctx, cudaMemsetAsync(st, 0, sizeof(CGState), s));
   CGState h0{};
   h0.maxit = maxit;
-  GT_CUDA(ctx, cudaMemcpyAsync(&st->maxit, &h0.maxit, sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  GT_CUDA(ctx, cudaMemcpyAsync(st, &h0, sizeof(CGState), cudaMemcpyHostToDevice, s));
   GT_TRY(find_diag(A));
   if (A->bs == 1) k_dinv<1, V, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
   else if (A->bs == 2) k_dinv<2, V, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
   else k_dinv<3, V, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
   GT_LAUNCH(ctx, "k_dinv");
-  // r = b - A x
-  GT_TRY((Ops<V, X>::spmv(ctx, A, val, x, b, r)));
-  k_cg_init<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(r, z, p, dinv, n, st, partials, rtol * rtol, bb_dev);
+  GT_TRY((Ops<V, X>::spmv(ctx, A, val, x, b, r)));  // r = b - A x
+  k_cg_init<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(r, z, p, dinv, n, st, sc.rb, rtol * rtol, bb_dev);
   GT_LAUNCH(ctx, "k_cg_init");
-  int status = GT_OK;
+  CGState h{};
   for (int it = 0; it < maxit; it += CHUNK) {
     for (int k = 0; k < CHUNK; k++) {
-      GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, partials)));
-      k_cg_update<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(x, r, z, p, q, dinv, n, st, partials);
-      k_cg_pupdate<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(p, z, n, st);
+      GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb)));
+      k_cg_update<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(x, r, z, p, q, dinv, n, st, sc.rb);
+      k_cg_pupdate<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(p, z, n, st);
     }
     GT_LAUNCH(ctx, "cg iteration");
     GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
     GT_CUDA(ctx, cudaStreamSynchronize(s));
-    CGState h;
     memcpy(&h, ctx->h_dscratch, sizeof(CGState));
     if (h.done) break;
   }
-  CGState h;
-  memcpy(&h, ctx->h_dscratch, sizeof(CGState));
   *iters_out = h.iters;
   *rr_out = h.rr;
   *bb_out = h.bb;
-  if (!(h.rr <= h.tol2)) status = GT_ERR_NOT_CONVERGED;
+  int status = (h.rr <= h.tol2) ? GT_OK : GT_ERR_NOT_CONVERGED;
   dfree(ctx, r);
   dfree(ctx, z);
   dfree(ctx, p);
   dfree(ctx, q);
   dfree(ctx, dinv);
   pool_free(ctx, st);
-  dfree(ctx, partials);
   return status;
-}
-
-static int norm2(Ctx* ctx, const double* v, int64_t n, double* out_dev, double* partials, uint32_t* counter) {
-  unsigned g = vec_grid(ctx, n);
-  k_norm2<double><<<GT_KC(ctx, g), RED_T, 0, ctx->stream>>>(v, n, out_dev, partials, counter);
-  GT_LAUNCH(ctx, "k_norm2");
-  return GT_OK;
 }
 
 int spmv64(Matrix* A, const double* x, double* y) {
   Ctx* ctx = A->space->mesh->ctx;
   if (!A->val64) return set_error(ctx, GT_ERR_INVALID, "matrix has no FP64 values");
   return Ops<double, double>::spmv(ctx, A, A->val64, x, nullptr, y);
+}
+
+// ||b - A x|| / ||b|| in FP64
+static int true_residual(Matrix* A, const double* b, const double* x, double* relres) {
+  Ctx* ctx = A->space->mesh->ctx;
+  int64_t n = A->nbrows * A->bs;
+  double *r = nullptr, *scal = nullptr;
+  Scratch sc;
+  GT_TRY(sc.alloc(ctx, vec_grid(n)));
+  GT_TRY(dalloc(ctx, &r, n));
+  GT_TRY(dalloc(ctx, &scal, 2));
+  GT_TRY((Ops<double, double>::spmv(ctx, A, A->val64, x, b, r)));
+  GT_TRY(norm2(ctx, (const double*)r, n, scal, sc.rb));
+  GT_TRY(norm2(ctx, b, n, scal + 1, sc.rb));
+  GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  double rn2 = ctx->h_dscratch[0], bn2 = ctx->h_dscratch[1];
+  *relres = bn2 > 0 ? sqrt(rn2 / bn2) : 0.0;
+  dfree(ctx, r);
+  dfree(ctx, scal);
+  return GT_OK;
 }
 
 int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mode, gt_solve_info* info) {
@@ -434,82 +532,71 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
     if (info) *info = inf;
     return GT_OK;
   }
+  unsigned gv = vec_grid(n);
   if (mode == GT_SOLVE_FP64) {
     if (!A->val64) return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_FP64 needs FP64 values (assemble with GT_FP64 or GT_MIXED)");
     int32_t it = 0;
-    double rr = 0, bb = 0;
-    double *bbd = nullptr, *partials = nullptr;
-    uint32_t* counter = nullptr;
-    unsigned g = vec_grid(ctx, n);
+    double rr = 0, bb = 0, *bbd = nullptr;
+    Scratch sc;
+    GT_TRY(sc.alloc(ctx, gv));
     GT_TRY(dalloc(ctx, &bbd, 1));
-    GT_TRY(dalloc(ctx, &partials, (int64_t)g + 2));
-    GT_TRY(dalloc(ctx, &counter, 4));
-    GT_CUDA(ctx, cudaMemsetAsync(counter, 0, 4 * sizeof(uint32_t), s));
-    GT_TRY(norm2(ctx, b, n, bbd, partials, counter));
+    GT_TRY(norm2(ctx, b, n, bbd, sc.rb));
     status = pcg<double, double>(A, A->val64, b, x, rtol, maxit, bbd, &it, &rr, &bb);
     dfree(ctx, bbd);
-    dfree(ctx, partials);
-    dfree(ctx, counter);
     inf.iterations = it;
-    inf.rel_residual = bb > 0 ? sqrt(rr / bb) : 0.0;
-    // the recurrence residual can drift from the true one; report b - A x
+    GT_TRY(true_residual(A, b, x, &inf.rel_residual));
   } else if (mode == GT_SOLVE_FP32) {
     if (!A->val32) return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_FP32 needs FP32 values (GT_FP32 or GT_MIXED)");
     float *bf = nullptr, *xf = nullptr;
     GT_TRY(dalloc(ctx, &bf, n));
     GT_TRY(dalloc(ctx, &xf, n));
-    double* one = nullptr;
-    GT_TRY(dalloc(ctx, &one, 1));
-    k_set_scalar<<<GT_KC(ctx, 1), 1, 0, s>>>(one, 1.0);
-    k_scale_to_f32<<<GT_KC(ctx, vec_grid(ctx, n)), RED_T, 0, s>>>(b, n, one, bf);
-    k_scale_to_f32<<<GT_KC(ctx, vec_grid(ctx, n)), RED_T, 0, s>>>(x, n, one, xf);
+    k_copy_f64_to_f32<<<GT_KC(ctx, gv), RED_T, 0, s>>>(b, n, bf);
+    k_copy_f64_to_f32<<<GT_KC(ctx, gv), RED_T, 0, s>>>(x, n, xf);
+    GT_LAUNCH(ctx, "k_copy_f64_to_f32");
     int32_t it = 0;
     double rr = 0, bb = 0;
     status = pcg<float, float>(A, A->val32, bf, xf, rtol, maxit, nullptr, &it, &rr, &bb);
-    GT_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-    k_add_scaled_f32<<<GT_KC(ctx, vec_grid(ctx, n)), RED_T, 0, s>>>(x, xf, n, one);
+    k_copy_f32_to_f64<<<GT_KC(ctx, gv), RED_T, 0, s>>>(xf, n, x);
+    GT_LAUNCH(ctx, "k_copy_f32_to_f64");
     inf.iterations = it;
+    inf.rel_residual = bb > 0 ? sqrt(rr / bb) : 0.0;
+    if (A->val64) GT_TRY(true_residual(A, b, x, &inf.rel_residual));
     dfree(ctx, bf);
     dfree(ctx, xf);
-    dfree(ctx, one);
   } else if (mode == GT_SOLVE_IR) {
     if (!A->val64 || !A->val32) return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_IR needs GT_MIXED values");
-    double *r = nullptr, *scal = nullptr, *partials = nullptr;
+    double *r = nullptr, *scal = nullptr;
     float *rf = nullptr, *df = nullptr;
-    uint32_t* counter = nullptr;
-    unsigned g = vec_grid(ctx, n);
+    Scratch sc;
+    GT_TRY(sc.alloc(ctx, gv));
     GT_TRY(dalloc(ctx, &r, n));
     GT_TRY(dalloc(ctx, &rf, n));
     GT_TRY(dalloc(ctx, &df, n));
     GT_TRY(dalloc(ctx, &scal, 4));
-    GT_TRY(dalloc(ctx, &partials, (int64_t)g + 2));
-    GT_TRY(dalloc(ctx, &counter, 4));
-    GT_CUDA(ctx, cudaMemsetAsync(counter, 0, 4 * sizeof(uint32_t), s));
-    GT_TRY(norm2(ctx, b, n, scal + 1, partials, counter));  // ||b||^2
-    double inner_tol = 1e-5;
+    GT_TRY(norm2(ctx, b, n, scal + 1, sc.rb));  // ||b||^2
+    const double inner_tol = 1e-5;
     int outer = 0, total_inner = 0;
     double relres = 1.0;
     status = GT_ERR_NOT_CONVERGED;
     for (outer = 0; outer < 60; outer++) {
       GT_TRY((Ops<double, double>::spmv(ctx, A, A->val64, x, b, r)));  // r = b - A x (FP64)
-      GT_TRY(norm2(ctx, r, n, scal, partials, counter));
+      GT_TRY(norm2(ctx, (const double*)r, n, scal, sc.rb));
       GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
       GT_CUDA(ctx, cudaStreamSynchronize(s));
       double rn2 = ctx->h_dscratch[0], bn2 = ctx->h_dscratch[1];
       relres = bn2 > 0 ? sqrt(rn2 / bn2) : 0.0;
       if (relres <= rtol) { status = GT_OK; break; }
       if (total_inner >= maxit) break;
-      // inner: A32 d = r / ||r||, from d = 0, to inner_tol
-      k_scale_to_f32<<<GT_KC(ctx, g), RED_T, 0, s>>>(r, n, scal, rf);
+      // inner: A32 d = r / ||r||, from d = 0
+      k_scale_to_f32<<<GT_KC(ctx, gv), RED_T, 0, s>>>(r, n, scal, rf);
       GT_CUDA(ctx, cudaMemsetAsync(df, 0, sizeof(float) * n, s));
       int32_t it = 0;
       double rr = 0, bb = 0;
       double tol_here = inner_tol;
       if (relres * 1e-3 < rtol) tol_here = fmax(inner_tol, 0.5 * rtol / relres);
-      int st2 = pcg<float, float>(A, A->val32, rf, df, tol_here, maxit - total_inner, nullptr, &it, &rr, &bb);
-      (void)st2;  // a stalled inner solve still improves x; the outer test decides
-      total_inner += it;
-      k_add_scaled_f32<<<GT_KC(ctx, g), RED_T, 0, s>>>(x, df, n, scal);
+      pcg<float, float>(A, A->val32, rf, df, tol_here, maxit - total_inner, nullptr, &it, &rr, &bb);
+      total_inner += it;  // a stalled inner solve still improves x; the outer test decides
+      k_add_scaled_f32<<<GT_KC(ctx, gv), RED_T, 0, s>>>(x, df, n, scal);
       GT_LAUNCH(ctx, "refinement update");
     }
     inf.iterations = total_inner;
@@ -519,34 +606,8 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
     dfree(ctx, rf);
     dfree(ctx, df);
     dfree(ctx, scal);
-    dfree(ctx, partials);
-    dfree(ctx, counter);
   } else {
     return set_error(ctx, GT_ERR_INVALID, "unknown solve mode");
-  }
-  if (mode != GT_SOLVE_IR) {
-    // true FP64 residual of the returned x
-    if (A->val64) {
-      double *r = nullptr, *scal = nullptr, *partials = nullptr;
-      uint32_t* counter = nullptr;
-      unsigned g = vec_grid(ctx, n);
-      GT_TRY(dalloc(ctx, &r, n));
-      GT_TRY(dalloc(ctx, &scal, 2));
-      GT_TRY(dalloc(ctx, &partials, (int64_t)g + 2));
-      GT_TRY(dalloc(ctx, &counter, 4));
-      GT_CUDA(ctx, cudaMemsetAsync(counter, 0, 4 * sizeof(uint32_t), s));
-      GT_TRY((Ops<double, double>::spmv(ctx, A, A->val64, x, b, r)));
-      GT_TRY(norm2(ctx, r, n, scal, partials, counter));
-      GT_TRY(norm2(ctx, b, n, scal + 1, partials, counter));
-      GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-      GT_CUDA(ctx, cudaStreamSynchronize(s));
-      double rn2 = ctx->h_dscratch[0], bn2 = ctx->h_dscratch[1];
-      inf.rel_residual = bn2 > 0 ? sqrt(rn2 / bn2) : 0.0;
-      dfree(ctx, r);
-      dfree(ctx, scal);
-      dfree(ctx, partials);
-      dfree(ctx, counter);
-    }
   }
   if (info) *info = inf;
   if (status == GT_ERR_NOT_CONVERGED) set_error(ctx, status, "solver did not reach the tolerance within maxit");
@@ -564,7 +625,6 @@ int gt_solve(gt_matrix* A, const double* b, double* x, double rtol, int maxit, i
   Ctx* ctx = A->space->mesh->ctx;
   cudaSetDevice(ctx->device);
   int64_t n = A->nbrows * A->bs;
-  // stage host vectors
   cudaPointerAttributes ab{}, ax{};
   bool bdev = cudaPointerGetAttributes(&ab, b) == cudaSuccess && ab.type == cudaMemoryTypeDevice;
   cudaGetLastError();
@@ -605,7 +665,7 @@ int gt_spmv(gt_matrix* A, const double* x, double* y) {
     GT_TRY(copy_in(ctx, xd, x, n));
   }
   if (!ydev) GT_TRY(dalloc(ctx, &yd, n));
-  int s = spmv64(A, xd, yd);
+  int s = n > 0 ? spmv64(A, xd, yd) : GT_OK;
   if (s == GT_OK && !ydev) s = copy_out(ctx, y, yd, n);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (s == GT_OK && e != cudaSuccess) s = check_cuda(ctx, e, "gt_spmv");
