@@ -953,6 +953,400 @@ int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precisio
   return launch_scatter<3, double, double>(A, K, v64, v32);
 }
 
+// ---------------------------------------------------------------------------
+// Sum-factorised path for affine quadrilaterals / hexahedra (Q1, Q2).
+// On an affine cell J is constant, so with tensor-product shape functions
+// and tensor Gauss quadrature the reference's quadrature sum factorises:
+//   sum_q w_q dV gradref_n[k] gradref_m[l] = |det J| prod_e F_e(n_e, m_e)
+// with F_e one of the 1-D matrices M = sum w L_i L_j, Dm = sum w L'_i L_j,
+// Kd = sum w L'_i L'_j (Kd on e = k = l, Dm on e = k, Dm^T on e = l, else M).
+// The physical gradients are J^-T gradref, so an element-matrix block is a
+// few products of 1-D entries and the per-cell J^-1 -- cheap enough to
+// compute inside the row-owner scatter for every (row, cell, column node),
+// so no element matrix ever goes through HBM.
+//   k_geom_affine: FP64 J, det, J^-1 per cell (+ the load vector), affinity
+//                  check; stores G[c] = {J^-1 or the metric J^-1 J^-T, scale}
+//   k_scatter_kron: like k_scatter, with blocks computed from G and the
+//                  1-D tables instead of read from Ke
+// ---------------------------------------------------------------------------
+constexpr int GSTRIDE = 10;  // per-cell geometry record: 9 + 1 values
+
+__device__ void lagrange_table_1d(int order, double* M, double* Dm, double* Kd, double* m1) {
+  int n1 = order + 1;
+  double g[3], gw[3];
+  if (n1 == 2) {
+    double s = 0.5 / sqrt(3.0);
+    g[0] = 0.5 - s; g[1] = 0.5 + s; gw[0] = gw[1] = 0.5;
+  } else {
+    double s = 0.5 * sqrt(0.6);
+    g[0] = 0.5 - s; g[1] = 0.5; g[2] = 0.5 + s;
+    gw[0] = 5.0 / 18.0; gw[1] = 8.0 / 18.0; gw[2] = 5.0 / 18.0;
+  }
+  for (int i = 0; i < 9; i++) M[i] = Dm[i] = Kd[i] = 0.0;
+  for (int i = 0; i < 3; i++) m1[i] = 0.0;
+  for (int q = 0; q < n1; q++) {
+    double v[3], dv[3];
+    lagrange1d(order, g[q], v, dv);
+    for (int i = 0; i < n1; i++) {
+      m1[i] += gw[q] * v[i];
+      for (int j = 0; j < n1; j++) {
+        M[i * 3 + j] += gw[q] * v[i] * v[j];
+        Dm[i * 3 + j] += gw[q] * dv[i] * v[j];
+        Kd[i * 3 + j] += gw[q] * dv[i] * dv[j];
+      }
+    }
+  }
+}
+
+template <int D, int NV>
+__global__ void __launch_bounds__(256) k_geom_affine(const double* __restrict__ coords,
+                                                     const int32_t* __restrict__ cell_nodes,
+                                                     const double* __restrict__ coef, int form, int order,
+                                                     int64_t ncells, int nn, int bs, void* __restrict__ Gout, int g64,
+                                                     double* __restrict__ be, const double* __restrict__ fsrc,
+                                                     const double* __restrict__ scoef, uint32_t* nonaffine,
+                                                     uint32_t* err) {
+  __shared__ double s_m1[3];
+  if (threadIdx.x == 0) {
+    double M[9], Dm[9], Kd[9];
+    lagrange_table_1d(order, M, Dm, Kd, s_m1);
+  }
+  __syncthreads();
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  double x[NV][D];
+#pragma unroll
+  for (int n = 0; n < NV; n++) {
+    const double* p = coords + (int64_t)cell_nodes[c * NV + n] * D;
+#pragma unroll
+    for (int d = 0; d < D; d++) x[n][d] = p[d];
+  }
+  double J[D][D], scale = 0.0;
+#pragma unroll
+  for (int i = 0; i < D; i++)
+#pragma unroll
+    for (int d = 0; d < D; d++) J[i][d] = x[1 << d][i] - x[0][i];
+  // affine iff every node is x0 + sum_d bit_d(n) J[:, d]
+  double hmax = 0.0;
+#pragma unroll
+  for (int i = 0; i < D; i++)
+#pragma unroll
+    for (int d = 0; d < D; d++) hmax = fmax(hmax, fabs(J[i][d]));
+  bool affine = true;
+#pragma unroll
+  for (int n = 3; n < NV; n++) {
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      double pred = x[0][i];
+#pragma unroll
+      for (int d = 0; d < D; d++)
+        if ((n >> d) & 1) pred += J[i][d];
+      if (fabs(x[n][i] - pred) > 1e-13 * hmax) affine = false;
+    }
+  }
+  if (!affine) atomicOr(nonaffine, 1u);
+  double inv[D][D], det;
+  if (D == 2) {
+    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    double r = 1.0 / det;
+    inv[0][0] = J[1][1] * r; inv[0][1] = -J[0][1] * r;
+    inv[1][0] = -J[1][0] * r; inv[1][1] = J[0][0] * r;
+  } else {
+    double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    double r = 1.0 / det;
+    inv[0][0] = c00 * r; inv[1][0] = c01 * r; inv[2][0] = c02 * r;
+    inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+    inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+    inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+    inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+    inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+    inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+  }
+  if (!(det != 0.0)) atomicOr(err, DEV_ERR_DEGENERATE);
+  double adet = fabs(det);
+  double gv[GSTRIDE];
+#pragma unroll
+  for (int i = 0; i < GSTRIDE; i++) gv[i] = 0.0;
+  if (form == GT_LAPLACE) {
+    // metric Gm[k][l] = sum_c J^-1[k][c] J^-1[l][c]
+#pragma unroll
+    for (int k = 0; k < D; k++)
+#pragma unroll
+      for (int l = 0; l < D; l++) {
+        double s = 0.0;
+#pragma unroll
+        for (int cc = 0; cc < D; cc++) s += inv[k][cc] * inv[l][cc];
+        gv[k * D + l] = s;
+      }
+  } else {
+#pragma unroll
+    for (int k = 0; k < D; k++)
+#pragma unroll
+      for (int l = 0; l < D; l++) gv[k * D + l] = inv[k][l];
+  }
+  scale = adet * (coef ? coef[c] : 1.0);
+  gv[GSTRIDE - 1] = scale;
+  if (g64) {
+    double* G = (double*)Gout + c * GSTRIDE;
+#pragma unroll
+    for (int i = 0; i < GSTRIDE; i++) G[i] = gv[i];
+  } else {
+    float* G = (float*)Gout + c * GSTRIDE;
+#pragma unroll
+    for (int i = 0; i < GSTRIDE; i++) G[i] = (float)gv[i];
+  }
+  if (be) {
+    int m1 = order + 1;
+    double sc = (scoef ? scoef[c] : 1.0) * adet;
+    for (int n = 0; n < nn; n++) {
+      int e0 = n % m1, e1 = (n / m1) % m1, e2 = n / (m1 * m1);
+      double w = s_m1[e0] * s_m1[e1] * (D == 3 ? s_m1[e2] : 1.0);
+      for (int k = 0; k < bs; k++) be[(c * nn + n) * bs + k] = sc * fsrc[k] * w;
+    }
+  }
+}
+
+// one BSxBS block (row node with 1-D indices na, column node nb) of an
+// affine cell from its geometry record g and the 1-D tables
+template <int D, int BS, int FORM, class T>
+__device__ __forceinline__ void kron_block(const int* na, const int* nb, const T* g, const T* M, const T* Dm,
+                                           const T* Kd, T lamf, T muf, T (&blk)[BS][BS]) {
+  const T scale = g[GSTRIDE - 1];
+  if constexpr (FORM == GT_MASS) {
+    T v = scale;
+#pragma unroll
+    for (int e = 0; e < D; e++) v *= M[na[e] * 3 + nb[e]];
+#pragma unroll
+    for (int a = 0; a < BS; a++)
+#pragma unroll
+      for (int b = 0; b < BS; b++) blk[a][b] = a == b ? v : (T)0;
+  } else {
+  // reference integrals I[k][l] = prod_e F_e
+  T I[D][D];
+#pragma unroll
+  for (int k = 0; k < D; k++)
+#pragma unroll
+    for (int l = 0; l < D; l++) {
+      T v = (T)1;
+#pragma unroll
+      for (int e = 0; e < D; e++) {
+        int i = na[e], j = nb[e];
+        T f = (e == k && e == l) ? Kd[i * 3 + j] : (e == k) ? Dm[i * 3 + j] : (e == l) ? Dm[j * 3 + i] : M[i * 3 + j];
+        v *= f;
+      }
+      I[k][l] = v;
+    }
+  if constexpr (FORM == GT_LAPLACE) {
+    T s = (T)0;
+#pragma unroll
+    for (int k = 0; k < D; k++)
+#pragma unroll
+      for (int l = 0; l < D; l++) s += g[k * D + l] * I[k][l];
+    s *= scale;
+#pragma unroll
+    for (int a = 0; a < BS; a++)
+#pragma unroll
+      for (int b = 0; b < BS; b++) blk[a][b] = a == b ? s : (T)0;
+  } else {
+  // elasticity: A[c][d] = scale sum_kl J^-1[k][c] J^-1[l][d] I[k][l]
+  T t1[D][D], A[D][D];
+#pragma unroll
+  for (int k = 0; k < D; k++)
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+      T s = (T)0;
+#pragma unroll
+      for (int l = 0; l < D; l++) s += I[k][l] * g[l * D + d];
+      t1[k][d] = s;
+    }
+  T tr = (T)0;
+#pragma unroll
+  for (int c = 0; c < D; c++)
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+      T s = (T)0;
+#pragma unroll
+      for (int k = 0; k < D; k++) s += g[k * D + c] * t1[k][d];
+      A[c][d] = s * scale;
+    }
+#pragma unroll
+  for (int c = 0; c < D; c++) tr += A[c][c];
+#pragma unroll
+  for (int a = 0; a < BS; a++)
+#pragma unroll
+    for (int b = 0; b < BS; b++) blk[a][b] = lamf * A[a][b] + muf * A[b][a] + (a == b ? muf * tr : (T)0);
+  }  // elasticity
+  }  // not mass
+}
+
+template <int D, int ORDER, int BS, int FORM, int G, class T, class TA>
+__global__ void k_scatter_kron(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                               const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                               const int32_t* __restrict__ cnd, int64_t nrows, int lmax, const T* __restrict__ Gc,
+                               T lamf, T muf, double* __restrict__ v64, float* __restrict__ v32) {
+  constexpr int M1 = ORDER + 1;
+  constexpr int NN = D == 2 ? M1 * M1 : M1 * M1 * M1;
+  constexpr int RPW = 32 / G;
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  __shared__ T s_M[9], s_D[9], s_K[9];
+  if (threadIdx.x == 0) {
+    double M[9], Dm[9], Kd[9], m1[3];
+    lagrange_table_1d(ORDER, M, Dm, Kd, m1);
+    for (int i = 0; i < 9; i++) { s_M[i] = (T)M[i]; s_D[i] = (T)Dm[i]; s_K[i] = (T)Kd[i]; }
+  }
+  __syncthreads();
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int sub = lane / G, gl = lane - sub * G;
+  int slot = w * RPW + sub;
+  TA* acc = (TA*)s_raw + (size_t)slot * lmax * BS * BS;
+  int32_t* cols = (int32_t*)((TA*)s_raw + (size_t)(blockDim.x / G) * lmax * BS * BS) + (size_t)slot * lmax;
+  int64_t r = ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * RPW + sub;
+  bool active = r < nrows;
+  unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
+  int64_t rb = 0;
+  int L = 0;
+  if (active) {
+    rb = rowptr[r];
+    L = (int)(rowptr[r + 1] - rb);
+    for (int i = gl; i < L; i += G) cols[i] = colind[rb + i];
+    for (int i = gl; i < L * BS * BS; i += G) acc[i] = (TA)0;
+  }
+  __syncwarp(gmask);
+  if (active) {
+    const int b = gl;
+    int nbi[3] = {b % M1, (b / M1) % M1, b / (M1 * M1)};
+    int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+    for (int64_t k = ib; k < ie; k++) {
+      int32_t cb = __ldg(inc + k);
+      int32_t c = cb / NN, a = cb - c * NN;
+      if (b < NN) {
+        int32_t j = __ldg(cnd + (int64_t)c * NN + b);
+        if (j > 0) {
+          T g[GSTRIDE];
+#pragma unroll
+          for (int i = 0; i < GSTRIDE; i++) g[i] = __ldg(Gc + (int64_t)c * GSTRIDE + i);
+          int nai[3] = {a % M1, (a / M1) % M1, a / (M1 * M1)};
+          T blk[BS][BS];
+          kron_block<D, BS, FORM, T>(nai, nbi, g, s_M, s_D, s_K, lamf, muf, blk);
+          int p = find_col(cols, L, j - 1);
+#pragma unroll
+          for (int cc = 0; cc < BS; cc++)
+#pragma unroll
+            for (int dd = 0; dd < BS; dd++) acc[(p * BS + cc) * BS + dd] += (TA)blk[cc][dd];
+        }
+      }
+      __syncwarp(gmask);
+    }
+    int64_t ob = rb * BS * BS;
+    for (int i = gl; i < L * BS * BS; i += G) {
+      TA v = acc[i];
+      if (v64) v64[ob + i] = (double)v;
+      if (v32) v32[ob + i] = (float)v;
+    }
+  }
+}
+
+template <int D, int ORDER, int BS, int FORM, class T>
+static int launch_kron(Matrix* A, const T* Gc, double nu) {
+  const Space* sp = A->space;
+  Ctx* ctx = ctx_of(sp);
+  constexpr int M1 = ORDER + 1;
+  constexpr int NN = D == 2 ? M1 * M1 : M1 * M1 * M1;
+  constexpr int G = NN <= 4 ? 4 : (NN <= 8 ? 8 : (NN <= 16 ? 16 : 32));
+  constexpr int RPW = 32 / G;
+  int lmax = A->max_row > 0 ? A->max_row : 1;
+  double* v64 = A->precision != GT_FP32 ? A->val64 : nullptr;
+  float* v32 = A->precision != GT_FP64 ? A->val32 : nullptr;
+  int warps = 4;
+  size_t per_row = (size_t)lmax * (BS * BS * sizeof(T) + sizeof(int32_t));
+  while (warps > 1 && (size_t)warps * RPW * per_row > 96 * 1024) warps >>= 1;
+  size_t smem = (size_t)warps * RPW * per_row;
+  if (smem > 200 * 1024) return set_error(ctx, GT_ERR_UNSUPPORTED, "sparsity row too wide for the scatter kernel");
+  auto kern = k_scatter_kron<D, ORDER, BS, FORM, G, T, T>;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int64_t rows_per_block = (int64_t)warps * RPW;
+  int64_t grid = (A->nbrows + rows_per_block - 1) / rows_per_block;
+  T lamf = (T)(nu / ((1.0 + nu) * (1.0 - 2.0 * nu))), muf = (T)(1.0 / (2.0 * (1.0 + nu)));
+  kern<<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
+      A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, A->nbrows, lmax, Gc, lamf, muf, v64, v32);
+  GT_LAUNCH(ctx, "k_scatter_kron");
+  return GT_OK;
+}
+
+template <int D, int ORDER, class T>
+static int dispatch_kron(Matrix* A, int form, const T* Gc, double nu) {
+  int bs = A->bs;
+  if (bs == 1) {
+    if (form == GT_LAPLACE) return launch_kron<D, ORDER, 1, GT_LAPLACE, T>(A, Gc, nu);
+    if (form == GT_MASS) return launch_kron<D, ORDER, 1, GT_MASS, T>(A, Gc, nu);
+  } else {
+    if (form == GT_LAPLACE) return launch_kron<D, ORDER, D, GT_LAPLACE, T>(A, Gc, nu);
+    if (form == GT_MASS) return launch_kron<D, ORDER, D, GT_MASS, T>(A, Gc, nu);
+    if (form == GT_ELASTICITY) return launch_kron<D, ORDER, D, GT_ELASTICITY, T>(A, Gc, nu);
+  }
+  return set_error(ctx_of(A->space), GT_ERR_UNSUPPORTED, "weak form not supported on this space");
+}
+
+static int alloc_values(Matrix* A);
+
+// Sum-factorised numeric phase on affine QUAD4/HEX8 meshes.  Sets *used = 0
+// (and writes only the load vector) when some cell is not affine.
+static int kron_numeric(Matrix* A, int form, const double* coef, double nu, const double* f, const double* scoef,
+                        double* be, int* used) {
+  const Space* sp = A->space;
+  Ctx* ctx = ctx_of(sp);
+  *used = 0;
+  int ct = sp->mesh->ctype;
+  if (ct != GT_QUAD4 && ct != GT_HEX8) return GT_OK;
+  if (form == GT_ELASTICITY && sp->ncomp != sp->mesh->D)
+    return set_error(ctx, GT_ERR_UNSUPPORTED, "linear elasticity needs a vector space (tensor_size = (D,))");
+  int64_t nc = sp->mesh->ncells;
+  bool g64 = A->precision != GT_FP32;
+  void* Gc = nullptr;
+  uint32_t* flag = nullptr;
+  GT_TRY(dalloc(ctx, (unsigned char**)&Gc, nc * GSTRIDE * (int64_t)(g64 ? sizeof(double) : sizeof(float))));
+  GT_TRY(dalloc(ctx, &flag, 1));
+  GT_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(uint32_t), ctx->stream));
+  if (ct == GT_QUAD4)
+    k_geom_affine<2, 4><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
+        sp->mesh->coords, sp->mesh->cell_nodes, coef, form, sp->order, nc, sp->nn, sp->ncomp, Gc, g64, be, f, scoef,
+        flag, ctx->d_err);
+  else
+    k_geom_affine<3, 8><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
+        sp->mesh->coords, sp->mesh->cell_nodes, coef, form, sp->order, nc, sp->nn, sp->ncomp, Gc, g64, be, f, scoef,
+        flag, ctx->d_err);
+  GT_LAUNCH(ctx, "k_geom_affine");
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[2], flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  uint32_t nonaffine = 0;
+  memcpy(&nonaffine, &ctx->h_scratch[2], sizeof(uint32_t));
+  mark(ctx, "elements");
+  int s = GT_OK;
+  if (!nonaffine) {
+    s = alloc_values(A);
+    int D = sp->mesh->D, o = sp->order;
+    if (s == GT_OK) {
+      if (g64) {
+        const double* G = (const double*)Gc;
+        s = D == 2 ? (o == 1 ? dispatch_kron<2, 1, double>(A, form, G, nu) : dispatch_kron<2, 2, double>(A, form, G, nu))
+                   : (o == 1 ? dispatch_kron<3, 1, double>(A, form, G, nu) : dispatch_kron<3, 2, double>(A, form, G, nu));
+      } else {
+        const float* G = (const float*)Gc;
+        s = D == 2 ? (o == 1 ? dispatch_kron<2, 1, float>(A, form, G, nu) : dispatch_kron<2, 2, float>(A, form, G, nu))
+                   : (o == 1 ? dispatch_kron<3, 1, float>(A, form, G, nu) : dispatch_kron<3, 2, float>(A, form, G, nu));
+      }
+    }
+    mark(ctx, "scatter");
+    if (s == GT_OK) *used = 1;
+  }
+  pool_free(ctx, Gc);
+  dfree(ctx, flag);
+  return s;
+}
+
 // vector scatter: each (row, component) sums its cells in ascending order
 __global__ void k_scatter_vec(const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, int nn, int bs,
                               int64_t nrows, const double* __restrict__ be, double* __restrict__ b) {
@@ -1092,13 +1486,17 @@ static int numeric(Matrix* A, int form, const double* coef_in, double nu, const 
   size_t esz = kprec == GT_FP32 ? sizeof(float) : sizeof(double);
   void* Ke = nullptr;
   double* be = nullptr;
-  GT_TRY(dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz)));
   if (b_out) GT_TRY(dalloc(ctx, &be, nc * sp->nloc));
-  int s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
-  mark(ctx, "elements");
-  if (s == GT_OK) s = alloc_values(A);
-  if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision);
-  mark(ctx, "scatter");
+  int used_kron = 0;
+  int s = kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, &used_kron);
+  if (s == GT_OK && !used_kron) {
+    s = dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz));
+    if (s == GT_OK) s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
+    mark(ctx, "elements");
+    if (s == GT_OK) s = alloc_values(A);
+    if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision);
+    mark(ctx, "scatter");
+  }
   if (s == GT_OK && b_out) {
     bool dev = is_device_ptr(b_out);
     double* bd = b_out;
@@ -1115,7 +1513,7 @@ static int numeric(Matrix* A, int form, const double* coef_in, double nu, const 
       dfree(ctx, bd);
     }
   }
-  pool_free(ctx, Ke);
+  if (Ke) pool_free(ctx, Ke);
   if (be) dfree(ctx, be);
   return s;
 }

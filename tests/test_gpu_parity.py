@@ -40,6 +40,10 @@ CASES = [
     ("q2quad_mass_vec", (3, 4), False, 2, 2, ["1-face-1", "1-face-3"], O.MASS, 0.0, 0.0),
     ("q2hex_elast_x0", (3, 4, 5), False, 2, 3, ["2-face-5"], O.ELASTICITY, 0.1, 0.5),
     ("q2hex_lap_free", (3, 3, 3), False, 2, 1, None, O.LAPLACE, 0.0, 0.0),
+    ("q2hex_elast_affine", (3, 3, 4), False, 2, 3, ["2-face-5"], O.ELASTICITY, 0.0, 0.5),
+    ("q1hex_lap_affine", (4, 5, 3), False, 1, 1, "boundary", O.LAPLACE, 0.0, 1.0),
+    ("q2quad_veclap_affine", (4, 3), False, 2, 2, ["1-face-3"], O.LAPLACE, 0.0, 1.0),
+    ("q1quad_elast_affine", (5, 4), False, 1, 2, ["1-face-3"], O.ELASTICITY, 0.0, 0.5),
     ("q1quad_1x1_alldiri", (1, 1), False, 1, 1, "boundary", O.LAPLACE, 0.0, 0.0),
     ("q2quad_1x1", (1, 1), False, 2, 1, "boundary", O.LAPLACE, 0.0, 0.0),
 ]
@@ -106,9 +110,11 @@ def test_vector(case):
     ob = O.assemble_vector(ref, 2 * order, f, coef=coef)
     if ob.size:
         assert np.abs(b - ob).max() <= TOL64 * np.abs(ob).max()
-    # combined entry point: same matrix and vector
+    # combined entry point: the same vector (its affine-cell path factorises
+    # the quadrature sum, so agreement is to rounding, not bitwise)
     A2, b2 = GT.assemble_matrix_and_vector(a, GT.source(f, coef), np.float64, V)
-    assert np.array_equal(b2, b)
+    if ob.size:
+        assert np.abs(b2 - ob).max() <= TOL64 * np.abs(ob).max()
 
 
 def test_assembly_is_deterministic():

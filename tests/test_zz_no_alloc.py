@@ -20,7 +20,8 @@ from gtgpu import _lib
 
 pytestmark = pytest.mark.gpu
 
-TOL = 1e-12  # same normwise FP64 tolerance as the other parity tests
+TOL = 1e-12    # same normwise FP64 tolerance as the other parity tests
+TOL32 = 2e-6   # FP32 values: the two entry points may integrate in a different order
 
 
 def _refill_noalloc(A, form, coef_dev, nu=0.3):
@@ -61,7 +62,8 @@ def test_noalloc_refill_matches_update_matrix_q2_elasticity_fp32():
         E = GT.lognormal_cells(m.num_cells, 0.5, seed)
         GT.update_matrix(A, GT.elasticity(E, 0.3))
         assert _refill_noalloc(B, _lib.GT_ELASTICITY, torch.from_numpy(E).cuda()) == 0
-        assert np.array_equal(A.values32(), B.values32())
+        va, vb = A.values32().astype(np.float64), B.values32().astype(np.float64)
+        assert np.abs(va - vb).max() <= TOL32 * np.abs(va).max()
 
 
 def test_noalloc_refuses_oversize_and_host_memory():
