@@ -77,6 +77,11 @@ SIGNATURES = [
     ("gt_assemble_vector", I32, [P, P, P, P]),
     ("gt_solve", I32, [P, P, P, DBL, I32, I32, C.POINTER(SolveInfo)]),
     ("gt_spmv", I32, [P, P, P]),
+    ("gt_batch_create", I32, [P, I32, P, C.POINTER(P)]),
+    ("gt_batch_set_lanes", I32, [P, I32]),
+    ("gt_batch_info", I32, [P, P]),
+    ("gt_batch_solve", I32, [P, P, P, DBL, I32, I32, P]),
+    ("gt_batch_destroy", I32, [P]),
 ]
 
 _lock = threading.Lock()

@@ -185,6 +185,26 @@ int gt_solve(gt_matrix* matrix, const double* b, double* x, double rtol, int max
 /* y = A x in the matrix's FP64 values (or FP32 when it has no FP64). */
 int gt_spmv(gt_matrix* matrix, const double* x, double* y);
 
+/* ---- batched solves ----------------------------------------------------- */
+/* No counterpart in the reference (which solves one problem per call).
+ * A batch of n assembled scalar matrices (block size 1) of one context,
+ * solved together: every launch advances all unconverged instances, each
+ * with its own CG scalars and deterministic reductions (an instance's
+ * result does not depend on the rest of the batch); iteration chunks are
+ * replayed from a captured CUDA graph.  b and x are the instances' vectors
+ * concatenated in batch order (num_free_dofs each, FP64); x is the output
+ * (every solve starts from 0).  infos: n entries.  GT_SOLVE_IR needs
+ * GT_MIXED matrices. */
+typedef struct gt_batch gt_batch;
+int gt_batch_create(gt_ctx* ctx, int n, gt_matrix* const* matrices, gt_batch** batch);
+/* lanes per matrix row in the batched SpMV (2, 4, 8 or 16; default 4) */
+int gt_batch_set_lanes(gt_batch* batch, int lanes);
+/* info[0]=instances info[1]=total rows info[2]=tiles info[3]=lanes */
+int gt_batch_info(const gt_batch* batch, int64_t* info);
+int gt_batch_solve(gt_batch* batch, const double* b, double* x, double rtol, int maxit, int mode,
+                   gt_solve_info* infos);
+int gt_batch_destroy(gt_batch* batch);
+
 #ifdef __cplusplus
 }
 #endif
