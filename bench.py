@@ -50,7 +50,147 @@ def parse():
     p.add_argument("--cells", type=int, default=96, help="cubes per direction (96 = the benchmark workload)")
     p.add_argument("--no-solve", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--workload", default="tets", choices=["tets", "elasticity", "batched", "serving"],
+                   help="tets: the headline workload; the others measure the remaining configurations")
+    p.add_argument("--instances", type=int, default=512, help="batched: number of instances")
+    p.add_argument("--requests", type=int, default=48, help="serving: number of requests")
+    p.add_argument("--budget-gb", type=float, default=150.0, help="batched/serving: HBM admission budget")
     return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# other configurations (one JSON line each; not the driver's headline)
+# ---------------------------------------------------------------------------
+def run_elasticity(args):
+    """3-D linear elasticity, 64^3 HEX8 cells, Q2 vector space (6.39M free
+    DOFs), E=1, nu=0.3, body force (0,0,-1), clamped at x=0, 3x3x3 Gauss.
+    Assembly in FP64, FP32 and mixed; solves: plain FP64 PCG and FP64
+    refinement around FP32 PCG to 1e-10."""
+    import torch
+    import gtgpu as GT
+    n = args.cells if args.cells != 96 else 64
+    m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (n, n, n))
+    ctx = GT.Context(0)
+    V = GT.lagrange_space(GT.interior(m), 2, tensor_size=(3,), dirichlet_boundary=GT.boundary(m, ["2-face-5"]),
+                          ctx=ctx)
+    a, l = GT.elasticity(1.0, 0.3), GT.source([0.0, 0.0, -1.0])
+    out = {"metric": "Q2 elasticity: nnz/s assembled and solve time, mixed vs plain FP64", "n_gpus": 1,
+           "config": {"workload": f"3-D linear elasticity, {n}^3 HEX8, Q2 vector (3 comp), E=1 nu=0.3, clamped x=0",
+                      "free_dofs": V.num_free_dofs}, "data": "synthetic (seeded)"}
+    res = {}
+    for T in (np.float64, np.float32, "mixed"):
+        name = {np.float64: "fp64", np.float32: "fp32", "mixed": "mixed"}[T]
+        ts = []
+        for _ in range(max(2, args.warmup)):
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            A, b = GT.assemble_matrix_and_vector(a, l, T, V)
+            ctx.synchronize()
+            ts.append(time.perf_counter() - t0)
+            if name != "mixed":
+                del A
+        res[name] = {"assemble_ms": 1e3 * min(ts), "nnz": A.nnz if name == "mixed" else None}
+    nnz = A.nnz
+    for k in res:
+        res[k]["nnz_per_s"] = nnz / (res[k]["assemble_ms"] * 1e-3)
+    A32 = GT.assemble_matrix(a, np.float32, V, V)
+    v32 = A32.values32().astype(np.float64)
+    _, _, v64 = A.csr()
+    res["fp32_values_rel_err_vs_fp64"] = float(np.abs(v32 - v64).max() / np.abs(v64).max())
+    del A32, v32
+    sol = {}
+    xs = {}
+    for mode in ("fp64", "ir"):
+        t0 = time.perf_counter()
+        x, info = GT.solve(A, b, rtol=1e-10, maxit=200000, mode=mode, raise_on_fail=False)
+        sol[mode] = {"solve_s": time.perf_counter() - t0, **info}
+        xs[mode] = x
+    sol["ir_vs_fp64_rel_err"] = float(np.abs(xs["ir"] - xs["fp64"]).max() / np.abs(xs["fp64"]).max())
+    out.update({"assembly": res, "solve": sol, "nnz": int(nnz)})
+    print(json.dumps(out), flush=True)
+
+
+def run_batched(args):
+    """512 independent Poisson instances (dim 2|3, order 1|2, cells
+    log-uniform 16^2..96^3, kappa lognormal(0,0.5), Dirichlet boundary),
+    solved to 1e-8: batched mixed path (HBM-budgeted waves; each wave
+    assembled then solved as one batch with FP64 refinement around FP32 PCG)
+    against the plain FP64 path (one instance at a time, FP64 assembly and
+    FP64 PCG)."""
+    import gtgpu as GT
+    from gtgpu import batch as GB
+    specs = GB.batch_workload(args.instances, seed=404)
+    budget = args.budget_gb * 1e9
+    ctx = GT.default_context()
+    # waves: largest first, greedy under the budget
+    order = sorted(specs, key=lambda s: -GB.estimate_bytes(s))
+    waves, cur, used = [], [], 0
+    for s in order:
+        e = GB.estimate_bytes(s)
+        if cur and used + e > budget:
+            waves.append(cur)
+            cur, used = [], 0
+        cur.append(s)
+        used += e
+    if cur:
+        waves.append(cur)
+    t_all = time.perf_counter()
+    iters, worst = [], 0.0
+    tune = None
+    for w in waves:
+        inst = [GB.assemble_instance(s, seed=404, T="mixed", ctx=ctx) for s in w]
+        B = GB.Batch([A for _, _, A, _ in inst])
+        b = np.concatenate([bb for _, _, _, bb in inst])
+        if tune is None:
+            tune = GB.autotune_lanes(B, b, iters=32)
+        else:
+            B.set_lanes(tune["lanes"])
+        x, infos = B.solve(b, rtol=1e-8, maxit=100000, mode="ir", raise_on_fail=False)
+        iters += [i["iterations"] for i in infos]
+        worst = max(worst, max(i["rel_residual"] for i in infos))
+        del B, inst
+        ctx.trim()
+    ctx.synchronize()
+    t_batched = time.perf_counter() - t_all
+    # plain FP64 path, one instance at a time
+    t0 = time.perf_counter()
+    worst64 = 0.0
+    for s in specs:
+        m, V, A, b = GB.assemble_instance(s, seed=404, T=np.float64, ctx=ctx)
+        x, info = GT.solve(A, b, rtol=1e-8, maxit=100000, mode="fp64", raise_on_fail=False)
+        worst64 = max(worst64, info["rel_residual"])
+        del A, V
+        if ctx.memory()[1] > 20e9:
+            ctx.trim()
+    t_plain = time.perf_counter() - t0
+    out = {"metric": "batched solves/s (assemble + solve to 1e-8), mixed batched vs plain FP64", "n_gpus": 1,
+           "config": {"workload": f"{args.instances} Poisson instances, dim 2|3, Q1|Q2, cells log-uniform 16^2..96^3",
+                      "waves": len(waves), "budget_gb": args.budget_gb, "lanes": tune["lanes"] if tune else None},
+           "batched": {"solves_per_s": len(specs) / t_batched, "seconds": t_batched, "worst_rel_residual": worst,
+                       "inner_iterations_max": int(max(iters))},
+           "plain_fp64": {"solves_per_s": len(specs) / t_plain, "seconds": t_plain, "worst_rel_residual": worst64},
+           "speedup": t_plain / t_batched, "data": "synthetic (seeded)"}
+    print(json.dumps(out), flush=True)
+
+
+def run_serving(args):
+    """Poisson-process stream (mean 2000 req/s) of assemble+solve requests:
+    Poisson or elasticity, Q1|Q2 hexahedra, cells log-uniform 1e3..2e6,
+    seeded coefficients, HBM admission budget; mixed path with 4 slots vs the
+    plain FP64 path with one slot.  p50/p99 latency = arrival -> result."""
+    from gtgpu.server import Server, request_stream
+    res = {}
+    for name, slots, prec in (("mixed_served", 4, "mixed"), ("plain_fp64", 1, "fp64")):
+        reqs = request_stream(args.requests, rate=2000.0, seed=505)
+        srv = Server(slots=slots, budget_bytes=args.budget_gb * 1e9, precision=prec, rtol=1e-8,
+                     keep_solutions=False)
+        res[name] = srv.serve(reqs, realtime=True)
+    out = {"metric": "serving: solves/s and p50/p99 latency, mixed served vs plain FP64", "n_gpus": 1,
+           "config": {"workload": f"{args.requests} requests, Poisson arrivals 2000/s, cells log-uniform 1e3..2e6",
+                      "budget_gb": args.budget_gb},
+           **res, "speedup": res["mixed_served"]["solves_per_s"] / max(res["plain_fp64"]["solves_per_s"], 1e-12),
+           "data": "synthetic (seeded)"}
+    print(json.dumps(out), flush=True)
 
 
 def workload(n):
@@ -178,6 +318,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "tets":
+        {"elasticity": run_elasticity, "batched": run_batched, "serving": run_serving}[args.workload](args)
         return
     import torch
     import torch.distributed as dist

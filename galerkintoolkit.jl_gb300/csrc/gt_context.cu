@@ -335,6 +335,13 @@ int gt_ctx_profile_end(gt_ctx* c, int max, char* names, double* ms, int* count) 
   return GT_OK;
 }
 
+int gt_ctx_trim(gt_ctx* c) {
+  if (!c) return GT_ERR_INVALID;
+  cudaSetDevice(c->device);
+  pool_trim(c);
+  return GT_OK;
+}
+
 int gt_ctx_memory(gt_ctx* c, int64_t* live, int64_t* pooled) {
   if (!c) return GT_ERR_INVALID;
   if (live) *live = c->live_bytes;

@@ -51,6 +51,10 @@ class Context:
         check(self.h, self.lib.gt_ctx_memory(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
 
+    def trim(self):
+        """Return the context's pooled device blocks to the driver."""
+        check(self.h, self.lib.gt_ctx_trim(self.h))
+
     def launches(self) -> int:
         n = C.c_int64()
         check(self.h, self.lib.gt_ctx_launch_count(self.h, C.byref(n)))

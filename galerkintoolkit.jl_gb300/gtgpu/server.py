@@ -154,6 +154,10 @@ class Server:
                 req.status = getattr(e, "code", _lib.GT_ERR_CUDA)
                 self.errors.append((req.rid, repr(e)))
             req.finished = self._now()
+            # pooled blocks of a finished request are not counted against the
+            # budget, so hand large pools back to the driver
+            if ctx is not None and hasattr(ctx, "memory") and ctx.memory()[1] > self.budget / (4 * self.slots):
+                ctx.trim()
             with self.lock:
                 self.in_use -= need
                 self.done.append(req)

@@ -82,6 +82,8 @@ int gt_ctx_synchronize(gt_ctx* ctx);
 int gt_ctx_set_stream(gt_ctx* ctx, void* stream);
 /* Bytes of device memory currently held by the context (live + pooled). */
 int gt_ctx_memory(gt_ctx* ctx, int64_t* live_bytes, int64_t* pooled_bytes);
+/* Returns the pooled (free) device blocks of the context to the driver. */
+int gt_ctx_trim(gt_ctx* ctx);
 /* Measured FMA throughput of the device in TFLOP/s (GT_FP64 or GT_FP32);
  * the roofline of the integration kernels.  No reference counterpart. */
 int gt_ctx_fma_rate(gt_ctx* ctx, int precision, double* tflops);
