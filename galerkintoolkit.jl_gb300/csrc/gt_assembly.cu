@@ -677,7 +677,7 @@ static int dispatch_form(const Space* sp, int form, const double* coef, double n
 //   mass       K_nm = coef * |det J| * sum_q w_q phi_n(q) phi_m(q)
 // -- the quadrature sums of the reference loop (src/compiler.jl:1865-1917
 // with dV = |det J| w, src/quadrature.jl:4-6) with the constant factors
-// taken out: one FP64 division and ~90 FP64 operations per cell.  J, its
+// taken out: one FP64 division and ~80 FP64 operations per cell.  J, its
 // cofactors and det stay FP64 in every precision; in FP32 mode the cofactor
 // columns are rounded to FP32 for the entries.
 template <int FORM, class T>
@@ -728,17 +728,27 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
   if (want_matrix) {
     T k[10];
     if (FORM == GT_LAPLACE) {
-      T g[4][3];
-      g[1][0] = (T)c10; g[1][1] = (T)c11; g[1][2] = (T)c12;
-      g[2][0] = (T)c20; g[2][1] = (T)c21; g[2][2] = (T)c22;
-      g[3][0] = (T)c30; g[3][1] = (T)c31; g[3][2] = (T)c32;
-      for (int d = 0; d < 3; d++) g[0][d] = -(g[1][d] + g[2][d] + g[3][d]);
+      // the six entries among vertices 1..3 from the cofactor columns; the
+      // entries of vertex 0 follow from c_0 = -(c_1 + c_2 + c_3), i.e. from
+      // the zero row sums of the Laplacian (8 additions instead of 4 dot
+      // products: the kernel is bound by the FP64 issue rate)
+      T g[3][3];
+      g[0][0] = (T)c10; g[0][1] = (T)c11; g[0][2] = (T)c12;
+      g[1][0] = (T)c20; g[1][1] = (T)c21; g[1][2] = (T)c22;
+      g[2][0] = (T)c30; g[2][1] = (T)c31; g[2][2] = (T)c32;
       T s = (T)(cf * s_wsum / adet);
-      int e = 0;
-#pragma unroll
-      for (int n = 0; n < 4; n++)
-#pragma unroll
-        for (int m = n; m < 4; m++) k[e++] = s * (g[n][0] * g[m][0] + g[n][1] * g[m][1] + g[n][2] * g[m][2]);
+      T k11 = s * (g[0][0] * g[0][0] + g[0][1] * g[0][1] + g[0][2] * g[0][2]);
+      T k12 = s * (g[0][0] * g[1][0] + g[0][1] * g[1][1] + g[0][2] * g[1][2]);
+      T k13 = s * (g[0][0] * g[2][0] + g[0][1] * g[2][1] + g[0][2] * g[2][2]);
+      T k22 = s * (g[1][0] * g[1][0] + g[1][1] * g[1][1] + g[1][2] * g[1][2]);
+      T k23 = s * (g[1][0] * g[2][0] + g[1][1] * g[2][1] + g[1][2] * g[2][2]);
+      T k33 = s * (g[2][0] * g[2][0] + g[2][1] * g[2][1] + g[2][2] * g[2][2]);
+      T k01 = -(k11 + k12 + k13), k02 = -(k12 + k22 + k23), k03 = -(k13 + k23 + k33);
+      T k00 = -(k01 + k02 + k03);
+      k[0] = k00; k[1] = k01; k[2] = k02; k[3] = k03;
+      k[4] = k11; k[5] = k12; k[6] = k13;
+      k[7] = k22; k[8] = k23;
+      k[9] = k33;
     } else {
       T s = (T)(cf * adet);
       int e = 0;

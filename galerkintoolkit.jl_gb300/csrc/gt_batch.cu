@@ -10,8 +10,9 @@
 // the instance (one counter per instance) sums that instance's partials in
 // tile order.  An instance's result is therefore bitwise the same whatever
 // else is in the batch.  A chunk of BCHUNK iterations is captured once in a
-// CUDA graph and replayed until no instance is live.  GT_SOLVE_IR wraps the
-// batched FP32 PCG with a batched FP64 residual, per instance.
+// CUDA graph and replayed until no instance is live.  GT_SOLVE_IR runs the
+// batched PCG in FP32 with per-instance FP64 reliable updates (true residual
+// b - A64 x whenever an instance's FP32 residual fell tenfold).
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -25,7 +26,8 @@ constexpr int BCHUNK = 16;  // iterations per captured graph
 
 struct BState {
   double rz, pq, rr, bb, alpha, beta, tol2;
-  int32_t done, iters, maxit, pad;
+  double rmax2, delta2, rzold;  // reliable updates (see k_brl_update)
+  int32_t done, iters, maxit, upd, nupd, pad;
 };
 
 struct BInst {
@@ -272,6 +274,151 @@ __global__ void __launch_bounds__(BT) k_bresid64(const BInst* __restrict__ insts
   }
 }
 
+// ---------------------------------------------------------------------------
+// Batched CG with FP64 reliable updates (GT_SOLVE_FP64 with delta = 0,
+// GT_SOLVE_IR in FP32 with delta = 0.1): per instance, the iteration runs on
+// the correction xs since the last update; when the recurrence residual fell
+// by delta (or claims convergence, or maxit is reached) x += xs and the FP64
+// true residual b - A x replaces the recurrence residual; the direction p is
+// then rebuilt from it.  Convergence is decided on the true residual.
+// ---------------------------------------------------------------------------
+
+// x = 0, xs = 0, r = (X) b, z = Dinv r, p = z; ||b||^2, tolerance
+template <class X>
+__global__ void __launch_bounds__(BT) k_brl_init(const BInst* __restrict__ insts, const int32_t* __restrict__ tinst,
+                                                 const int64_t* __restrict__ trow0, int tile_rows,
+                                                 const double* __restrict__ b, double* __restrict__ x,
+                                                 X* __restrict__ xs, X* __restrict__ r, X* __restrict__ z,
+                                                 X* __restrict__ p, const X* __restrict__ dinv, BState* st,
+                                                 double* partials, uint32_t* ctr, double rtol2, double delta2,
+                                                 int maxit, int32_t* active) {
+  int t = blockIdx.x;
+  int i = tinst[t];
+  BInst in = insts[i];
+  double v[2] = {0.0, 0.0};
+  int64_t row = trow0[t] + threadIdx.x;
+  if (threadIdx.x < tile_rows && row < in.nrows) {
+    int64_t g = in.off + row;
+    double bi = b[g];
+    X rx = (X)bi;
+    X zx = dinv[g] * rx;
+    x[g] = 0.0;
+    xs[g] = (X)0;
+    r[g] = rx;
+    z[g] = zx;
+    p[g] = zx;
+    v[0] = (double)rx * (double)zx;
+    v[1] = bi * bi;
+  }
+  if (inst_reduce<2, double>(v, partials, ctr + i, in, t) && threadIdx.x == 0) {
+    BState s{};
+    s.rz = v[0];
+    s.rr = v[1];
+    s.bb = v[1];
+    s.tol2 = rtol2 * v[1];
+    s.rmax2 = v[1];
+    s.delta2 = delta2;
+    s.maxit = maxit;
+    s.done = v[1] == 0.0;
+    st[i] = s;
+    if (!s.done) atomicAdd(active, 1);
+  }
+}
+
+template <class X>
+__global__ void __launch_bounds__(BT) k_brl_update(const BInst* __restrict__ insts, const int32_t* __restrict__ tinst,
+                                                   const int64_t* __restrict__ trow0, int tile_rows, X* __restrict__ xs,
+                                                   X* __restrict__ r, X* __restrict__ z, const X* __restrict__ p,
+                                                   const X* __restrict__ q, const X* __restrict__ dinv, BState* st,
+                                                   double* partials, uint32_t* ctr) {
+  int t = blockIdx.x;
+  int i = tinst[t];
+  if (st[i].done) return;
+  BInst in = insts[i];
+  X alpha = (X)st[i].alpha;
+  X v[2] = {(X)0, (X)0};
+  int64_t row = trow0[t] + threadIdx.x;
+  if (threadIdx.x < tile_rows && row < in.nrows) {
+    int64_t g = in.off + row;
+    X ri = r[g] - alpha * q[g];
+    xs[g] += alpha * p[g];
+    X zi = dinv[g] * ri;
+    r[g] = ri;
+    z[g] = zi;
+    v[0] = ri * zi;
+    v[1] = ri * ri;
+  }
+  if (inst_reduce<2, X>(v, partials, ctr + i, in, t) && threadIdx.x == 0) {
+    double rz = (double)v[0], rr = (double)v[1];
+    BState& s = st[i];
+    s.rzold = s.rz;
+    s.beta = rz / s.rz;
+    s.rz = rz;
+    s.rr = rr;
+    s.iters += 1;
+    if (rr <= s.tol2 || rr <= s.delta2 * s.rmax2 || s.iters >= s.maxit || !(rr == rr)) s.upd = 1;
+  }
+}
+
+// x += xs, xs = 0 for the instances with an update due
+template <class X>
+__global__ void __launch_bounds__(BT) k_brl_xupdate(const BInst* __restrict__ insts, const int32_t* __restrict__ tinst,
+                                                    const int64_t* __restrict__ trow0, int tile_rows,
+                                                    double* __restrict__ x, X* __restrict__ xs, const BState* st) {
+  int t = blockIdx.x;
+  int i = tinst[t];
+  if (st[i].done || !st[i].upd) return;
+  BInst in = insts[i];
+  int64_t row = trow0[t] + threadIdx.x;
+  if (threadIdx.x < tile_rows && row < in.nrows) {
+    int64_t g = in.off + row;
+    x[g] += (double)xs[g];
+    xs[g] = (X)0;
+  }
+}
+
+// r64 = b - A64 x, r = (X) r64, z = Dinv r; true-residual convergence test
+template <int G, class X>
+__global__ void __launch_bounds__(BT) k_brl_resid(const BInst* __restrict__ insts, const int32_t* __restrict__ tinst,
+                                                  const int64_t* __restrict__ trow0, const double* __restrict__ b,
+                                                  const double* __restrict__ x, X* __restrict__ r, X* __restrict__ z,
+                                                  const X* __restrict__ dinv, BState* st, double* partials,
+                                                  uint32_t* ctr, int32_t* active) {
+  int t = blockIdx.x;
+  int i = tinst[t];
+  if (st[i].done || !st[i].upd) return;
+  BInst in = insts[i];
+  int grp = threadIdx.x / G, gl = threadIdx.x - grp * G;
+  int64_t row = trow0[t] + grp;
+  bool valid = row < in.nrows;
+  int64_t rr = valid ? row : in.nrows - 1;
+  double o = brow_dot<G, double, double>(in.rowptr, in.colind, in.v64, x + in.off, rr, gl);
+  double v[2] = {0.0, 0.0};
+  if (gl == 0 && valid) {
+    int64_t g = in.off + row;
+    double ri = b[g] - o;
+    X rx = (X)ri;
+    X zx = dinv[g] * rx;
+    r[g] = rx;
+    z[g] = zx;
+    v[0] = (double)rx * (double)zx;
+    v[1] = ri * ri;
+  }
+  if (inst_reduce<2, double>(v, partials, ctr + i, in, t) && threadIdx.x == 0) {
+    BState& s = st[i];
+    s.beta = s.rzold != 0.0 ? v[0] / s.rzold : 0.0;
+    s.rz = v[0];
+    s.rr = v[1];
+    s.nupd += 1;
+    s.rmax2 = v[1];
+    s.upd = 0;
+    if (v[1] <= s.tol2 || s.iters >= s.maxit || !(v[1] == v[1])) {
+      s.done = 1;
+      atomicSub(active, 1);
+    }
+  }
+}
+
 template <class X>
 __global__ void k_bdinv(const BInst* __restrict__ insts, const int32_t* __restrict__ tinst,
                         const int64_t* __restrict__ trow0, int tile_rows, X* __restrict__ dinv) {
@@ -364,6 +511,41 @@ static void enqueue_iteration(gt_batch* B, X* x, X* r, X* z, X* p, X* q, const X
   k_bcg_pupdate<X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, B->tile_rows, p, z, st);
 }
 
+// Captures BCHUNK iterations (enqueue() once per iteration) in a CUDA graph
+// and replays it until no instance is live or maxit iterations ran.
+template <class F>
+static int run_chunks(gt_batch* B, int maxit, F&& enqueue) {
+  Ctx* ctx = B->ctx;
+  cudaStream_t s = ctx->stream;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  GT_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int64_t l0 = ctx->launches;
+  for (int k = 0; k < BCHUNK; k++) enqueue();
+  int64_t per_chunk = ctx->launches - l0;
+  cudaError_t ce = cudaStreamEndCapture(s, &graph);
+  if (ce != cudaSuccess) return check_cuda(ctx, ce, "cudaStreamEndCapture");
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  if (ce != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return check_cuda(ctx, ce, "cudaGraphInstantiate");
+  }
+  int status = GT_OK;
+  ctx->launches -= per_chunk;  // counted per replay below
+  for (int it = 0; it < maxit + BCHUNK; it += BCHUNK) {
+    ce = cudaGraphLaunch(exec, s);
+    if (ce != cudaSuccess) { status = check_cuda(ctx, ce, "cudaGraphLaunch"); break; }
+    ctx->launches += per_chunk;
+    cudaMemcpyAsync(B->h_active, B->d_active, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) { status = check_cuda(ctx, ce, "batched PCG"); break; }
+    if (*B->h_active <= 0) break;
+  }
+  cudaGraphExecDestroy(exec);
+  cudaGraphDestroy(graph);
+  return status;
+}
+
 // batched PCG from x = 0 on values of type X; per-instance iteration counts
 // and final recurrence residuals in hst
 template <class X>
@@ -382,38 +564,63 @@ static int batch_pcg(gt_batch* B, const X* rhs, X* x, const X* dinv, double rtol
                                                                B->tile_rows, rhs, x, r, z, p, dinv, st, partials,
                                                                B->d_counter, rtol * rtol, maxit, skip, B->d_active);
   GT_LAUNCH(ctx, "k_bcg_init");
-  // capture one chunk of iterations, replay until no instance is live
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  GT_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  int64_t l0 = ctx->launches;
-  for (int k = 0; k < BCHUNK; k++) enqueue_iteration<X>(B, x, r, z, p, q, dinv, st, partials);
-  int64_t per_chunk = ctx->launches - l0;
-  cudaError_t ce = cudaStreamEndCapture(s, &graph);
-  if (ce != cudaSuccess) return check_cuda(ctx, ce, "cudaStreamEndCapture");
-  ce = cudaGraphInstantiate(&exec, graph, 0);
-  if (ce != cudaSuccess) {
-    cudaGraphDestroy(graph);
-    return check_cuda(ctx, ce, "cudaGraphInstantiate");
-  }
-  int status = GT_OK;
-  ctx->launches -= per_chunk;  // counted per replay below
-  for (int it = 0; it < maxit; it += BCHUNK) {
-    ce = cudaGraphLaunch(exec, s);
-    if (ce != cudaSuccess) { status = check_cuda(ctx, ce, "cudaGraphLaunch"); break; }
-    ctx->launches += per_chunk;
-    cudaMemcpyAsync(B->h_active, B->d_active, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
-    ce = cudaStreamSynchronize(s);
-    if (ce != cudaSuccess) { status = check_cuda(ctx, ce, "batched PCG"); break; }
-    if (*B->h_active <= 0) break;
-  }
-  cudaGraphExecDestroy(exec);
-  cudaGraphDestroy(graph);
+  int status = run_chunks(B, maxit, [&]() { enqueue_iteration<X>(B, x, r, z, p, q, dinv, st, partials); });
   hst.resize(B->n);
   if (status == GT_OK) {
     GT_CUDA(ctx, cudaMemcpyAsync(hst.data(), st, sizeof(BState) * B->n, cudaMemcpyDeviceToHost, s));
     GT_CUDA(ctx, cudaStreamSynchronize(s));
   }
+  dfree(ctx, r);
+  dfree(ctx, z);
+  dfree(ctx, p);
+  dfree(ctx, q);
+  return status;
+}
+
+// batched CG with FP64 reliable updates from x = 0 (iteration in X)
+template <class X>
+static int batch_rpcg(gt_batch* B, const double* b, double* x, const X* dinv, double rtol, int maxit, double delta,
+                      BState* st, double* partials, std::vector<BState>& hst) {
+  Ctx* ctx = B->ctx;
+  cudaStream_t s = ctx->stream;
+  int64_t n = B->ntot;
+  unsigned g = (unsigned)B->ntiles;
+  X *xs = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
+  GT_TRY(dalloc(ctx, &xs, n));
+  GT_TRY(dalloc(ctx, &r, n));
+  GT_TRY(dalloc(ctx, &z, n));
+  GT_TRY(dalloc(ctx, &p, n));
+  GT_TRY(dalloc(ctx, &q, n));
+  GT_CUDA(ctx, cudaMemsetAsync(B->d_active, 0, sizeof(int32_t), s));
+  k_brl_init<X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, B->tile_rows, b, x, xs, r, z,
+                                             p, dinv, st, partials, B->d_counter, rtol * rtol, delta * delta, maxit,
+                                             B->d_active);
+  GT_LAUNCH(ctx, "k_brl_init");
+  auto iteration = [&]() {
+    switch (B->G) {
+      case 2: k_bcg_spmv<2, X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, p, q, st, partials, B->d_counter); break;
+      case 4: k_bcg_spmv<4, X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, p, q, st, partials, B->d_counter); break;
+      case 8: k_bcg_spmv<8, X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, p, q, st, partials, B->d_counter); break;
+      default: k_bcg_spmv<16, X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, p, q, st, partials, B->d_counter); break;
+    }
+    k_brl_update<X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, B->tile_rows, xs, r, z, p, q,
+                                                 dinv, st, partials, B->d_counter);
+    k_brl_xupdate<X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, B->tile_rows, x, xs, st);
+    switch (B->G) {
+      case 2: k_brl_resid<2, X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, b, x, r, z, dinv, st, partials, B->d_counter, B->d_active); break;
+      case 4: k_brl_resid<4, X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, b, x, r, z, dinv, st, partials, B->d_counter, B->d_active); break;
+      case 8: k_brl_resid<8, X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, b, x, r, z, dinv, st, partials, B->d_counter, B->d_active); break;
+      default: k_brl_resid<16, X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, b, x, r, z, dinv, st, partials, B->d_counter, B->d_active); break;
+    }
+    k_bcg_pupdate<X><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, B->tile_rows, p, z, st);
+  };
+  int status = run_chunks(B, maxit, iteration);
+  hst.resize(B->n);
+  if (status == GT_OK) {
+    GT_CUDA(ctx, cudaMemcpyAsync(hst.data(), st, sizeof(BState) * B->n, cudaMemcpyDeviceToHost, s));
+    GT_CUDA(ctx, cudaStreamSynchronize(s));
+  }
+  dfree(ctx, xs);
   dfree(ctx, r);
   dfree(ctx, z);
   dfree(ctx, p);
@@ -467,9 +674,12 @@ static int batch_solve(gt_batch* B, const double* b, double* x, double rtol, int
     GT_TRY(dalloc(ctx, &dinv, n));
     k_bdinv<double><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, B->tile_rows, dinv);
     GT_LAUNCH(ctx, "k_bdinv");
-    status = batch_pcg<double>(B, b, x, dinv, rtol, maxit, nullptr, st, partials, hst);
+    status = batch_rpcg<double>(B, b, x, dinv, rtol, maxit, 0.0, st, partials, hst);
     dfree(ctx, dinv);
-    for (int i = 0; i < ni && status == GT_OK; i++) info[i].iterations = hst[i].iters;
+    for (int i = 0; i < ni && status == GT_OK; i++) {
+      info[i].iterations = hst[i].iters;
+      info[i].outer_iterations = hst[i].nupd;
+    }
   } else if (mode == GT_SOLVE_FP32) {
     float *dinv = nullptr, *bf = nullptr, *xf = nullptr;
     GT_TRY(dalloc(ctx, &dinv, n));
@@ -493,53 +703,17 @@ static int batch_solve(gt_batch* B, const double* b, double* x, double rtol, int
     dfree(ctx, bf);
     dfree(ctx, xf);
   } else {
-    // FP64 refinement: r = b - A64 x; inner FP32 PCG on r / ||r||; x += ||r|| d
-    double* r = nullptr;
-    float *dinv = nullptr, *rf = nullptr, *df = nullptr;
-    GT_TRY(dalloc(ctx, &r, n));
+    // FP32 CG with FP64 reliable updates, per instance
+    float* dinv = nullptr;
     GT_TRY(dalloc(ctx, &dinv, n));
-    GT_TRY(dalloc(ctx, &rf, n));
-    GT_TRY(dalloc(ctx, &df, n));
     k_bdinv<float><<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, B->tile_rows, dinv);
-    GT_CUDA(ctx, cudaMemsetAsync(x, 0, sizeof(double) * n, s));
-    std::vector<double> hn(2 * ni);
-    std::vector<int32_t> hskip(ni, 0);
-    const double inner_tol = 1e-5;
-    int total_inner_max = 0;
-    for (int outer = 0; outer < 40; outer++) {
-      GT_TRY(batch_resid(B, b, x, r, norms, partials));
-      GT_CUDA(ctx, cudaMemcpyAsync(hn.data(), norms, sizeof(double) * 2 * ni, cudaMemcpyDeviceToHost, s));
-      GT_CUDA(ctx, cudaStreamSynchronize(s));
-      int live = 0;
-      for (int i = 0; i < ni; i++) {
-        double rel = hn[2 * i + 1] > 0 ? sqrt(hn[2 * i] / hn[2 * i + 1]) : 0.0;
-        info[i].rel_residual = rel;
-        bool done = rel <= rtol || info[i].iterations >= maxit;
-        hskip[i] = done;
-        if (!done) {
-          live++;
-          info[i].outer_iterations = outer + 1;
-        }
-      }
-      if (!live) break;
-      GT_TRY(copy_in(ctx, skip, hskip.data(), ni));
-      k_bscale<<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, B->tile_rows, r, norms, rf);
-      GT_LAUNCH(ctx, "k_bscale");
-      status = batch_pcg<float>(B, rf, df, dinv, inner_tol, maxit - total_inner_max, skip, st, partials, hst);
-      if (status != GT_OK) break;
-      for (int i = 0; i < ni; i++)
-        if (!hskip[i]) {
-          info[i].iterations += hst[i].iters;
-          total_inner_max = info[i].iterations > total_inner_max ? info[i].iterations : total_inner_max;
-        }
-      k_baddscaled<<<GT_KC(ctx, g), BT, 0, s>>>(B->d_inst, B->d_tile_inst, B->d_tile_row0, B->tile_rows, x, df, norms,
-                                                skip);
-      GT_LAUNCH(ctx, "k_baddscaled");
-    }
-    dfree(ctx, r);
+    GT_LAUNCH(ctx, "k_bdinv");
+    status = batch_rpcg<float>(B, b, x, dinv, rtol, maxit, 0.1, st, partials, hst);
     dfree(ctx, dinv);
-    dfree(ctx, rf);
-    dfree(ctx, df);
+    for (int i = 0; i < ni && status == GT_OK; i++) {
+      info[i].iterations = hst[i].iters;
+      info[i].outer_iterations = hst[i].nupd;
+    }
   }
   // true FP64 residuals where FP64 values exist (FP64 and IR modes)
   if (status == GT_OK && mode != GT_SOLVE_FP32) {

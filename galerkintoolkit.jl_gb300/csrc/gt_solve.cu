@@ -28,8 +28,11 @@ constexpr int CHUNK = 16;   // CG iterations between host polls
 // device-resident CG state (one per solve)
 struct CGState {
   double rz, pq, rr, bb, alpha, beta;
-  double tol2;  // (rtol * ||b||)^2
-  int32_t done, iters, maxit, pad;
+  double tol2;    // (rtol * ||b||)^2
+  double rmax2;   // ||r||^2 at the last reliable update
+  double delta2;  // reliable update when the recurrence residual fell by delta
+  double rzold;   // r.z before the last recurrence step
+  int32_t done, iters, maxit, upd, nupd, pad;
 };
 
 // reduction scratch sized for the largest grid of a solve
@@ -495,6 +498,209 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
   return status;
 }
 
+// ---------------------------------------------------------------------------
+// CG with FP64 reliable updates.  The iteration runs in X (FP32 for the
+// mixed mode, FP64 for the plain mode) on the correction xs since the last
+// update; whenever the recurrence residual has dropped by delta (or claims
+// convergence, or maxit is reached) the FP64 solution takes the correction
+// (x += xs) and the FP64 true residual b - A x, computed with the FP64
+// values, replaces the recurrence residual.  The search direction is kept,
+// so the Krylov information survives the update and the iteration count
+// stays near that of FP64 CG, at the per-iteration cost of X.  Convergence
+// is declared on the FP64 true residual only.
+// ---------------------------------------------------------------------------
+template <class X>
+__global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __restrict__ r, X* __restrict__ z,
+                                                     const X* __restrict__ p, const X* __restrict__ q,
+                                                     const X* __restrict__ dinv, int64_t n, CGState* st, RedBuf rb) {
+  if (st->done) return;
+  const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
+  const X alpha = (X)st->alpha;
+  X rv[IPT], qv[IPT], pv[IPT], xv[IPT], dv[IPT];
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    int64_t i = base + (int64_t)j * blockDim.x;
+    bool ok = i < n;
+    rv[j] = ok ? r[i] : (X)0;
+    qv[j] = ok ? q[i] : (X)0;
+    pv[j] = ok ? p[i] : (X)0;
+    xv[j] = ok ? xs[i] : (X)0;
+    dv[j] = ok ? dinv[i] : (X)0;
+  }
+  X v[2] = {(X)0, (X)0};
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    int64_t i = base + (int64_t)j * blockDim.x;
+    X ri = rv[j] - alpha * qv[j];
+    X zi = dv[j] * ri;
+    if (i < n) {
+      xs[i] = xv[j] + alpha * pv[j];
+      r[i] = ri;
+      z[i] = zi;
+    }
+    v[0] += ri * zi;
+    v[1] += ri * ri;
+  }
+  if (reduce_last<2, X>(v, rb) && threadIdx.x == 0) {
+    double rz = (double)v[0], rr = (double)v[1];
+    st->rzold = st->rz;
+    st->beta = rz / st->rz;
+    st->rz = rz;
+    st->rr = rr;
+    st->iters += 1;
+    if (rr <= st->tol2 || rr <= st->delta2 * st->rmax2 || st->iters >= st->maxit || !(rr == rr)) st->upd = 1;
+  }
+}
+
+// x += xs; xs = 0 (when an update is due)
+template <class X>
+__global__ void __launch_bounds__(RED_T) k_rl_xupdate(double* __restrict__ x, X* __restrict__ xs, int64_t n,
+                                                      const CGState* st) {
+  if (st->done || !st->upd) return;
+  const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < IPT; j++) {
+    int64_t i = base + (int64_t)j * blockDim.x;
+    if (i < n) {
+      x[i] += (double)xs[i];
+      xs[i] = (X)0;
+    }
+  }
+}
+
+// r64 = b - A x (FP64), r = (X) r64, z = Dinv r; rz and ||r64||^2; decides
+// convergence on the true residual
+template <int BS, int G, class X>
+__global__ void __launch_bounds__(RED_T) k_rl_resid(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                                                    const double* __restrict__ val, const double* __restrict__ b,
+                                                    const double* __restrict__ x, X* __restrict__ r, X* __restrict__ z,
+                                                    const X* __restrict__ dinv, int64_t nrows, CGState* st, RedBuf rb) {
+  if (st->done || !st->upd) return;
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t row = t / G;
+  int gl = (int)(t - row * G);
+  bool valid = row < nrows;
+  if (!valid) row = nrows - 1;
+  double o[BS];
+  row_product<BS, G, double, double>(rowptr, colind, val, x, row, gl, o);
+  double v[2] = {0.0, 0.0};
+  if (gl == 0 && valid) {
+#pragma unroll
+    for (int c = 0; c < BS; c++) {
+      int64_t i = row * BS + c;
+      double ri = b[i] - o[c];
+      X rx = (X)ri;
+      X zx = dinv[i] * rx;
+      r[i] = rx;
+      z[i] = zx;
+      v[0] += (double)rx * (double)zx;
+      v[1] += ri * ri;
+    }
+  }
+  if (reduce_last<2, double, G>(v, rb) && threadIdx.x == 0) {
+    // the next direction is built from the true residual
+    st->beta = st->rzold != 0.0 ? v[0] / st->rzold : 0.0;
+    st->rz = v[0];
+    st->rr = v[1];
+    st->nupd += 1;
+    if (v[1] <= st->tol2 || st->iters >= st->maxit || !(v[1] == v[1])) st->done = 1;
+    st->rmax2 = v[1];
+    st->upd = 0;
+  }
+}
+
+template <class X>
+__global__ void k_copy_vec(const X* __restrict__ a, X* __restrict__ out, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i];
+}
+
+__global__ void k_rl_setup(CGState* st, const double* bb, double rtol2, double delta2, int maxit) {
+  st->bb = *bb;
+  st->tol2 = rtol2 * (*bb);
+  st->delta2 = delta2;
+  st->maxit = maxit;
+  st->iters = 0;
+  st->done = 0;
+  st->upd = 1;
+  st->nupd = 0;
+  st->rmax2 = 1e300;
+  st->beta = 0.0;
+}
+
+// Solve A x = b with CG in X plus FP64 reliable updates (see above); x (FP64)
+// holds the start value on entry.  V: value type of the iteration's SpMV.
+template <class V, class X>
+static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, double rtol, int maxit, double delta,
+                        int32_t* iters_out, int32_t* nupd_out, double* relres_out) {
+  Ctx* ctx = A->space->mesh->ctx;
+  cudaStream_t s = ctx->stream;
+  int64_t n = A->nbrows * A->bs;
+  X *xs = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
+  CGState* st = nullptr;
+  double* bb = nullptr;
+  unsigned gs = cg_spmv_grid(A), gv = vec_grid(n), gi = ipt_grid(n), gr = spmv_grid(A);
+  unsigned gmax = gs > gv ? gs : gv;
+  if (gr > gmax) gmax = gr;
+  Scratch sc;
+  GT_TRY(sc.alloc(ctx, gmax));
+  GT_TRY(dalloc(ctx, &xs, n));
+  GT_TRY(dalloc(ctx, &r, n));
+  GT_TRY(dalloc(ctx, &z, n));
+  GT_TRY(dalloc(ctx, &p, n));
+  GT_TRY(dalloc(ctx, &q, n));
+  GT_TRY(dalloc(ctx, &dinv, n));
+  GT_TRY(dalloc(ctx, &bb, 1));
+  GT_TRY(dalloc(ctx, (unsigned char**)&st, sizeof(CGState)));
+  GT_CUDA(ctx, cudaMemsetAsync(st, 0, sizeof(CGState), s));
+  GT_CUDA(ctx, cudaMemsetAsync(xs, 0, sizeof(X) * n, s));
+  GT_TRY(find_diag(A));
+  if (A->bs == 1) k_dinv<1, double, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, A->val64, A->nbrows, dinv);
+  else if (A->bs == 2) k_dinv<2, double, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, A->val64, A->nbrows, dinv);
+  else k_dinv<3, double, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, A->val64, A->nbrows, dinv);
+  GT_LAUNCH(ctx, "k_dinv");
+  GT_TRY(norm2(ctx, b, n, bb, sc.rb));
+  k_rl_setup<<<GT_KC(ctx, 1), 1, 0, s>>>(st, bb, rtol * rtol, delta * delta, maxit);
+  auto resid = [&]() {
+    Ops<double, double>::dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
+      constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
+      k_rl_resid<BS, GG, X><<<GT_KC(ctx, gr), RED_T, 0, s>>>(A->rowptr, A->colind, A->val64, b, x, r, z, dinv,
+                                                            A->nbrows, st, sc.rb);
+    });
+  };
+  resid();  // r = b - A x0, z, rz
+  k_copy_vec<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(z, p, n);
+  GT_LAUNCH(ctx, "reliable CG start");
+  CGState h{};
+  for (int it = 0; it < maxit + CHUNK; it += CHUNK) {
+    for (int k = 0; k < CHUNK; k++) {
+      GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb)));
+      k_rl_update<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(xs, r, z, p, q, dinv, n, st, sc.rb);
+      k_rl_xupdate<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(x, xs, n, st);
+      resid();
+      k_cg_pupdate<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(p, z, n, st);
+    }
+    GT_LAUNCH(ctx, "reliable CG iteration");
+    GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+    GT_CUDA(ctx, cudaStreamSynchronize(s));
+    memcpy(&h, ctx->h_dscratch, sizeof(CGState));
+    if (h.done) break;
+  }
+  *iters_out = h.iters;
+  *nupd_out = h.nupd;
+  *relres_out = h.bb > 0 ? sqrt(h.rr / h.bb) : 0.0;
+  int status = (h.rr <= h.tol2) ? GT_OK : GT_ERR_NOT_CONVERGED;
+  dfree(ctx, xs);
+  dfree(ctx, r);
+  dfree(ctx, z);
+  dfree(ctx, p);
+  dfree(ctx, q);
+  dfree(ctx, dinv);
+  dfree(ctx, bb);
+  pool_free(ctx, st);
+  return status;
+}
+
 int spmv64(Matrix* A, const double* x, double* y) {
   Ctx* ctx = A->space->mesh->ctx;
   if (!A->val64) return set_error(ctx, GT_ERR_INVALID, "matrix has no FP64 values");
@@ -535,16 +741,13 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
   unsigned gv = vec_grid(n);
   if (mode == GT_SOLVE_FP64) {
     if (!A->val64) return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_FP64 needs FP64 values (assemble with GT_FP64 or GT_MIXED)");
-    int32_t it = 0;
-    double rr = 0, bb = 0, *bbd = nullptr;
-    Scratch sc;
-    GT_TRY(sc.alloc(ctx, gv));
-    GT_TRY(dalloc(ctx, &bbd, 1));
-    GT_TRY(norm2(ctx, b, n, bbd, sc.rb));
-    status = pcg<double, double>(A, A->val64, b, x, rtol, maxit, bbd, &it, &rr, &bb);
-    dfree(ctx, bbd);
+    // FP64 CG; a recurrence residual below the tolerance is checked against
+    // the true residual (delta = 0: updates only there) and the iteration
+    // goes on from the true residual when that is still above it
+    int32_t it = 0, nupd = 0;
+    status = pcg_reliable<double, double>(A, A->val64, b, x, rtol, maxit, 0.0, &it, &nupd, &inf.rel_residual);
     inf.iterations = it;
-    GT_TRY(true_residual(A, b, x, &inf.rel_residual));
+    inf.outer_iterations = nupd;
   } else if (mode == GT_SOLVE_FP32) {
     if (!A->val32) return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_FP32 needs FP32 values (GT_FP32 or GT_MIXED)");
     float *bf = nullptr, *xf = nullptr;
@@ -565,47 +768,12 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
     dfree(ctx, xf);
   } else if (mode == GT_SOLVE_IR) {
     if (!A->val64 || !A->val32) return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_IR needs GT_MIXED values");
-    double *r = nullptr, *scal = nullptr;
-    float *rf = nullptr, *df = nullptr;
-    Scratch sc;
-    GT_TRY(sc.alloc(ctx, gv));
-    GT_TRY(dalloc(ctx, &r, n));
-    GT_TRY(dalloc(ctx, &rf, n));
-    GT_TRY(dalloc(ctx, &df, n));
-    GT_TRY(dalloc(ctx, &scal, 4));
-    GT_TRY(norm2(ctx, b, n, scal + 1, sc.rb));  // ||b||^2
-    const double inner_tol = 1e-5;
-    int outer = 0, total_inner = 0;
-    double relres = 1.0;
-    status = GT_ERR_NOT_CONVERGED;
-    for (outer = 0; outer < 60; outer++) {
-      GT_TRY((Ops<double, double>::spmv(ctx, A, A->val64, x, b, r)));  // r = b - A x (FP64)
-      GT_TRY(norm2(ctx, (const double*)r, n, scal, sc.rb));
-      GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
-      GT_CUDA(ctx, cudaStreamSynchronize(s));
-      double rn2 = ctx->h_dscratch[0], bn2 = ctx->h_dscratch[1];
-      relres = bn2 > 0 ? sqrt(rn2 / bn2) : 0.0;
-      if (relres <= rtol) { status = GT_OK; break; }
-      if (total_inner >= maxit) break;
-      // inner: A32 d = r / ||r||, from d = 0
-      k_scale_to_f32<<<GT_KC(ctx, gv), RED_T, 0, s>>>(r, n, scal, rf);
-      GT_CUDA(ctx, cudaMemsetAsync(df, 0, sizeof(float) * n, s));
-      int32_t it = 0;
-      double rr = 0, bb = 0;
-      double tol_here = inner_tol;
-      if (relres * 1e-3 < rtol) tol_here = fmax(inner_tol, 0.5 * rtol / relres);
-      pcg<float, float>(A, A->val32, rf, df, tol_here, maxit - total_inner, nullptr, &it, &rr, &bb);
-      total_inner += it;  // a stalled inner solve still improves x; the outer test decides
-      k_add_scaled_f32<<<GT_KC(ctx, gv), RED_T, 0, s>>>(x, df, n, scal);
-      GT_LAUNCH(ctx, "refinement update");
-    }
-    inf.iterations = total_inner;
-    inf.outer_iterations = outer;
-    inf.rel_residual = relres;
-    dfree(ctx, r);
-    dfree(ctx, rf);
-    dfree(ctx, df);
-    dfree(ctx, scal);
+    // FP32 CG (FP32 values, vectors and inner sums) with an FP64 true
+    // residual and solution update each time the residual fell tenfold
+    int32_t it = 0, nupd = 0;
+    status = pcg_reliable<float, float>(A, A->val32, b, x, rtol, maxit, 0.1, &it, &nupd, &inf.rel_residual);
+    inf.iterations = it;
+    inf.outer_iterations = nupd;
   } else {
     return set_error(ctx, GT_ERR_INVALID, "unknown solve mode");
   }

@@ -408,8 +408,8 @@ _MODES = {"fp64": _lib.GT_SOLVE_FP64, "ir": _lib.GT_SOLVE_IR, "mixed": _lib.GT_S
 
 
 def solve(p: LinearProblem | Matrix, b=None, x=None, rtol=1e-10, maxit=20000, mode="fp64", raise_on_fail=True):
-    """Jacobi-PCG (mode "fp64"), FP64 refinement around FP32 PCG ("ir"), or
-    FP32 PCG ("fp32").  Returns (x, info dict)."""
+    """Jacobi-PCG (mode "fp64"), FP32 PCG with FP64 reliable updates ("ir" or
+    "mixed"), or FP32 PCG ("fp32").  Returns (x, info dict)."""
     if isinstance(p, LinearProblem):
         A, b, x = p.A, p.b, p.x if x is None else x
     else:

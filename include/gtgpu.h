@@ -55,8 +55,12 @@ extern "C" {
 #define GT_MIXED 2 /* FP64 integration, FP64 values plus an FP32 copy sharing the index arrays */
 
 /* solve modes */
+/* Convergence of GT_SOLVE_FP64 and GT_SOLVE_IR is decided on the FP64 true
+ * residual ||b - A x|| <= rtol ||b||. */
 #define GT_SOLVE_FP64 0 /* Jacobi-PCG in FP64 */
-#define GT_SOLVE_IR 1   /* FP64 iterative refinement around an FP32 Jacobi-PCG */
+#define GT_SOLVE_IR 1   /* Jacobi-PCG in FP32 with FP64 reliable updates: the
+                           FP64 true residual and solution replace the FP32
+                           recurrence whenever its residual fell tenfold */
 #define GT_SOLVE_FP32 2 /* Jacobi-PCG in FP32 (needs FP32 values) */
 
 typedef struct gt_ctx gt_ctx;
@@ -65,8 +69,8 @@ typedef struct gt_space gt_space;
 typedef struct gt_matrix gt_matrix;
 
 typedef struct gt_solve_info {
-  int32_t iterations;       /* total inner (PCG) iterations */
-  int32_t outer_iterations; /* refinement steps (GT_SOLVE_IR), else 0 */
+  int32_t iterations;       /* PCG iterations */
+  int32_t outer_iterations; /* FP64 true-residual updates (GT_SOLVE_FP64/IR), else 0 */
   double rel_residual;      /* final ||b - A x|| / ||b|| in FP64 */
 } gt_solve_info;
 
