@@ -14,8 +14,9 @@ coordinates and the coefficient are copied in from pinned host memory and
 the CSR arrays and the vector are read back into pinned host memory, every
 step.  The JSON line also carries the roofline of the dominant kernel, the
 CPU baseline (the oracle restatement of the reference algorithm on the
-host's cores), the solve rates (plain FP64 PCG vs FP64-refined FP32 PCG) and
-the SM clocks sampled during the timed region.
+host's cores), the solve rates (plain FP64 PCG vs FP32 PCG with FP64 reliable
+updates), the HBM rooflines of the scatter and of the FP64 SpMV, and the SM
+clocks sampled during the timed region.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -39,6 +40,9 @@ sys.path.insert(0, os.path.join(ROOT, "galerkintoolkit.jl_gb300"))
 
 METRIC = "nnz/s assembled (assemble_matrix + assemble_vector, plain FP64)"
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
+# DRAM bytes (read + write) per launch on the default workload, from one ncu
+# capture of each kernel (summaries under profiles/); None until captured
+TRAFFIC: dict = {}
 
 
 def parse():
@@ -191,6 +195,32 @@ def run_serving(args):
            **res, "speedup": res["mixed_served"]["solves_per_s"] / max(res["plain_fp64"]["solves_per_s"], 1e-12),
            "data": "synthetic (seeded)"}
     print(json.dumps(out), flush=True)
+
+
+def spmv_roofline(A, flush, stream, reps=20):
+    """y = A x with the FP64 block-CSR SpMV (gt_spmv, device vectors), L2
+    flushed before each launch; algorithmic bytes = values + column indices +
+    row pointers + x + y."""
+    import torch
+    from gtgpu.api import _ptr
+    n = A.shape[0]
+    x = torch.ones(n, dtype=torch.float64, device="cuda")
+    y = torch.empty(n, dtype=torch.float64, device="cuda")
+    lib = A.ctx.lib
+    ts = []
+    for i in range(reps + 3):
+        flush.fill_(2)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lib.gt_spmv(A.h, _ptr(x), _ptr(y))
+        e1.record(stream)
+        e1.synchronize()
+        if i >= 3:
+            ts.append(e0.elapsed_time(e1))
+    ms = statistics.median(ts)
+    nb = A.nnz * (8 + 4) + (n + 1) * 8 + 2 * n * 8
+    return {"kernel": "k_spmv<1, G, double, double>", "achieved": nb / (ms * 1e-3) / 1e9, "unit": "GB/s",
+            "algorithmic_bytes": nb, "ms": ms, "traffic": TRAFFIC.get("spmv")}
 
 
 def workload(n):
@@ -389,8 +419,11 @@ def main():
     ctx.profile_begin()
     A = step()
     phases = ctx.profile_end()
+    spmv = spmv_roofline(A, flush, stream)
     del A
     peaks, peaks_kind = load_peaks()
+    spmv["frac"] = spmv["achieved"] / peaks["hbm_gbs"]
+    spmv["peak"] = peaks["hbm_gbs"]
     fp64_tf = ctx.fma_rate(fp64=True)
     nc, nn = m.num_cells, 4
     nfree = V.num_free_dofs
@@ -400,19 +433,28 @@ def main():
         "elements": nc * (4 * 4 + 8) + m.num_nodes * 24 + nc * 16 * 8 + nc * 4 * 8,  # reads + Ke/be writes
         "scatter": nc * 16 * 8 + nc * 4 * 4 + nfree * 8 + nnz * (4 + 8),               # Ke, inc, rowptr, colind+values
     }
-    flops_el = nc * 130.0  # FP64 flops per P1 tetrahedron (geometry + 10 entries)
+    # FP64 flops per P1 tetrahedron (FMA = 2, the division = 1): J 9, cofactors
+    # 27, det 5, scale 2, six vertex-1..3 entries 36, vertex-0 entries 8, load 6
+    flops_el = nc * 93.0
     dom = max((k for k in ph if k in ("elements", "scatter", "pattern_count", "pattern_fill", "incidence")),
               key=lambda k: ph[k])
+    hbm = {}
+    for k in ("scatter", "elements"):
+        if k in ph:
+            gbs = alg[k] / (ph[k] * 1e-3) / 1e9
+            hbm[k] = {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
+                      "algorithmic_bytes": alg[k], "ms": ph[k], "traffic": TRAFFIC.get(k)}
     if dom == "elements":
         achieved = flops_el / (ph[dom] * 1e-3) / 1e12
-        roof = {"bound": "fp64", "kernel": "k_elements<P1 tet, Laplacian, FP64>", "achieved": achieved,
+        roof = {"bound": "fp64", "kernel": "k_elements_p1<Laplacian, double>", "achieved": achieved,
                 "peak": fp64_tf, "unit": "TFLOP/s", "frac": achieved / fp64_tf,
-                "peak_source": "measured FP64 FMA rate of this device (gt_ctx_fma_rate)", "traffic": None}
+                "peak_source": "measured FP64 FMA rate of this device (gt_ctx_fma_rate); FP64 units, not tensor",
+                "algorithmic_flops": flops_el, "traffic": TRAFFIC.get("elements")}
     else:
         bytes_dom = alg.get(dom, nnz * 12)
         achieved = bytes_dom / (ph[dom] * 1e-3) / 1e9
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks_kind, "traffic": None}
+                "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks_kind, "traffic": TRAFFIC.get(dom)}
     b_asm = nnz * 8 + nc * 4 * 4 + m.num_nodes * 24 + nc * 8
     step_roof = {"algorithmic_bytes": b_asm, "GB/s": b_asm / (ms * 1e-3) / 1e9,
                  "frac_of_hbm": b_asm / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}
@@ -462,7 +504,8 @@ def main():
             lat.sort()
             res[mode] = {"solves_per_s": 1.0 / statistics.mean(lat), "p50_ms": 1e3 * lat[len(lat) // 2],
                          "p99_ms": 1e3 * lat[-1], "iterations": info["iterations"],
-                         "outer": info["outer_iterations"], "rel_residual": info["rel_residual"]}
+                         "true_residual_updates": info["outer_iterations"], "rel_residual": info["rel_residual"],
+                         "ms_per_iteration": 1e3 * lat[0] / max(1, info["iterations"])}
         res["ir_vs_fp64_rel_err"] = float(np.abs(xs["ir"] - xs["fp64"]).max() / np.abs(xs["fp64"]).max())
         res["rtol"] = 1e-10
         solve = res
@@ -480,7 +523,7 @@ def main():
             "config": wl_config(n, {"nnz": int(nnz), "free_dofs": int(nfree), "parallelism": f"replicas x{world}"}),
             "e2e": {"value": world * nnz / (e2e_ms * 1e-3), "unit": "nnz/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
-            "roofline": roof, "step_roofline": step_roof,
+            "roofline": roof, "step_roofline": step_roof, "hbm_kernels": {**hbm, "spmv_fp64": spmv},
             "phases_ms": {k: round(v, 4) for k, v in phases},
             "cpu_baseline": cpu, "solve": solve, "clocks": clocks.summary(),
             "gpu_launches": int(launches), "wall_s_timed": t_wall}

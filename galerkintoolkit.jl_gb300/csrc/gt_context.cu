@@ -1,6 +1,7 @@
 // gt_context.cu -- context, device buffer pool, error plumbing, scans.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "gt_internal.cuh"
@@ -28,7 +29,9 @@ static size_t size_class(size_t b) {
 }
 
 void* pool_alloc(Ctx* ctx, size_t bytes) {
-  size_t sc = size_class(bytes);
+  // every block has at least 16 bytes past its end: bulk (TMA) copies of a
+  // segment round its end up to a 16-byte boundary
+  size_t sc = size_class(bytes + 16);
   auto it = ctx->pool.lower_bound(sc);
   if (it != ctx->pool.end() && it->first <= sc + sc / 4) {
     void* p = it->second;
@@ -256,6 +259,10 @@ int gt_ctx_create(int device, gt_ctx** out) {
     return GT_ERR_CUDA;
   }
   c->stream = c->own_stream;
+  const char* pcg = getenv("GTGPU_PCG");
+  c->pcg_path = !pcg ? 0 : strcmp(pcg, "launches") == 0 ? 1 : strcmp(pcg, "persistent") == 0 ? 2 : 0;
+  const char* sp = getenv("GTGPU_SPMV");
+  c->tiles_spmv = sp && strcmp(sp, "tiles") == 0;
   cudaMemset(c->d_err, 0, sizeof(uint32_t));
   cudaDeviceSynchronize();
   *out = c;

@@ -78,6 +78,12 @@ struct Ctx {
   int64_t* h_scratch = nullptr;    // pinned small readbacks (64 words)
   double* h_dscratch = nullptr;    // pinned small FP64 readbacks (64 words)
   int64_t launches = 0;            // kernels launched by this context
+  // PCG path: 0 = by size (persistent kernel for small systems, separate
+  // launches per phase for large ones), 1 = always launches, 2 = always
+  // persistent (environment GTGPU_PCG=launches|persistent at context creation)
+  int pcg_path = 0;
+  // bulk-copied row tiles instead of the row-group SpMV (GTGPU_SPMV=tiles)
+  bool tiles_spmv = false;
   // phase profiling: CUDA events recorded on the stream between phases
   bool prof = false;
   std::vector<std::pair<std::string, cudaEvent_t>> marks;
@@ -192,6 +198,9 @@ int scatter_vector(const Space* sp, const int64_t* inc_ptr, const int32_t* inc, 
                    double* b);
 int find_diag(Matrix* A);
 int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mode, gt_solve_info* info);
+// persistent cooperative Jacobi-PCG (gt_pcg.cu); x holds the start value
+int pcg_persistent(Matrix* A, int mode, const double* b, double* x, double rtol, int maxit, int32_t* iters,
+                   int32_t* nupd, int32_t* iters64, double* relres);
 int spmv64(Matrix* A, const double* x, double* y);
 
 // device scans (exclusive prefix sum; out has n+1 entries, out[n] = total)

@@ -1,0 +1,584 @@
+// gt_pcg.cu -- Jacobi-PCG as one persistent, cooperative kernel.
+//
+// The whole iteration runs inside one cooperative launch (chunks of
+// iterations per launch): CTA c owns a contiguous range of block rows, every
+// phase works on the CTA's own rows, and phases are separated by a grid-wide
+// barrier.  A reduction is two-level and identical in every CTA: each CTA
+// writes its partial sums, and after the barrier every CTA adds all partials
+// in the same fixed order, so alpha, beta and the convergence decisions are
+// bitwise the same in all CTAs without a further broadcast.  Per iteration:
+//
+//   P1  q = A p (own rows), p.q            -> barrier, alpha = rz / pq
+//   P2  xs += alpha p, r -= alpha q,       -> barrier, beta, convergence
+//       z = Dinv r, r.z, r.r
+//   [reliable update, when due]
+//   P3  x += xs, xs = 0                    -> barrier
+//   P4  r = b - A64 x (FP64), z = Dinv r   -> barrier, r.z, ||r||^2
+//   P5  p = z + beta p                     -> barrier
+//
+// The iteration runs in X (FP64 or FP32) on the correction xs since the last
+// update, with SpMV values of type V.  With reliable updates (RELIABLE) the
+// FP64 solution takes the correction and the FP64 true residual replaces the
+// recurrence residual whenever the recurrence residual fell by delta since
+// the last update, claims convergence, or maxit is reached; the direction p
+// is then rebuilt from the true residual.  Convergence is decided on the
+// FP64 true residual.  Without reliable updates (the FP32-only mode) the
+// recurrence residual decides and x takes xs at the end.
+//
+// Every grid barrier waits with a time limit: a barrier that does not
+// complete within a second records an error and the kernel returns (the
+// cooperative launch makes all CTAs co-resident, so this does not happen in
+// a correct run).
+#include <cmath>
+#include <cstring>
+
+#include "gt_internal.cuh"
+#include "gt_rowdot.cuh"
+
+namespace gt {
+
+namespace {
+
+constexpr int PT = 256;          // threads per CTA
+constexpr int NW = PT / 32;      // warps per CTA
+constexpr int PSLOT = 4;         // doubles per CTA partial
+constexpr uint64_t BAR_TIMEOUT_NS = 1000000000ull;
+constexpr int PCG_STALLED = 1;   // internal status: the FP32 iteration stalled
+
+struct PState {
+  double rz, rzold, rr, rmax2, bb, tol2;
+  int32_t iters, nupd;
+  int32_t done;     // 1 converged or maxit, 2 FP32 iteration stalled or slowed down: continue in FP64
+  int32_t stall;    // consecutive reliable updates with less than a halving of the true residual
+  int32_t it_upd;   // iteration of the last reliable update
+  int32_t max_cyc;  // longest cycle between reliable updates so far
+};
+
+struct PArgs {
+  const int64_t* rowptr;
+  const int32_t* colind;
+  const void* val;       // iteration values (V)
+  const double* val64;   // FP64 values (true residual), may be null without reliable updates
+  int64_t nrows;         // block rows
+  const double* b;
+  double* x;
+  void *xs, *r, *z, *p, *q;
+  const void* dinv;
+  const float* pcont;    // FP32 direction to continue from (init mode 2)
+  double* part;          // 3 slots x gridDim.x x PSLOT
+  uint32_t* bar;         // barrier counter, zero at launch
+  int32_t* err;          // set to 1 when a barrier timed out
+  PState* st;
+  double rtol2, delta2;
+  int maxit;
+};
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// grid-wide barrier number `target / gridDim.x`; false when it timed out
+__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, int32_t* err, int* s_abort) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    uint64_t t0 = global_ns();
+    while (ld_acquire(bar) < target) {
+      if (global_ns() - t0 > BAR_TIMEOUT_NS) {
+        atomicExch(err, 1);
+        *s_abort = 1;
+        break;
+      }
+      __nanosleep(32);
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *s_abort == 0;
+}
+
+// CTA sum of K values -> out[0..K) (written by thread 0)
+template <int K>
+__device__ __forceinline__ void cta_sum(double (&v)[K], double* s_red, double* out) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+    double t = v[k];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) s_red[k * NW + w] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      double t = 0.0;
+#pragma unroll
+      for (int i = 0; i < NW; i++) t += s_red[k * NW + i];
+      __stcg(out + k, t);
+    }
+  }
+}
+
+// sum of the CTA partials of a slot, in one fixed order that is identical in
+// every CTA: each thread loads its (at most a few) partials at once, warp
+// butterflies (whose result is the same in all lanes), then the warp totals
+// in warp order; result in s_tot[0..K).  s_red is free again at this point.
+template <int K>
+__device__ __forceinline__ void grid_total(const double* slot, int nb, double* s_red, double* s_tot) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double t[K];
+#pragma unroll
+  for (int k = 0; k < K; k++) t[k] = 0.0;
+  for (int i = threadIdx.x; i < nb; i += PT) {
+    const double2 v01 = __ldcg(reinterpret_cast<const double2*>(slot + (size_t)i * PSLOT));
+    t[0] += v01.x;
+    if (K > 1) t[1] += v01.y;
+    if (K > 2) t[2] += __ldcg(slot + (size_t)i * PSLOT + 2);
+  }
+#pragma unroll
+  for (int k = 0; k < K; k++) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) t[k] += __shfl_xor_sync(0xffffffffu, t[k], o);
+    if (lane == 0) s_red[k * NW + w] = t[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < K) {
+    double s = 0.0;
+#pragma unroll
+    for (int i = 0; i < NW; i++) s += s_red[threadIdx.x * NW + i];
+    s_tot[threadIdx.x] = s;
+  }
+  __syncthreads();
+}
+
+template <int BS, int G, class V, class X, bool RELIABLE>
+__global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
+  __shared__ double s_red[3 * NW];
+  __shared__ double s_tot[4];
+  __shared__ int s_abort;
+  constexpr int NG = PT / G;  // row groups per CTA
+  if (threadIdx.x == 0) s_abort = 0;
+  const int nb = gridDim.x, blk = blockIdx.x, tid = threadIdx.x;
+  const int gl = tid % G, grp = tid / G;
+  const int64_t rows_per = (a.nrows + nb - 1) / nb;
+  const int64_t r0 = min(a.nrows, (int64_t)blk * rows_per), r1 = min(a.nrows, r0 + rows_per);
+  const int64_t e0 = r0 * BS, e1 = r1 * BS;
+  X* xs = (X*)a.xs;
+  X* r = (X*)a.r;
+  X* z = (X*)a.z;
+  X* p = (X*)a.p;
+  X* q = (X*)a.q;
+  const X* dinv = (const X*)a.dinv;
+  const V* val = (const V*)a.val;
+  double* slot0 = a.part;
+  double* slot1 = a.part + (size_t)nb * PSLOT;
+  double* slot2 = a.part + (size_t)2 * nb * PSLOT;
+  uint32_t nbar = 0;
+  PState S = *a.st;
+  __syncthreads();
+
+  if (init == 2) {
+    // continuation of an FP32 run in FP64: x holds the FP64 solution, pcont
+    // the FP32 direction; r = b - A x, z = Dinv r, p = z + beta pcont with
+    // beta = r.z / rzold, so the Krylov direction carries over
+    double v[2] = {0.0, 0.0};
+    for (int64_t base = r0; base < r1; base += NG) {
+      int64_t row = base + grp;
+      const bool valid = row < r1;
+      if (!valid) row = r1 - 1;
+      double o[BS];
+      row_dot<BS, G, double, double, double, true>(a.rowptr, a.colind, a.val64, a.x, row, gl, o);
+      if (gl == 0 && valid) {
+#pragma unroll
+        for (int c = 0; c < BS; c++) {
+          const int64_t i = row * BS + c;
+          const double ri = a.b[i] - o[c];
+          const X rx = (X)ri, zx = dinv[i] * rx;
+          r[i] = rx;
+          z[i] = zx;
+          xs[i] = (X)0;
+          v[0] += (double)rx * (double)zx;
+          v[1] += ri * ri;
+        }
+      }
+    }
+    cta_sum<2>(v, s_red, slot2 + (size_t)blk * PSLOT);
+    if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
+    grid_total<2>(slot2, nb, s_red, s_tot);
+    const X bx = (X)(S.rzold != 0.0 ? s_tot[0] / S.rzold : 0.0);
+    for (int64_t i = e0 + tid; i < e1; i += PT) p[i] = z[i] + bx * (X)a.pcont[i];
+    S.rz = s_tot[0];
+    S.rr = s_tot[1];
+    S.rmax2 = S.rr;
+    S.it_upd = S.iters;
+    S.max_cyc = 0;
+    S.stall = 0;
+    S.done = S.rr <= S.tol2;
+    if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
+  } else if (init) {
+    // r = b - A x0 (FP64 products), z = Dinv r, p = z, xs = 0; r.z, r.r, b.b
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int64_t base = r0; base < r1; base += NG) {
+      int64_t row = base + grp;
+      const bool valid = row < r1;
+      if (!valid) row = r1 - 1;
+      double o[BS];
+      if constexpr (RELIABLE) row_dot<BS, G, double, double, double, true>(a.rowptr, a.colind, a.val64, a.x, row, gl, o);
+      else row_dot<BS, G, V, double, double, true>(a.rowptr, a.colind, val, a.x, row, gl, o);
+      if (gl == 0 && valid) {
+#pragma unroll
+        for (int c = 0; c < BS; c++) {
+          const int64_t i = row * BS + c;
+          const double bi = a.b[i], ri = bi - o[c];
+          const X rx = (X)ri, zx = dinv[i] * rx;
+          r[i] = rx;
+          z[i] = zx;
+          p[i] = zx;
+          xs[i] = (X)0;
+          v[0] += (double)rx * (double)zx;
+          v[1] += ri * ri;
+          v[2] += bi * bi;
+        }
+      }
+    }
+    cta_sum<3>(v, s_red, slot2 + (size_t)blk * PSLOT);
+    if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
+    grid_total<3>(slot2, nb, s_red, s_tot);
+    S.rz = s_tot[0];
+    S.rr = s_tot[1];
+    S.bb = s_tot[2];
+    S.tol2 = a.rtol2 * S.bb;
+    S.rmax2 = S.rr;
+    S.rzold = 0.0;
+    S.iters = 0;
+    S.nupd = 0;
+    S.done = S.rr <= S.tol2;
+  }
+
+  while (!S.done && S.iters < it_end) {
+    // P1: q = A p, p.q
+    double pq;
+    {
+      X acc = (X)0;
+      for (int64_t base = r0; base < r1; base += 2 * NG) {
+        int64_t ra = base + grp, rb = base + NG + grp;
+        const bool va = ra < r1, vb = rb < r1;
+        if (!va) ra = r1 - 1;
+        if (!vb) rb = r1 - 1;
+        X oa[BS], ob[BS];
+        row_dot<BS, G, V, X, X, true>(a.rowptr, a.colind, val, p, ra, gl, oa);
+        row_dot<BS, G, V, X, X, true>(a.rowptr, a.colind, val, p, rb, gl, ob);
+        if (gl == 0) {
+#pragma unroll
+          for (int c = 0; c < BS; c++) {
+            if (va) {
+              q[ra * BS + c] = oa[c];
+              acc += oa[c] * __ldcg(p + ra * BS + c);
+            }
+            if (vb) {
+              q[rb * BS + c] = ob[c];
+              acc += ob[c] * __ldcg(p + rb * BS + c);
+            }
+          }
+        }
+      }
+      double v[1] = {(double)acc};
+      cta_sum<1>(v, s_red, slot0 + (size_t)blk * PSLOT);
+      if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
+      grid_total<1>(slot0, nb, s_red, s_tot);
+      pq = s_tot[0];
+    }
+    const X alpha = (X)(S.rz / pq);
+    // P2: xs += alpha p, r -= alpha q, z = Dinv r; r.z, r.r
+    double rzn, rr;
+    {
+      X v0 = (X)0, v1 = (X)0;
+#pragma unroll 4
+      for (int64_t i = e0 + tid; i < e1; i += PT) {
+        const X ri = r[i] - alpha * q[i];
+        const X zi = dinv[i] * ri;
+        xs[i] += alpha * p[i];
+        r[i] = ri;
+        z[i] = zi;
+        v0 += ri * zi;
+        v1 += ri * ri;
+      }
+      double v[2] = {(double)v0, (double)v1};
+      cta_sum<2>(v, s_red, slot1 + (size_t)blk * PSLOT);
+      if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
+      grid_total<2>(slot1, nb, s_red, s_tot);
+      rzn = s_tot[0];
+      rr = s_tot[1];
+    }
+    S.iters += 1;
+    double beta = rzn / S.rz;
+    S.rzold = S.rz;
+    S.rz = rzn;
+    S.rr = rr;
+    const bool stop = rr <= S.tol2 || S.iters >= a.maxit || !(rr == rr);
+    if constexpr (RELIABLE) {
+      // an FP32 cycle (recurrence residual down by delta) that runs past 2.5x
+      // the longest earlier cycle: the FP32 iteration has lost the rate of
+      // the exact iteration (eps32 * cond(A) too large); hand over to FP64
+      const int cyc = S.iters - S.it_upd;
+      const bool slow = sizeof(X) < sizeof(double) && S.max_cyc > 0 && cyc > (5 * S.max_cyc) / 2 + 16;
+      if (stop || slow || rr <= a.delta2 * S.rmax2) {
+        // P3: x += xs
+        for (int64_t i = e0 + tid; i < e1; i += PT) {
+          a.x[i] += (double)xs[i];
+          xs[i] = (X)0;
+        }
+        if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
+        // P4: true residual in FP64
+        double v[2] = {0.0, 0.0};
+        for (int64_t base = r0; base < r1; base += NG) {
+          int64_t row = base + grp;
+          const bool valid = row < r1;
+          if (!valid) row = r1 - 1;
+          double o[BS];
+          row_dot<BS, G, double, double, double, true>(a.rowptr, a.colind, a.val64, a.x, row, gl, o);
+          if (gl == 0 && valid) {
+#pragma unroll
+            for (int c = 0; c < BS; c++) {
+              const int64_t i = row * BS + c;
+              const double ri = a.b[i] - o[c];
+              const X rx = (X)ri, zx = dinv[i] * rx;
+              r[i] = rx;
+              z[i] = zx;
+              v[0] += (double)rx * (double)zx;
+              v[1] += ri * ri;
+            }
+          }
+        }
+        cta_sum<2>(v, s_red, slot2 + (size_t)blk * PSLOT);
+        if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
+        grid_total<2>(slot2, nb, s_red, s_tot);
+        beta = S.rzold != 0.0 ? s_tot[0] / S.rzold : 0.0;
+        const double prev = S.rmax2;
+        S.rz = s_tot[0];
+        S.rr = s_tot[1];
+        S.rmax2 = s_tot[1];
+        S.nupd += 1;
+        S.done = s_tot[1] <= S.tol2 || S.iters >= a.maxit || !(s_tot[1] == s_tot[1]);
+        if (sizeof(X) < sizeof(double) && !S.done) {
+          // the recurrence fell by delta but the true residual did not halve:
+          // the FP32 operator no longer resolves the error (eps32 * cond ~ 1)
+          S.stall = s_tot[1] > 0.25 * prev ? S.stall + 1 : 0;
+          if (S.stall >= 3 || slow) S.done = 2;
+        }
+        if (cyc > S.max_cyc) S.max_cyc = cyc;
+        S.it_upd = S.iters;
+      }
+    } else {
+      S.done = stop;
+    }
+    if (S.done) break;
+    // P5: p = z + beta p
+    const X bx = (X)beta;
+#pragma unroll 4
+    for (int64_t i = e0 + tid; i < e1; i += PT) p[i] = z[i] + bx * p[i];
+    if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
+  }
+  if (!RELIABLE && S.done) {
+    for (int64_t i = e0 + tid; i < e1; i += PT) {
+      a.x[i] += (double)xs[i];
+      xs[i] = (X)0;
+    }
+  }
+  if (blk == 0 && tid == 0) *a.st = S;
+}
+
+template <int BS, class V, class X>
+__global__ void k_pdinv(const int64_t* rowptr, const int32_t* diag_pos, const V* val, int64_t nbrows, X* dinv) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (t >= nbrows * BS) return;
+  int64_t r = t / BS;
+  int c = (int)(t - r * BS);
+  int64_t k = rowptr[r] + diag_pos[r];
+  dinv[t] = (X)(1.0 / (double)val[k * BS * BS + c * BS + c]);
+}
+
+int lanes_for(const Matrix* A) { return row_lanes(A->nbrows > 0 ? (double)A->bnnz / (double)A->nbrows : 1.0); }
+
+// result of one persistent run; a stalled FP32 run keeps its direction p32
+// for the FP64 continuation
+struct PRun {
+  PState st{};
+  bool stalled = false;
+  float* p32 = nullptr;
+};
+
+template <int BS, int G, class V, class X, bool REL>
+int run_typed(Matrix* A, const V* val, const double* b, double* x, double rtol, int maxit, double delta,
+              const PRun* from, PRun* out) {
+  Ctx* ctx = A->ctx;
+  cudaStream_t s = ctx->stream;
+  const int64_t n = A->nbrows * BS;
+  auto kern = k_pcg<BS, G, V, X, REL>;
+  int per_sm = 0;
+  GT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PT, 0));
+  if (per_sm < 1) return set_error(ctx, GT_ERR_CUDA, "persistent PCG kernel does not fit on an SM");
+  constexpr int NG = PT / G;
+  int64_t want = (A->nbrows + 2 * NG - 1) / (2 * NG);  // at least two row passes per CTA
+  int64_t cap = (int64_t)per_sm * ctx->num_sms;
+  int nb = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+  X *xs = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
+  double* part = nullptr;
+  uint32_t* bar = nullptr;
+  int32_t* err = nullptr;
+  PState* st = nullptr;
+  GT_TRY(dalloc(ctx, &xs, n));
+  GT_TRY(dalloc(ctx, &r, n));
+  GT_TRY(dalloc(ctx, &z, n));
+  GT_TRY(dalloc(ctx, &p, n));
+  GT_TRY(dalloc(ctx, &q, n));
+  GT_TRY(dalloc(ctx, &dinv, n));
+  GT_TRY(dalloc(ctx, &part, (int64_t)3 * nb * PSLOT));
+  GT_TRY(dalloc(ctx, &bar, 2));
+  GT_TRY(dalloc(ctx, &err, 2));
+  GT_TRY(dalloc(ctx, (unsigned char**)&st, sizeof(PState)));
+  GT_CUDA(ctx, cudaMemsetAsync(err, 0, 2 * sizeof(int32_t), s));
+  if (from) {
+    // continuation: scalars of the FP32 run (iteration count, ||b||, rzold)
+    PState* h0 = reinterpret_cast<PState*>(ctx->h_dscratch);
+    *h0 = from->st;
+    h0->done = 0;
+    GT_CUDA(ctx, cudaMemcpyAsync(st, h0, sizeof(PState), cudaMemcpyHostToDevice, s));
+    GT_CUDA(ctx, cudaStreamSynchronize(s));
+  } else {
+    GT_CUDA(ctx, cudaMemsetAsync(st, 0, sizeof(PState), s));
+  }
+  GT_TRY(find_diag(A));
+  const double* dval = REL ? A->val64 : (const double*)nullptr;
+  if (REL || A->val64)
+    k_pdinv<BS, double, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, A->val64, A->nbrows, dinv);
+  else
+    k_pdinv<BS, V, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
+  GT_LAUNCH(ctx, "k_pdinv");
+  PArgs args{};
+  args.rowptr = A->rowptr;
+  args.colind = A->colind;
+  args.val = val;
+  args.val64 = dval;
+  args.nrows = A->nbrows;
+  args.b = b;
+  args.x = x;
+  args.xs = xs;
+  args.r = r;
+  args.z = z;
+  args.p = p;
+  args.q = q;
+  args.dinv = dinv;
+  args.pcont = from ? from->p32 : nullptr;
+  args.part = part;
+  args.bar = bar;
+  args.err = err;
+  args.st = st;
+  args.rtol2 = rtol * rtol;
+  args.delta2 = delta * delta;
+  args.maxit = maxit;
+  PState h{};
+  int status = GT_OK;
+  int chunk = 32, done_iters = from ? from->st.iters : 0;
+  for (int launch = 0;; launch++) {
+    int init = launch == 0 ? (from ? 2 : 1) : 0;
+    int it_end = done_iters + chunk;
+    if (it_end > maxit || it_end < 0) it_end = maxit;
+    GT_CUDA(ctx, cudaMemsetAsync(bar, 0, sizeof(uint32_t), s));
+    void* kargs[] = {&args, &init, &it_end};
+    ctx->launches++;
+    GT_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(nb), dim3(PT), kargs, 0, s));
+    GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, st, sizeof(PState), cudaMemcpyDeviceToHost, s));
+    GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_scratch, err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    GT_CUDA(ctx, cudaStreamSynchronize(s));
+    memcpy(&h, ctx->h_dscratch, sizeof(PState));
+    int32_t e = 0;
+    memcpy(&e, ctx->h_scratch, sizeof(int32_t));
+    if (e) {
+      status = set_error(ctx, GT_ERR_TIMEOUT, "persistent PCG: a grid barrier timed out");
+      break;
+    }
+    done_iters = h.iters;
+    if (h.done || h.iters >= maxit) break;
+    if (chunk < 2048) chunk *= 2;
+  }
+  out->st = h;
+  if (status == GT_OK && h.done == 2) {
+    status = PCG_STALLED;
+    out->stalled = true;
+    if constexpr (sizeof(X) == sizeof(float)) {
+      out->p32 = reinterpret_cast<float*>(p);
+      p = nullptr;
+    }
+  } else if (status == GT_OK && !(h.rr <= h.tol2)) {
+    status = GT_ERR_NOT_CONVERGED;
+  }
+  dfree(ctx, xs);
+  dfree(ctx, r);
+  dfree(ctx, z);
+  dfree(ctx, p);
+  dfree(ctx, q);
+  dfree(ctx, dinv);
+  dfree(ctx, part);
+  dfree(ctx, bar);
+  dfree(ctx, err);
+  pool_free(ctx, st);
+  return status;
+}
+
+template <class V, class X, bool REL>
+int run_dispatch(Matrix* A, const V* val, const double* b, double* x, double rtol, int maxit, double delta,
+                 const PRun* from, PRun* out) {
+  const int G = lanes_for(A);
+#define GT_PCG_CASE(BS_, G_)                                                                                   \
+  if (A->bs == BS_ && G == G_) return run_typed<BS_, G_, V, X, REL>(A, val, b, x, rtol, maxit, delta, from, out);
+  GT_PCG_CASE(1, 1) GT_PCG_CASE(1, 2) GT_PCG_CASE(1, 4) GT_PCG_CASE(1, 8)
+  GT_PCG_CASE(2, 1) GT_PCG_CASE(2, 2) GT_PCG_CASE(2, 4) GT_PCG_CASE(2, 8)
+  GT_PCG_CASE(3, 1) GT_PCG_CASE(3, 2) GT_PCG_CASE(3, 4) GT_PCG_CASE(3, 8)
+#undef GT_PCG_CASE
+  return set_error(A->ctx, GT_ERR_UNSUPPORTED, "persistent PCG: unsupported block size");
+}
+
+}  // namespace
+
+int pcg_persistent(Matrix* A, int mode, const double* b, double* x, double rtol, int maxit, int32_t* iters,
+                   int32_t* nupd, int32_t* iters64, double* relres) {
+  PRun run;
+  int s;
+  *iters64 = 0;
+  if (mode == GT_SOLVE_FP64) {
+    s = run_dispatch<double, double, true>(A, A->val64, b, x, rtol, maxit, 0.0, nullptr, &run);
+    *iters64 = run.st.iters;
+  } else if (mode == GT_SOLVE_IR) {
+    s = run_dispatch<float, float, true>(A, A->val32, b, x, rtol, maxit, 0.1, nullptr, &run);
+    if (s == PCG_STALLED) {
+      // the FP32 iteration stalled or lost its rate (eps32 * cond(A) too
+      // large): the same Krylov iteration goes on in FP64 from the current
+      // FP64 solution and the FP32 direction
+      PRun r32 = run;
+      PRun r64;
+      s = run_dispatch<double, double, true>(A, A->val64, b, x, rtol, maxit, 0.0, &r32, &r64);
+      if (r32.p32) pool_free(A->ctx, r32.p32);
+      *iters64 = r64.st.iters - r32.st.iters;
+      run = r64;
+    }
+  } else {
+    s = run_dispatch<float, float, false>(A, A->val32, b, x, rtol, maxit, 0.0, nullptr, &run);
+  }
+  *iters = run.st.iters;
+  *nupd = run.st.nupd;
+  *relres = run.st.bb > 0 ? sqrt(run.st.rr / run.st.bb) : 0.0;
+  return s;
+}
+
+}  // namespace gt

@@ -18,12 +18,16 @@
 #include <type_traits>
 
 #include "gt_internal.cuh"
+#include "gt_rowdot.cuh"
+#include "gt_tiles.cuh"
 
 namespace gt {
 
 constexpr int RED_T = 256;  // threads per CTA of the reduction kernels
 constexpr int GROUP = 256;  // CTAs per first-level reduction group
 constexpr int CHUNK = 16;   // CG iterations between host polls
+constexpr int CG_STALLED = 1;  // internal status: the FP32 iteration stalled
+constexpr int64_t kPersistentMaxRows = 262144;  // scalar rows solved by the persistent kernel
 
 // device-resident CG state (one per solve)
 struct CGState {
@@ -32,7 +36,9 @@ struct CGState {
   double rmax2;   // ||r||^2 at the last reliable update
   double delta2;  // reliable update when the recurrence residual fell by delta
   double rzold;   // r.z before the last recurrence step
-  int32_t done, iters, maxit, upd, nupd, pad;
+  int32_t done;   // 1 converged or maxit, 2 FP32 iteration stalled or slowed down
+  int32_t iters, maxit, upd, nupd;
+  int32_t it_upd, max_cyc, stall, slow;  // reliable-update cycle bookkeeping
 };
 
 // reduction scratch sized for the largest grid of a solve
@@ -121,50 +127,15 @@ __device__ bool reduce_last(A (&v)[K], RedBuf rb) {
 }
 
 // ---------------------------------------------------------------------------
-// SpMV: G lanes per block row (whole groups stay in the shuffles; rows past
-// the end compute the last row again and write nothing)
+// SpMV: G lanes per block row (row_dot, gt_rowdot.cuh); whole groups stay in
+// the shuffles, rows past the end compute the last row again and write
+// nothing
 // ---------------------------------------------------------------------------
 template <int BS, int G, class V, class X>
 __device__ __forceinline__ void row_product(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                                             const V* __restrict__ val, const X* __restrict__ x, int64_t r, int gl,
                                             X* out) {
-  X acc[BS];
-#pragma unroll
-  for (int c = 0; c < BS; c++) acc[c] = (X)0;
-  int64_t b = rowptr[r], e = rowptr[r + 1];
-  // two entries per lane per trip: both index loads, then both gathers, are
-  // independent and in flight together
-  int64_t k = b + gl;
-  for (; k + G < e; k += 2 * G) {
-    int32_t j0 = __ldg(colind + k), j1 = __ldg(colind + k + G);
-    const V* b0 = val + k * BS * BS;
-    const V* b1 = val + (k + G) * BS * BS;
-#pragma unroll
-    for (int d = 0; d < BS; d++) {
-      X x0 = x[(int64_t)j0 * BS + d], x1 = x[(int64_t)j1 * BS + d];
-#pragma unroll
-      for (int c = 0; c < BS; c++) {
-        acc[c] = fma((X)__ldg(b0 + c * BS + d), x0, acc[c]);
-        acc[c] = fma((X)__ldg(b1 + c * BS + d), x1, acc[c]);
-      }
-    }
-  }
-  if (k < e) {
-    int32_t j = __ldg(colind + k);
-    const V* blk = val + k * BS * BS;
-#pragma unroll
-    for (int d = 0; d < BS; d++) {
-      X xj = x[(int64_t)j * BS + d];
-#pragma unroll
-      for (int c = 0; c < BS; c++) acc[c] = fma((X)__ldg(blk + c * BS + d), xj, acc[c]);
-    }
-  }
-#pragma unroll
-  for (int c = 0; c < BS; c++) {
-#pragma unroll
-    for (int o = G >> 1; o; o >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-    out[c] = acc[c];
-  }
+  row_dot<BS, G, V, X, X, false>(rowptr, colind, val, x, r, gl, out);
 }
 
 // y = A x   (or y = bsub - A x)
@@ -327,17 +298,6 @@ __global__ void k_dinv(const int64_t* rowptr, const int32_t* diag_pos, const V* 
   dinv[t] = (X)(1.0 / (double)val[k * BS * BS + c * BS + c]);
 }
 
-// mixed precision helpers: rf = r / ||r|| (FP32), x += ||r|| d
-__global__ void k_scale_to_f32(const double* r, int64_t n, const double* norm2, float* out) {
-  double sc = *norm2 > 0.0 ? 1.0 / sqrt(*norm2) : 1.0;
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) out[i] = (float)(r[i] * sc);
-}
-__global__ void k_add_scaled_f32(double* x, const float* d, int64_t n, const double* norm2) {
-  double sc = *norm2 > 0.0 ? sqrt(*norm2) : 1.0;
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (i < n) x[i] += sc * (double)d[i];
-}
 __global__ void k_copy_f64_to_f32(const double* a, int64_t n, float* out) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i < n) out[i] = (float)a[i];
@@ -347,17 +307,40 @@ __global__ void k_copy_f32_to_f64(const float* a, int64_t n, double* out) {
   if (i < n) out[i] = (double)a[i];
 }
 
+// scalar CSR SpMV over bulk-copied row tiles (gt_tiles.cuh): y = A x or
+// y = bsub - A x
+template <int G, class V, class X>
+__global__ void __launch_bounds__(TILE_T) k_spmv_tiles(const int64_t* __restrict__ rowptr,
+                                                       const int32_t* __restrict__ colind, const V* __restrict__ val,
+                                                       const X* __restrict__ x, int64_t nrows,
+                                                       const X* __restrict__ bsub, X* __restrict__ y, uint32_t* err) {
+  extern __shared__ __align__(128) unsigned char tsm[];
+  spmv_tiles<G, V, X, false>(rowptr, colind, val, x, bsub, y, nrows, tsm, err, nullptr);
+}
+
+// q = A p and p.q over bulk-copied row tiles; the last CTA sets alpha
+template <int G, class V, class X>
+__global__ void __launch_bounds__(TILE_T) k_cg_spmv_tiles(const int64_t* __restrict__ rowptr,
+                                                          const int32_t* __restrict__ colind, const V* __restrict__ val,
+                                                          const X* __restrict__ p, X* __restrict__ q, int64_t nrows,
+                                                          CGState* st, RedBuf rb, uint32_t* err) {
+  extern __shared__ __align__(128) unsigned char tsm[];
+  if (st->done) return;
+  X dot = (X)0;
+  spmv_tiles<G, V, X, true>(rowptr, colind, val, p, nullptr, q, nrows, tsm, err, &dot);
+  X v[1] = {dot};
+  if (reduce_last<1, X>(v, rb) && threadIdx.x == 0) {
+    st->pq = (double)v[0];
+    st->alpha = st->rz / (double)v[0];
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-// lanes per block row: about 4 entries per lane, so that many rows are in
-// flight per SM (the SpMV is latency-bound with one entry per lane)
+// lanes per block row (row_lanes, gt_rowdot.cuh)
 static int pick_group(const Matrix* A) {
-  double avg = A->nbrows > 0 ? (double)A->bnnz / (double)A->nbrows : 1.0;
-  if (avg <= 16) return 4;
-  if (avg <= 32) return 8;
-  if (avg <= 64) return 16;
-  return 32;
+  return row_lanes(A->nbrows > 0 ? (double)A->bnnz / (double)A->nbrows : 1.0);
 }
 static unsigned spmv_grid(const Matrix* A) {
   int64_t g = (A->nbrows * pick_group(A) + RED_T - 1) / RED_T;
@@ -406,16 +389,57 @@ struct Ops {
     using I2 = std::integral_constant<int, 2>;
     using I3 = std::integral_constant<int, 3>;
     auto byg = [&](auto bst) {
-      if (G == 4) go(bst, std::integral_constant<int, 4>());
-      else if (G == 8) go(bst, std::integral_constant<int, 8>());
-      else if (G == 16) go(bst, std::integral_constant<int, 16>());
-      else go(bst, std::integral_constant<int, 32>());
+      if (G == 1) go(bst, std::integral_constant<int, 1>());
+      else if (G == 2) go(bst, std::integral_constant<int, 2>());
+      else if (G == 4) go(bst, std::integral_constant<int, 4>());
+      else go(bst, std::integral_constant<int, 8>());
     };
     if (bs == 1) byg(I1());
     else if (bs == 2) byg(I2());
     else byg(I3());
   }
+  // lanes per row of the tiled SpMV (R = 256 / G rows per tile, at most
+  // TILE_CAP entries per tile); 0 when the tiled kernel does not apply
+  static int tile_lanes(const Matrix* A) {
+    if (A->bs != 1 || !A->ctx->tiles_spmv) return 0;
+    for (int g = 1; g <= 32; g *= 2)
+      if ((int64_t)(TILE_T / g) * A->max_row <= TILE_CAP) return g;
+    return 0;
+  }
+  template <class F>
+  static void by_lanes(int g, F&& go) {
+    switch (g) {
+      case 1: go(std::integral_constant<int, 1>()); break;
+      case 2: go(std::integral_constant<int, 2>()); break;
+      case 4: go(std::integral_constant<int, 4>()); break;
+      case 8: go(std::integral_constant<int, 8>()); break;
+      case 16: go(std::integral_constant<int, 16>()); break;
+      default: go(std::integral_constant<int, 32>()); break;
+    }
+  }
+  // persistent grid of the tiled kernels: every resident CTA walks tiles
+  template <class K>
+  static unsigned tiles_grid(Ctx* ctx, const Matrix* A, int g, K kern) {
+    const size_t smem = tiles_smem_bytes<V>();
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TILE_T, smem);
+    int64_t ntiles = (A->nbrows + TILE_T / g - 1) / (TILE_T / g);
+    int64_t cap = (int64_t)(per_sm > 0 ? per_sm : 1) * ctx->num_sms;
+    return (unsigned)(ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap);
+  }
   static int spmv(Ctx* ctx, const Matrix* A, const V* val, const X* x, const X* bsub, X* y) {
+    if (int tg = tile_lanes(A)) {
+      by_lanes(tg, [&](auto g_t) {
+        constexpr int GG = decltype(g_t)::value;
+        auto kern = k_spmv_tiles<GG, V, X>;
+        unsigned grid = tiles_grid(ctx, A, GG, kern);
+        kern<<<GT_KC(ctx, grid), TILE_T, tiles_smem_bytes<V>(), ctx->stream>>>(A->rowptr, A->colind, val, x, A->nbrows,
+                                                                               bsub, y, ctx->d_err);
+      });
+      GT_LAUNCH(ctx, "k_spmv_tiles");
+      return GT_OK;
+    }
     unsigned grid = spmv_grid(A);
     dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
@@ -425,6 +449,17 @@ struct Ops {
     return GT_OK;
   }
   static int cg_spmv(Ctx* ctx, const Matrix* A, const V* val, const X* p, X* q, CGState* st, RedBuf rb) {
+    if (int tg = tile_lanes(A)) {
+      by_lanes(tg, [&](auto g_t) {
+        constexpr int GG = decltype(g_t)::value;
+        auto kern = k_cg_spmv_tiles<GG, V, X>;
+        unsigned grid = tiles_grid(ctx, A, GG, kern);
+        kern<<<GT_KC(ctx, grid), TILE_T, tiles_smem_bytes<V>(), ctx->stream>>>(A->rowptr, A->colind, val, p, q,
+                                                                               A->nbrows, st, rb, ctx->d_err);
+      });
+      GT_LAUNCH(ctx, "k_cg_spmv_tiles");
+      return GT_OK;
+    }
     unsigned grid = cg_spmv_grid(A);
     dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
@@ -548,7 +583,12 @@ __global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __re
     st->rz = rz;
     st->rr = rr;
     st->iters += 1;
-    if (rr <= st->tol2 || rr <= st->delta2 * st->rmax2 || st->iters >= st->maxit || !(rr == rr)) st->upd = 1;
+    // an FP32 cycle running past 2.5x the longest earlier one: the FP32
+    // iteration has lost the rate of the exact iteration (eps32 * cond(A))
+    const int cyc = st->iters - st->it_upd;
+    st->slow = sizeof(X) < sizeof(double) && st->max_cyc > 0 && cyc > (5 * st->max_cyc) / 2 + 16;
+    if (rr <= st->tol2 || rr <= st->delta2 * st->rmax2 || st->iters >= st->maxit || !(rr == rr) || st->slow)
+      st->upd = 1;
   }
 }
 
@@ -600,10 +640,20 @@ __global__ void __launch_bounds__(RED_T) k_rl_resid(const int64_t* __restrict__ 
   if (reduce_last<2, double, G>(v, rb) && threadIdx.x == 0) {
     // the next direction is built from the true residual
     st->beta = st->rzold != 0.0 ? v[0] / st->rzold : 0.0;
+    const double prev = st->rmax2;
     st->rz = v[0];
     st->rr = v[1];
     st->nupd += 1;
     if (v[1] <= st->tol2 || st->iters >= st->maxit || !(v[1] == v[1])) st->done = 1;
+    if (sizeof(X) < sizeof(double) && !st->done && st->nupd > 1) {
+      // the recurrence fell by delta but the true residual did not halve,
+      // three times running, or the cycle slowed down: continue in FP64
+      st->stall = v[1] > 0.25 * prev ? st->stall + 1 : 0;
+      if (st->stall >= 3 || st->slow) st->done = 2;
+    }
+    const int cyc = st->iters - st->it_upd;
+    if (st->nupd > 1 && cyc > st->max_cyc) st->max_cyc = cyc;
+    st->it_upd = st->iters;
     st->rmax2 = v[1];
     st->upd = 0;
   }
@@ -689,7 +739,7 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
   *iters_out = h.iters;
   *nupd_out = h.nupd;
   *relres_out = h.bb > 0 ? sqrt(h.rr / h.bb) : 0.0;
-  int status = (h.rr <= h.tol2) ? GT_OK : GT_ERR_NOT_CONVERGED;
+  int status = h.done == 2 ? CG_STALLED : (h.rr <= h.tol2) ? GT_OK : GT_ERR_NOT_CONVERGED;
   dfree(ctx, xs);
   dfree(ctx, r);
   dfree(ctx, z);
@@ -739,8 +789,31 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
     return GT_OK;
   }
   unsigned gv = vec_grid(n);
+  if (mode == GT_SOLVE_FP64 && !A->val64)
+    return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_FP64 needs FP64 values (assemble with GT_FP64 or GT_MIXED)");
+  if (mode == GT_SOLVE_FP32 && !A->val32)
+    return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_FP32 needs FP32 values (GT_FP32 or GT_MIXED)");
+  if (mode == GT_SOLVE_IR && (!A->val64 || !A->val32))
+    return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_IR needs GT_MIXED values");
+  if (mode != GT_SOLVE_FP64 && mode != GT_SOLVE_FP32 && mode != GT_SOLVE_IR)
+    return set_error(ctx, GT_ERR_INVALID, "unknown solve mode");
+  // the persistent kernel saves the per-phase launches and grid-wide
+  // reduction tails that dominate small systems; large systems keep more
+  // loads in flight with one launch per phase (measured crossover)
+  const bool persistent = ctx->pcg_path == 2 || (ctx->pcg_path == 0 && n <= kPersistentMaxRows);
+  if (persistent) {
+    int32_t it = 0, nupd = 0, it64 = 0;
+    status = pcg_persistent(A, mode, b, x, rtol, maxit, &it, &nupd, &it64, &inf.rel_residual);
+    if (status != GT_OK && status != GT_ERR_NOT_CONVERGED) return status;
+    inf.iterations = it;
+    inf.outer_iterations = mode == GT_SOLVE_FP32 ? 0 : nupd;
+    inf.fp64_iterations = it64;
+    if (mode == GT_SOLVE_FP32 && A->val64) GT_TRY(true_residual(A, b, x, &inf.rel_residual));
+    if (info) *info = inf;
+    if (status == GT_ERR_NOT_CONVERGED) set_error(ctx, status, "solver did not reach the tolerance within maxit");
+    return status;
+  }
   if (mode == GT_SOLVE_FP64) {
-    if (!A->val64) return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_FP64 needs FP64 values (assemble with GT_FP64 or GT_MIXED)");
     // FP64 CG; a recurrence residual below the tolerance is checked against
     // the true residual (delta = 0: updates only there) and the iteration
     // goes on from the true residual when that is still above it
@@ -748,6 +821,7 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
     status = pcg_reliable<double, double>(A, A->val64, b, x, rtol, maxit, 0.0, &it, &nupd, &inf.rel_residual);
     inf.iterations = it;
     inf.outer_iterations = nupd;
+    inf.fp64_iterations = it;
   } else if (mode == GT_SOLVE_FP32) {
     if (!A->val32) return set_error(ctx, GT_ERR_INVALID, "GT_SOLVE_FP32 needs FP32 values (GT_FP32 or GT_MIXED)");
     float *bf = nullptr, *xf = nullptr;
@@ -772,12 +846,24 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
     // residual and solution update each time the residual fell tenfold
     int32_t it = 0, nupd = 0;
     status = pcg_reliable<float, float>(A, A->val32, b, x, rtol, maxit, 0.1, &it, &nupd, &inf.rel_residual);
+    if (status == CG_STALLED) {
+      // eps32 * cond(A) too large for the FP32 iteration: FP64 CG from the
+      // current FP64 solution
+      int32_t it2 = 0, nu2 = 0;
+      status = pcg_reliable<double, double>(A, A->val64, b, x, rtol, maxit - it, 0.0, &it2, &nu2, &inf.rel_residual);
+      inf.fp64_iterations = it2;
+      it += it2;
+      nupd += nu2;
+    }
     inf.iterations = it;
     inf.outer_iterations = nupd;
   } else {
     return set_error(ctx, GT_ERR_INVALID, "unknown solve mode");
   }
   if (info) *info = inf;
+  uint32_t bits = 0;
+  GT_TRY(take_device_error(ctx, &bits));
+  if (bits & DEV_ERR_TIMEOUT) return set_error(ctx, GT_ERR_TIMEOUT, "solve: a tile copy did not complete");
   if (status == GT_ERR_NOT_CONVERGED) set_error(ctx, status, "solver did not reach the tolerance within maxit");
   return status;
 }
@@ -837,6 +923,9 @@ int gt_spmv(gt_matrix* A, const double* x, double* y) {
   if (s == GT_OK && !ydev) s = copy_out(ctx, y, yd, n);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (s == GT_OK && e != cudaSuccess) s = check_cuda(ctx, e, "gt_spmv");
+  uint32_t bits = 0;
+  if (s == GT_OK) s = take_device_error(ctx, &bits);
+  if (s == GT_OK && (bits & DEV_ERR_TIMEOUT)) s = set_error(ctx, GT_ERR_TIMEOUT, "gt_spmv: a tile copy did not complete");
   if (!xdev) dfree(ctx, xd);
   if (!ydev) dfree(ctx, yd);
   return s;

@@ -39,7 +39,8 @@ class GTError(RuntimeError):
 
 
 class SolveInfo(C.Structure):
-    _fields_ = [("iterations", C.c_int32), ("outer_iterations", C.c_int32), ("rel_residual", C.c_double)]
+    _fields_ = [("iterations", C.c_int32), ("outer_iterations", C.c_int32), ("rel_residual", C.c_double),
+                ("fp64_iterations", C.c_int32), ("reserved", C.c_int32)]
 
 
 P = C.c_void_p

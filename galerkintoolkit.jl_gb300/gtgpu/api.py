@@ -91,7 +91,10 @@ def default_context() -> Context:
 
 
 def _ptr(a):
-    """Pointer of a numpy array or a torch tensor (host or device)."""
+    """Pointer of a numpy array or a torch tensor (host or device).  The
+    caller keeps the array referenced until the C call returns: ctypes
+    releases the GIL during the call, so a temporary's memory could be reused
+    by another thread meanwhile."""
     if a is None:
         return None
     if isinstance(a, np.ndarray):
@@ -366,7 +369,8 @@ def assemble_vector(l: Source, T, V: Space, out=None):
         raise NotImplementedError("only source terms int coef*f*v are supported (use gtgpu.source)")
     b = out if out is not None else np.zeros(V.num_free_dofs, np.float64)
     coef = None if l.coef is None else (np.full(V.mesh.num_cells, float(l.coef)) if np.isscalar(l.coef) else l.coef)
-    check(V.ctx.h, V.ctx.lib.gt_assemble_vector(V.h, _ptr(l.fvec(V.ncomp)), _ptr(coef), _ptr(b)))
+    fv = l.fvec(V.ncomp)  # kept alive across the call (ctypes releases the GIL)
+    check(V.ctx.h, V.ctx.lib.gt_assemble_vector(V.h, _ptr(fv), _ptr(coef), _ptr(b)))
     return b
 
 
@@ -382,8 +386,9 @@ def assemble_matrix_and_vector(a: Form, l: Source, T, U: Space, V: Space | None 
     b = out if out is not None else np.zeros(U.num_free_dofs, np.float64)
     coef = a.cell_coef(U.mesh.num_cells)
     scoef = None if l.coef is None else (np.full(U.mesh.num_cells, float(l.coef)) if np.isscalar(l.coef) else l.coef)
+    fv = l.fvec(U.ncomp)  # kept alive across the call (ctypes releases the GIL)
     check(U.ctx.h, U.ctx.lib.gt_assemble_matrix_and_vector(U.h, a.kind, _ptr(coef), a.nu, _precision(T),
-                                                           _ptr(l.fvec(U.ncomp)), _ptr(scoef), _ptr(b), C.byref(h)))
+                                                           _ptr(fv), _ptr(scoef), _ptr(b), C.byref(h)))
     return Matrix(U, h, a), b
 
 
@@ -420,4 +425,4 @@ def solve(p: LinearProblem | Matrix, b=None, x=None, rtol=1e-10, maxit=20000, mo
     if st != 0 and (raise_on_fail or st != _lib.GT_ERR_NOT_CONVERGED):
         check(A.ctx.h, st)
     return x, dict(iterations=info.iterations, outer_iterations=info.outer_iterations,
-                   rel_residual=info.rel_residual, converged=st == 0)
+                   rel_residual=info.rel_residual, fp64_iterations=info.fp64_iterations, converged=st == 0)

@@ -1,11 +1,14 @@
 """Batched assembly + solve of many independent problems.
 
-``Batch`` wraps ``gt_batch_*``: all instances' CG iterations run as one set
-of launches (one CTA per row tile of every live instance), each instance with
-its own CG scalars and deterministic reductions, iteration chunks replayed
-from a captured CUDA graph.  ``autotune_lanes`` picks the lanes per matrix row
-of the batched SpMV by timing the candidates on the batch itself and caches
-the choice in a JSON file keyed by the batch's shape.
+``Batch`` wraps ``gt_batch_*``: the small instances (up to 32768 rows) are
+solved by one persistent launch in which every CTA takes instances from a
+queue (largest first) and runs each one's whole Jacobi-PCG alone; the large
+instances, which fill the GPU by themselves, run one after the other through
+the persistent cooperative solver.  Each instance keeps its own CG scalars
+and a summation order that depends only on the instance.
+``autotune_lanes`` picks the lanes per matrix row of the per-CTA SpMV by
+timing the candidates on the batch itself and caches the choice in a JSON
+file keyed by the batch's shape.
 
 ``batch_workload`` draws the seeded instance list of the batched benchmark:
 independent Poisson problems on unit boxes, dimension 2 or 3 and order 1 or 2
@@ -53,7 +56,7 @@ class Batch:
     def info(self):
         a = np.zeros(4, np.int64)
         check(self.ctx.h, self.ctx.lib.gt_batch_info(self.h, _ptr(a)))
-        return dict(instances=int(a[0]), rows=int(a[1]), tiles=int(a[2]), lanes=int(a[3]))
+        return dict(instances=int(a[0]), rows=int(a[1]), small_instances=int(a[2]), lanes=int(a[3]))
 
     def solve(self, b, rtol=1e-8, maxit=20000, mode="ir", raise_on_fail=True, out=None):
         """b: concatenated right-hand sides (numpy or device tensor) or a list of
@@ -65,8 +68,8 @@ class Batch:
         st = self.ctx.lib.gt_batch_solve(self.h, _ptr(b), _ptr(x), float(rtol), int(maxit), _MODES[mode], infos)
         if st != 0 and (raise_on_fail or st != _lib.GT_ERR_NOT_CONVERGED):
             check(self.ctx.h, st)
-        return x, [dict(iterations=i.iterations, outer_iterations=i.outer_iterations, rel_residual=i.rel_residual)
-                   for i in infos]
+        return x, [dict(iterations=i.iterations, outer_iterations=i.outer_iterations, rel_residual=i.rel_residual,
+                        fp64_iterations=i.fp64_iterations) for i in infos]
 
     def split(self, x):
         return [x[self.offsets[i]:self.offsets[i + 1]] for i in range(len(self.mats))]
@@ -90,7 +93,7 @@ def _cache_path(path=None):
                                   os.path.join(os.path.expanduser("~"), ".cache", "gtgpu", "autotune.json"))
 
 
-def autotune_lanes(batch: Batch, b, candidates=(2, 4, 8, 16), iters=48, cache=None, use_cache=True):
+def autotune_lanes(batch: Batch, b, candidates=(1, 2, 4, 8), iters=48, cache=None, use_cache=True):
     """Pick the lanes per row of the batched SpMV by timing a short FP32 solve
     of the batch with each candidate; the result is cached by batch shape."""
     path = _cache_path(cache)

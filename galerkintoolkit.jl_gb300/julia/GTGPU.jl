@@ -25,6 +25,8 @@ struct SolveInfo
     iterations::Int32
     outer_iterations::Int32
     rel_residual::Float64
+    fp64_iterations::Int32
+    reserved::Int32
 end
 
 function check(ctx, st)
@@ -162,7 +164,7 @@ end
 """
 function solve(dm::DeviceMatrix, b::Vector{Float64}; rtol=1e-10, maxit=20000, mode=GT_SOLVE_FP64)
     x = zeros(Float64, length(b))
-    info = Ref(SolveInfo(0, 0, 0.0))
+    info = Ref(SolveInfo(0, 0, 0.0, 0, 0))
     check(dm.space.ctx.h, ccall((:gt_solve, LIB), Cint,
                                 (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Float64, Cint, Cint, Ref{SolveInfo}),
                                 dm.h, b, x, rtol, maxit, mode, info))

@@ -72,6 +72,9 @@ typedef struct gt_solve_info {
   int32_t iterations;       /* PCG iterations */
   int32_t outer_iterations; /* FP64 true-residual updates (GT_SOLVE_FP64/IR), else 0 */
   double rel_residual;      /* final ||b - A x|| / ||b|| in FP64 */
+  int32_t fp64_iterations;  /* iterations run in FP64 (all of GT_SOLVE_FP64; in GT_SOLVE_IR
+                               those after an FP32 stall, when eps32 * cond(A) ~ 1) */
+  int32_t reserved;
 } gt_solve_info;
 
 /* ---- context ------------------------------------------------------------ */
@@ -194,18 +197,21 @@ int gt_spmv(gt_matrix* matrix, const double* x, double* y);
 /* ---- batched solves ----------------------------------------------------- */
 /* No counterpart in the reference (which solves one problem per call).
  * A batch of n assembled scalar matrices (block size 1) of one context,
- * solved together: every launch advances all unconverged instances, each
- * with its own CG scalars and deterministic reductions (an instance's
- * result does not depend on the rest of the batch); iteration chunks are
- * replayed from a captured CUDA graph.  b and x are the instances' vectors
+ * solved together: instances of up to 32768 rows in one persistent launch
+ * in which each CTA takes instances from a queue (largest first) and runs
+ * each one's whole PCG alone; larger instances one after the other through
+ * the single-system solver.  An instance's result does not depend on the
+ * rest of the batch.  b and x are the instances' vectors
  * concatenated in batch order (num_free_dofs each, FP64); x is the output
  * (every solve starts from 0).  infos: n entries.  GT_SOLVE_IR needs
  * GT_MIXED matrices. */
 typedef struct gt_batch gt_batch;
 int gt_batch_create(gt_ctx* ctx, int n, gt_matrix* const* matrices, gt_batch** batch);
-/* lanes per matrix row in the batched SpMV (2, 4, 8 or 16; default 4) */
+/* lanes per matrix row in the SpMV of the one-CTA-per-instance solves (1, 2,
+ * 4 or 8; 0, the default: each instance's own, from its mean row length) */
 int gt_batch_set_lanes(gt_batch* batch, int lanes);
-/* info[0]=instances info[1]=total rows info[2]=tiles info[3]=lanes */
+/* info[0]=instances info[1]=total rows info[2]=instances solved one per CTA
+ * info[3]=lanes */
 int gt_batch_info(const gt_batch* batch, int64_t* info);
 int gt_batch_solve(gt_batch* batch, const double* b, double* x, double rtol, int maxit, int mode,
                    gt_solve_info* infos);
