@@ -118,9 +118,11 @@ def run_batched(args):
     """512 independent Poisson instances (dim 2|3, order 1|2, cells
     log-uniform 16^2..96^3, kappa lognormal(0,0.5), Dirichlet boundary),
     solved to 1e-8: batched mixed path (HBM-budgeted waves; each wave
-    assembled then solved as one batch with FP64 refinement around FP32 PCG)
-    against the plain FP64 path (one instance at a time, FP64 assembly and
-    FP64 PCG)."""
+    assembled in mixed precision, then solved as one batch: FP32 PCG with FP64
+    reliable updates, instances up to 32768 rows one per CTA in one
+    persistent launch) against the plain FP64 path (one instance at a time,
+    FP64 assembly and FP64 PCG).  The lanes autotuner runs once before the
+    timed region (its choice is cached by batch shape)."""
     import gtgpu as GT
     from gtgpu import batch as GB
     specs = GB.batch_workload(args.instances, seed=404)
@@ -138,19 +140,32 @@ def run_batched(args):
         used += e
     if cur:
         waves.append(cur)
+    # autotune the per-CTA SpMV lanes on the smallest wave (untimed, cached)
+    inst = [GB.assemble_instance(s, seed=404, T="mixed", ctx=ctx) for s in waves[-1]]
+    B = GB.Batch([A for _, _, A, _ in inst])
+    tune = GB.autotune_lanes(B, np.concatenate([bb for _, _, _, bb in inst]), iters=32)
+    del B, inst
+    ctx.trim()
+    ctx.synchronize()
     t_all = time.perf_counter()
-    iters, worst = [], 0.0
-    tune = None
+    iters, fp64_its, worst = [], [], 0.0
+    t_asm = t_solve = t_small = t_large = 0.0
     for w in waves:
+        t0 = time.perf_counter()
         inst = [GB.assemble_instance(s, seed=404, T="mixed", ctx=ctx) for s in w]
         B = GB.Batch([A for _, _, A, _ in inst])
         b = np.concatenate([bb for _, _, _, bb in inst])
-        if tune is None:
-            tune = GB.autotune_lanes(B, b, iters=32)
-        else:
-            B.set_lanes(tune["lanes"])
+        t1 = time.perf_counter()
+        B.set_lanes(tune["lanes"])
+        ctx.profile_begin()
         x, infos = B.solve(b, rtol=1e-8, maxit=100000, mode="ir", raise_on_fail=False)
+        ph = dict(ctx.profile_end())
+        t_small += ph.get("batch_small", 0.0) * 1e-3
+        t_large += ph.get("batch_large", 0.0) * 1e-3
+        t_asm += t1 - t0
+        t_solve += time.perf_counter() - t1
         iters += [i["iterations"] for i in infos]
+        fp64_its += [i["fp64_iterations"] for i in infos]
         worst = max(worst, max(i["rel_residual"] for i in infos))
         del B, inst
         ctx.trim()
@@ -159,9 +174,16 @@ def run_batched(args):
     # plain FP64 path, one instance at a time
     t0 = time.perf_counter()
     worst64 = 0.0
+    p_asm = p_solve = 0.0
+    its64 = []
     for s in specs:
+        ta = time.perf_counter()
         m, V, A, b = GB.assemble_instance(s, seed=404, T=np.float64, ctx=ctx)
+        tb = time.perf_counter()
         x, info = GT.solve(A, b, rtol=1e-8, maxit=100000, mode="fp64", raise_on_fail=False)
+        p_asm += tb - ta
+        p_solve += time.perf_counter() - tb
+        its64.append(info["iterations"])
         worst64 = max(worst64, info["rel_residual"])
         del A, V
         if ctx.memory()[1] > 20e9:
@@ -169,10 +191,14 @@ def run_batched(args):
     t_plain = time.perf_counter() - t0
     out = {"metric": "batched solves/s (assemble + solve to 1e-8), mixed batched vs plain FP64", "n_gpus": 1,
            "config": {"workload": f"{args.instances} Poisson instances, dim 2|3, Q1|Q2, cells log-uniform 16^2..96^3",
-                      "waves": len(waves), "budget_gb": args.budget_gb, "lanes": tune["lanes"] if tune else None},
-           "batched": {"solves_per_s": len(specs) / t_batched, "seconds": t_batched, "worst_rel_residual": worst,
-                       "inner_iterations_max": int(max(iters))},
-           "plain_fp64": {"solves_per_s": len(specs) / t_plain, "seconds": t_plain, "worst_rel_residual": worst64},
+                      "waves": len(waves), "budget_gb": args.budget_gb, "lanes": tune["lanes"]},
+           "batched": {"solves_per_s": len(specs) / t_batched, "seconds": t_batched, "assemble_s": t_asm,
+                       "solve_s": t_solve, "solve_small_tier_s": t_small, "solve_large_tier_s": t_large,
+                       "worst_rel_residual": worst, "iterations_max": int(max(iters)),
+                       "iterations_sum": int(sum(iters)), "fp64_iterations_sum": int(sum(fp64_its)),
+                       "instances_handed_to_fp64": int(sum(1 for v in fp64_its if v > 0))},
+           "plain_fp64": {"solves_per_s": len(specs) / t_plain, "seconds": t_plain, "assemble_s": p_asm,
+                          "solve_s": p_solve, "worst_rel_residual": worst64, "iterations_sum": int(sum(its64))},
            "speedup": t_plain / t_batched, "data": "synthetic (seeded)"}
     print(json.dumps(out), flush=True)
 
@@ -199,24 +225,23 @@ def run_serving(args):
 
 def spmv_roofline(A, flush, stream, reps=20):
     """y = A x with the FP64 block-CSR SpMV (gt_spmv, device vectors), L2
-    flushed before each launch; algorithmic bytes = values + column indices +
-    row pointers + x + y."""
+    flushed before each launch, timed by the library's phase marks (CUDA
+    events on its stream right before and after the kernel); algorithmic
+    bytes = values + column indices + row pointers + x + y."""
     import torch
     from gtgpu.api import _ptr
     n = A.shape[0]
     x = torch.ones(n, dtype=torch.float64, device="cuda")
     y = torch.empty(n, dtype=torch.float64, device="cuda")
-    lib = A.ctx.lib
+    ctx = A.ctx
     ts = []
     for i in range(reps + 3):
         flush.fill_(2)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        lib.gt_spmv(A.h, _ptr(x), _ptr(y))
-        e1.record(stream)
-        e1.synchronize()
+        ctx.profile_begin()
+        ctx.lib.gt_spmv(A.h, _ptr(x), _ptr(y))
+        ph = dict(ctx.profile_end())
         if i >= 3:
-            ts.append(e0.elapsed_time(e1))
+            ts.append(ph["spmv"])
     ms = statistics.median(ts)
     nb = A.nnz * (8 + 4) + (n + 1) * 8 + 2 * n * 8
     return {"kernel": "k_spmv<1, G, double, double>", "achieved": nb / (ms * 1e-3) / 1e9, "unit": "GB/s",

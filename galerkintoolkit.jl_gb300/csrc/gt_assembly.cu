@@ -359,6 +359,19 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
   }
 }
 
+// colind of the rows whose sorted columns the count pass left in their slot
+// of S entries: one thread per slot entry, coalesced reads and writes
+template <int S>
+__global__ void k_copy_slots(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ slots, int64_t nrows,
+                             int32_t* __restrict__ colind) {
+  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t r = t / S;
+  int i = (int)(t - r * S);
+  if (r >= nrows) return;
+  int64_t o = rowptr[r];
+  if (i < rowptr[r + 1] - o) colind[o + i] = slots[t];
+}
+
 __global__ void k_max_diff(const int64_t* ptr, int64_t n, int32_t* out) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int32_t v = 0;
@@ -424,11 +437,16 @@ static int launch_pattern(Matrix* A, int maxinc) {
   memcpy(&mr, &ctx->h_scratch[1], sizeof(int32_t));
   A->max_row = mr;
   GT_TRY(dalloc(ctx, &A->colind, A->bnnz));
-  if (nrows > 0)
+  if (nrows > 0 && mr <= S) {
+    // every row fit its slot: a plain coalesced copy
+    k_copy_slots<S><<<GT_KC(ctx, grid_for(nrows * S, 256)), 256, 0, st>>>(A->rowptr, slots, nrows, A->colind);
+    GT_LAUNCH(ctx, "k_copy_slots");
+  } else if (nrows > 0) {
     k_pattern<NN, S, true><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, nrows,
                                                                        hcap, icap, nullptr, A->rowptr, A->colind,
                                                                        slots, small, dmax, ctx->d_err);
-  GT_LAUNCH(ctx, "k_pattern<fill>");
+    GT_LAUNCH(ctx, "k_pattern<fill>");
+  }
   mark(ctx, "pattern_fill");
   dfree(ctx, rowcnt);
   dfree(ctx, dmax);
@@ -849,11 +867,15 @@ __device__ __forceinline__ int find_col(const int32_t* cols, int L, int32_t j) {
   return lo;
 }
 
+// With be != nullptr the group's lane 0 also sums the element vectors of the
+// row's incidences, in the same ascending order as k_scatter_vec (so the
+// load vector is bitwise the one of the separate pass), and writes bvec.
 template <int BS, int G, class TK, class TA>
 __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                           const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                           const int32_t* __restrict__ cnd, int nn, int64_t nrows, int lmax,
-                          const TK* __restrict__ Ke, double* __restrict__ v64, float* __restrict__ v32) {
+                          const TK* __restrict__ Ke, double* __restrict__ v64, float* __restrict__ v32,
+                          const double* __restrict__ be, double* __restrict__ bvec) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   constexpr int RPW = 32 / G;  // rows per warp
   const int nloc = nn * BS;
@@ -881,6 +903,10 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
     // group barrier between cells, which keeps the summation order fixed.
     constexpr int U = BS == 1 ? 4 : 2;
     const int b = gl;
+    const bool vec = be != nullptr && gl == 0;
+    double bsum[BS];
+#pragma unroll
+    for (int cc = 0; cc < BS; cc++) bsum[cc] = 0.0;
     int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
     for (int64_t k0 = ib; k0 < ie; k0 += U) {
       int32_t jj[U];
@@ -892,6 +918,9 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
         if (k < ie && b < nn) {
           int32_t cb = __ldg(inc + k);
           int32_t c = cb / nn, a = cb - c * nn;
+          if (vec)
+#pragma unroll
+            for (int cc = 0; cc < BS; cc++) bsum[cc] += __ldg(be + (int64_t)c * nloc + a * BS + cc);
           jj[u] = __ldg(cnd + (int64_t)c * nn + b);
           const TK* Krow = Ke + (int64_t)c * nloc * nloc + (int64_t)(a * BS) * nloc + b * BS;
 #pragma unroll
@@ -916,11 +945,14 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
       if (v64) v64[ob + i] = (double)v;
       if (v32) v32[ob + i] = (float)v;
     }
+    if (vec)
+#pragma unroll
+      for (int cc = 0; cc < BS; cc++) bvec[r * BS + cc] = bsum[cc];
   }
 }
 
 template <int BS, class TK, class TA>
-static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32) {
+static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, const double* be, double* bvec) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   int nn = sp->nn;
@@ -937,7 +969,7 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32) {
     int64_t rows_per_block = (int64_t)warps * RPW;
     int64_t grid = (A->nbrows + rows_per_block - 1) / rows_per_block;
     k_scatter<BS, G, TK, TA><<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
-        A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, A->nbrows, lmax, Ke, v64, v32);
+        A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, A->nbrows, lmax, Ke, v64, v32, be, bvec);
     GT_LAUNCH(ctx, "k_scatter");
     return GT_OK;
   };
@@ -947,20 +979,20 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32) {
   return go(std::integral_constant<int, 32>());
 }
 
-int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision) {
+int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be, double* bvec) {
   double* v64 = (out_precision == GT_FP64 || out_precision == GT_MIXED) ? A->val64 : nullptr;
   float* v32 = (out_precision == GT_FP32 || out_precision == GT_MIXED) ? A->val32 : nullptr;
   int bs = A->bs;
   if (ke_precision == GT_FP32) {
     const float* K = (const float*)Ke;
-    if (bs == 1) return launch_scatter<1, float, float>(A, K, v64, v32);
-    if (bs == 2) return launch_scatter<2, float, float>(A, K, v64, v32);
-    return launch_scatter<3, float, float>(A, K, v64, v32);
+    if (bs == 1) return launch_scatter<1, float, float>(A, K, v64, v32, be, bvec);
+    if (bs == 2) return launch_scatter<2, float, float>(A, K, v64, v32, be, bvec);
+    return launch_scatter<3, float, float>(A, K, v64, v32, be, bvec);
   }
   const double* K = (const double*)Ke;
-  if (bs == 1) return launch_scatter<1, double, double>(A, K, v64, v32);
-  if (bs == 2) return launch_scatter<2, double, double>(A, K, v64, v32);
-  return launch_scatter<3, double, double>(A, K, v64, v32);
+  if (bs == 1) return launch_scatter<1, double, double>(A, K, v64, v32, be, bvec);
+  if (bs == 2) return launch_scatter<2, double, double>(A, K, v64, v32, be, bvec);
+  return launch_scatter<3, double, double>(A, K, v64, v32, be, bvec);
 }
 
 // ---------------------------------------------------------------------------
@@ -1497,6 +1529,10 @@ static int numeric(Matrix* A, int form, const double* coef_in, double nu, const 
   void* Ke = nullptr;
   double* be = nullptr;
   if (b_out) GT_TRY(dalloc(ctx, &be, nc * sp->nloc));
+  const bool dev = b_out && is_device_ptr(b_out);
+  double* bd = b_out;
+  const int64_t nb = sp->nfree_nodes * sp->ncomp;
+  if (b_out && !dev) GT_TRY(dalloc(ctx, &bd, nb));
   int used_kron = 0;
   int s = kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, &used_kron);
   if (s == GT_OK && !used_kron) {
@@ -1504,25 +1540,23 @@ static int numeric(Matrix* A, int form, const double* coef_in, double nu, const 
     if (s == GT_OK) s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
     mark(ctx, "elements");
     if (s == GT_OK) s = alloc_values(A);
-    if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision);
+    // the load vector is summed inside the matrix scatter (same incidences)
+    if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr);
     mark(ctx, "scatter");
+  } else if (s == GT_OK && b_out) {
+    s = scatter_vector(sp, A->inc_ptr, A->inc, be, bd);
+    mark(ctx, "scatter_vector");
   }
   if (s == GT_OK && b_out) {
-    bool dev = is_device_ptr(b_out);
-    double* bd = b_out;
-    int64_t nb = sp->nfree_nodes * sp->ncomp;
-    if (!dev) s = dalloc(ctx, &bd, nb);
-    if (s == GT_OK) s = scatter_vector(sp, A->inc_ptr, A->inc, be, bd);
-    mark(ctx, "scatter_vector");
     if (s == GT_OK && !dev) {
       s = copy_out(ctx, b_out, bd, nb);
       if (s == GT_OK) {
         cudaError_t e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) s = check_cuda(ctx, e, "assemble_vector");
       }
-      dfree(ctx, bd);
     }
   }
+  if (b_out && !dev) dfree(ctx, bd);
   if (Ke) pool_free(ctx, Ke);
   if (be) dfree(ctx, be);
   return s;

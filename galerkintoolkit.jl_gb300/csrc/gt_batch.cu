@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, co
       const bool stop = rr <= tol2 || iters >= maxit || !(rr == rr);
       if constexpr (REL) {
         const int cyc = iters - it_upd;
-        const bool slow = sizeof(X) < sizeof(double) && max_cyc > 0 && cyc > (5 * max_cyc) / 2 + 16;
+        const bool slow = sizeof(X) < sizeof(double) && (cyc > kSlowCycle || (max_cyc > 0 && cyc > (5 * max_cyc) / 2 + 16));
         if (stop || slow || rr <= delta2 * rmax2) {
           for (int64_t i = tid; i < n; i += BT) {
             xi[i] += (double)xsi[i];
@@ -405,6 +405,7 @@ static int batch_solve(gt_batch* B, const double* b, double* x, double rtol, int
     if (mode == GT_SOLVE_FP64) info[i].fp64_iterations = hres[i].iters;
     if (hres[i].status != 0) status = GT_ERR_NOT_CONVERGED;
   }
+  mark(ctx, "batch_small");
   // large instances: the single-system solver, one after the other (each
   // fills the device by itself)
   for (int i : B->large) {
@@ -415,6 +416,7 @@ static int batch_solve(gt_batch* B, const double* b, double* x, double rtol, int
     if (s != GT_OK && s != GT_ERR_NOT_CONVERGED) return s;
     if (s == GT_ERR_NOT_CONVERGED) status = s;
   }
+  mark(ctx, "batch_large");
   if (infos)
     for (int i = 0; i < ni; i++) infos[i] = info[i];
   if (status == GT_ERR_NOT_CONVERGED) set_error(ctx, status, "batch solve: some instance missed the tolerance");

@@ -190,7 +190,9 @@ int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc,
 int build_pattern(Matrix* A);
 int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision,
                      const double* f, const double* d_scoef, void* Ke, double* be, int want_matrix);
-int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision);
+// be/bvec (optional): element vectors and the load vector summed in the same pass
+int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be = nullptr,
+                   double* bvec = nullptr);
 int tabulation_doubles(const Space* sp);
 int compute_elements_with_tab(const Space* sp, int form, const double* d_coef, double nu, int precision,
                               double* tab, void* Ke);
@@ -198,6 +200,16 @@ int scatter_vector(const Space* sp, const int64_t* inc_ptr, const int32_t* inc, 
                    double* b);
 int find_diag(Matrix* A);
 int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mode, gt_solve_info* info);
+// Mixed-precision CG: a reliable-update cycle (recurrence residual down by
+// a decade) of more than kSlowCycle FP32 iterations means cond(A) >~ 1e6 in
+// CG terms (about 1.15 sqrt(cond) iterations per decade), where eps32 *
+// cond(A) ~ 0.1 slows the FP32 iteration several-fold below the FP64 rate;
+// the solve then continues in FP64.  Also a cycle 2.5x longer than the
+// longest earlier one, or three updates that did not halve the true
+// residual.  (Measured: problems at 300-450 FP32 iterations per decade still
+// gain from FP32; one at ~2500 per decade needed 4x the FP64 count.)
+constexpr int kSlowCycle = 1000;
+
 // persistent cooperative Jacobi-PCG (gt_pcg.cu); x holds the start value
 int pcg_persistent(Matrix* A, int mode, const double* b, double* x, double rtol, int maxit, int32_t* iters,
                    int32_t* nupd, int32_t* iters64, double* relres);

@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
       // the longest earlier cycle: the FP32 iteration has lost the rate of
       // the exact iteration (eps32 * cond(A) too large); hand over to FP64
       const int cyc = S.iters - S.it_upd;
-      const bool slow = sizeof(X) < sizeof(double) && S.max_cyc > 0 && cyc > (5 * S.max_cyc) / 2 + 16;
+      const bool slow = sizeof(X) < sizeof(double) && (cyc > kSlowCycle || (S.max_cyc > 0 && cyc > (5 * S.max_cyc) / 2 + 16));
       if (stop || slow || rr <= a.delta2 * S.rmax2) {
         // P3: x += xs
         for (int64_t i = e0 + tid; i < e1; i += PT) {

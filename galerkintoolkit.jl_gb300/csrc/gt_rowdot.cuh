@@ -24,7 +24,7 @@ inline int row_lanes(double avg) {
 // all gathers of a trip are independent and in flight together.
 template <int BS, int G>
 struct RowUnroll {
-  static constexpr int value = BS > 1 ? 2 : (G <= 2 ? 8 : 4);
+  static constexpr int value = BS > 1 ? 2 : (G == 1 ? 8 : 4);
 };
 
 // out[c] = sum_k A[r, k] x[col k] for the BS components of block row r.

@@ -586,7 +586,7 @@ __global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __re
     // an FP32 cycle running past 2.5x the longest earlier one: the FP32
     // iteration has lost the rate of the exact iteration (eps32 * cond(A))
     const int cyc = st->iters - st->it_upd;
-    st->slow = sizeof(X) < sizeof(double) && st->max_cyc > 0 && cyc > (5 * st->max_cyc) / 2 + 16;
+    st->slow = sizeof(X) < sizeof(double) && (cyc > kSlowCycle || (st->max_cyc > 0 && cyc > (5 * st->max_cyc) / 2 + 16));
     if (rr <= st->tol2 || rr <= st->delta2 * st->rmax2 || st->iters >= st->maxit || !(rr == rr) || st->slow)
       st->upd = 1;
   }
@@ -754,7 +754,10 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
 int spmv64(Matrix* A, const double* x, double* y) {
   Ctx* ctx = A->space->mesh->ctx;
   if (!A->val64) return set_error(ctx, GT_ERR_INVALID, "matrix has no FP64 values");
-  return Ops<double, double>::spmv(ctx, A, A->val64, x, nullptr, y);
+  mark(ctx, "spmv_setup");
+  int s = Ops<double, double>::spmv(ctx, A, A->val64, x, nullptr, y);
+  mark(ctx, "spmv");  // the phase "spmv" of a profile is the kernel alone
+  return s;
 }
 
 // ||b - A x|| / ||b|| in FP64
