@@ -40,9 +40,14 @@ sys.path.insert(0, os.path.join(ROOT, "galerkintoolkit.jl_gb300"))
 
 METRIC = "nnz/s assembled (assemble_matrix + assemble_vector, plain FP64)"
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
-# DRAM bytes (read + write) per launch on the default workload, from one ncu
-# capture of each kernel (summaries under profiles/); None until captured
-TRAFFIC: dict = {}
+# DRAM bytes (read + write) per launch on the default workload (96^3 x 6 P1
+# tets), from ncu captures (summaries under profiles/): the element and
+# scatter kernels captured on 64^3 x 6 tets (1,572,864 cells) and scaled by
+# the cell ratio 3.375 (their traffic is proportional to the cells); the FP64
+# CG SpMV captured on the full workload
+TRAFFIC: dict = {"elements": (44.539136e6 + 192.030464e6) * 3.375,
+                 "scatter": (329.769472e6 + 26.009088e6) * 3.375,
+                 "spmv": 165.773568e6 + 5.912320e6}
 
 
 def parse():
@@ -456,7 +461,8 @@ def main():
     # algorithmic bytes per launch of the phases (stated in the design doc)
     alg = {
         "elements": nc * (4 * 4 + 8) + m.num_nodes * 24 + nc * 16 * 8 + nc * 4 * 8,  # reads + Ke/be writes
-        "scatter": nc * 16 * 8 + nc * 4 * 4 + nfree * 8 + nnz * (4 + 8),               # Ke, inc, rowptr, colind+values
+        # Ke, be, incidences, cell dofs, rowptr, colind + values, load vector
+        "scatter": nc * 16 * 8 + nc * 4 * 8 + nc * 4 * 4 + nc * 4 * 4 + nfree * 8 + nnz * (4 + 8) + nfree * 8,
     }
     # FP64 flops per P1 tetrahedron (FMA = 2, the division = 1): J 9, cofactors
     # 27, det 5, scale 2, six vertex-1..3 entries 36, vertex-0 entries 8, load 6

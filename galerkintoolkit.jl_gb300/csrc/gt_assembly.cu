@@ -38,7 +38,9 @@ static inline Ctx* ctx_of(const Space* sp) { return sp->mesh->ctx; }
 // ---------------------------------------------------------------------------
 struct TabLayout {
   int D, nlv, nn, nq;
-  int off_w, off_gg, off_sv, off_sg, total;
+  int off_w, off_gg, off_sv, off_sg;
+  int off_k;  // 32 doubles of per-reference-cell quadrature sums (P1 path)
+  int total;
 };
 inline TabLayout tab_layout(int ctype, int order) {
   TabLayout L{};
@@ -51,7 +53,8 @@ inline TabLayout tab_layout(int ctype, int order) {
   L.off_gg = L.nq;
   L.off_sv = L.off_gg + L.nq * L.nlv * L.D;
   L.off_sg = L.off_sv + L.nq * L.nn;
-  L.total = L.off_sg + L.nq * L.nn * L.D;
+  L.off_k = L.off_sg + L.nq * L.nn * L.D;
+  L.total = L.off_k + 32;
   return L;
 }
 
@@ -274,7 +277,7 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
   int64_t ib = inc_ptr[r];
   int ninc = (int)(inc_ptr[r + 1] - ib);
   int ncand = ninc * NN;
-  if (2 * ncand > hcap || ninc > icap) {
+  if (ncand + (ncand >> 2) > hcap || ncand > icap) {
     if (lane == 0) { atomicOr(err, DEV_ERR_ROW_CAP); if (!FILL) { rowcnt[r] = 0; small[r] = 1; } }
     return;
   }
@@ -360,16 +363,31 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
 }
 
 // colind of the rows whose sorted columns the count pass left in their slot
-// of S entries: one thread per slot entry, coalesced reads and writes
+// of S entries: four lanes per row, each copying a quarter of the row with
+// 16-byte slot loads (slots are 16-byte aligned), all loads in flight
 template <int S>
 __global__ void k_copy_slots(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ slots, int64_t nrows,
                              int32_t* __restrict__ colind) {
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int64_t r = t / S;
-  int i = (int)(t - r * S);
+  int64_t r = t >> 2;
+  int q = (int)(t & 3);
   if (r >= nrows) return;
-  int64_t o = rowptr[r];
-  if (i < rowptr[r + 1] - o) colind[o + i] = slots[t];
+  const int64_t o = rowptr[r];
+  const int n = (int)(rowptr[r + 1] - o);
+  constexpr int V4 = S / 16;  // int4 loads per lane
+  const int4* src = reinterpret_cast<const int4*>(slots + r * S) + q * V4;
+  int4 v[V4];
+#pragma unroll
+  for (int k = 0; k < V4; k++)
+    if ((q * V4 + k) * 4 < n) v[k] = __ldg(src + k);
+#pragma unroll
+  for (int k = 0; k < V4; k++) {
+    const int b = (q * V4 + k) * 4;
+    if (b < n) colind[o + b] = v[k].x;
+    if (b + 1 < n) colind[o + b + 1] = v[k].y;
+    if (b + 2 < n) colind[o + b + 2] = v[k].z;
+    if (b + 3 < n) colind[o + b + 3] = v[k].w;
+  }
 }
 
 __global__ void k_max_diff(const int64_t* ptr, int64_t n, int32_t* out) {
@@ -402,10 +420,12 @@ static int launch_pattern(Matrix* A, int maxinc) {
   Ctx* ctx = sp->mesh->ctx;
   cudaStream_t st = ctx->stream;
   int64_t nrows = A->nbrows;
-  int hcap = 64, icap = 32;
-  while (hcap < 2 * maxinc * NN) hcap <<= 1;
-  while (icap < maxinc) icap <<= 1;
-  if (icap < hcap / 2) icap = hcap / 2;  // room for the compacted keys (<= candidates)
+  // hash table: load factor <= 0.8 even if every candidate were distinct;
+  // ibuf holds the row's incidences, then the compacted keys (<= candidates)
+  const int ncand_max = maxinc * NN;
+  int hcap = 32, icap = 32;
+  while (hcap < ncand_max + ncand_max / 4) hcap <<= 1;
+  while (icap < ncand_max) icap <<= 1;
   if (hcap > 8192) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells for the sparsity kernel");
   int warps = hcap >= 4096 ? 2 : (hcap >= 2048 ? 4 : 8);
   size_t smem = (size_t)warps * (hcap + icap) * sizeof(int32_t);
@@ -439,7 +459,7 @@ static int launch_pattern(Matrix* A, int maxinc) {
   GT_TRY(dalloc(ctx, &A->colind, A->bnnz));
   if (nrows > 0 && mr <= S) {
     // every row fit its slot: a plain coalesced copy
-    k_copy_slots<S><<<GT_KC(ctx, grid_for(nrows * S, 256)), 256, 0, st>>>(A->rowptr, slots, nrows, A->colind);
+    k_copy_slots<S><<<GT_KC(ctx, grid_for(nrows * 4, 256)), 256, 0, st>>>(A->rowptr, slots, nrows, A->colind);
     GT_LAUNCH(ctx, "k_copy_slots");
   } else if (nrows > 0) {
     k_pattern<NN, S, true><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, nrows,
@@ -698,31 +718,33 @@ static int dispatch_form(const Space* sp, int form, const double* coef, double n
 // taken out: one FP64 division and ~80 FP64 operations per cell.  J, its
 // cofactors and det stay FP64 in every precision; in FP32 mode the cofactor
 // columns are rounded to FP32 for the entries.
+// the quadrature sums of the P1 reference cell, once per assembly:
+// k[0] = sum_q w_q, k[1..4] = sum_q w_q phi_n(q), k[5..20] = sum_q w_q phi_n phi_m
+__global__ void k_p1_consts(const double* __restrict__ tab, TabLayout L, double* __restrict__ k) {
+  const int t = threadIdx.x;
+  double s = 0.0;
+  if (t == 0) {
+    for (int q = 0; q < 4; q++) s += tab[L.off_w + q];
+  } else if (t < 5) {
+    for (int q = 0; q < 4; q++) s += tab[L.off_w + q] * tab[L.off_sv + q * 4 + (t - 1)];
+  } else if (t < 21) {
+    const int n = (t - 5) >> 2, m = (t - 5) & 3;
+    for (int q = 0; q < 4; q++) s += tab[L.off_w + q] * tab[L.off_sv + q * 4 + n] * tab[L.off_sv + q * 4 + m];
+  }
+  if (t < 21) k[t] = s;
+}
+
 template <int FORM, class T>
 __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ coords,
                                                      const int32_t* __restrict__ cell_nodes,
-                                                     const double* __restrict__ coef, const double* __restrict__ tab,
-                                                     TabLayout L, int64_t ncells, T* __restrict__ Ke,
-                                                     double* __restrict__ be, const double* __restrict__ fsrc,
+                                                     const double* __restrict__ coef,
+                                                     const double* __restrict__ consts, int64_t ncells,
+                                                     T* __restrict__ Ke, double* __restrict__ be,
+                                                     const double* __restrict__ fsrc,
                                                      const double* __restrict__ scoef, int want_matrix, uint32_t* err) {
-  __shared__ double s_mass[16], s_load[4], s_wsum;
-  if (threadIdx.x < 16) {
-    int n = threadIdx.x >> 2, m = threadIdx.x & 3;
-    double s = 0.0;
-    for (int q = 0; q < 4; q++) s += tab[L.off_w + q] * tab[L.off_sv + q * 4 + n] * tab[L.off_sv + q * 4 + m];
-    s_mass[threadIdx.x] = s;
-  }
-  if (threadIdx.x < 4) {
-    double s = 0.0;
-    for (int q = 0; q < 4; q++) s += tab[L.off_w + q] * tab[L.off_sv + q * 4 + threadIdx.x];
-    s_load[threadIdx.x] = s;
-  }
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int q = 0; q < 4; q++) s += tab[L.off_w + q];
-    s_wsum = s;
-  }
-  __syncthreads();
+  const double* s_load = consts + 1;
+  const double* s_mass = consts + 5;
+  const double s_wsum = __ldg(consts);
   int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (c >= ncells) return;
   int4 nd = *reinterpret_cast<const int4*>(cell_nodes + 4 * c);
@@ -773,7 +795,7 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
 #pragma unroll
       for (int n = 0; n < 4; n++)
 #pragma unroll
-        for (int m = n; m < 4; m++) k[e++] = s * (T)s_mass[n * 4 + m];
+        for (int m = n; m < 4; m++) k[e++] = s * (T)__ldg(s_mass + n * 4 + m);
     }
     T* K = Ke + 16 * c;
     const int up[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
@@ -785,7 +807,7 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
   if (be) {
     double sc = (scoef ? scoef[c] : 1.0) * fsrc[0] * adet;
 #pragma unroll
-    for (int n = 0; n < 4; n++) be[4 * c + n] = sc * s_load[n];
+    for (int n = 0; n < 4; n++) be[4 * c + n] = sc * __ldg(s_load + n);
   }
 }
 
@@ -797,12 +819,14 @@ static int elements_T(const Space* sp, int form, const double* coef, double nu, 
   if (ct == GT_TET4 && sp->ncomp == 1 && (form == GT_LAPLACE || form == GT_MASS)) {
     Ctx* ctx = ctx_of(sp);
     int64_t nc = sp->mesh->ncells;
+    double* consts = const_cast<double*>(tab) + L.off_k;  // inside the tabulation buffer: no allocation
+    k_p1_consts<<<GT_KC(ctx, 1), 32, 0, ctx->stream>>>(tab, L, consts);
     if (form == GT_LAPLACE)
       k_elements_p1<GT_LAPLACE, T><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
-          sp->mesh->coords, sp->mesh->cell_nodes, coef, tab, L, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
+          sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
     else
       k_elements_p1<GT_MASS, T><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
-          sp->mesh->coords, sp->mesh->cell_nodes, coef, tab, L, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
+          sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
     GT_LAUNCH(ctx, "k_elements_p1");
     return GT_OK;
   }
