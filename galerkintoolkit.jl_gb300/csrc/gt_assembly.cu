@@ -515,7 +515,11 @@ __global__ void __launch_bounds__(128) k_elements(const double* __restrict__ coo
   __shared__ double s_tab[NQ * (1 + NLV * D + NN + NN * D)];
   const int tid = threadIdx.x;
   const int64_t c0 = (int64_t)blockIdx.x * CPB;
-  for (int i = tid; i < L.total; i += blockDim.x) s_tab[i] = tab[i];
+  // the tabulation proper (L.off_k entries; the P1 constants after it are not
+  // staged) -- s_tab is sized for exactly this part
+  static_assert(sizeof(s_tab) / sizeof(double) == NQ * (1 + NLV * D + NN + NN * D), "s_tab size");
+  const int ntab = min(L.off_k, (int)(sizeof(s_tab) / sizeof(double)));
+  for (int i = tid; i < ntab; i += blockDim.x) s_tab[i] = tab[i];
   for (int i = tid; i < CPB * NLV * D; i += blockDim.x) {
     int cl = i / (NLV * D), r = i - cl * NLV * D, n = r / D, d = r - n * D;
     int64_t c = c0 + cl;
@@ -899,7 +903,8 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
                           const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                           const int32_t* __restrict__ cnd, int nn, int64_t nrows, int lmax,
                           const TK* __restrict__ Ke, double* __restrict__ v64, float* __restrict__ v32,
-                          const double* __restrict__ be, double* __restrict__ bvec) {
+                          const double* __restrict__ be, double* __restrict__ bvec,
+                          const double* __restrict__ xd) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   constexpr int RPW = 32 / G;  // rows per warp
   const int nloc = nn * BS;
@@ -960,6 +965,25 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
 #pragma unroll
           for (int e = 0; e < BS * BS; e++) acc[p * BS * BS + e] += kv[u][e];
         }
+        if (xd != nullptr && be != nullptr) {
+          // Dirichlet lift b -= Ad xd: this incidence's Dirichlet columns,
+          // summed over the group's lanes in a fixed butterfly
+          double lv[BS];
+#pragma unroll
+          for (int cc = 0; cc < BS; cc++) lv[cc] = 0.0;
+          if (jj[u] < 0)
+#pragma unroll
+            for (int cc = 0; cc < BS; cc++)
+#pragma unroll
+              for (int dd = 0; dd < BS; dd++)
+                lv[cc] += (double)kv[u][cc * BS + dd] * __ldg(xd + (int64_t)(-jj[u] - 1) * BS + dd);
+#pragma unroll
+          for (int cc = 0; cc < BS; cc++) {
+#pragma unroll
+            for (int o = G >> 1; o; o >>= 1) lv[cc] += __shfl_xor_sync(gmask, lv[cc], o);
+            if (gl == 0) bsum[cc] -= lv[cc];
+          }
+        }
         __syncwarp(gmask);
       }
     }
@@ -976,7 +1000,8 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
 }
 
 template <int BS, class TK, class TA>
-static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, const double* be, double* bvec) {
+static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, const double* be, double* bvec,
+                          const double* xd) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   int nn = sp->nn;
@@ -993,7 +1018,7 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
     int64_t rows_per_block = (int64_t)warps * RPW;
     int64_t grid = (A->nbrows + rows_per_block - 1) / rows_per_block;
     k_scatter<BS, G, TK, TA><<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
-        A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, A->nbrows, lmax, Ke, v64, v32, be, bvec);
+        A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, A->nbrows, lmax, Ke, v64, v32, be, bvec, xd);
     GT_LAUNCH(ctx, "k_scatter");
     return GT_OK;
   };
@@ -1003,20 +1028,21 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
   return go(std::integral_constant<int, 32>());
 }
 
-int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be, double* bvec) {
+int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be, double* bvec,
+                   const double* xd) {
   double* v64 = (out_precision == GT_FP64 || out_precision == GT_MIXED) ? A->val64 : nullptr;
   float* v32 = (out_precision == GT_FP32 || out_precision == GT_MIXED) ? A->val32 : nullptr;
   int bs = A->bs;
   if (ke_precision == GT_FP32) {
     const float* K = (const float*)Ke;
-    if (bs == 1) return launch_scatter<1, float, float>(A, K, v64, v32, be, bvec);
-    if (bs == 2) return launch_scatter<2, float, float>(A, K, v64, v32, be, bvec);
-    return launch_scatter<3, float, float>(A, K, v64, v32, be, bvec);
+    if (bs == 1) return launch_scatter<1, float, float>(A, K, v64, v32, be, bvec, xd);
+    if (bs == 2) return launch_scatter<2, float, float>(A, K, v64, v32, be, bvec, xd);
+    return launch_scatter<3, float, float>(A, K, v64, v32, be, bvec, xd);
   }
   const double* K = (const double*)Ke;
-  if (bs == 1) return launch_scatter<1, double, double>(A, K, v64, v32, be, bvec);
-  if (bs == 2) return launch_scatter<2, double, double>(A, K, v64, v32, be, bvec);
-  return launch_scatter<3, double, double>(A, K, v64, v32, be, bvec);
+  if (bs == 1) return launch_scatter<1, double, double>(A, K, v64, v32, be, bvec, xd);
+  if (bs == 2) return launch_scatter<2, double, double>(A, K, v64, v32, be, bvec, xd);
+  return launch_scatter<3, double, double>(A, K, v64, v32, be, bvec, xd);
 }
 
 // ---------------------------------------------------------------------------
@@ -1252,7 +1278,8 @@ template <int D, int ORDER, int BS, int FORM, int G, class T, class TA>
 __global__ void k_scatter_kron(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                                const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                const int32_t* __restrict__ cnd, int64_t nrows, int lmax, const T* __restrict__ Gc,
-                               T lamf, T muf, double* __restrict__ v64, float* __restrict__ v32) {
+                               T lamf, T muf, double* __restrict__ v64, float* __restrict__ v32,
+                               const double* __restrict__ be, double* __restrict__ bvec, const double* __restrict__ xd) {
   constexpr int M1 = ORDER + 1;
   constexpr int NN = D == 2 ? M1 * M1 : M1 * M1 * M1;
   constexpr int RPW = 32 / G;
@@ -1284,26 +1311,53 @@ __global__ void k_scatter_kron(const int64_t* __restrict__ rowptr, const int32_t
   if (active) {
     const int b = gl;
     int nbi[3] = {b % M1, (b / M1) % M1, b / (M1 * M1)};
+    // with be: the group's lane 0 also sums the load vector of the row (same
+    // incidence order as k_scatter_vec), minus the Dirichlet lift when xd
+    const bool vec = be != nullptr && gl == 0;
+    const bool lift = be != nullptr && xd != nullptr;
+    double bsum[BS];
+#pragma unroll
+    for (int cc = 0; cc < BS; cc++) bsum[cc] = 0.0;
     int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
     for (int64_t k = ib; k < ie; k++) {
       int32_t cb = __ldg(inc + k);
       int32_t c = cb / NN, a = cb - c * NN;
+      if (vec)
+#pragma unroll
+        for (int cc = 0; cc < BS; cc++) bsum[cc] += __ldg(be + (int64_t)c * NN * BS + a * BS + cc);
+      double lv[BS];
+#pragma unroll
+      for (int cc = 0; cc < BS; cc++) lv[cc] = 0.0;
       if (b < NN) {
         int32_t j = __ldg(cnd + (int64_t)c * NN + b);
-        if (j > 0) {
+        if (j > 0 || (j < 0 && lift)) {
           T g[GSTRIDE];
 #pragma unroll
           for (int i = 0; i < GSTRIDE; i++) g[i] = __ldg(Gc + (int64_t)c * GSTRIDE + i);
           int nai[3] = {a % M1, (a / M1) % M1, a / (M1 * M1)};
           T blk[BS][BS];
           kron_block<D, BS, FORM, T>(nai, nbi, g, s_M, s_D, s_K, lamf, muf, blk);
-          int p = find_col(cols, L, j - 1);
+          if (j > 0) {
+            int p = find_col(cols, L, j - 1);
 #pragma unroll
-          for (int cc = 0; cc < BS; cc++)
+            for (int cc = 0; cc < BS; cc++)
 #pragma unroll
-            for (int dd = 0; dd < BS; dd++) acc[(p * BS + cc) * BS + dd] += (TA)blk[cc][dd];
+              for (int dd = 0; dd < BS; dd++) acc[(p * BS + cc) * BS + dd] += (TA)blk[cc][dd];
+          } else {
+#pragma unroll
+            for (int cc = 0; cc < BS; cc++)
+#pragma unroll
+              for (int dd = 0; dd < BS; dd++) lv[cc] += (double)blk[cc][dd] * __ldg(xd + (int64_t)(-j - 1) * BS + dd);
+          }
         }
       }
+      if (lift)
+#pragma unroll
+        for (int cc = 0; cc < BS; cc++) {
+#pragma unroll
+          for (int o = G >> 1; o; o >>= 1) lv[cc] += __shfl_xor_sync(gmask, lv[cc], o);
+          if (gl == 0) bsum[cc] -= lv[cc];
+        }
       __syncwarp(gmask);
     }
     int64_t ob = rb * BS * BS;
@@ -1312,11 +1366,14 @@ __global__ void k_scatter_kron(const int64_t* __restrict__ rowptr, const int32_t
       if (v64) v64[ob + i] = (double)v;
       if (v32) v32[ob + i] = (float)v;
     }
+    if (vec)
+#pragma unroll
+      for (int cc = 0; cc < BS; cc++) bvec[r * BS + cc] = bsum[cc];
   }
 }
 
 template <int D, int ORDER, int BS, int FORM, class T>
-static int launch_kron(Matrix* A, const T* Gc, double nu) {
+static int launch_kron(Matrix* A, const T* Gc, double nu, const double* be, double* bvec, const double* xd) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   constexpr int M1 = ORDER + 1;
@@ -1337,21 +1394,22 @@ static int launch_kron(Matrix* A, const T* Gc, double nu) {
   int64_t grid = (A->nbrows + rows_per_block - 1) / rows_per_block;
   T lamf = (T)(nu / ((1.0 + nu) * (1.0 - 2.0 * nu))), muf = (T)(1.0 / (2.0 * (1.0 + nu)));
   kern<<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
-      A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, A->nbrows, lmax, Gc, lamf, muf, v64, v32);
+      A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, A->nbrows, lmax, Gc, lamf, muf, v64, v32, be, bvec, xd);
   GT_LAUNCH(ctx, "k_scatter_kron");
   return GT_OK;
 }
 
 template <int D, int ORDER, class T>
-static int dispatch_kron(Matrix* A, int form, const T* Gc, double nu) {
+static int dispatch_kron(Matrix* A, int form, const T* Gc, double nu, const double* be, double* bvec,
+                         const double* xd) {
   int bs = A->bs;
   if (bs == 1) {
-    if (form == GT_LAPLACE) return launch_kron<D, ORDER, 1, GT_LAPLACE, T>(A, Gc, nu);
-    if (form == GT_MASS) return launch_kron<D, ORDER, 1, GT_MASS, T>(A, Gc, nu);
+    if (form == GT_LAPLACE) return launch_kron<D, ORDER, 1, GT_LAPLACE, T>(A, Gc, nu, be, bvec, xd);
+    if (form == GT_MASS) return launch_kron<D, ORDER, 1, GT_MASS, T>(A, Gc, nu, be, bvec, xd);
   } else {
-    if (form == GT_LAPLACE) return launch_kron<D, ORDER, D, GT_LAPLACE, T>(A, Gc, nu);
-    if (form == GT_MASS) return launch_kron<D, ORDER, D, GT_MASS, T>(A, Gc, nu);
-    if (form == GT_ELASTICITY) return launch_kron<D, ORDER, D, GT_ELASTICITY, T>(A, Gc, nu);
+    if (form == GT_LAPLACE) return launch_kron<D, ORDER, D, GT_LAPLACE, T>(A, Gc, nu, be, bvec, xd);
+    if (form == GT_MASS) return launch_kron<D, ORDER, D, GT_MASS, T>(A, Gc, nu, be, bvec, xd);
+    if (form == GT_ELASTICITY) return launch_kron<D, ORDER, D, GT_ELASTICITY, T>(A, Gc, nu, be, bvec, xd);
   }
   return set_error(ctx_of(A->space), GT_ERR_UNSUPPORTED, "weak form not supported on this space");
 }
@@ -1361,7 +1419,7 @@ static int alloc_values(Matrix* A);
 // Sum-factorised numeric phase on affine QUAD4/HEX8 meshes.  Sets *used = 0
 // (and writes only the load vector) when some cell is not affine.
 static int kron_numeric(Matrix* A, int form, const double* coef, double nu, const double* f, const double* scoef,
-                        double* be, int* used) {
+                        double* be, double* bvec, const double* xd, int* used) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   *used = 0;
@@ -1397,12 +1455,16 @@ static int kron_numeric(Matrix* A, int form, const double* coef, double nu, cons
     if (s == GT_OK) {
       if (g64) {
         const double* G = (const double*)Gc;
-        s = D == 2 ? (o == 1 ? dispatch_kron<2, 1, double>(A, form, G, nu) : dispatch_kron<2, 2, double>(A, form, G, nu))
-                   : (o == 1 ? dispatch_kron<3, 1, double>(A, form, G, nu) : dispatch_kron<3, 2, double>(A, form, G, nu));
+        s = D == 2 ? (o == 1 ? dispatch_kron<2, 1, double>(A, form, G, nu, be, bvec, xd)
+                             : dispatch_kron<2, 2, double>(A, form, G, nu, be, bvec, xd))
+                   : (o == 1 ? dispatch_kron<3, 1, double>(A, form, G, nu, be, bvec, xd)
+                             : dispatch_kron<3, 2, double>(A, form, G, nu, be, bvec, xd));
       } else {
         const float* G = (const float*)Gc;
-        s = D == 2 ? (o == 1 ? dispatch_kron<2, 1, float>(A, form, G, nu) : dispatch_kron<2, 2, float>(A, form, G, nu))
-                   : (o == 1 ? dispatch_kron<3, 1, float>(A, form, G, nu) : dispatch_kron<3, 2, float>(A, form, G, nu));
+        s = D == 2 ? (o == 1 ? dispatch_kron<2, 1, float>(A, form, G, nu, be, bvec, xd)
+                             : dispatch_kron<2, 2, float>(A, form, G, nu, be, bvec, xd))
+                   : (o == 1 ? dispatch_kron<3, 1, float>(A, form, G, nu, be, bvec, xd)
+                             : dispatch_kron<3, 2, float>(A, form, G, nu, be, bvec, xd));
       }
     }
     mark(ctx, "scatter");
@@ -1539,15 +1601,18 @@ static int alloc_values(Matrix* A) {
 }
 
 // element matrices + scatter on the existing pattern (and optionally b)
+// xd_in (optional, with b_out): Dirichlet values, ndiri_nodes * ncomp in the
+// Dirichlet numbering; b_out then receives b - Ad xd (src/problems.jl:439-453)
 static int numeric(Matrix* A, int form, const double* coef_in, double nu, const double* f_in, const double* scoef_in,
-                   double* b_out) {
+                   double* b_out, const double* xd_in = nullptr) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   int64_t nc = sp->mesh->ncells;
-  DevIn<double> coef, f, scoef;
+  DevIn<double> coef, f, scoef, xd;
   GT_TRY(coef.init(ctx, coef_in, nc));
   GT_TRY(f.init(ctx, f_in, sp->ncomp));
   GT_TRY(scoef.init(ctx, scoef_in, nc));
+  GT_TRY(xd.init(ctx, b_out ? xd_in : nullptr, sp->ndiri_nodes * sp->ncomp));
   int kprec = A->precision == GT_FP32 ? GT_FP32 : GT_FP64;
   size_t esz = kprec == GT_FP32 ? sizeof(float) : sizeof(double);
   void* Ke = nullptr;
@@ -1558,18 +1623,16 @@ static int numeric(Matrix* A, int form, const double* coef_in, double nu, const 
   const int64_t nb = sp->nfree_nodes * sp->ncomp;
   if (b_out && !dev) GT_TRY(dalloc(ctx, &bd, nb));
   int used_kron = 0;
-  int s = kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, &used_kron);
+  // the load vector (and the Dirichlet lift) is summed inside the matrix
+  // scatter, over the same incidences
+  int s = kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, b_out ? bd : nullptr, xd.p, &used_kron);
   if (s == GT_OK && !used_kron) {
     s = dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz));
     if (s == GT_OK) s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
     mark(ctx, "elements");
     if (s == GT_OK) s = alloc_values(A);
-    // the load vector is summed inside the matrix scatter (same incidences)
-    if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr);
+    if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, xd.p);
     mark(ctx, "scatter");
-  } else if (s == GT_OK && b_out) {
-    s = scatter_vector(sp, A->inc_ptr, A->inc, be, bd);
-    mark(ctx, "scatter_vector");
   }
   if (s == GT_OK && b_out) {
     if (s == GT_OK && !dev) {
@@ -1611,8 +1674,24 @@ static void matrix_release(gt_matrix* A) {
 
 extern "C" {
 
+static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double nu, int precision, const double* f,
+                       const double* source_coef, const double* xd, double* b, gt_matrix** out);
+
 int gt_assemble_matrix_and_vector(gt_space* sp, int form, const double* cell_coef, double nu, int precision,
                                   const double* f, const double* source_coef, double* b, gt_matrix** out) {
+  return assemble_mv(sp, form, cell_coef, nu, precision, f, source_coef, nullptr, b, out);
+}
+
+int gt_linear_problem(gt_space* sp, int form, const double* cell_coef, double nu, int precision, const double* f,
+                      const double* source_coef, const double* dirichlet_values, double* b, gt_matrix** out) {
+  if (!sp || !b || !f) return GT_ERR_INVALID;
+  return assemble_mv(sp, form, cell_coef, nu, precision, f, source_coef, dirichlet_values, b, out);
+}
+
+}  // extern "C"
+
+static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double nu, int precision, const double* f,
+                       const double* source_coef, const double* xd, double* b, gt_matrix** out) {
   if (!sp || !out) return GT_ERR_INVALID;
   *out = nullptr;
   Ctx* ctx = sp->mesh->ctx;
@@ -1633,7 +1712,7 @@ int gt_assemble_matrix_and_vector(gt_space* sp, int form, const double* cell_coe
   int s = build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc, false);
   mark(ctx, "incidence");
   if (s == GT_OK) s = build_pattern(A);
-  if (s == GT_OK) s = numeric(A, form, cell_coef, nu, f, source_coef, b);
+  if (s == GT_OK) s = numeric(A, form, cell_coef, nu, f, source_coef, b, xd);
   if (s == GT_OK) s = device_status(ctx, "assemble_matrix");
   if (s != GT_OK) {
     matrix_release(A);
@@ -1643,6 +1722,8 @@ int gt_assemble_matrix_and_vector(gt_space* sp, int form, const double* cell_coe
   *out = A;
   return GT_OK;
 }
+
+extern "C" {
 
 int gt_assemble_matrix(gt_space* sp, int form, const double* cell_coef, double nu, int precision, gt_matrix** out) {
   return gt_assemble_matrix_and_vector(sp, form, cell_coef, nu, precision, nullptr, nullptr, nullptr, out);

@@ -192,7 +192,7 @@ int compute_elements(const Space* sp, int form, const double* d_coef, double nu,
                      const double* f, const double* d_scoef, void* Ke, double* be, int want_matrix);
 // be/bvec (optional): element vectors and the load vector summed in the same pass
 int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be = nullptr,
-                   double* bvec = nullptr);
+                   double* bvec = nullptr, const double* xd = nullptr);
 int tabulation_doubles(const Space* sp);
 int compute_elements_with_tab(const Space* sp, int form, const double* d_coef, double nu, int precision,
                               double* tab, void* Ke);

@@ -201,6 +201,35 @@ class Space:
         self.num_dirichlet_dofs = int(info[1])
         self.num_local_dofs = int(info[2])
 
+    def node_coordinates(self):
+        """Physical coordinates of the space's nodes, ``(free, dirichlet)``
+        arrays of shape (nodes, D) in the free and the Dirichlet node
+        numbering: the geometry map of each cell (P1: its vertices; QUAD4/HEX8:
+        multilinear) at the reference Lagrange nodes (lexicographic, spacing
+        1/order) -- the points at which the reference interpolates Dirichlet
+        data (src/space.jl:1127-1177)."""
+        m, D, nc = self.mesh, self.mesh.D, self.ncomp
+        cd = self.face_dofs()
+        first = cd[:, ::nc]  # component 0 of every local node
+        nd = np.where(first > 0, (first - 1) // nc + 1, -((-first - 1) // nc + 1))
+        nn = nd.shape[1]
+        X = m.coords[m.cell_nodes.astype(np.int64) - 1]  # (cells, vertices, D)
+        if m.cell_type == _lib.GT_TET4:
+            N = np.eye(4)
+        else:
+            k = self.order
+            e = np.array(np.unravel_index(np.arange(nn), (k + 1,) * D, order="F")).T / k  # (nn, D)
+            nv = 1 << D
+            bits = np.array([[(v >> d) & 1 for d in range(D)] for v in range(nv)])  # (nv, D)
+            N = np.prod(np.where(bits[None, :, :] == 1, e[:, None, :], 1.0 - e[:, None, :]), axis=2)  # (nn, nv)
+        Xn = np.einsum("av,cvd->cad", N, X)
+        free = np.zeros((self.num_free_dofs // nc, D))
+        diri = np.zeros((self.num_dirichlet_dofs // nc, D))
+        f, d = nd > 0, nd < 0
+        free[nd[f] - 1] = Xn[f]
+        diri[-nd[d] - 1] = Xn[d]
+        return free, diri
+
     def face_dofs(self) -> np.ndarray:
         """GT.face_dofs(V): (ncells, nloc) int32, free > 0, Dirichlet < 0."""
         out = np.zeros((self.mesh.num_cells, self.num_local_dofs), np.int32)
@@ -402,11 +431,44 @@ class LinearProblem:
     x: np.ndarray
 
 
-def linear_problem(U: Space, a: Form, l: Source, T=np.float64, V=None) -> LinearProblem:
-    """GT.PartitionedSolvers_linear_problem(T, U, a, l) with homogeneous
-    Dirichlet data: A, b assembled on the GPU, x = 0."""
-    A, b = assemble_matrix_and_vector(a, l, T, U, V)
-    return LinearProblem(A, b, np.zeros_like(b))
+def interpolate_dirichlet(g, V: Space) -> np.ndarray:
+    """GT.interpolate_dirichlet(g, V): the Dirichlet values of the function
+    g at the space's Dirichlet nodes, in the Dirichlet DOF numbering (DOF -k
+    -> xd[k-1]).  g maps an (n, D) array of points to (n,) values or, on a
+    vector space, to (n, ncomp)."""
+    _, xdir = V.node_coordinates()
+    vals = np.asarray(g(xdir), np.float64)
+    if V.ncomp == 1:
+        vals = vals.reshape(-1)
+    else:
+        vals = vals.reshape(-1, V.ncomp)
+    return np.ascontiguousarray(vals.reshape(-1))
+
+
+def linear_problem(U: Space, a: Form, l: Source, T=np.float64, V=None, dirichlet_values=None) -> LinearProblem:
+    """GT.PartitionedSolvers_linear_problem: A and b assembled on the GPU,
+    x = 0.  With dirichlet_values (e.g. interpolate_dirichlet(g, U)) the
+    Dirichlet lift b -= Ad * xd is applied in the same pass
+    (src/problems.jl:439-453); without, homogeneous Dirichlet data."""
+    if dirichlet_values is None:
+        A, b = assemble_matrix_and_vector(a, l, T, U, V)
+        return LinearProblem(A, b, np.zeros_like(b))
+    _check_form(a)
+    if not isinstance(l, Source):
+        raise NotImplementedError("only source terms int coef*f*v are supported")
+    if V is not None and V is not U:
+        raise NotImplementedError("trial and test spaces must be the same space")
+    xd = np.ascontiguousarray(dirichlet_values, np.float64)
+    if xd.size != U.num_dirichlet_dofs:
+        raise ValueError(f"dirichlet_values has {xd.size} entries, the space has {U.num_dirichlet_dofs} Dirichlet DOFs")
+    h = C.c_void_p()
+    b = np.zeros(U.num_free_dofs, np.float64)
+    coef = a.cell_coef(U.mesh.num_cells)
+    scoef = None if l.coef is None else (np.full(U.mesh.num_cells, float(l.coef)) if np.isscalar(l.coef) else l.coef)
+    fv = l.fvec(U.ncomp)  # kept alive across the call (ctypes releases the GIL)
+    check(U.ctx.h, U.ctx.lib.gt_linear_problem(U.h, a.kind, _ptr(coef), a.nu, _precision(T), _ptr(fv), _ptr(scoef),
+                                               _ptr(xd), _ptr(b), C.byref(h)))
+    return LinearProblem(Matrix(U, h, a), b, np.zeros_like(b))
 
 
 _MODES = {"fp64": _lib.GT_SOLVE_FP64, "ir": _lib.GT_SOLVE_IR, "mixed": _lib.GT_SOLVE_IR, "fp32": _lib.GT_SOLVE_FP32}

@@ -151,6 +151,16 @@ int gt_assemble_matrix(gt_space* space, int form, const double* cell_coef, doubl
 int gt_assemble_matrix_and_vector(gt_space* space, int form, const double* cell_coef, double nu,
                                   int precision, const double* f, const double* source_coef, double* b,
                                   gt_matrix** matrix);
+/* Replaces GT.PartitionedSolvers_linear_problem(uhd, a, l) with Dirichlet
+ * data (src/problems.jl:439-453): assembles A (free x free) and the load
+ * vector, and subtracts the Dirichlet lift Ad * xd (Ad = free x Dirichlet
+ * columns of the form) in the same pass, without assembling Ad.
+ * dirichlet_values: num_dirichlet_dofs values in the Dirichlet numbering
+ * (DOF -k -> dirichlet_values[k-1]), e.g. the interpolated boundary data;
+ * b receives b - Ad * xd.  f and b are required. */
+int gt_linear_problem(gt_space* space, int form, const double* cell_coef, double nu, int precision,
+                      const double* f, const double* source_coef, const double* dirichlet_values, double* b,
+                      gt_matrix** matrix);
 /* Replaces GT.update_matrix!(A, cache) (src/problems.jl:352-361): new values
  * on the existing sparsity. */
 int gt_update_matrix(gt_matrix* matrix, int form, const double* cell_coef, double nu);
