@@ -868,6 +868,7 @@ int tabulation_doubles(const Space* sp) { return tab_layout(sp->mesh->ctype, sp-
 int compute_elements_with_tab(const Space* sp, int form, const double* d_coef, double nu, int precision, double* tab,
                               void* Ke) {
   Ctx* ctx = ctx_of(sp);
+  mesh_wait_coords(sp->mesh);
   if (form != GT_LAPLACE && form != GT_MASS && form != GT_ELASTICITY)
     return set_error(ctx, GT_ERR_UNSUPPORTED, "weak form not supported (Laplacian, mass, linear elasticity only)");
   if (form == GT_ELASTICITY && sp->ncomp != sp->mesh->D)
@@ -1558,12 +1559,16 @@ __global__ void k_expand_entries(const int64_t* rowptr, const int32_t* colind, c
 // ---------------------------------------------------------------------------
 // a pointer the kernels can read: device pointers pass through, host data is
 // staged into a pooled device buffer
+// With async, a host source is uploaded on the copy stream and wait()
+// orders the main stream after it (the upload overlaps the kernels queued
+// before the consumer).
 template <class T>
 struct DevIn {
-  Ctx* ctx;
+  Ctx* ctx = nullptr;
   const T* p = nullptr;
   T* owned = nullptr;
-  int init(Ctx* c, const T* src, int64_t n) {
+  cudaEvent_t ev = nullptr;
+  int init(Ctx* c, const T* src, int64_t n, bool async = false) {
     ctx = c;
     if (!src) return GT_OK;
     cudaPointerAttributes at{};
@@ -1574,12 +1579,43 @@ struct DevIn {
     }
     cudaGetLastError();
     GT_TRY(dalloc(c, &owned, n));
-    GT_TRY(copy_in(c, owned, src, n));
+    if (async) GT_TRY(side_copy_in(c, owned, src, sizeof(T) * (size_t)n, &ev));
+    else GT_TRY(copy_in(c, owned, src, n));
     p = owned;
     return GT_OK;
   }
+  void wait() {
+    if (ev) {
+      cudaStreamWaitEvent(ctx->stream, ev, 0);
+      event_put(ctx, ev);
+      ev = nullptr;
+    }
+  }
   ~DevIn() {
+    wait();
     if (owned) dfree(ctx, owned);
+  }
+};
+
+// the per-call inputs of the numeric phase (per-cell coefficient, source,
+// source coefficient, Dirichlet values), staged before the sparsity phase
+struct NumIn {
+  DevIn<double> coef, f, scoef, xd;
+  int init(const Space* sp, const double* coef_in, const double* f_in, const double* scoef_in, const double* xd_in,
+           bool async) {
+    Ctx* ctx = sp->mesh->ctx;
+    int64_t nc = sp->mesh->ncells;
+    GT_TRY(coef.init(ctx, coef_in, nc, async));
+    GT_TRY(f.init(ctx, f_in, sp->ncomp, async));
+    GT_TRY(scoef.init(ctx, scoef_in, nc, async));
+    GT_TRY(xd.init(ctx, xd_in, sp->ndiri_nodes * sp->ncomp, async));
+    return GT_OK;
+  }
+  void wait() {
+    coef.wait();
+    f.wait();
+    scoef.wait();
+    xd.wait();
   }
 };
 
@@ -1601,18 +1637,15 @@ static int alloc_values(Matrix* A) {
 }
 
 // element matrices + scatter on the existing pattern (and optionally b)
-// xd_in (optional, with b_out): Dirichlet values, ndiri_nodes * ncomp in the
+// in.xd (optional, with b_out): Dirichlet values, ndiri_nodes * ncomp in the
 // Dirichlet numbering; b_out then receives b - Ad xd (src/problems.jl:439-453)
-static int numeric(Matrix* A, int form, const double* coef_in, double nu, const double* f_in, const double* scoef_in,
-                   double* b_out, const double* xd_in = nullptr) {
+static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   int64_t nc = sp->mesh->ncells;
-  DevIn<double> coef, f, scoef, xd;
-  GT_TRY(coef.init(ctx, coef_in, nc));
-  GT_TRY(f.init(ctx, f_in, sp->ncomp));
-  GT_TRY(scoef.init(ctx, scoef_in, nc));
-  GT_TRY(xd.init(ctx, b_out ? xd_in : nullptr, sp->ndiri_nodes * sp->ncomp));
+  in.wait();
+  mesh_wait_coords(sp->mesh);
+  DevIn<double>&coef = in.coef, &f = in.f, &scoef = in.scoef, &xd = in.xd;
   int kprec = A->precision == GT_FP32 ? GT_FP32 : GT_FP64;
   size_t esz = kprec == GT_FP32 ? sizeof(float) : sizeof(double);
   void* Ke = nullptr;
@@ -1625,28 +1658,31 @@ static int numeric(Matrix* A, int form, const double* coef_in, double nu, const 
   int used_kron = 0;
   // the load vector (and the Dirichlet lift) is summed inside the matrix
   // scatter, over the same incidences
-  int s = kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, b_out ? bd : nullptr, xd.p, &used_kron);
+  int s = kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr,
+                       &used_kron);
   if (s == GT_OK && !used_kron) {
     s = dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz));
     if (s == GT_OK) s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
     mark(ctx, "elements");
     if (s == GT_OK) s = alloc_values(A);
-    if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, xd.p);
+    if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr);
     mark(ctx, "scatter");
   }
-  if (s == GT_OK && b_out) {
-    if (s == GT_OK && !dev) {
-      s = copy_out(ctx, b_out, bd, nb);
-      if (s == GT_OK) {
-        cudaError_t e = cudaStreamSynchronize(ctx->stream);
-        if (e != cudaSuccess) s = check_cuda(ctx, e, "assemble_vector");
-      }
-    }
-  }
+  // host b: the copy is queued here; the caller's device_status() call
+  // synchronises the stream before returning (the freed staging block is only
+  // reused by work queued after the copy)
+  if (s == GT_OK && b_out && !dev) s = copy_out(ctx, b_out, bd, nb);
   if (b_out && !dev) dfree(ctx, bd);
   if (Ke) pool_free(ctx, Ke);
   if (be) dfree(ctx, be);
   return s;
+}
+
+static int numeric(Matrix* A, int form, const double* coef_in, double nu, const double* f_in, const double* scoef_in,
+                   double* b_out, const double* xd_in = nullptr) {
+  NumIn in;
+  GT_TRY(in.init(A->space, coef_in, f_in, scoef_in, b_out ? xd_in : nullptr, false));
+  return numeric_in(A, form, in, nu, b_out);
 }
 
 static int device_status(Ctx* ctx, const char* where) {
@@ -1674,8 +1710,18 @@ static void matrix_release(gt_matrix* A) {
 
 extern "C" {
 
+// host CSR outputs filled by the assembly call itself (scalar entries)
+struct HostCsr {
+  int64_t* rowptr;
+  int32_t* colind;
+  double* v64;
+  float* v32;
+  int64_t capacity;  // entries colind / values can hold
+};
+
 static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double nu, int precision, const double* f,
-                       const double* source_coef, const double* xd, double* b, gt_matrix** out);
+                       const double* source_coef, const double* xd, double* b, gt_matrix** out,
+                       const HostCsr* hc = nullptr);
 
 int gt_assemble_matrix_and_vector(gt_space* sp, int form, const double* cell_coef, double nu, int precision,
                                   const double* f, const double* source_coef, double* b, gt_matrix** out) {
@@ -1688,10 +1734,18 @@ int gt_linear_problem(gt_space* sp, int form, const double* cell_coef, double nu
   return assemble_mv(sp, form, cell_coef, nu, precision, f, source_coef, dirichlet_values, b, out);
 }
 
+int gt_assemble_csr(gt_space* sp, int form, const double* cell_coef, double nu, int precision, const double* f,
+                    const double* source_coef, double* b, int64_t capacity, int64_t* rowptr, int32_t* colind,
+                    double* values64, float* values32, gt_matrix** out) {
+  if (!sp || !rowptr || !colind) return GT_ERR_INVALID;
+  HostCsr hc{rowptr, colind, values64, values32, capacity};
+  return assemble_mv(sp, form, cell_coef, nu, precision, f, source_coef, nullptr, b, out, &hc);
+}
+
 }  // extern "C"
 
 static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double nu, int precision, const double* f,
-                       const double* source_coef, const double* xd, double* b, gt_matrix** out) {
+                       const double* source_coef, const double* xd, double* b, gt_matrix** out, const HostCsr* hc) {
   if (!sp || !out) return GT_ERR_INVALID;
   *out = nullptr;
   Ctx* ctx = sp->mesh->ctx;
@@ -1709,12 +1763,51 @@ static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double n
   A->bs = sp->ncomp;
   A->precision = precision;
   mark(ctx, "setup");
-  int s = build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc, false);
+  // host inputs upload on the copy stream while the sparsity is built
+  NumIn in;
+  int s = in.init(sp, cell_coef, f, source_coef, b ? xd : nullptr, true);
+  if (s == GT_OK) s = build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc, false);
   mark(ctx, "incidence");
   if (s == GT_OK) s = build_pattern(A);
-  if (s == GT_OK) s = numeric(A, form, cell_coef, nu, f, source_coef, b, xd);
-  if (s == GT_OK) s = device_status(ctx, "assemble_matrix");
+  cudaEvent_t side_done = nullptr;
+  const int bs = A->bs;
+  const int64_t nscal = A->nbrows * bs, nnz = A->bnnz * bs * bs;
+  if (s == GT_OK && hc && nnz > hc->capacity)
+    s = set_error(ctx, GT_ERR_INVALID, "gt_assemble_csr: capacity " + std::to_string(hc->capacity) +
+                                           " below the " + std::to_string(nnz) + " entries");
+  if (s == GT_OK && hc && bs == 1) {
+    // the pattern goes back to the host while the values are computed
+    cudaEvent_t pat = event_get(ctx);
+    side_done = event_get(ctx);
+    if (!pat || !side_done) s = set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
+    if (s == GT_OK && cudaEventRecord(pat, ctx->stream) != cudaSuccess) s = check_cuda(ctx, cudaGetLastError(), "event");
+    if (s == GT_OK) cudaStreamWaitEvent(ctx->side, pat, 0);
+    if (s == GT_OK && cudaMemcpyAsync(hc->rowptr, A->rowptr, sizeof(int64_t) * (nscal + 1), cudaMemcpyDefault,
+                                      ctx->side) != cudaSuccess)
+      s = check_cuda(ctx, cudaGetLastError(), "rowptr download");
+    if (s == GT_OK && nnz > 0 &&
+        cudaMemcpyAsync(hc->colind, A->colind, sizeof(int32_t) * nnz, cudaMemcpyDefault, ctx->side) != cudaSuccess)
+      s = check_cuda(ctx, cudaGetLastError(), "colind download");
+    if (s == GT_OK) cudaEventRecord(side_done, ctx->side);
+    event_put(ctx, pat);
+  }
+  if (s == GT_OK) s = numeric_in(A, form, in, nu, b);
+  if (s == GT_OK && hc) {
+    if (bs == 1) {
+      if (hc->v64 && A->val64 && nnz > 0) s = copy_out(ctx, hc->v64, A->val64, nnz);
+      if (s == GT_OK && hc->v32 && A->val32 && nnz > 0) s = copy_out(ctx, hc->v32, A->val32, nnz);
+    } else {
+      s = gt_matrix_download_csr(A, hc->rowptr, hc->colind, hc->v64, hc->v32);
+    }
+  }
+  if (s == GT_OK) s = device_status(ctx, "assemble_matrix");  // synchronises the stream
+  if (side_done) {
+    cudaError_t e = cudaEventSynchronize(side_done);
+    if (s == GT_OK && e != cudaSuccess) s = check_cuda(ctx, e, "pattern download");
+    event_put(ctx, side_done);
+  }
   if (s != GT_OK) {
+    cudaStreamSynchronize(ctx->side);
     matrix_release(A);
     delete A;
     return s;
@@ -1756,6 +1849,7 @@ int gt_assemble_vector(gt_space* sp, const double* f, const double* cell_coef, d
   GT_TRY(fd.init(ctx, f, sp->ncomp));
   double* be = nullptr;
   GT_TRY(dalloc(ctx, &be, nc * sp->nloc));
+  mesh_wait_coords(sp->mesh);
   int s = compute_elements(sp, GT_MASS, nullptr, 0.0, GT_FP64, fd.p, coef.p, nullptr, be, 0);
   int64_t nb = sp->nfree_nodes * sp->ncomp;
   bool dev = is_device_ptr(b);

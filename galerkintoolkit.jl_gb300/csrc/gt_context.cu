@@ -76,6 +76,44 @@ void pool_trim(Ctx* ctx) {
   ctx->pooled_bytes = 0;
 }
 
+cudaEvent_t event_get(Ctx* ctx) {
+  if (!ctx->free_events.empty()) {
+    cudaEvent_t e = ctx->free_events.back();
+    ctx->free_events.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return e;
+}
+
+void event_put(Ctx* ctx, cudaEvent_t e) {
+  if (e) ctx->free_events.push_back(e);
+}
+
+int side_copy_in(Ctx* ctx, void* dst, const void* src, size_t bytes, cudaEvent_t* done) {
+  *done = nullptr;
+  cudaEvent_t after = event_get(ctx), ev = event_get(ctx);
+  if (!after || !ev) return set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
+  GT_CUDA(ctx, cudaEventRecord(after, ctx->stream));
+  GT_CUDA(ctx, cudaStreamWaitEvent(ctx->side, after, 0));
+  GT_CUDA(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, ctx->side));
+  GT_CUDA(ctx, cudaEventRecord(ev, ctx->side));
+  event_put(ctx, after);  // the wait above captured its state: reusable
+  *done = ev;
+  return GT_OK;
+}
+
+void mesh_wait_coords(Mesh* m) {
+  if (m->coords_pending && m->coords_ev) {
+    cudaStreamWaitEvent(m->ctx->stream, m->coords_ev, 0);
+    m->coords_pending = false;
+  }
+}
+
 void mark(Ctx* ctx, const char* name) {
   if (!ctx->prof) return;
   cudaEvent_t e;
@@ -250,6 +288,7 @@ int gt_ctx_create(int device, gt_ctx** out) {
   c->device = device;
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaMalloc(&c->d_err, sizeof(uint32_t)) != cudaSuccess ||
       cudaMallocHost(&c->h_err, sizeof(uint32_t)) != cudaSuccess ||
       cudaMallocHost(&c->h_scratch, 64 * sizeof(int64_t)) != cudaSuccess ||
@@ -273,6 +312,7 @@ int gt_ctx_destroy(gt_ctx* c) {
   if (!c) return GT_ERR_INVALID;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  if (c->side) cudaStreamSynchronize(c->side);
   for (auto& kv : c->live) cudaFree(kv.first);
   for (auto& kv : c->pool) cudaFree(kv.second);
   cudaFree(c->d_err);
@@ -281,7 +321,9 @@ int gt_ctx_destroy(gt_ctx* c) {
   cudaFreeHost(c->h_dscratch);
   for (auto& m : c->marks) cudaEventDestroy(m.second);
   for (auto e : c->spare_events) cudaEventDestroy(e);
+  for (auto e : c->free_events) cudaEventDestroy(e);
   cudaStreamDestroy(c->own_stream);
+  if (c->side) cudaStreamDestroy(c->side);
   delete c;
   return GT_OK;
 }
@@ -291,6 +333,7 @@ const char* gt_last_error(const gt_ctx* c) { return c ? c->err.c_str() : "null c
 int gt_ctx_synchronize(gt_ctx* c) {
   if (!c) return GT_ERR_INVALID;
   GT_CUDA(c, cudaStreamSynchronize(c->stream));
+  GT_CUDA(c, cudaStreamSynchronize(c->side));
   return GT_OK;
 }
 

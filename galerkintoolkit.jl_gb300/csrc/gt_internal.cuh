@@ -68,6 +68,10 @@ struct Ctx {
   int num_sms = 0;
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
+  // copy stream: host<->device transfers that overlap the kernels of the
+  // main stream (ordered against it with events)
+  cudaStream_t side = nullptr;
+  std::vector<cudaEvent_t> free_events;
   std::string err;
   // size-bucketed pool of device blocks (no cudaMalloc in steady state)
   std::multimap<size_t, void*> pool;
@@ -89,6 +93,16 @@ struct Ctx {
   std::vector<std::pair<std::string, cudaEvent_t>> marks;
   std::vector<cudaEvent_t> spare_events;
 };
+
+// events without timing, recycled by the context
+cudaEvent_t event_get(Ctx* ctx);
+void event_put(Ctx* ctx, cudaEvent_t e);
+// Copies bytes from a host pointer to device memory on the copy stream,
+// after the work already queued on the main stream (so a buffer still read
+// by queued kernels is not overwritten early).  *done receives the event the
+// main stream must wait on before using dst.  A pinned source may still be
+// read after the call returns.
+int side_copy_in(Ctx* ctx, void* dst, const void* src, size_t bytes, cudaEvent_t* done);
 
 // counts a kernel launch; used as the grid argument: k<<<GT_KC(ctx, g), ...>>>
 #define GT_KC(ctx, g) ((ctx)->launches++, (g))
@@ -151,7 +165,13 @@ struct Mesh {
   int32_t* bgroup = nullptr;
   int64_t nbedges = 0;
   int32_t* bedges = nullptr;     // 3-D parent 1-faces, 0-based
+  // coordinates uploaded on the copy stream: kernels reading coords wait
+  cudaEvent_t coords_ev = nullptr;
+  bool coords_pending = false;
 };
+
+// orders the main stream after a pending coordinate upload of the mesh
+void mesh_wait_coords(Mesh* m);
 
 struct Space {
   Ctx* ctx = nullptr;  // owning context (also reachable as mesh->ctx while the mesh lives)

@@ -585,12 +585,27 @@ int gt_mesh_create(gt_ctx* ctx, int cell_type, int64_t nnodes, const double* coo
 
 int gt_mesh_set_coords(gt_mesh* M, const double* coords) {
   if (!M || !coords) return GT_ERR_INVALID;
-  return copy_in(M->ctx, M->coords, coords, M->nnodes * M->D);
+  Ctx* ctx = M->ctx;
+  cudaPointerAttributes at{};
+  bool dev = cudaPointerGetAttributes(&at, coords) == cudaSuccess &&
+             (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged);
+  cudaGetLastError();
+  if (dev) return copy_in(ctx, M->coords, coords, M->nnodes * M->D);
+  // host source: uploaded on the copy stream, overlapping whatever the next
+  // call runs before it needs coordinates (numbering, sparsity)
+  cudaEvent_t ev = nullptr;
+  GT_TRY(side_copy_in(ctx, M->coords, coords, sizeof(double) * M->nnodes * M->D, &ev));
+  if (M->coords_ev) event_put(ctx, M->coords_ev);
+  M->coords_ev = ev;
+  M->coords_pending = true;
+  return GT_OK;
 }
 
 int gt_mesh_destroy(gt_mesh* M) {
   if (!M) return GT_ERR_INVALID;
   Ctx* c = M->ctx;
+  mesh_wait_coords(M);  // no upload may still target the freed buffer
+  if (M->coords_ev) event_put(c, M->coords_ev);
   dfree(c, M->coords);
   dfree(c, M->cell_nodes);
   dfree(c, M->corners);

@@ -71,6 +71,7 @@ SIGNATURES = [
     ("gt_assemble_matrix", I32, [P, I32, P, DBL, I32, C.POINTER(P)]),
     ("gt_assemble_matrix_and_vector", I32, [P, I32, P, DBL, I32, P, P, P, C.POINTER(P)]),
     ("gt_linear_problem", I32, [P, I32, P, DBL, I32, P, P, P, P, C.POINTER(P)]),
+    ("gt_assemble_csr", I32, [P, I32, P, DBL, I32, P, P, P, I64, P, P, P, P, C.POINTER(P)]),
     ("gt_update_matrix", I32, [P, I32, P, DBL]),
     ("gt_update_matrix_and_vector", I32, [P, I32, P, DBL, P, P, P]),
     ("gt_update_matrix_noalloc", I32, [P, I32, P, DBL]),

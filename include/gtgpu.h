@@ -115,7 +115,10 @@ int gt_mesh_create(gt_ctx* ctx, int cell_type, int64_t nnodes, const double* coo
                    const int32_t* corner_nodes, int64_t nbfaces, const int32_t* bface_nodes,
                    const int32_t* bface_group, int64_t nbedges, const int32_t* bedge_nodes,
                    gt_mesh** mesh);
-/* Replaces GT.replace_node_coordinates (src/mesh.jl:698-713) in place. */
+/* Replaces GT.replace_node_coordinates (src/mesh.jl:698-713) in place.  A
+ * host source is uploaded on the context's copy stream, ordered before every
+ * later use of the coordinates; a pinned source must stay unchanged until
+ * the next call that returns results to the host. */
 int gt_mesh_set_coords(gt_mesh* mesh, const double* coords);
 int gt_mesh_destroy(gt_mesh* mesh);
 
@@ -161,6 +164,18 @@ int gt_assemble_matrix_and_vector(gt_space* space, int form, const double* cell_
 int gt_linear_problem(gt_space* space, int form, const double* cell_coef, double nu, int precision,
                       const double* f, const double* source_coef, const double* dirichlet_values, double* b,
                       gt_matrix** matrix);
+/* GT.assemble_matrix_and_vector returning the host CSR arrays in one call
+ * (the reference returns a host SparseMatrixCSC, src/problems.jl:391-414):
+ * assembles like gt_assemble_matrix_and_vector and fills rowptr (rows + 1,
+ * int64), colind and values64 / values32 (either may be NULL) with the
+ * scalar CSR.  capacity: entries colind / values can hold; a smaller
+ * capacity returns GT_ERR_INVALID (gt_matrix_info gives the count of a
+ * previous assembly of the same space).  Host inputs are uploaded, and the
+ * pattern downloaded, on a copy stream while the device works on other
+ * phases: with pinned host buffers the transfers overlap the kernels. */
+int gt_assemble_csr(gt_space* space, int form, const double* cell_coef, double nu, int precision, const double* f,
+                    const double* source_coef, double* b, int64_t capacity, int64_t* rowptr, int32_t* colind,
+                    double* values64, float* values32, gt_matrix** matrix);
 /* Replaces GT.update_matrix!(A, cache) (src/problems.jl:352-361): new values
  * on the existing sparsity. */
 int gt_update_matrix(gt_matrix* matrix, int form, const double* cell_coef, double nu);
