@@ -902,7 +902,7 @@ __device__ __forceinline__ int find_col(const int32_t* cols, int L, int32_t j) {
 template <int BS, int G, class TK, class TA>
 __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                           const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
-                          const int32_t* __restrict__ cnd, int nn, int64_t nrows, int lmax,
+                          const int32_t* __restrict__ cnd, int nn, int64_t row_begin, int64_t row_end, int lmax,
                           const TK* __restrict__ Ke, double* __restrict__ v64, float* __restrict__ v32,
                           const double* __restrict__ be, double* __restrict__ bvec,
                           const double* __restrict__ xd) {
@@ -914,8 +914,8 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
   int slot = w * RPW + sub;
   TA* acc = (TA*)s_raw + (size_t)slot * lmax * BS * BS;
   int32_t* cols = (int32_t*)((TA*)s_raw + (size_t)(blockDim.x / G) * lmax * BS * BS) + (size_t)slot * lmax;
-  int64_t r = ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * RPW + sub;
-  bool active = r < nrows;
+  int64_t r = row_begin + ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * RPW + sub;
+  bool active = r < row_end;
   unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
   int64_t rb = 0;
   int L = 0;
@@ -1002,7 +1002,7 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
 
 template <int BS, class TK, class TA>
 static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, const double* be, double* bvec,
-                          const double* xd) {
+                          const double* xd, int64_t r0, int64_t r1) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   int nn = sp->nn;
@@ -1017,9 +1017,9 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
     if (smem > 200 * 1024) return set_error(ctx, GT_ERR_UNSUPPORTED, "sparsity row too wide for the scatter kernel");
     cudaFuncSetAttribute(k_scatter<BS, G, TK, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int64_t rows_per_block = (int64_t)warps * RPW;
-    int64_t grid = (A->nbrows + rows_per_block - 1) / rows_per_block;
+    int64_t grid = (r1 - r0 + rows_per_block - 1) / rows_per_block;
     k_scatter<BS, G, TK, TA><<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
-        A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, A->nbrows, lmax, Ke, v64, v32, be, bvec, xd);
+        A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, r0, r1, lmax, Ke, v64, v32, be, bvec, xd);
     GT_LAUNCH(ctx, "k_scatter");
     return GT_OK;
   };
@@ -1030,20 +1030,21 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
 }
 
 int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be, double* bvec,
-                   const double* xd) {
+                   const double* xd, int64_t r0, int64_t r1) {
+  if (r1 < 0) r1 = A->nbrows;
   double* v64 = (out_precision == GT_FP64 || out_precision == GT_MIXED) ? A->val64 : nullptr;
   float* v32 = (out_precision == GT_FP32 || out_precision == GT_MIXED) ? A->val32 : nullptr;
   int bs = A->bs;
   if (ke_precision == GT_FP32) {
     const float* K = (const float*)Ke;
-    if (bs == 1) return launch_scatter<1, float, float>(A, K, v64, v32, be, bvec, xd);
-    if (bs == 2) return launch_scatter<2, float, float>(A, K, v64, v32, be, bvec, xd);
-    return launch_scatter<3, float, float>(A, K, v64, v32, be, bvec, xd);
+    if (bs == 1) return launch_scatter<1, float, float>(A, K, v64, v32, be, bvec, xd, r0, r1);
+    if (bs == 2) return launch_scatter<2, float, float>(A, K, v64, v32, be, bvec, xd, r0, r1);
+    return launch_scatter<3, float, float>(A, K, v64, v32, be, bvec, xd, r0, r1);
   }
   const double* K = (const double*)Ke;
-  if (bs == 1) return launch_scatter<1, double, double>(A, K, v64, v32, be, bvec, xd);
-  if (bs == 2) return launch_scatter<2, double, double>(A, K, v64, v32, be, bvec, xd);
-  return launch_scatter<3, double, double>(A, K, v64, v32, be, bvec, xd);
+  if (bs == 1) return launch_scatter<1, double, double>(A, K, v64, v32, be, bvec, xd, r0, r1);
+  if (bs == 2) return launch_scatter<2, double, double>(A, K, v64, v32, be, bvec, xd, r0, r1);
+  return launch_scatter<3, double, double>(A, K, v64, v32, be, bvec, xd, r0, r1);
 }
 
 // ---------------------------------------------------------------------------
@@ -1636,10 +1637,24 @@ static int alloc_values(Matrix* A) {
   return GT_OK;
 }
 
-// element matrices + scatter on the existing pattern (and optionally b)
+// host CSR outputs filled by the assembly call itself (scalar entries)
+struct HostCsr {
+  int64_t* rowptr;
+  int32_t* colind;
+  double* v64;
+  float* v32;
+  int64_t capacity;  // entries colind / values can hold
+};
+
+// element matrices + scatter on the existing pattern (and optionally b).
 // in.xd (optional, with b_out): Dirichlet values, ndiri_nodes * ncomp in the
-// Dirichlet numbering; b_out then receives b - Ad xd (src/problems.jl:439-453)
-static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out) {
+// Dirichlet numbering; b_out then receives b - Ad xd (src/problems.jl:439-453).
+// hc (optional, scalar matrices): host CSR outputs whose pattern is being
+// downloaded on the copy stream (pat_down: its event); the values are then
+// scattered in row chunks, each chunk's download overlapping the next chunk's
+// scatter (*values_done set when that happened).
+static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, const HostCsr* hc = nullptr,
+                      cudaEvent_t pat_down = nullptr, bool* values_done = nullptr) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   int64_t nc = sp->mesh->ncells;
@@ -1665,7 +1680,33 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out) 
     if (s == GT_OK) s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
     mark(ctx, "elements");
     if (s == GT_OK) s = alloc_values(A);
-    if (s == GT_OK) s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr);
+    if (s == GT_OK && hc && pat_down && A->bs == 1 && values_done) {
+      // the host row pointers (downloaded meanwhile) give each chunk's range
+      cudaError_t e = cudaEventSynchronize(pat_down);
+      if (e != cudaSuccess) s = check_cuda(ctx, e, "pattern download");
+      constexpr int NCH = 4;
+      for (int k = 0; k < NCH && s == GT_OK; k++) {
+        const int64_t r0 = A->nbrows * k / NCH, r1 = A->nbrows * (k + 1) / NCH;
+        s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr, r0, r1);
+        const int64_t o0 = hc->rowptr[r0], o1 = hc->rowptr[r1];
+        cudaEvent_t ev = event_get(ctx);
+        if (s == GT_OK && !ev) s = set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
+        if (s == GT_OK && o1 > o0) {
+          cudaEventRecord(ev, ctx->stream);
+          cudaStreamWaitEvent(ctx->side, ev, 0);
+          if (hc->v64 && A->val64)
+            cudaMemcpyAsync(hc->v64 + o0, A->val64 + o0, sizeof(double) * (o1 - o0), cudaMemcpyDefault, ctx->side);
+          if (hc->v32 && A->val32)
+            cudaMemcpyAsync(hc->v32 + o0, A->val32 + o0, sizeof(float) * (o1 - o0), cudaMemcpyDefault, ctx->side);
+          cudaError_t ce = cudaGetLastError();
+          if (ce != cudaSuccess) s = check_cuda(ctx, ce, "values download");
+        }
+        event_put(ctx, ev);
+      }
+      if (s == GT_OK) *values_done = true;
+    } else if (s == GT_OK) {
+      s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr);
+    }
     mark(ctx, "scatter");
   }
   // host b: the copy is queued here; the caller's device_status() call
@@ -1709,15 +1750,6 @@ static void matrix_release(gt_matrix* A) {
 }
 
 extern "C" {
-
-// host CSR outputs filled by the assembly call itself (scalar entries)
-struct HostCsr {
-  int64_t* rowptr;
-  int32_t* colind;
-  double* v64;
-  float* v32;
-  int64_t capacity;  // entries colind / values can hold
-};
 
 static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double nu, int precision, const double* f,
                        const double* source_coef, const double* xd, double* b, gt_matrix** out,
@@ -1791,8 +1823,9 @@ static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double n
     if (s == GT_OK) cudaEventRecord(side_done, ctx->side);
     event_put(ctx, pat);
   }
-  if (s == GT_OK) s = numeric_in(A, form, in, nu, b);
-  if (s == GT_OK && hc) {
+  bool values_done = false;
+  if (s == GT_OK) s = numeric_in(A, form, in, nu, b, hc, side_done, &values_done);
+  if (s == GT_OK && hc && !values_done) {
     if (bs == 1) {
       if (hc->v64 && A->val64 && nnz > 0) s = copy_out(ctx, hc->v64, A->val64, nnz);
       if (s == GT_OK && hc->v32 && A->val32 && nnz > 0) s = copy_out(ctx, hc->v32, A->val32, nnz);
@@ -1802,8 +1835,8 @@ static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double n
   }
   if (s == GT_OK) s = device_status(ctx, "assemble_matrix");  // synchronises the stream
   if (side_done) {
-    cudaError_t e = cudaEventSynchronize(side_done);
-    if (s == GT_OK && e != cudaSuccess) s = check_cuda(ctx, e, "pattern download");
+    cudaError_t e = cudaStreamSynchronize(ctx->side);  // pattern and chunked value downloads
+    if (s == GT_OK && e != cudaSuccess) s = check_cuda(ctx, e, "host CSR download");
     event_put(ctx, side_done);
   }
   if (s != GT_OK) {

@@ -210,9 +210,10 @@ int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc,
 int build_pattern(Matrix* A);
 int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision,
                      const double* f, const double* d_scoef, void* Ke, double* be, int want_matrix);
-// be/bvec (optional): element vectors and the load vector summed in the same pass
+// be/bvec (optional): element vectors and the load vector summed in the same
+// pass; xd: Dirichlet values (lift); [r0, r1): block rows (r1 < 0: all)
 int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be = nullptr,
-                   double* bvec = nullptr, const double* xd = nullptr);
+                   double* bvec = nullptr, const double* xd = nullptr, int64_t r0 = 0, int64_t r1 = -1);
 int tabulation_doubles(const Space* sp);
 int compute_elements_with_tab(const Space* sp, int form, const double* d_coef, double nu, int precision,
                               double* tab, void* Ke);
