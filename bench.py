@@ -396,8 +396,11 @@ def main():
     m, kappa = workload(n)
     ctx = GT.Context(local)
     # one stream for torch and the library: the CUDA events below bracket
-    # exactly the library's work
-    stream = torch.cuda.Stream()
+    # exactly the library's work.  Above the default priority, like the
+    # library's own main stream, so that the element kernels the library
+    # queues on its lowest-priority stream fill the gaps of the sparsity
+    # kernels instead of holding the SMs ahead of them
+    stream = torch.cuda.Stream(priority=-1)
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     V = GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m), ctx=ctx)

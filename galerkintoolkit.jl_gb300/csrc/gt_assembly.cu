@@ -144,19 +144,32 @@ static int get_tab(Ctx* ctx, int ctype, int order, double** tab, TabLayout* L) {
 // ---------------------------------------------------------------------------
 // 1. incidence
 // ---------------------------------------------------------------------------
-__global__ void k_inc_count(const int32_t* cnd, int64_t n, int32_t* cnt) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    int32_t d = cnd[i];
-    if (d > 0) atomicAdd(&cnt[d - 1], 1);
+// count the incidences of every free node and give each (cell, node) entry
+// its rank among the entries of its node.  Entries of one warp that name the
+// same node (consecutive cells share nodes) take one atomic for the group
+// (the atomics, one L2 round trip each, bound this pass).  Ranks follow the
+// atomics' order; the sparsity pass sorts every row's list afterwards.
+__global__ void k_inc_count(const int32_t* __restrict__ cnd, int64_t n, int32_t* __restrict__ cnt,
+                            int32_t* __restrict__ rank) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // warp-uniform loop: every lane takes part in the match below
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
+    const int64_t i = i0 + lane;
+    const int32_t d = i < n ? __ldg(cnd + i) : 0;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    int32_t base = 0;
+    if (lane == leader && d > 0) base = atomicAdd(&cnt[d - 1], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (d > 0) rank[i] = base + __popc(peers & ((1u << lane) - 1u));
   }
 }
-__global__ void k_inc_fill(const int32_t* cnd, int64_t n, const int64_t* ptr, int32_t* cursor, int32_t* inc) {
+__global__ void k_inc_fill(const int32_t* __restrict__ cnd, int64_t n, const int64_t* __restrict__ ptr,
+                           const int32_t* __restrict__ rank, int32_t* __restrict__ inc) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    int32_t d = cnd[i];
-    if (d > 0) {
-      int32_t p = atomicAdd(&cursor[d - 1], 1);
-      inc[ptr[d - 1] + p] = (int32_t)i;  // cell * nn + local node
-    }
+    const int32_t d = __ldg(cnd + i);
+    if (d > 0) inc[__ldg(ptr + d - 1) + __ldg(rank + i)] = (int32_t)i;  // cell * nn + local node
   }
 }
 // sort each row's incidences ascending (= by cell): one warp per row,
@@ -199,17 +212,16 @@ static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out);
 int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc, bool sort) {
   cudaStream_t st = ctx->stream;
   int64_t nrows = sp->nfree_nodes, n = sp->mesh->ncells * sp->nn;
-  int32_t *cnt = nullptr, *cursor = nullptr;
+  int32_t *cnt = nullptr, *rank = nullptr;
   GT_TRY(dalloc(ctx, &cnt, nrows + 1));
-  GT_TRY(dalloc(ctx, &cursor, nrows + 1));
+  GT_TRY(dalloc(ctx, &rank, n > 0 ? n : 1));
   GT_TRY(dalloc(ctx, inc_ptr, nrows + 1));
   GT_TRY(dalloc(ctx, inc, n));  // upper bound: every (cell, node) free
   GT_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), st));
-  GT_CUDA(ctx, cudaMemsetAsync(cursor, 0, sizeof(int32_t) * (nrows + 1), st));
-  k_inc_count<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, cnt);
+  if (n > 0) k_inc_count<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, cnt, rank);
   GT_LAUNCH(ctx, "k_inc_count");
   GT_TRY(exclusive_scan_i64(ctx, cnt, *inc_ptr, nrows));
-  k_inc_fill<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, *inc_ptr, cursor, *inc);
+  if (n > 0) k_inc_fill<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, *inc_ptr, rank, *inc);
   GT_LAUNCH(ctx, "k_inc_fill");
   *ninc = -1;  // not read back: the sparsity pass knows the row extents
   if (sort) {
@@ -226,35 +238,46 @@ int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc,
     GT_LAUNCH(ctx, "k_inc_sort");
   }
   dfree(ctx, cnt);
-  dfree(ctx, cursor);
+  dfree(ctx, rank);
   return GT_OK;
 }
 
 // ---------------------------------------------------------------------------
 // 2. pattern
 // ---------------------------------------------------------------------------
-// ascending bitonic sort of 32 keys held one per lane (register shuffles)
-__device__ __forceinline__ int32_t warp_sort32(int32_t v, int lane) {
+// ascending bitonic sort of NK (16 or 32) keys held one per lane (register
+// shuffles).  In stage (k = 2^a, j = 2^b) a lane keeps the larger key iff
+// bits a and b of its lane index differ, i.e. bit b of lane ^ (lane >> (a-b));
+// the shifted indices are formed once, so a stage is a shuffle, a bit
+// test and a min/max.  With NK = 16 both half-warps sort their own lanes
+// (lanes 0..15 ascending).
+template <int NK>
+__device__ __forceinline__ int32_t warp_sort(int32_t v, int lane) {
+  const int x[6] = {0, lane ^ (lane >> 1), lane ^ (lane >> 2), lane ^ (lane >> 3), lane ^ (lane >> 4), lane};
 #pragma unroll
-  for (int k = 2; k <= 32; k <<= 1)
+  for (int a = 1; (1 << a) <= NK; a++)
 #pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      int32_t o = __shfl_xor_sync(0xffffffffu, v, j);
-      bool up = (lane & k) == 0, lower = (lane & j) == 0;
-      v = (lower == up) ? min(v, o) : max(v, o);
+    for (int b = a - 1; b >= 0; b--) {
+      const int32_t o = __shfl_xor_sync(0xffffffffu, v, 1 << b);
+      v = (x[a - b] >> b) & 1 ? max(v, o) : min(v, o);
     }
   return v;
 }
 
 // Per block row: the sorted union of the free node DOFs of its cells.
-// One warp per row.  Candidates go into a shared-memory hash set (atomicCAS
-// on 32-bit keys, linear probing).  The count pass counts the distinct keys
-// and, for rows of at most S columns, compacts and sorts them (register
-// shuffles for <= 32 keys, shared-memory bitonic sort above) into the row's
-// slot of S entries; the fill pass copies those slots and runs the hash
-// again only for longer rows.  The count pass also sorts the row's
-// incidence list in place (ascending = by cell), which fixes the scatter's
-// summation order.
+// One warp per row.  The row's incidences are sorted ascending (= by cell;
+// the count pass writes them back, which fixes the scatter's summation
+// order) and held one per lane.  The row's own DOF (block row r is node
+// r + 1, present in every incident cell) goes in first; the other nodes of
+// the incident cells follow in rounds of 32 candidates.  In a round, lanes
+// holding the same key elect one leader (match.any), so a shared-memory hash
+// set (linear probing, empty = -1) sees each key at most once per round and
+// its compare-and-swaps never serialise on one address; a leader that
+// inserted appends its key to the row's list (ballot + prefix count).  The
+// count pass counts the distinct keys and, for rows of at most S columns,
+// sorts them (register shuffles for <= 32 keys, shared-memory bitonic sort
+// above) into the row's slot of S entries; the fill pass copies those slots
+// and runs the hash again only for longer rows.
 template <int NN, int S, bool FILL>
 __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc_ptr, int32_t* __restrict__ inc,
                                                  const int32_t* __restrict__ cnd, int64_t nrows, int hcap, int icap,
@@ -262,10 +285,11 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
                                                  int32_t* __restrict__ colind, int32_t* __restrict__ slots,
                                                  uint8_t* __restrict__ small, int32_t* maxrow, uint32_t* err) {
   extern __shared__ int32_t s_buf[];
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int32_t* tab = s_buf + w * (hcap + icap);  // hash set
-  int32_t* ibuf = tab + hcap;                 // the row's incidences, later the compacted keys
-  int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t* tab = s_buf + (size_t)w * (hcap + 2 * icap);  // hash set
+  int32_t* ibuf = tab + hcap;                            // sorted incidences of rows with more than 32
+  int32_t* keys = ibuf + icap;                           // the row's distinct columns, insertion order
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + w;
   if (r >= nrows) return;
   if (FILL && small[r]) {
     // the count pass already wrote this row's sorted columns to its slot
@@ -274,83 +298,103 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
     for (int i = lane; i < n; i += 32) colind[o + i] = slots[r * S + i];
     return;
   }
-  int64_t ib = inc_ptr[r];
-  int ninc = (int)(inc_ptr[r + 1] - ib);
-  int ncand = ninc * NN;
+  const int64_t ib = inc_ptr[r];
+  const int ninc = (int)(inc_ptr[r + 1] - ib);
+  const int ncand = ninc * NN;
   if (ncand + (ncand >> 2) > hcap || ncand > icap) {
     if (lane == 0) { atomicOr(err, DEV_ERR_ROW_CAP); if (!FILL) { rowcnt[r] = 0; small[r] = 1; } }
     return;
   }
-  for (int i = lane; i < hcap; i += 32) tab[i] = -1;
-  if (!FILL) {
-    if (ninc <= 32) {
-      int32_t v = warp_sort32(lane < ninc ? inc[ib + lane] : INT_MAX, lane);
-      if (lane < ninc) {
-        inc[ib + lane] = v;
-        ibuf[lane] = v;
-      }
+  for (int i = lane; i < (hcap >> 2); i += 32) reinterpret_cast<int4*>(tab)[i] = make_int4(-1, -1, -1, -1);
+  int32_t myinc = INT_MAX;  // lane k: the k-th incidence (rows of at most 32)
+  if (ninc <= 32) {
+    const int32_t u = lane < ninc ? inc[ib + lane] : INT_MAX;
+    if (FILL) {
+      myinc = u;  // sorted by the count pass
     } else {
-      int P2 = 32;
-      while (P2 < ninc) P2 <<= 1;
-      for (int i = lane; i < P2; i += 32) ibuf[i] = i < ninc ? inc[ib + i] : INT_MAX;
-      __syncwarp();
-      warp_bitonic_sort(ibuf, P2, lane);
-      for (int i = lane; i < ninc; i += 32) inc[ib + i] = ibuf[i];
+      myinc = ninc <= 16 ? warp_sort<16>(u, lane) : warp_sort<32>(u, lane);
+      if (lane < ninc) inc[ib + lane] = myinc;
     }
+  } else if (!FILL) {
+    int P2 = 64;
+    while (P2 < ninc) P2 <<= 1;
+    for (int i = lane; i < P2; i += 32) ibuf[i] = i < ninc ? inc[ib + i] : INT_MAX;
+    __syncwarp();
+    warp_bitonic_sort(ibuf, P2, lane);
+    for (int i = lane; i < ninc; i += 32) inc[ib + i] = ibuf[i];
   } else {
     for (int i = lane; i < ninc; i += 32) ibuf[i] = inc[ib + i];
   }
   __syncwarp();
-  int mine = 0;  // distinct keys this lane inserted
   const unsigned hmask = (unsigned)hcap - 1u;
-  for (int i = lane; i < ncand; i += 32) {
-    int k = i / NN, b = i - k * NN;
-    int32_t c = ibuf[k] / NN;
-    int32_t d = cnd[(int64_t)c * NN + b];
-    if (d <= 0) continue;
-    int32_t key = d - 1;
-    unsigned h = ((unsigned)key * 2654435761u) & hmask;
-    for (;;) {
-      int32_t old = atomicCAS(&tab[h], -1, key);
-      if (old == -1) { mine++; break; }
-      if (old == key) break;
-      h = (h + 1) & hmask;
+  const unsigned lt = (1u << lane) - 1u;
+  if (lane == 0 && ninc > 0) {
+    tab[((unsigned)r * 2654435761u) & hmask] = (int32_t)r;
+    keys[0] = (int32_t)r;
+  }
+  int total = ninc > 0 ? 1 : 0;
+  __syncwarp();
+  bool lost = false;  // a probe sequence ran through the whole table (cannot happen: a slot stays free)
+  const int nround = (ncand + 31) >> 5;
+  for (int t = 0; t < nround; t++) {
+    const int i = t * 32 + lane;
+    const int k = i / NN, b = i - k * NN;
+    int32_t e = 0;
+    if (ninc <= 32) e = __shfl_sync(0xffffffffu, myinc, k & 31);
+    else if (i < ncand) e = ibuf[k];
+    int32_t key = -1;
+    if (i < ncand) {
+      const int32_t c = e / NN;
+      if (b != e - c * NN) {
+        const int32_t d = __ldg(cnd + (int64_t)c * NN + b);
+        if (d > 0) key = d - 1;
+      }
     }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    bool ins = false;
+    if (key >= 0 && (peers & lt) == 0) {
+      unsigned h = ((unsigned)key * 2654435761u) & hmask;
+      bool done = false;
+      for (unsigned probe = 0; probe <= hmask; probe++) {
+        const int32_t old = atomicCAS(&tab[h], -1, key);
+        if (old == -1) { ins = true; done = true; break; }
+        if (old == key) { done = true; break; }
+        h = (h + 1) & hmask;
+      }
+      lost |= !done;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, ins);
+    if (ins) keys[total + __popc(m & lt)] = key;
+    total += __popc(m);
+  }
+  if (__any_sync(0xffffffffu, lost)) {
+    if (lane == 0) { atomicOr(err, DEV_ERR_HASH_FULL); if (!FILL) { rowcnt[r] = 0; small[r] = 1; } }
+    return;
   }
   __syncwarp();
-  int total = mine;
-  for (int o = 16; o; o >>= 1) total += __shfl_xor_sync(0xffffffffu, total, o);
   if (!FILL) {
     if (lane == 0) {
       rowcnt[r] = total;
-      atomicMax(maxrow, total);
+      // the running maximum changes rarely: skip the same-address atomic
+      // (one per row otherwise, serialised in one L2 slice) when not above it
+      if (total > __ldcg(maxrow)) atomicMax(maxrow, total);
       small[r] = total <= S;
     }
     if (total > S) return;
   }
-  // compact the distinct keys (icap >= P: the host keeps icap >= hcap / 2 >=
-  // ncand >= total), sort them, and write them to the row's slot (count
-  // pass, rows of at most S columns) or to colind (fill pass)
-  int P = 32;
-  while (P < total) P <<= 1;
-  int32_t* keys = ibuf;
-  int base = 0;
-  for (int s0 = 0; s0 < hcap; s0 += 32) {
-    int32_t v = tab[s0 + lane];
-    bool keep = v >= 0;
-    unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (keep) keys[base + __popc(m & ((1u << lane) - 1u))] = v;
-    base += __popc(m);
-  }
-  __syncwarp();
-  if (P == 32) {
-    int32_t v = warp_sort32(lane < total ? keys[lane] : INT_MAX, lane);
+  // sort the distinct keys (total <= ncand <= icap) and write them to the
+  // row's slot (count pass) or to colind (fill pass)
+  if (total <= 32) {
+    const int32_t u = lane < total ? keys[lane] : INT_MAX;
+    const int32_t v = total <= 16 ? warp_sort<16>(u, lane) : warp_sort<32>(u, lane);
     if (lane < total) {
       if (FILL) colind[rowptr[r] + lane] = v;
       else slots[r * S + lane] = v;
     }
     return;
   }
+  int P = 64;
+  while (P < total) P <<= 1;
   for (int i = total + lane; i < P; i += 32) keys[i] = INT_MAX;
   __syncwarp();
   warp_bitonic_sort(keys, P, lane);
@@ -428,7 +472,7 @@ static int launch_pattern(Matrix* A, int maxinc) {
   while (icap < ncand_max) icap <<= 1;
   if (hcap > 8192) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells for the sparsity kernel");
   int warps = hcap >= 4096 ? 2 : (hcap >= 2048 ? 4 : 8);
-  size_t smem = (size_t)warps * (hcap + icap) * sizeof(int32_t);
+  size_t smem = (size_t)warps * (hcap + 2 * icap) * sizeof(int32_t);
   cudaFuncSetAttribute(k_pattern<NN, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaFuncSetAttribute(k_pattern<NN, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int32_t *rowcnt = nullptr, *dmax = nullptr, *slots = nullptr;
@@ -451,7 +495,10 @@ static int launch_pattern(Matrix* A, int maxinc) {
   GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[1], dmax, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   uint32_t bits = 0;
   GT_TRY(take_device_error(ctx, &bits));  // synchronises
-  if (bits) return set_error(ctx, GT_ERR_INVALID, "sparsity: row capacity exceeded");
+  // bits of kernels on other streams (element checks) go back for the next take
+  const uint32_t own = DEV_ERR_ROW_CAP | DEV_ERR_HASH_FULL;
+  ctx->held_err |= bits & ~own;
+  if (bits & own) return set_error(ctx, GT_ERR_INVALID, "sparsity: row capacity exceeded");
   A->bnnz = ctx->h_scratch[0];
   int32_t mr = 0;
   memcpy(&mr, &ctx->h_scratch[1], sizeof(int32_t));
@@ -749,69 +796,70 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
   const double* s_load = consts + 1;
   const double* s_mass = consts + 5;
   const double s_wsum = __ldg(consts);
-  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
-  int4 nd = *reinterpret_cast<const int4*>(cell_nodes + 4 * c);
-  const double* p0 = coords + 3 * (int64_t)nd.x;
-  const double* p1 = coords + 3 * (int64_t)nd.y;
-  const double* p2 = coords + 3 * (int64_t)nd.z;
-  const double* p3 = coords + 3 * (int64_t)nd.w;
-  double x0 = p0[0], y0 = p0[1], z0 = p0[2];
-  // J columns
-  double a0 = p1[0] - x0, a1 = p1[1] - y0, a2 = p1[2] - z0;
-  double b0 = p2[0] - x0, b1 = p2[1] - y0, b2 = p2[2] - z0;
-  double d0 = p3[0] - x0, d1 = p3[1] - y0, d2 = p3[2] - z0;
-  // J = [[a0 b0 d0],[a1 b1 d1],[a2 b2 d2]]; cofactor columns C[:,j]
-  double c10 = b1 * d2 - b2 * d1, c11 = b2 * d0 - b0 * d2, c12 = b0 * d1 - b1 * d0;  // column 0 (row of J^-1 #0)
-  double c20 = d1 * a2 - d2 * a1, c21 = d2 * a0 - d0 * a2, c22 = d0 * a1 - d1 * a0;  // column 1
-  double c30 = a1 * b2 - a2 * b1, c31 = a2 * b0 - a0 * b2, c32 = a0 * b1 - a1 * b0;  // column 2
-  double det = a0 * c10 + a1 * c11 + a2 * c12;
-  if (!(det != 0.0)) atomicOr(err, DEV_ERR_DEGENERATE);
-  double adet = fabs(det);
-  double cf = coef ? coef[c] : 1.0;
-  if (want_matrix) {
-    T k[10];
-    if (FORM == GT_LAPLACE) {
-      // the six entries among vertices 1..3 from the cofactor columns; the
-      // entries of vertex 0 follow from c_0 = -(c_1 + c_2 + c_3), i.e. from
-      // the zero row sums of the Laplacian (8 additions instead of 4 dot
-      // products: the kernel is bound by the FP64 issue rate)
-      T g[3][3];
-      g[0][0] = (T)c10; g[0][1] = (T)c11; g[0][2] = (T)c12;
-      g[1][0] = (T)c20; g[1][1] = (T)c21; g[1][2] = (T)c22;
-      g[2][0] = (T)c30; g[2][1] = (T)c31; g[2][2] = (T)c32;
-      T s = (T)(cf * s_wsum / adet);
-      T k11 = s * (g[0][0] * g[0][0] + g[0][1] * g[0][1] + g[0][2] * g[0][2]);
-      T k12 = s * (g[0][0] * g[1][0] + g[0][1] * g[1][1] + g[0][2] * g[1][2]);
-      T k13 = s * (g[0][0] * g[2][0] + g[0][1] * g[2][1] + g[0][2] * g[2][2]);
-      T k22 = s * (g[1][0] * g[1][0] + g[1][1] * g[1][1] + g[1][2] * g[1][2]);
-      T k23 = s * (g[1][0] * g[2][0] + g[1][1] * g[2][1] + g[1][2] * g[2][2]);
-      T k33 = s * (g[2][0] * g[2][0] + g[2][1] * g[2][1] + g[2][2] * g[2][2]);
-      T k01 = -(k11 + k12 + k13), k02 = -(k12 + k22 + k23), k03 = -(k13 + k23 + k33);
-      T k00 = -(k01 + k02 + k03);
-      k[0] = k00; k[1] = k01; k[2] = k02; k[3] = k03;
-      k[4] = k11; k[5] = k12; k[6] = k13;
-      k[7] = k22; k[8] = k23;
-      k[9] = k33;
-    } else {
-      T s = (T)(cf * adet);
-      int e = 0;
-#pragma unroll
+  // grid-stride over the cells (one thread per cell)
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
+    int4 nd = *reinterpret_cast<const int4*>(cell_nodes + 4 * c);
+    const double* p0 = coords + 3 * (int64_t)nd.x;
+    const double* p1 = coords + 3 * (int64_t)nd.y;
+    const double* p2 = coords + 3 * (int64_t)nd.z;
+    const double* p3 = coords + 3 * (int64_t)nd.w;
+    double x0 = p0[0], y0 = p0[1], z0 = p0[2];
+    // J columns
+    double a0 = p1[0] - x0, a1 = p1[1] - y0, a2 = p1[2] - z0;
+    double b0 = p2[0] - x0, b1 = p2[1] - y0, b2 = p2[2] - z0;
+    double d0 = p3[0] - x0, d1 = p3[1] - y0, d2 = p3[2] - z0;
+    // J = [[a0 b0 d0],[a1 b1 d1],[a2 b2 d2]]; cofactor columns C[:,j]
+    double c10 = b1 * d2 - b2 * d1, c11 = b2 * d0 - b0 * d2, c12 = b0 * d1 - b1 * d0;  // column 0 (row of J^-1 #0)
+    double c20 = d1 * a2 - d2 * a1, c21 = d2 * a0 - d0 * a2, c22 = d0 * a1 - d1 * a0;  // column 1
+    double c30 = a1 * b2 - a2 * b1, c31 = a2 * b0 - a0 * b2, c32 = a0 * b1 - a1 * b0;  // column 2
+    double det = a0 * c10 + a1 * c11 + a2 * c12;
+    if (!(det != 0.0)) atomicOr(err, DEV_ERR_DEGENERATE);
+    double adet = fabs(det);
+    double cf = coef ? coef[c] : 1.0;
+    if (want_matrix) {
+      T k[10];
+      if (FORM == GT_LAPLACE) {
+        // the six entries among vertices 1..3 from the cofactor columns; the
+        // entries of vertex 0 follow from c_0 = -(c_1 + c_2 + c_3), i.e. from
+        // the zero row sums of the Laplacian (8 additions instead of 4 dot
+        // products: the kernel is bound by the FP64 issue rate)
+        T g[3][3];
+        g[0][0] = (T)c10; g[0][1] = (T)c11; g[0][2] = (T)c12;
+        g[1][0] = (T)c20; g[1][1] = (T)c21; g[1][2] = (T)c22;
+        g[2][0] = (T)c30; g[2][1] = (T)c31; g[2][2] = (T)c32;
+        T s = (T)(cf * s_wsum / adet);
+        T k11 = s * (g[0][0] * g[0][0] + g[0][1] * g[0][1] + g[0][2] * g[0][2]);
+        T k12 = s * (g[0][0] * g[1][0] + g[0][1] * g[1][1] + g[0][2] * g[1][2]);
+        T k13 = s * (g[0][0] * g[2][0] + g[0][1] * g[2][1] + g[0][2] * g[2][2]);
+        T k22 = s * (g[1][0] * g[1][0] + g[1][1] * g[1][1] + g[1][2] * g[1][2]);
+        T k23 = s * (g[1][0] * g[2][0] + g[1][1] * g[2][1] + g[1][2] * g[2][2]);
+        T k33 = s * (g[2][0] * g[2][0] + g[2][1] * g[2][1] + g[2][2] * g[2][2]);
+        T k01 = -(k11 + k12 + k13), k02 = -(k12 + k22 + k23), k03 = -(k13 + k23 + k33);
+        T k00 = -(k01 + k02 + k03);
+        k[0] = k00; k[1] = k01; k[2] = k02; k[3] = k03;
+        k[4] = k11; k[5] = k12; k[6] = k13;
+        k[7] = k22; k[8] = k23;
+        k[9] = k33;
+      } else {
+        T s = (T)(cf * adet);
+        int e = 0;
+  #pragma unroll
+        for (int n = 0; n < 4; n++)
+  #pragma unroll
+          for (int m = n; m < 4; m++) k[e++] = s * (T)__ldg(s_mass + n * 4 + m);
+      }
+      T* K = Ke + 16 * c;
+      const int up[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
+  #pragma unroll
       for (int n = 0; n < 4; n++)
-#pragma unroll
-        for (int m = n; m < 4; m++) k[e++] = s * (T)__ldg(s_mass + n * 4 + m);
+  #pragma unroll
+        for (int m = 0; m < 4; m++) K[n * 4 + m] = k[up[n][m]];
     }
-    T* K = Ke + 16 * c;
-    const int up[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
-#pragma unroll
-    for (int n = 0; n < 4; n++)
-#pragma unroll
-      for (int m = 0; m < 4; m++) K[n * 4 + m] = k[up[n][m]];
-  }
-  if (be) {
-    double sc = (scoef ? scoef[c] : 1.0) * fsrc[0] * adet;
-#pragma unroll
-    for (int n = 0; n < 4; n++) be[4 * c + n] = sc * __ldg(s_load + n);
+    if (be) {
+      double sc = (scoef ? scoef[c] : 1.0) * fsrc[0] * adet;
+  #pragma unroll
+      for (int n = 0; n < 4; n++) be[4 * c + n] = sc * __ldg(s_load + n);
+    }
   }
 }
 
@@ -825,11 +873,12 @@ static int elements_T(const Space* sp, int form, const double* coef, double nu, 
     int64_t nc = sp->mesh->ncells;
     double* consts = const_cast<double*>(tab) + L.off_k;  // inside the tabulation buffer: no allocation
     k_p1_consts<<<GT_KC(ctx, 1), 32, 0, ctx->stream>>>(tab, L, consts);
+    const int grid = grid_for(nc, 256);
     if (form == GT_LAPLACE)
-      k_elements_p1<GT_LAPLACE, T><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
+      k_elements_p1<GT_LAPLACE, T><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
           sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
     else
-      k_elements_p1<GT_MASS, T><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
+      k_elements_p1<GT_MASS, T><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
           sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
     GT_LAUNCH(ctx, "k_elements_p1");
     return GT_OK;
@@ -843,7 +892,7 @@ static int elements_T(const Space* sp, int form, const double* coef, double nu, 
 }
 
 int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision, const double* f,
-                     const double* d_scoef, void* Ke, double* be, int want_matrix) {
+                     const double* d_scoef, void* Ke, double* be, int want_matrix, double** keep_tab) {
   Ctx* ctx = ctx_of(sp);
   if (form != GT_LAPLACE && form != GT_MASS && form != GT_ELASTICITY)
     return set_error(ctx, GT_ERR_UNSUPPORTED, "weak form not supported (Laplacian, mass, linear elasticity only)");
@@ -857,7 +906,8 @@ int compute_elements(const Space* sp, int form, const double* d_coef, double nu,
     s = elements_T<float>(sp, form, d_coef, nu, tab, L, (float*)Ke, be, f, d_scoef, want_matrix);
   else
     s = elements_T<double>(sp, form, d_coef, nu, tab, L, (double*)Ke, be, f, d_scoef, want_matrix);
-  dfree(ctx, tab);
+  if (keep_tab) *keep_tab = tab;
+  else dfree(ctx, tab);
   return s;
 }
 
@@ -1592,6 +1642,10 @@ struct DevIn {
       ev = nullptr;
     }
   }
+  // orders stream s after the upload (which stays pending for the main stream)
+  void wait_on(cudaStream_t s) const {
+    if (ev) cudaStreamWaitEvent(s, ev, 0);
+  }
   ~DevIn() {
     wait();
     if (owned) dfree(ctx, owned);
@@ -1618,7 +1672,83 @@ struct NumIn {
     scoef.wait();
     xd.wait();
   }
+  void wait_on(cudaStream_t s) const {
+    coef.wait_on(s);
+    f.wait_on(s);
+    scoef.wait_on(s);
+    xd.wait_on(s);
+  }
 };
+
+// Element matrices (and vectors) launched on the auxiliary compute stream
+// before the sparsity kernels; numeric_in joins the streams before the
+// scatter.  The auxiliary stream has the lowest priority, so its blocks fill
+// the SMs the sparsity kernels leave idle (their host round trips, their
+// tails) rather than run beside them: measured on GB300, FP64-bound blocks
+// co-resident with the sparsity kernels slow those 2.5x (an FP64 warp
+// instruction holds its SM sub-partition's dispatch for many cycles), while
+// the sparsity result is what the host downloads first.  Taken for the cells
+// without the factored (Kronecker) path -- tetrahedra -- and not while phases
+// are being timed (the phase marks time each kernel alone).  All of the
+// stage's device blocks are held until the join: a block freed earlier could
+// be handed to main-stream work while the auxiliary kernels still use it.
+struct EarlyElems {
+  bool active = false;
+  void* Ke = nullptr;
+  double* be = nullptr;
+  double* tab = nullptr;
+  cudaEvent_t done = nullptr;
+};
+
+static int elements_early(const Space* sp, int form, const NumIn& in, double nu, int precision, bool want_b,
+                          EarlyElems* E) {
+  Ctx* ctx = ctx_of(sp);
+  if (ctx->prof || !ctx->overlap || !ctx->aux || sp->mesh->ctype != GT_TET4) return GT_OK;
+  if (form != GT_LAPLACE && form != GT_MASS && form != GT_ELASTICITY) return GT_OK;  // reported by numeric_in
+  const int64_t nc = sp->mesh->ncells;
+  const int kprec = precision == GT_FP32 ? GT_FP32 : GT_FP64;
+  const size_t esz = kprec == GT_FP32 ? sizeof(float) : sizeof(double);
+  cudaEvent_t start = event_get(ctx);
+  E->done = event_get(ctx);
+  if (!start || !E->done) return set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
+  // the auxiliary stream starts after all work queued so far (mesh, space,
+  // and every block the pool may hand out below) and after the uploads
+  GT_CUDA(ctx, cudaEventRecord(start, ctx->stream));
+  GT_CUDA(ctx, cudaStreamWaitEvent(ctx->aux, start, 0));
+  event_put(ctx, start);
+  in.wait_on(ctx->aux);
+  mesh_wait_coords_on(sp->mesh, ctx->aux);
+  if (want_b) GT_TRY(dalloc(ctx, &E->be, nc * sp->nloc));
+  GT_TRY(dalloc(ctx, (unsigned char**)&E->Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz)));
+  cudaStream_t main_stream = ctx->stream;
+  ctx->stream = ctx->aux;
+  int s = compute_elements(sp, form, in.coef.p, nu, precision, in.f.p, in.scoef.p, E->Ke, E->be, 1, &E->tab);
+  if (s == GT_OK && cudaEventRecord(E->done, ctx->aux) != cudaSuccess) s = check_cuda(ctx, cudaGetLastError(), "event");
+  ctx->stream = main_stream;
+  if (s != GT_OK) {
+    // nothing of the stage may be reused before the auxiliary stream drains
+    cudaStreamSynchronize(ctx->aux);
+    if (E->tab) dfree(ctx, E->tab);
+    if (E->Ke) pool_free(ctx, E->Ke);
+    if (E->be) dfree(ctx, E->be);
+    event_put(ctx, E->done);
+    *E = EarlyElems{};
+    return s;
+  }
+  E->active = true;
+  return GT_OK;
+}
+
+// releases a stage that numeric_in did not take over (error paths)
+static void early_release(Ctx* ctx, EarlyElems* E) {
+  if (!E->active) return;
+  cudaStreamSynchronize(ctx->aux);
+  dfree(ctx, E->tab);
+  pool_free(ctx, E->Ke);
+  if (E->be) dfree(ctx, E->be);
+  event_put(ctx, E->done);
+  *E = EarlyElems{};
+}
 
 static bool is_device_ptr(const void* p) {
   cudaPointerAttributes at{};
@@ -1654,7 +1784,7 @@ struct HostCsr {
 // scattered in row chunks, each chunk's download overlapping the next chunk's
 // scatter (*values_done set when that happened).
 static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, const HostCsr* hc = nullptr,
-                      cudaEvent_t pat_down = nullptr, bool* values_done = nullptr) {
+                      cudaEvent_t pat_down = nullptr, bool* values_done = nullptr, EarlyElems* early = nullptr) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   int64_t nc = sp->mesh->ncells;
@@ -1665,7 +1795,18 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
   size_t esz = kprec == GT_FP32 ? sizeof(float) : sizeof(double);
   void* Ke = nullptr;
   double* be = nullptr;
-  if (b_out) GT_TRY(dalloc(ctx, &be, nc * sp->nloc));
+  const bool pre = early && early->active;
+  if (pre) {
+    // element stage already queued on the auxiliary stream: join it
+    GT_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, early->done, 0));
+    event_put(ctx, early->done);
+    Ke = early->Ke;
+    be = early->be;
+    dfree(ctx, early->tab);  // later users of the block are ordered after the join
+    *early = EarlyElems{};
+  } else if (b_out) {
+    GT_TRY(dalloc(ctx, &be, nc * sp->nloc));
+  }
   const bool dev = b_out && is_device_ptr(b_out);
   double* bd = b_out;
   const int64_t nb = sp->nfree_nodes * sp->ncomp;
@@ -1673,36 +1814,49 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
   int used_kron = 0;
   // the load vector (and the Dirichlet lift) is summed inside the matrix
   // scatter, over the same incidences
-  int s = kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr,
-                       &used_kron);
+  int s = pre ? GT_OK
+              : kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr,
+                             &used_kron);
   if (s == GT_OK && !used_kron) {
-    s = dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz));
-    if (s == GT_OK) s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
+    if (!pre) {
+      s = dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz));
+      if (s == GT_OK) s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
+    }
     mark(ctx, "elements");
     if (s == GT_OK) s = alloc_values(A);
     if (s == GT_OK && hc && pat_down && A->bs == 1 && values_done) {
-      // the host row pointers (downloaded meanwhile) give each chunk's range
-      cudaError_t e = cudaEventSynchronize(pat_down);
-      if (e != cudaSuccess) s = check_cuda(ctx, e, "pattern download");
+      // all chunks are queued first (the device never waits for the host),
+      // then the host row pointers -- downloaded meanwhile -- give each
+      // chunk's range for its download behind the chunk's event
       constexpr int NCH = 4;
-      for (int k = 0; k < NCH && s == GT_OK; k++) {
+      cudaEvent_t evs[NCH] = {};
+      int nq = 0;
+      for (int k = 0; k < NCH && s == GT_OK; k++, nq++) {
         const int64_t r0 = A->nbrows * k / NCH, r1 = A->nbrows * (k + 1) / NCH;
         s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr, r0, r1);
-        const int64_t o0 = hc->rowptr[r0], o1 = hc->rowptr[r1];
-        cudaEvent_t ev = event_get(ctx);
-        if (s == GT_OK && !ev) s = set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
-        if (s == GT_OK && o1 > o0) {
-          cudaEventRecord(ev, ctx->stream);
-          cudaStreamWaitEvent(ctx->side, ev, 0);
-          if (hc->v64 && A->val64)
-            cudaMemcpyAsync(hc->v64 + o0, A->val64 + o0, sizeof(double) * (o1 - o0), cudaMemcpyDefault, ctx->side);
-          if (hc->v32 && A->val32)
-            cudaMemcpyAsync(hc->v32 + o0, A->val32 + o0, sizeof(float) * (o1 - o0), cudaMemcpyDefault, ctx->side);
-          cudaError_t ce = cudaGetLastError();
-          if (ce != cudaSuccess) s = check_cuda(ctx, ce, "values download");
-        }
-        event_put(ctx, ev);
+        evs[k] = event_get(ctx);
+        if (s == GT_OK && !evs[k]) s = set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
+        if (s == GT_OK && cudaEventRecord(evs[k], ctx->stream) != cudaSuccess)
+          s = check_cuda(ctx, cudaGetLastError(), "event");
       }
+      if (s == GT_OK) {
+        cudaError_t e = cudaEventSynchronize(pat_down);
+        if (e != cudaSuccess) s = check_cuda(ctx, e, "pattern download");
+      }
+      for (int k = 0; k < NCH && s == GT_OK; k++) {
+        const int64_t r0 = A->nbrows * k / NCH, r1 = A->nbrows * (k + 1) / NCH;
+        const int64_t o0 = hc->rowptr[r0], o1 = hc->rowptr[r1];
+        if (o1 <= o0) continue;
+        cudaStreamWaitEvent(ctx->side, evs[k], 0);
+        if (hc->v64 && A->val64)
+          cudaMemcpyAsync(hc->v64 + o0, A->val64 + o0, sizeof(double) * (o1 - o0), cudaMemcpyDefault, ctx->side);
+        if (hc->v32 && A->val32)
+          cudaMemcpyAsync(hc->v32 + o0, A->val32 + o0, sizeof(float) * (o1 - o0), cudaMemcpyDefault, ctx->side);
+        cudaError_t ce = cudaGetLastError();
+        if (ce != cudaSuccess) s = check_cuda(ctx, ce, "values download");
+      }
+      for (int k = 0; k < nq; k++)
+        if (evs[k]) event_put(ctx, evs[k]);
       if (s == GT_OK) *values_done = true;
     } else if (s == GT_OK) {
       s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr);
@@ -1798,6 +1952,9 @@ static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double n
   // host inputs upload on the copy stream while the sparsity is built
   NumIn in;
   int s = in.init(sp, cell_coef, f, source_coef, b ? xd : nullptr, true);
+  // element kernels on the auxiliary stream, beside the sparsity kernels
+  EarlyElems early;
+  if (s == GT_OK) s = elements_early(sp, form, in, nu, precision, b != nullptr, &early);
   if (s == GT_OK) s = build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc, false);
   mark(ctx, "incidence");
   if (s == GT_OK) s = build_pattern(A);
@@ -1824,7 +1981,8 @@ static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double n
     event_put(ctx, pat);
   }
   bool values_done = false;
-  if (s == GT_OK) s = numeric_in(A, form, in, nu, b, hc, side_done, &values_done);
+  if (s == GT_OK) s = numeric_in(A, form, in, nu, b, hc, side_done, &values_done, &early);
+  early_release(ctx, &early);  // error paths: a stage numeric_in did not take over
   if (s == GT_OK && hc && !values_done) {
     if (bs == 1) {
       if (hc->v64 && A->val64 && nnz > 0) s = copy_out(ctx, hc->v64, A->val64, nnz);

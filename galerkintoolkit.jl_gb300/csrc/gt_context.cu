@@ -71,6 +71,7 @@ void pool_free(Ctx* ctx, void* p) {
 void pool_trim(Ctx* ctx) {
   if (ctx->pool.empty()) return;
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->aux) cudaStreamSynchronize(ctx->aux);
   for (auto& kv : ctx->pool) cudaFree(kv.second);
   ctx->pool.clear();
   ctx->pooled_bytes = 0;
@@ -114,6 +115,10 @@ void mesh_wait_coords(Mesh* m) {
   }
 }
 
+void mesh_wait_coords_on(Mesh* m, cudaStream_t s) {
+  if (m->coords_pending && m->coords_ev) cudaStreamWaitEvent(s, m->coords_ev, 0);
+}
+
 void mark(Ctx* ctx, const char* name) {
   if (!ctx->prof) return;
   cudaEvent_t e;
@@ -131,8 +136,10 @@ void mark(Ctx* ctx, const char* name) {
 int take_device_error(Ctx* ctx, uint32_t* bits) {
   GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_err, ctx->d_err, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  *bits = *ctx->h_err;
-  if (*bits) GT_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream));
+  const uint32_t dev = *ctx->h_err;
+  *bits = dev | ctx->held_err;
+  ctx->held_err = 0;
+  if (dev) GT_CUDA(ctx, cudaMemsetAsync(ctx->d_err, 0, sizeof(uint32_t), ctx->stream));
   return GT_OK;
 }
 
@@ -287,13 +294,26 @@ int gt_ctx_create(int device, gt_ctx** out) {
   gt_ctx* c = new gt_ctx();
   c->device = device;
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+  // the auxiliary compute stream takes the lowest priority and the main
+  // stream the highest: pending blocks of the main stream's kernels (the
+  // sparsity kernels, whose result the host downloads first) are dispatched
+  // before those of the element kernels beside them
+  int prio_least = 0, prio_greatest = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest);
+  if (cudaStreamCreateWithPriority(&c->own_stream, cudaStreamNonBlocking, prio_greatest) != cudaSuccess ||
       cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->aux, cudaStreamNonBlocking, prio_least) != cudaSuccess ||
       cudaMalloc(&c->d_err, sizeof(uint32_t)) != cudaSuccess ||
       cudaMallocHost(&c->h_err, sizeof(uint32_t)) != cudaSuccess ||
       cudaMallocHost(&c->h_scratch, 64 * sizeof(int64_t)) != cudaSuccess ||
       cudaMallocHost(&c->h_dscratch, 64 * sizeof(double)) != cudaSuccess) {
     cudaGetLastError();
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->aux) cudaStreamDestroy(c->aux);
+    if (c->d_err) cudaFree(c->d_err);
+    if (c->h_err) cudaFreeHost(c->h_err);
+    if (c->h_scratch) cudaFreeHost(c->h_scratch);
     delete c;
     return GT_ERR_CUDA;
   }
@@ -302,6 +322,8 @@ int gt_ctx_create(int device, gt_ctx** out) {
   c->pcg_path = !pcg ? 0 : strcmp(pcg, "launches") == 0 ? 1 : strcmp(pcg, "persistent") == 0 ? 2 : 0;
   const char* sp = getenv("GTGPU_SPMV");
   c->tiles_spmv = sp && strcmp(sp, "tiles") == 0;
+  const char* ov = getenv("GTGPU_OVERLAP");
+  c->overlap = !(ov && strcmp(ov, "0") == 0);
   cudaMemset(c->d_err, 0, sizeof(uint32_t));
   cudaDeviceSynchronize();
   *out = c;
@@ -313,6 +335,7 @@ int gt_ctx_destroy(gt_ctx* c) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   if (c->side) cudaStreamSynchronize(c->side);
+  if (c->aux) cudaStreamSynchronize(c->aux);
   for (auto& kv : c->live) cudaFree(kv.first);
   for (auto& kv : c->pool) cudaFree(kv.second);
   cudaFree(c->d_err);
@@ -324,6 +347,7 @@ int gt_ctx_destroy(gt_ctx* c) {
   for (auto e : c->free_events) cudaEventDestroy(e);
   cudaStreamDestroy(c->own_stream);
   if (c->side) cudaStreamDestroy(c->side);
+  if (c->aux) cudaStreamDestroy(c->aux);
   delete c;
   return GT_OK;
 }
@@ -334,6 +358,7 @@ int gt_ctx_synchronize(gt_ctx* c) {
   if (!c) return GT_ERR_INVALID;
   GT_CUDA(c, cudaStreamSynchronize(c->stream));
   GT_CUDA(c, cudaStreamSynchronize(c->side));
+  GT_CUDA(c, cudaStreamSynchronize(c->aux));
   return GT_OK;
 }
 

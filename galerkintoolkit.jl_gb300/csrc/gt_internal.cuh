@@ -71,6 +71,10 @@ struct Ctx {
   // copy stream: host<->device transfers that overlap the kernels of the
   // main stream (ordered against it with events)
   cudaStream_t side = nullptr;
+  // second compute stream: element kernels that run beside the sparsity
+  // kernels of the main stream (FP64-pipe work next to integer/shared-memory
+  // work on the same SMs), joined with an event before the scatter
+  cudaStream_t aux = nullptr;
   std::vector<cudaEvent_t> free_events;
   std::string err;
   // size-bucketed pool of device blocks (no cudaMalloc in steady state)
@@ -79,6 +83,7 @@ struct Ctx {
   int64_t live_bytes = 0, pooled_bytes = 0;
   uint32_t* d_err = nullptr;       // device error word
   uint32_t* h_err = nullptr;       // pinned mirror
+  uint32_t held_err = 0;           // bits taken by a pass that checks only its own, returned on the next take
   int64_t* h_scratch = nullptr;    // pinned small readbacks (64 words)
   double* h_dscratch = nullptr;    // pinned small FP64 readbacks (64 words)
   int64_t launches = 0;            // kernels launched by this context
@@ -88,6 +93,9 @@ struct Ctx {
   int pcg_path = 0;
   // bulk-copied row tiles instead of the row-group SpMV (GTGPU_SPMV=tiles)
   bool tiles_spmv = false;
+  // element kernels on the auxiliary stream beside the sparsity kernels
+  // (GTGPU_OVERLAP=0 at context creation: one stream, in order)
+  bool overlap = true;
   // phase profiling: CUDA events recorded on the stream between phases
   bool prof = false;
   std::vector<std::pair<std::string, cudaEvent_t>> marks;
@@ -172,6 +180,8 @@ struct Mesh {
 
 // orders the main stream after a pending coordinate upload of the mesh
 void mesh_wait_coords(Mesh* m);
+// orders stream s after it too (the upload stays pending for the main stream)
+void mesh_wait_coords_on(Mesh* m, cudaStream_t s);
 
 struct Space {
   Ctx* ctx = nullptr;  // owning context (also reachable as mesh->ctx while the mesh lives)
@@ -208,8 +218,12 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups);
 // incidence lists; sort = false leaves the order to the sparsity count pass
 int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc, bool sort);
 int build_pattern(Matrix* A);
+// keep_tab (optional): receives the tabulation buffer the kernels read
+// instead of freeing it (for launches on a stream other than the main one,
+// whose reuse of the block must wait for them)
 int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision,
-                     const double* f, const double* d_scoef, void* Ke, double* be, int want_matrix);
+                     const double* f, const double* d_scoef, void* Ke, double* be, int want_matrix,
+                     double** keep_tab = nullptr);
 // be/bvec (optional): element vectors and the load vector summed in the same
 // pass; xd: Dirichlet values (lift); [r0, r1): block rows (r1 < 0: all)
 int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be = nullptr,
