@@ -66,17 +66,40 @@ __device__ __forceinline__ void row_dot(const int64_t* __restrict__ rowptr, cons
 #pragma unroll
         for (int d = 0; d < BS; d++) acc[c] = fma((A)a[u][c * BS + d], xv[u][d], acc[c]);
   }
-  for (; k < e; k += G) {
-    const int32_t jj = __ldg(colind + k);
-    const V* blk = val + k * BS * BS;
+  // the lane's remaining entries (at most U - 1 once the loop above ends):
+  // one predicated trip, all loads in flight together, added in the same
+  // order as a serial loop over them (a short row otherwise pays one
+  // index-then-gather latency per leftover entry)
+  {
+    constexpr int R = U - 1;
+    int32_t j[R];
+    V a[R][BS * BS];
+    A xv[R][BS];
 #pragma unroll
-    for (int d = 0; d < BS; d++) {
-      A xj;
-      if constexpr (L2ONLY) xj = (A)__ldcg(x + (int64_t)jj * BS + d);
-      else xj = (A)x[(int64_t)jj * BS + d];
+    for (int u = 0; u < R; u++) {
+      const int64_t kk = k + u * G;
+      j[u] = kk < e ? __ldg(colind + kk) : 0;
 #pragma unroll
-      for (int c = 0; c < BS; c++) acc[c] = fma((A)__ldg(blk + c * BS + d), xj, acc[c]);
+      for (int q = 0; q < BS * BS; q++) a[u][q] = kk < e ? __ldg(val + kk * BS * BS + q) : (V)0;
     }
+#pragma unroll
+    for (int u = 0; u < R; u++)
+#pragma unroll
+      for (int d = 0; d < BS; d++) {
+        if (k + u * G < e) {
+          if constexpr (L2ONLY) xv[u][d] = (A)__ldcg(x + (int64_t)j[u] * BS + d);
+          else xv[u][d] = (A)x[(int64_t)j[u] * BS + d];
+        } else {
+          xv[u][d] = (A)0;
+        }
+      }
+#pragma unroll
+    for (int u = 0; u < R; u++)
+      if (k + u * G < e)
+#pragma unroll
+        for (int c = 0; c < BS; c++)
+#pragma unroll
+          for (int d = 0; d < BS; d++) acc[c] = fma((A)a[u][c * BS + d], xv[u][d], acc[c]);
   }
 #pragma unroll
   for (int c = 0; c < BS; c++) {

@@ -29,6 +29,31 @@ constexpr int CHUNK = 16;   // CG iterations between host polls
 constexpr int CG_STALLED = 1;  // internal status: the FP32 iteration stalled
 constexpr int64_t kPersistentMaxRows = 262144;  // scalar rows solved by the persistent kernel
 
+// Programmatic dependent launch (sm_90 and later) for the kernels of a CG
+// iteration: each is launched with programmatic stream serialisation, so its
+// CTAs may be scheduled while its predecessor on the stream is still in its
+// last-CTA reduction; it waits for that predecessor to complete (and its
+// writes to be visible) before it touches any memory.  Every CTA of a
+// reduction kernel lets the dependents launch once its own share is done.
+// Without the launch attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_release() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+static void launch_pdl(Ctx* ctx, void (*kern)(KArgs...), unsigned grid, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(GT_KC(ctx, grid));
+  cfg.blockDim = dim3(RED_T);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
 // device-resident CG state (one per solve)
 struct CGState {
   double rz, pq, rr, bb, alpha, beta;
@@ -163,6 +188,7 @@ template <int BS, int G, class V, class X>
 __global__ void __launch_bounds__(RED_T) k_cg_spmv(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                                                    const V* __restrict__ val, const X* __restrict__ p, X* __restrict__ q,
                                                    int64_t nrows, CGState* st, RedBuf rb) {
+  pdl_wait();
   if (st->done) return;
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   int64_t grp = t / G;
@@ -183,6 +209,7 @@ __global__ void __launch_bounds__(RED_T) k_cg_spmv(const int64_t* __restrict__ r
       }
     }
   }
+  pdl_release();
   if (reduce_last<1, X, G>(v, rb) && threadIdx.x == 0) {
     st->pq = (double)v[0];
     st->alpha = st->rz / (double)v[0];
@@ -196,6 +223,7 @@ template <class X>
 __global__ void __launch_bounds__(RED_T) k_cg_update(X* __restrict__ x, X* __restrict__ r, X* __restrict__ z,
                                                      const X* __restrict__ p, const X* __restrict__ q,
                                                      const X* __restrict__ dinv, int64_t n, CGState* st, RedBuf rb) {
+  pdl_wait();
   if (st->done) return;
   const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
   const X alpha = (X)st->alpha;
@@ -224,6 +252,7 @@ __global__ void __launch_bounds__(RED_T) k_cg_update(X* __restrict__ x, X* __res
     v[0] += ri * zi;
     v[1] += ri * ri;
   }
+  pdl_release();
   if (reduce_last<2, X>(v, rb) && threadIdx.x == 0) {
     double rz = (double)v[0], rr = (double)v[1];
     st->beta = rz / st->rz;
@@ -237,6 +266,7 @@ __global__ void __launch_bounds__(RED_T) k_cg_update(X* __restrict__ x, X* __res
 template <class X>
 __global__ void __launch_bounds__(RED_T) k_cg_pupdate(X* __restrict__ p, const X* __restrict__ z, int64_t n,
                                                       const CGState* st) {
+  pdl_wait();
   if (st->done) return;
   const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
   const X beta = (X)st->beta;
@@ -340,6 +370,11 @@ __global__ void __launch_bounds__(TILE_T) k_cg_spmv_tiles(const int64_t* __restr
 // ---------------------------------------------------------------------------
 // lanes per block row (row_lanes, gt_rowdot.cuh)
 static int pick_group(const Matrix* A) {
+  const char* ov = getenv("GTGPU_SPMV_LANES");
+  if (ov) {
+    const int g = atoi(ov);
+    if (g == 1 || g == 2 || g == 4 || g == 8) return g;
+  }
   return row_lanes(A->nbrows > 0 ? (double)A->bnnz / (double)A->nbrows : 1.0);
 }
 static unsigned spmv_grid(const Matrix* A) {
@@ -358,6 +393,11 @@ static unsigned ipt_grid(int64_t n) {
 static unsigned vec_grid(int64_t n) {
   int64_t g = (n + RED_T - 1) / RED_T;
   return (unsigned)(g > 0 ? g : 1);
+}
+// grid-stride kernels that run at few iterations and exit at the others
+static unsigned resident_grid(const Ctx* ctx, unsigned g) {
+  const unsigned cap = 4u * (unsigned)(ctx->num_sms > 0 ? ctx->num_sms : 1);
+  return g < cap ? g : cap;
 }
 
 struct Scratch {
@@ -463,7 +503,7 @@ struct Ops {
     unsigned grid = cg_spmv_grid(A);
     dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
-      k_cg_spmv<BS, GG, V, X><<<GT_KC(ctx, grid), RED_T, 0, ctx->stream>>>(A->rowptr, A->colind, val, p, q, A->nbrows, st, rb);
+      launch_pdl(ctx, k_cg_spmv<BS, GG, V, X>, grid, ctx->stream, A->rowptr, A->colind, val, p, q, A->nbrows, st, rb);
     });
     GT_LAUNCH(ctx, "k_cg_spmv");
     return GT_OK;
@@ -511,8 +551,8 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
   for (int it = 0; it < maxit; it += CHUNK) {
     for (int k = 0; k < CHUNK; k++) {
       GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb)));
-      k_cg_update<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(x, r, z, p, q, dinv, n, st, sc.rb);
-      k_cg_pupdate<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(p, z, n, st);
+      launch_pdl(ctx, k_cg_update<X>, gi, s, x, r, z, p, q, dinv, n, st, sc.rb);
+      launch_pdl(ctx, k_cg_pupdate<X>, gi, s, p, z, n, st);
     }
     GT_LAUNCH(ctx, "cg iteration");
     GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
@@ -548,6 +588,7 @@ template <class X>
 __global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __restrict__ r, X* __restrict__ z,
                                                      const X* __restrict__ p, const X* __restrict__ q,
                                                      const X* __restrict__ dinv, int64_t n, CGState* st, RedBuf rb) {
+  pdl_wait();
   if (st->done) return;
   const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
   const X alpha = (X)st->alpha;
@@ -576,6 +617,7 @@ __global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __re
     v[0] += ri * zi;
     v[1] += ri * ri;
   }
+  pdl_release();
   if (reduce_last<2, X>(v, rb) && threadIdx.x == 0) {
     double rz = (double)v[0], rr = (double)v[1];
     st->rzold = st->rz;
@@ -592,51 +634,55 @@ __global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __re
   }
 }
 
-// x += xs; xs = 0 (when an update is due)
+// x += xs; xs = 0 (when an update is due).  Grid-stride over a grid of a
+// few CTAs per SM: at the iterations without an update (nearly all) the
+// launch costs only those CTAs reading the flag.
 template <class X>
 __global__ void __launch_bounds__(RED_T) k_rl_xupdate(double* __restrict__ x, X* __restrict__ xs, int64_t n,
                                                       const CGState* st) {
+  pdl_wait();
   if (st->done || !st->upd) return;
-  const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
-#pragma unroll
-  for (int j = 0; j < IPT; j++) {
-    int64_t i = base + (int64_t)j * blockDim.x;
-    if (i < n) {
-      x[i] += (double)xs[i];
-      xs[i] = (X)0;
-    }
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += (double)xs[i];
+    xs[i] = (X)0;
   }
 }
 
 // r64 = b - A x (FP64), r = (X) r64, z = Dinv r; rz and ||r64||^2; decides
-// convergence on the true residual
+// convergence on the true residual.  Grid-stride (block-uniform trips, so
+// whole groups stay in row_dot's shuffles) over a grid of a few CTAs per SM,
+// like k_rl_xupdate.
 template <int BS, int G, class X>
 __global__ void __launch_bounds__(RED_T) k_rl_resid(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                                                     const double* __restrict__ val, const double* __restrict__ b,
                                                     const double* __restrict__ x, X* __restrict__ r, X* __restrict__ z,
                                                     const X* __restrict__ dinv, int64_t nrows, CGState* st, RedBuf rb) {
+  pdl_wait();
   if (st->done || !st->upd) return;
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int64_t row = t / G;
-  int gl = (int)(t - row * G);
-  bool valid = row < nrows;
-  if (!valid) row = nrows - 1;
-  double o[BS];
-  row_product<BS, G, double, double>(rowptr, colind, val, x, row, gl, o);
   double v[2] = {0.0, 0.0};
-  if (gl == 0 && valid) {
+  for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x; t0 < nrows * G; t0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = t0 + threadIdx.x;
+    int64_t row = t / G;
+    const int gl = (int)(t - row * G);
+    const bool valid = row < nrows;
+    if (!valid) row = nrows - 1;
+    double o[BS];
+    row_product<BS, G, double, double>(rowptr, colind, val, x, row, gl, o);
+    if (gl == 0 && valid) {
 #pragma unroll
-    for (int c = 0; c < BS; c++) {
-      int64_t i = row * BS + c;
-      double ri = b[i] - o[c];
-      X rx = (X)ri;
-      X zx = dinv[i] * rx;
-      r[i] = rx;
-      z[i] = zx;
-      v[0] += (double)rx * (double)zx;
-      v[1] += ri * ri;
+      for (int c = 0; c < BS; c++) {
+        int64_t i = row * BS + c;
+        double ri = b[i] - o[c];
+        X rx = (X)ri;
+        X zx = dinv[i] * rx;
+        r[i] = rx;
+        z[i] = zx;
+        v[0] += (double)rx * (double)zx;
+        v[1] += ri * ri;
+      }
     }
   }
+  pdl_release();
   if (reduce_last<2, double, G>(v, rb) && threadIdx.x == 0) {
     // the next direction is built from the true residual
     st->beta = st->rzold != 0.0 ? v[0] / st->rzold : 0.0;
@@ -714,8 +760,8 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
   auto resid = [&]() {
     Ops<double, double>::dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
-      k_rl_resid<BS, GG, X><<<GT_KC(ctx, gr), RED_T, 0, s>>>(A->rowptr, A->colind, A->val64, b, x, r, z, dinv,
-                                                            A->nbrows, st, sc.rb);
+      launch_pdl(ctx, k_rl_resid<BS, GG, X>, resident_grid(ctx, gr), s, A->rowptr, A->colind, A->val64, b, x, r, z,
+                 dinv, A->nbrows, st, sc.rb);
     });
   };
   resid();  // r = b - A x0, z, rz
@@ -725,10 +771,10 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
   for (int it = 0; it < maxit + CHUNK; it += CHUNK) {
     for (int k = 0; k < CHUNK; k++) {
       GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb)));
-      k_rl_update<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(xs, r, z, p, q, dinv, n, st, sc.rb);
-      k_rl_xupdate<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(x, xs, n, st);
+      launch_pdl(ctx, k_rl_update<X>, gi, s, xs, r, z, p, q, dinv, n, st, sc.rb);
+      launch_pdl(ctx, k_rl_xupdate<X>, resident_grid(ctx, gv), s, x, xs, n, st);
       resid();
-      k_cg_pupdate<X><<<GT_KC(ctx, gi), RED_T, 0, s>>>(p, z, n, st);
+      launch_pdl(ctx, k_cg_pupdate<X>, gi, s, p, z, n, st);
     }
     GT_LAUNCH(ctx, "reliable CG iteration");
     GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
