@@ -190,22 +190,27 @@ __global__ void __launch_bounds__(RED_T) k_cg_spmv(const int64_t* __restrict__ r
                                                    int64_t nrows, CGState* st, RedBuf rb) {
   pdl_wait();
   if (st->done) return;
-  int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int64_t grp = t / G;
-  int gl = (int)(t - grp * G);
   X v[1] = {(X)0};
+  // grid-stride with block-uniform trips (whole groups stay in the shuffles):
+  // a grid of one wave pays the reduction tail once per CTA
+  const int64_t ngroups = (nrows + RPG - 1) / RPG;
+  for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x; t0 < ngroups * G; t0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = t0 + threadIdx.x;
+    const int64_t grp = t / G;
+    const int gl = (int)(t - grp * G);
 #pragma unroll
-  for (int u = 0; u < RPG; u++) {
-    int64_t r = grp * RPG + u;
-    bool valid = r < nrows;
-    if (!valid) r = nrows - 1;
-    X o[BS];
-    row_product<BS, G, V, X>(rowptr, colind, val, p, r, gl, o);
-    if (gl == 0 && valid) {
+    for (int u = 0; u < RPG; u++) {
+      int64_t r = grp * RPG + u;
+      bool valid = r < nrows;
+      if (!valid) r = nrows - 1;
+      X o[BS];
+      row_product<BS, G, V, X>(rowptr, colind, val, p, r, gl, o);
+      if (gl == 0 && valid) {
 #pragma unroll
-      for (int c = 0; c < BS; c++) {
-        q[r * BS + c] = o[c];
-        v[0] += o[c] * p[r * BS + c];
+        for (int c = 0; c < BS; c++) {
+          q[r * BS + c] = o[c];
+          v[0] += o[c] * p[r * BS + c];
+        }
       }
     }
   }
@@ -225,32 +230,34 @@ __global__ void __launch_bounds__(RED_T) k_cg_update(X* __restrict__ x, X* __res
                                                      const X* __restrict__ dinv, int64_t n, CGState* st, RedBuf rb) {
   pdl_wait();
   if (st->done) return;
-  const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
   const X alpha = (X)st->alpha;
-  X rv[IPT], qv[IPT], pv[IPT], xv[IPT], dv[IPT];
-#pragma unroll
-  for (int j = 0; j < IPT; j++) {
-    int64_t i = base + (int64_t)j * blockDim.x;
-    bool ok = i < n;
-    rv[j] = ok ? r[i] : (X)0;
-    qv[j] = ok ? q[i] : (X)0;
-    pv[j] = ok ? p[i] : (X)0;
-    xv[j] = ok ? x[i] : (X)0;
-    dv[j] = ok ? dinv[i] : (X)0;
-  }
   X v[2] = {(X)0, (X)0};
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x; base < n;
+       base += (int64_t)gridDim.x * blockDim.x * IPT) {
+    X rv[IPT], qv[IPT], pv[IPT], xv[IPT], dv[IPT];
 #pragma unroll
-  for (int j = 0; j < IPT; j++) {
-    int64_t i = base + (int64_t)j * blockDim.x;
-    X ri = rv[j] - alpha * qv[j];
-    X zi = dv[j] * ri;
-    if (i < n) {
-      x[i] = xv[j] + alpha * pv[j];
-      r[i] = ri;
-      z[i] = zi;
+    for (int j = 0; j < IPT; j++) {
+      int64_t i = base + (int64_t)j * blockDim.x;
+      bool ok = i < n;
+      rv[j] = ok ? r[i] : (X)0;
+      qv[j] = ok ? q[i] : (X)0;
+      pv[j] = ok ? p[i] : (X)0;
+      xv[j] = ok ? x[i] : (X)0;
+      dv[j] = ok ? dinv[i] : (X)0;
     }
-    v[0] += ri * zi;
-    v[1] += ri * ri;
+#pragma unroll
+    for (int j = 0; j < IPT; j++) {
+      int64_t i = base + (int64_t)j * blockDim.x;
+      X ri = rv[j] - alpha * qv[j];
+      X zi = dv[j] * ri;
+      if (i < n) {
+        x[i] = xv[j] + alpha * pv[j];
+        r[i] = ri;
+        z[i] = zi;
+      }
+      v[0] += ri * zi;
+      v[1] += ri * ri;
+    }
   }
   pdl_release();
   if (reduce_last<2, X>(v, rb) && threadIdx.x == 0) {
@@ -394,10 +401,166 @@ static unsigned vec_grid(int64_t n) {
   int64_t g = (n + RED_T - 1) / RED_T;
   return (unsigned)(g > 0 ? g : 1);
 }
+// one wave of a grid-stride kernel: at most the CTAs of kern resident at once
+template <class K>
+static unsigned one_wave(const Ctx* ctx, K kern, unsigned g) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, RED_T, 0) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  const unsigned cap = (unsigned)per_sm * (unsigned)(ctx->num_sms > 0 ? ctx->num_sms : 1);
+  return g < cap ? g : cap;
+}
 // grid-stride kernels that run at few iterations and exit at the others
 static unsigned resident_grid(const Ctx* ctx, unsigned g) {
   const unsigned cap = 4u * (unsigned)(ctx->num_sms > 0 ? ctx->num_sms : 1);
   return g < cap ? g : cap;
+}
+
+// ---------------------------------------------------------------------------
+// Sliced-ELL copy of a scalar matrix for the CG SpMV, built per solve.
+// Slices of 32 consecutive rows, one lane per row; a slice stores its rows
+// padded to its longest one, column-major (entry k of row 32 s + l at
+// sptr[s] + 32 k + l; padding: the row's own column, value 0).  A warp then
+// reads 32 rows' k-th column ids and values as two full 128-byte lines where
+// the CSR row kernel issued 4-byte loads of lanes on different rows (whose
+// load-queue occupancy, not DRAM, bounded the short P1/Q1 rows).  Each row
+// is summed serially in column order.  Taken when the padding stays within
+// a quarter of the entries.
+// ---------------------------------------------------------------------------
+constexpr int SELL_C = 32;
+
+template <class V>
+struct Sell {
+  Ctx* ctx = nullptr;
+  int64_t nslices = 0;
+  int64_t* sptr = nullptr;  // first entry of each slice (nslices + 1)
+  int32_t* slen = nullptr;  // entries per row of each slice
+  int32_t* col = nullptr;
+  V* val = nullptr;
+  bool on() const { return val != nullptr; }
+  ~Sell() {
+    if (ctx) {
+      dfree(ctx, sptr);
+      dfree(ctx, slen);
+      dfree(ctx, col);
+      dfree(ctx, val);
+    }
+  }
+};
+
+// warp per slice: the slice's longest row (and 32x it for the scan)
+__global__ void k_sell_len(const int64_t* __restrict__ rowptr, int64_t nrows, int64_t nslices, int32_t* __restrict__ slen,
+                           int32_t* __restrict__ slen32) {
+  const int64_t sl = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (sl >= nslices) return;  // warp-uniform
+  const int64_t r = sl * SELL_C + lane;
+  int len = r < nrows ? (int)(rowptr[r + 1] - rowptr[r]) : 0;
+  for (int o = 16; o; o >>= 1) len = max(len, __shfl_xor_sync(0xffffffffu, len, o));
+  if (lane == 0) {
+    slen[sl] = len;
+    slen32[sl] = len * SELL_C;
+  }
+}
+
+template <class V>
+__global__ void k_sell_fill(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                            const V* __restrict__ val, int64_t nrows, int64_t nslices, const int64_t* __restrict__ sptr,
+                            const int32_t* __restrict__ slen, int32_t* __restrict__ scol, V* __restrict__ sval) {
+  const int64_t sl = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (sl >= nslices) return;
+  const int64_t r = sl * SELL_C + lane;
+  int64_t b = 0, e = 0;
+  if (r < nrows) {
+    b = rowptr[r];
+    e = rowptr[r + 1];
+  }
+  const int32_t pad = r < nrows ? (int32_t)r : 0;
+  const int L = slen[sl];
+  const int64_t o = sptr[sl] + lane;
+  for (int k = 0; k < L; k++) {
+    const bool in = b + k < e;
+    scol[o + (int64_t)k * SELL_C] = in ? colind[b + k] : pad;
+    sval[o + (int64_t)k * SELL_C] = in ? val[b + k] : (V)0;
+  }
+}
+
+// q = A p and p.q on the sliced copy; warp per slice, grid-stride over the
+// slices (one wave), 4 entries per lane in flight
+template <class V, class X>
+__global__ void __launch_bounds__(RED_T) k_cg_spmv_sell(const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                                                        const int32_t* __restrict__ scol, const V* __restrict__ sval,
+                                                        const X* __restrict__ p, X* __restrict__ q, int64_t nrows,
+                                                        int64_t nslices, CGState* st, RedBuf rb) {
+  pdl_wait();
+  if (st->done) return;
+  const int lane = threadIdx.x & 31;
+  X v[1] = {(X)0};
+  const int64_t wstride = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t sl = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; sl < nslices; sl += wstride) {
+    const int64_t o = __ldg(sptr + sl) + lane;
+    const int L = __ldg(slen + sl);
+    X acc = (X)0;
+    for (int k = 0; k < L; k += 4) {
+      int32_t j[4];
+      V a[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const bool in = k + u < L;
+        j[u] = in ? __ldg(scol + o + (int64_t)(k + u) * SELL_C) : 0;
+        a[u] = in ? __ldg(sval + o + (int64_t)(k + u) * SELL_C) : (V)0;
+      }
+      X xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) xv[u] = k + u < L ? p[j[u]] : (X)0;
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (k + u < L) acc = fma((X)a[u], xv[u], acc);
+    }
+    const int64_t r = sl * SELL_C + lane;
+    if (r < nrows) {
+      q[r] = acc;
+      v[0] += acc * p[r];
+    }
+  }
+  pdl_release();
+  if (reduce_last<1, X>(v, rb) && threadIdx.x == 0) {
+    st->pq = (double)v[0];
+    st->alpha = st->rz / (double)v[0];
+  }
+}
+
+// builds the sliced copy of a scalar matrix (values val) unless the padding
+// would exceed a quarter of the entries; leaves S off (no error) then
+template <class V>
+static int sell_build(Ctx* ctx, const Matrix* A, const V* val, Sell<V>* S) {
+  if (A->bs != 1 || A->nbrows == 0 || A->bnnz == 0) return GT_OK;
+  const int64_t nrows = A->nbrows, ns = (nrows + SELL_C - 1) / SELL_C;
+  S->ctx = ctx;
+  S->nslices = ns;
+  int32_t* len32 = nullptr;
+  GT_TRY(dalloc(ctx, &S->slen, ns));
+  GT_TRY(dalloc(ctx, &S->sptr, ns + 1));
+  GT_TRY(dalloc(ctx, &len32, ns));
+  const unsigned g = (unsigned)((ns * 32 + 255) / 256);
+  k_sell_len<<<GT_KC(ctx, g), 256, 0, ctx->stream>>>(A->rowptr, nrows, ns, S->slen, len32);
+  GT_LAUNCH(ctx, "k_sell_len");
+  int st = exclusive_scan_i64(ctx, len32, S->sptr, ns);
+  dfree(ctx, len32);
+  GT_TRY(st);
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[4], S->sptr + ns, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  const int64_t total = ctx->h_scratch[4];
+  if (total > A->bnnz + A->bnnz / 4) return GT_OK;  // too much padding: the CSR kernel
+  GT_TRY(dalloc(ctx, &S->col, total));
+  GT_TRY(dalloc(ctx, &S->val, total));
+  k_sell_fill<V><<<GT_KC(ctx, g), 256, 0, ctx->stream>>>(A->rowptr, A->colind, val, nrows, ns, S->sptr, S->slen,
+                                                         S->col, S->val);
+  GT_LAUNCH(ctx, "k_sell_fill");
+  return GT_OK;
 }
 
 struct Scratch {
@@ -488,7 +651,16 @@ struct Ops {
     GT_LAUNCH(ctx, "k_spmv");
     return GT_OK;
   }
-  static int cg_spmv(Ctx* ctx, const Matrix* A, const V* val, const X* p, X* q, CGState* st, RedBuf rb) {
+  static int cg_spmv(Ctx* ctx, const Matrix* A, const V* val, const X* p, X* q, CGState* st, RedBuf rb,
+                     const Sell<V>* sell = nullptr) {
+    if (sell && sell->on()) {
+      auto kern = k_cg_spmv_sell<V, X>;
+      const unsigned g = one_wave(ctx, kern, (unsigned)((sell->nslices * 32 + RED_T - 1) / RED_T));
+      launch_pdl(ctx, kern, g, ctx->stream, sell->sptr, sell->slen, sell->col, sell->val, p, q, A->nbrows,
+                 sell->nslices, st, rb);
+      GT_LAUNCH(ctx, "k_cg_spmv_sell");
+      return GT_OK;
+    }
     if (int tg = tile_lanes(A)) {
       by_lanes(tg, [&](auto g_t) {
         constexpr int GG = decltype(g_t)::value;
@@ -503,7 +675,8 @@ struct Ops {
     unsigned grid = cg_spmv_grid(A);
     dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
-      launch_pdl(ctx, k_cg_spmv<BS, GG, V, X>, grid, ctx->stream, A->rowptr, A->colind, val, p, q, A->nbrows, st, rb);
+      launch_pdl(ctx, k_cg_spmv<BS, GG, V, X>, one_wave(ctx, k_cg_spmv<BS, GG, V, X>, grid), ctx->stream, A->rowptr,
+                 A->colind, val, p, q, A->nbrows, st, rb);
     });
     GT_LAUNCH(ctx, "k_cg_spmv");
     return GT_OK;
@@ -547,11 +720,14 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
   GT_TRY((Ops<V, X>::spmv(ctx, A, val, x, b, r)));  // r = b - A x
   k_cg_init<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(r, z, p, dinv, n, st, sc.rb, rtol * rtol, bb_dev);
   GT_LAUNCH(ctx, "k_cg_init");
+  Sell<V> sell;
+  if (!Ops<V, X>::tile_lanes(A)) GT_TRY(sell_build(ctx, A, val, &sell));
+  const unsigned gu = one_wave(ctx, k_cg_update<X>, gi);  // update kernel: one wave, grid-stride
   CGState h{};
   for (int it = 0; it < maxit; it += CHUNK) {
     for (int k = 0; k < CHUNK; k++) {
-      GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb)));
-      launch_pdl(ctx, k_cg_update<X>, gi, s, x, r, z, p, q, dinv, n, st, sc.rb);
+      GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb, &sell)));
+      launch_pdl(ctx, k_cg_update<X>, gu, s, x, r, z, p, q, dinv, n, st, sc.rb);
       launch_pdl(ctx, k_cg_pupdate<X>, gi, s, p, z, n, st);
     }
     GT_LAUNCH(ctx, "cg iteration");
@@ -590,32 +766,34 @@ __global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __re
                                                      const X* __restrict__ dinv, int64_t n, CGState* st, RedBuf rb) {
   pdl_wait();
   if (st->done) return;
-  const int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x;
   const X alpha = (X)st->alpha;
-  X rv[IPT], qv[IPT], pv[IPT], xv[IPT], dv[IPT];
-#pragma unroll
-  for (int j = 0; j < IPT; j++) {
-    int64_t i = base + (int64_t)j * blockDim.x;
-    bool ok = i < n;
-    rv[j] = ok ? r[i] : (X)0;
-    qv[j] = ok ? q[i] : (X)0;
-    pv[j] = ok ? p[i] : (X)0;
-    xv[j] = ok ? xs[i] : (X)0;
-    dv[j] = ok ? dinv[i] : (X)0;
-  }
   X v[2] = {(X)0, (X)0};
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x; base < n;
+       base += (int64_t)gridDim.x * blockDim.x * IPT) {
+    X rv[IPT], qv[IPT], pv[IPT], xv[IPT], dv[IPT];
 #pragma unroll
-  for (int j = 0; j < IPT; j++) {
-    int64_t i = base + (int64_t)j * blockDim.x;
-    X ri = rv[j] - alpha * qv[j];
-    X zi = dv[j] * ri;
-    if (i < n) {
-      xs[i] = xv[j] + alpha * pv[j];
-      r[i] = ri;
-      z[i] = zi;
+    for (int j = 0; j < IPT; j++) {
+      int64_t i = base + (int64_t)j * blockDim.x;
+      bool ok = i < n;
+      rv[j] = ok ? r[i] : (X)0;
+      qv[j] = ok ? q[i] : (X)0;
+      pv[j] = ok ? p[i] : (X)0;
+      xv[j] = ok ? xs[i] : (X)0;
+      dv[j] = ok ? dinv[i] : (X)0;
     }
-    v[0] += ri * zi;
-    v[1] += ri * ri;
+#pragma unroll
+    for (int j = 0; j < IPT; j++) {
+      int64_t i = base + (int64_t)j * blockDim.x;
+      X ri = rv[j] - alpha * qv[j];
+      X zi = dv[j] * ri;
+      if (i < n) {
+        xs[i] = xv[j] + alpha * pv[j];
+        r[i] = ri;
+        z[i] = zi;
+      }
+      v[0] += ri * zi;
+      v[1] += ri * ri;
+    }
   }
   pdl_release();
   if (reduce_last<2, X>(v, rb) && threadIdx.x == 0) {
@@ -767,11 +945,14 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
   resid();  // r = b - A x0, z, rz
   k_copy_vec<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(z, p, n);
   GT_LAUNCH(ctx, "reliable CG start");
+  Sell<V> sell;
+  if (!Ops<V, X>::tile_lanes(A)) GT_TRY(sell_build(ctx, A, val, &sell));
+  const unsigned gu = one_wave(ctx, k_rl_update<X>, gi);  // update kernel: one wave, grid-stride
   CGState h{};
   for (int it = 0; it < maxit + CHUNK; it += CHUNK) {
     for (int k = 0; k < CHUNK; k++) {
-      GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb)));
-      launch_pdl(ctx, k_rl_update<X>, gi, s, xs, r, z, p, q, dinv, n, st, sc.rb);
+      GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb, &sell)));
+      launch_pdl(ctx, k_rl_update<X>, gu, s, xs, r, z, p, q, dinv, n, st, sc.rb);
       launch_pdl(ctx, k_rl_xupdate<X>, resident_grid(ctx, gv), s, x, xs, n, st);
       resid();
       launch_pdl(ctx, k_cg_pupdate<X>, gi, s, p, z, n, st);
