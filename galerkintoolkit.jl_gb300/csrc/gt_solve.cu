@@ -25,6 +25,7 @@ namespace gt {
 
 constexpr int RED_T = 256;  // threads per CTA of the reduction kernels
 constexpr int GROUP = 256;  // CTAs per first-level reduction group
+constexpr unsigned kOneLevel = 4096;  // grids up to this size reduce in one level
 constexpr int CHUNK = 16;   // CG iterations between host polls
 constexpr int CG_STALLED = 1;  // internal status: the FP32 iteration stalled
 constexpr int64_t kPersistentMaxRows = 262144;  // scalar rows solved by the persistent kernel
@@ -99,6 +100,44 @@ __device__ bool reduce_last(A (&v)[K], RedBuf rb) {
   }
   __syncthreads();
   const unsigned nb = gridDim.x, b = blockIdx.x;
+  if (nb <= kOneLevel) {
+    // one level: every CTA posts its partials and takes a ticket (release);
+    // the CTA with the last ticket (acquire) sums all partials in a fixed
+    // order -- each thread a strided run of CTAs, then a butterfly per warp
+    // and the warp totals in order.  One fence and one atomic per CTA and a
+    // single round of partial loads: the two-level scheme's extra fence,
+    // atomic and load round trips sat on the critical path of every
+    // reduction kernel's last CTA.
+    if (tid == 0) {
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        A t = (A)0;
+        for (int i = 0; i < nw; i++) t += sred[k][i];
+        rb.p1[(size_t)b * K + k] = (double)t;
+      }
+      unsigned prev;
+      asm volatile("atom.acq_rel.gpu.global.inc.u32 %0, [%1], %2;" : "=r"(prev) : "l"(rb.ctr), "r"(nb - 1) : "memory");
+      s_flag = prev == nb - 1;
+    }
+    __syncthreads();
+    if (!s_flag) return false;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      double t = 0.0;
+      for (unsigned i = tid; i < nb; i += RED_T) t += __ldcg(&rb.p1[(size_t)i * K + k]);
+      for (int o = 16; o; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) tree[k][w] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      double t = 0.0;
+      for (int i = 0; i < nw; i++) t += tree[k][i];
+      v[k] = (A)t;
+    }
+    __syncthreads();
+    return true;
+  }
   const unsigned ng = (nb + GROUP - 1) / GROUP, g = b / GROUP;
   const unsigned gs = min((unsigned)GROUP, nb - g * GROUP);
   if (tid == 0) {
@@ -401,7 +440,11 @@ static unsigned vec_grid(int64_t n) {
   int64_t g = (n + RED_T - 1) / RED_T;
   return (unsigned)(g > 0 ? g : 1);
 }
-// one wave of a grid-stride kernel: at most the CTAs of kern resident at once
+// One wave of a grid-stride kernel whose work is g CTA-sized trips: at most
+// the CTAs of kern resident at once, and balanced -- T = ceil(g / cap) trips
+// each for ceil(g / T) CTAs, so no CTA makes one trip more than most (with
+// the plain cap, CTAs making two trips against others' one doubled the
+// kernel's critical path).
 template <class K>
 static unsigned one_wave(const Ctx* ctx, K kern, unsigned g) {
   int per_sm = 0;
@@ -410,7 +453,9 @@ static unsigned one_wave(const Ctx* ctx, K kern, unsigned g) {
     per_sm = 1;
   }
   const unsigned cap = (unsigned)per_sm * (unsigned)(ctx->num_sms > 0 ? ctx->num_sms : 1);
-  return g < cap ? g : cap;
+  if (g <= cap) return g > 0 ? g : 1;
+  const unsigned trips = (g + cap - 1) / cap;
+  return (g + trips - 1) / trips;
 }
 // grid-stride kernels that run at few iterations and exit at the others
 static unsigned resident_grid(const Ctx* ctx, unsigned g) {
