@@ -229,10 +229,12 @@ def run_serving(args):
 
 
 def spmv_roofline(A, flush, stream, reps=20):
-    """y = A x with the FP64 block-CSR SpMV (gt_spmv, device vectors), L2
+    """y = A x with the FP64 SpMV (gt_spmv, device vectors; on the sliced-ELL
+    copy the library keeps for scalar matrices, built by the first call), L2
     flushed before each launch, timed by the library's phase marks (CUDA
     events on its stream right before and after the kernel); algorithmic
-    bytes = values + column indices + row pointers + x + y."""
+    bytes = those of the CSR matrix: values + column indices + row pointers
+    + x + y (the copy's padding and slice pointers are not counted)."""
     import torch
     from gtgpu.api import _ptr
     n = A.shape[0]
@@ -249,7 +251,7 @@ def spmv_roofline(A, flush, stream, reps=20):
             ts.append(ph["spmv"])
     ms = statistics.median(ts)
     nb = A.nnz * (8 + 4) + (n + 1) * 8 + 2 * n * 8
-    return {"kernel": "k_spmv<1, G, double, double>", "achieved": nb / (ms * 1e-3) / 1e9, "unit": "GB/s",
+    return {"kernel": "k_spmv_sell<double, double>", "achieved": nb / (ms * 1e-3) / 1e9, "unit": "GB/s",
             "algorithmic_bytes": nb, "ms": ms, "traffic": TRAFFIC.get("spmv")}
 
 

@@ -1082,6 +1082,7 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
 int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be, double* bvec,
                    const double* xd, int64_t r0, int64_t r1) {
   if (r1 < 0) r1 = A->nbrows;
+  matrix_values_changed(A);
   double* v64 = (out_precision == GT_FP64 || out_precision == GT_MIXED) ? A->val64 : nullptr;
   float* v32 = (out_precision == GT_FP32 || out_precision == GT_MIXED) ? A->val32 : nullptr;
   int bs = A->bs;
@@ -1433,6 +1434,7 @@ static int launch_kron(Matrix* A, const T* Gc, double nu, const double* be, doub
   constexpr int G = NN <= 4 ? 4 : (NN <= 8 ? 8 : (NN <= 16 ? 16 : 32));
   constexpr int RPW = 32 / G;
   int lmax = A->max_row > 0 ? A->max_row : 1;
+  matrix_values_changed(A);
   double* v64 = A->precision != GT_FP32 ? A->val64 : nullptr;
   float* v32 = A->precision != GT_FP64 ? A->val32 : nullptr;
   int warps = 4;
@@ -1901,6 +1903,7 @@ static void matrix_release(gt_matrix* A) {
   dfree(c, A->inc_ptr);
   dfree(c, A->inc);
   dfree(c, A->diag_pos);
+  sell_release(A);
 }
 
 extern "C" {

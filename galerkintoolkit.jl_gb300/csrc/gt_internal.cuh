@@ -209,7 +209,25 @@ struct Matrix {
   int32_t* inc = nullptr;          // cell * nn + local node
   int64_t ninc = 0;
   int32_t* diag_pos = nullptr;     // position of the diagonal block in each row
+  // sliced-ELL copy of a scalar matrix for the SpMV (32-row slices, see
+  // gt_solve.cu): built on first use, values refreshed after every update
+  int sell_state = 0;              // 0 not built, 1 built, -1 not taken (padding)
+  int64_t sell_nslices = 0, sell_total = 0;
+  int64_t* sell_ptr = nullptr;     // nslices + 1
+  int32_t* sell_len = nullptr;     // nslices
+  int32_t* sell_col = nullptr;
+  double* sell_v64 = nullptr;
+  float* sell_v32 = nullptr;
+  bool sell_cur64 = false, sell_cur32 = false;  // values match val64 / val32
 };
+
+// called by every kernel launch that rewrites a matrix's values
+inline void matrix_values_changed(Matrix* A) {
+  A->sell_cur64 = false;
+  A->sell_cur32 = false;
+}
+// frees the sliced-ELL copy
+void sell_release(Matrix* A);
 
 // ---------------------------------------------------------------------------
 // library-internal entry points (implemented across the .cu files)

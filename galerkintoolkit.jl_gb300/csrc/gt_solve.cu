@@ -476,23 +476,14 @@ static unsigned resident_grid(const Ctx* ctx, unsigned g) {
 // ---------------------------------------------------------------------------
 constexpr int SELL_C = 32;
 
+// view of a matrix's sliced copy in value type V (val == nullptr: not used)
 template <class V>
-struct Sell {
-  Ctx* ctx = nullptr;
+struct SellView {
   int64_t nslices = 0;
-  int64_t* sptr = nullptr;  // first entry of each slice (nslices + 1)
-  int32_t* slen = nullptr;  // entries per row of each slice
-  int32_t* col = nullptr;
-  V* val = nullptr;
-  bool on() const { return val != nullptr; }
-  ~Sell() {
-    if (ctx) {
-      dfree(ctx, sptr);
-      dfree(ctx, slen);
-      dfree(ctx, col);
-      dfree(ctx, val);
-    }
-  }
+  const int64_t* ptr = nullptr;
+  const int32_t* len = nullptr;
+  const int32_t* col = nullptr;
+  const V* val = nullptr;
 };
 
 // warp per slice: the slice's longest row (and 32x it for the scan)
@@ -578,34 +569,117 @@ __global__ void __launch_bounds__(RED_T) k_cg_spmv_sell(const int64_t* __restric
   }
 }
 
-// builds the sliced copy of a scalar matrix (values val) unless the padding
-// would exceed a quarter of the entries; leaves S off (no error) then
 template <class V>
-static int sell_build(Ctx* ctx, const Matrix* A, const V* val, Sell<V>* S) {
-  if (A->bs != 1 || A->nbrows == 0 || A->bnnz == 0) return GT_OK;
+static V*& sell_values(Matrix* A);
+template <>
+double*& sell_values<double>(Matrix* A) { return A->sell_v64; }
+template <>
+float*& sell_values<float>(Matrix* A) { return A->sell_v32; }
+template <class V>
+static bool& sell_current(Matrix* A);
+template <>
+bool& sell_current<double>(Matrix* A) { return A->sell_cur64; }
+template <>
+bool& sell_current<float>(Matrix* A) { return A->sell_cur32; }
+
+void sell_release(Matrix* A) {
+  Ctx* ctx = A->ctx;
+  dfree(ctx, A->sell_ptr);
+  dfree(ctx, A->sell_len);
+  dfree(ctx, A->sell_col);
+  dfree(ctx, A->sell_v64);
+  dfree(ctx, A->sell_v32);
+  A->sell_ptr = nullptr;
+  A->sell_len = nullptr;
+  A->sell_col = nullptr;
+  A->sell_v64 = nullptr;
+  A->sell_v32 = nullptr;
+  A->sell_state = 0;
+  A->sell_cur64 = A->sell_cur32 = false;
+}
+
+// The sliced copy of a scalar matrix with values val (A->val64 or A->val32),
+// built on first use and refilled after value updates; view->val stays null
+// when the copy does not apply (block rows, the opt-in tiled kernel, or a
+// padding above a quarter of the entries -- then never retried).
+template <class V>
+static int sell_prepare(Matrix* A, const V* val, SellView<V>* view) {
+  *view = SellView<V>{};
+  Ctx* ctx = A->ctx;
+  if (A->bs != 1 || A->nbrows == 0 || A->bnnz == 0 || A->sell_state < 0 || ctx->tiles_spmv || !val) return GT_OK;
   const int64_t nrows = A->nbrows, ns = (nrows + SELL_C - 1) / SELL_C;
-  S->ctx = ctx;
-  S->nslices = ns;
-  int32_t* len32 = nullptr;
-  GT_TRY(dalloc(ctx, &S->slen, ns));
-  GT_TRY(dalloc(ctx, &S->sptr, ns + 1));
-  GT_TRY(dalloc(ctx, &len32, ns));
   const unsigned g = (unsigned)((ns * 32 + 255) / 256);
-  k_sell_len<<<GT_KC(ctx, g), 256, 0, ctx->stream>>>(A->rowptr, nrows, ns, S->slen, len32);
-  GT_LAUNCH(ctx, "k_sell_len");
-  int st = exclusive_scan_i64(ctx, len32, S->sptr, ns);
-  dfree(ctx, len32);
-  GT_TRY(st);
-  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[4], S->sptr + ns, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
-  GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  const int64_t total = ctx->h_scratch[4];
-  if (total > A->bnnz + A->bnnz / 4) return GT_OK;  // too much padding: the CSR kernel
-  GT_TRY(dalloc(ctx, &S->col, total));
-  GT_TRY(dalloc(ctx, &S->val, total));
-  k_sell_fill<V><<<GT_KC(ctx, g), 256, 0, ctx->stream>>>(A->rowptr, A->colind, val, nrows, ns, S->sptr, S->slen,
-                                                         S->col, S->val);
-  GT_LAUNCH(ctx, "k_sell_fill");
+  if (A->sell_state == 0) {
+    int32_t* len32 = nullptr;
+    GT_TRY(dalloc(ctx, &A->sell_len, ns));
+    GT_TRY(dalloc(ctx, &A->sell_ptr, ns + 1));
+    GT_TRY(dalloc(ctx, &len32, ns));
+    k_sell_len<<<GT_KC(ctx, g), 256, 0, ctx->stream>>>(A->rowptr, nrows, ns, A->sell_len, len32);
+    GT_LAUNCH(ctx, "k_sell_len");
+    int st = exclusive_scan_i64(ctx, len32, A->sell_ptr, ns);
+    dfree(ctx, len32);
+    GT_TRY(st);
+    GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[4], A->sell_ptr + ns, sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const int64_t total = ctx->h_scratch[4];
+    if (total > A->bnnz + A->bnnz / 4) {
+      sell_release(A);
+      A->sell_state = -1;
+      return GT_OK;
+    }
+    GT_TRY(dalloc(ctx, &A->sell_col, total));
+    A->sell_total = total;
+    A->sell_nslices = ns;
+    A->sell_state = 1;
+    A->sell_cur64 = A->sell_cur32 = false;
+  }
+  V*& sv = sell_values<V>(A);
+  if (!sv) GT_TRY(dalloc(ctx, &sv, A->sell_total));
+  bool& cur = sell_current<V>(A);
+  if (!cur) {
+    k_sell_fill<V><<<GT_KC(ctx, g), 256, 0, ctx->stream>>>(A->rowptr, A->colind, val, nrows, ns, A->sell_ptr,
+                                                           A->sell_len, A->sell_col, sv);
+    GT_LAUNCH(ctx, "k_sell_fill");
+    cur = true;
+  }
+  view->nslices = ns;
+  view->ptr = A->sell_ptr;
+  view->len = A->sell_len;
+  view->col = A->sell_col;
+  view->val = sv;
   return GT_OK;
+}
+
+// y = A x (or y = bsub - A x) on the sliced copy: warp per slice
+template <class V, class X>
+__global__ void k_spmv_sell(const int64_t* __restrict__ sptr, const int32_t* __restrict__ slen,
+                            const int32_t* __restrict__ scol, const V* __restrict__ sval, const X* __restrict__ x,
+                            int64_t nrows, int64_t nslices, const X* __restrict__ bsub, X* __restrict__ y) {
+  const int64_t sl = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (sl >= nslices) return;
+  const int64_t o = __ldg(sptr + sl) + lane;
+  const int L = __ldg(slen + sl);
+  X acc = (X)0;
+  for (int k = 0; k < L; k += 4) {
+    int32_t j[4];
+    V a[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const bool in = k + u < L;
+      j[u] = in ? __ldg(scol + o + (int64_t)(k + u) * SELL_C) : 0;
+      a[u] = in ? __ldg(sval + o + (int64_t)(k + u) * SELL_C) : (V)0;
+    }
+    X xv[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) xv[u] = k + u < L ? x[j[u]] : (X)0;
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (k + u < L) acc = fma((X)a[u], xv[u], acc);
+  }
+  const int64_t r = sl * SELL_C + lane;
+  if (r < nrows) y[r] = bsub ? bsub[r] - acc : acc;
 }
 
 struct Scratch {
@@ -697,11 +771,11 @@ struct Ops {
     return GT_OK;
   }
   static int cg_spmv(Ctx* ctx, const Matrix* A, const V* val, const X* p, X* q, CGState* st, RedBuf rb,
-                     const Sell<V>* sell = nullptr) {
-    if (sell && sell->on()) {
+                     const SellView<V>* sell = nullptr) {
+    if (sell && sell->val) {
       auto kern = k_cg_spmv_sell<V, X>;
       const unsigned g = one_wave(ctx, kern, (unsigned)((sell->nslices * 32 + RED_T - 1) / RED_T));
-      launch_pdl(ctx, kern, g, ctx->stream, sell->sptr, sell->slen, sell->col, sell->val, p, q, A->nbrows,
+      launch_pdl(ctx, kern, g, ctx->stream, sell->ptr, sell->len, sell->col, sell->val, p, q, A->nbrows,
                  sell->nslices, st, rb);
       GT_LAUNCH(ctx, "k_cg_spmv_sell");
       return GT_OK;
@@ -765,8 +839,8 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
   GT_TRY((Ops<V, X>::spmv(ctx, A, val, x, b, r)));  // r = b - A x
   k_cg_init<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(r, z, p, dinv, n, st, sc.rb, rtol * rtol, bb_dev);
   GT_LAUNCH(ctx, "k_cg_init");
-  Sell<V> sell;
-  if (!Ops<V, X>::tile_lanes(A)) GT_TRY(sell_build(ctx, A, val, &sell));
+  SellView<V> sell;
+  GT_TRY(sell_prepare(A, val, &sell));
   const unsigned gu = one_wave(ctx, k_cg_update<X>, gi);  // update kernel: one wave, grid-stride
   CGState h{};
   for (int it = 0; it < maxit; it += CHUNK) {
@@ -990,8 +1064,8 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
   resid();  // r = b - A x0, z, rz
   k_copy_vec<X><<<GT_KC(ctx, gv), RED_T, 0, s>>>(z, p, n);
   GT_LAUNCH(ctx, "reliable CG start");
-  Sell<V> sell;
-  if (!Ops<V, X>::tile_lanes(A)) GT_TRY(sell_build(ctx, A, val, &sell));
+  SellView<V> sell;
+  GT_TRY(sell_prepare(A, val, &sell));
   const unsigned gu = one_wave(ctx, k_rl_update<X>, gi);  // update kernel: one wave, grid-stride
   CGState h{};
   for (int it = 0; it < maxit + CHUNK; it += CHUNK) {
@@ -1027,7 +1101,18 @@ int spmv64(Matrix* A, const double* x, double* y) {
   Ctx* ctx = A->space->mesh->ctx;
   if (!A->val64) return set_error(ctx, GT_ERR_INVALID, "matrix has no FP64 values");
   mark(ctx, "spmv_setup");
-  int s = Ops<double, double>::spmv(ctx, A, A->val64, x, nullptr, y);
+  SellView<double> sv;
+  int s = sell_prepare(A, A->val64, &sv);  // first call: builds the sliced copy
+  mark(ctx, "spmv_prepare");
+  if (s == GT_OK && sv.val) {
+    const unsigned g = (unsigned)((sv.nslices * 32 + 255) / 256);
+    k_spmv_sell<double, double><<<GT_KC(ctx, g), 256, 0, ctx->stream>>>(sv.ptr, sv.len, sv.col, sv.val, x, A->nbrows,
+                                                                        sv.nslices, nullptr, y);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) s = check_cuda(ctx, e, "k_spmv_sell");
+  } else if (s == GT_OK) {
+    s = Ops<double, double>::spmv(ctx, A, A->val64, x, nullptr, y);
+  }
   mark(ctx, "spmv");  // the phase "spmv" of a profile is the kernel alone
   return s;
 }

@@ -165,3 +165,38 @@ def test_solve_q2_elasticity_ir():
     assert info["converged"]
     xd = sla.spsolve(A.tocsr().tocsc(), b)
     assert np.abs(x - xd).max() / np.abs(xd).max() < 1e-8
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
+def test_spmv_matches_csr(case):
+    """gt_spmv (the sliced-ELL copy for scalar matrices, the block-CSR kernel
+    otherwise) against the downloaded CSR times the same vector on the host."""
+    m, V, ref, a, coef, form, order = _build(case)
+    A = GT.assemble_matrix(a, np.float64, V, V)
+    n = A.shape[0]
+    if n == 0:
+        return
+    x = np.random.default_rng(5).standard_normal(n)
+    y = A @ x
+    yr = A.tocsr() @ x
+    assert np.abs(y - yr).max() <= 1e-13 * max(1.0, np.abs(yr).max())
+
+
+def test_spmv_copy_follows_value_updates():
+    """the SpMV's cached copy is refilled after update_matrix: a product after
+    the update equals the product with the updated CSR, not the first one"""
+    m, V, ref, a, coef, form, order = _build(CASES[1])
+    A = GT.assemble_matrix(a, np.float64, V, V)
+    x = np.random.default_rng(6).standard_normal(A.shape[0])
+    y1 = A @ x  # builds the copy
+    k2 = GT.lognormal_cells(m.num_cells, 1.0, 99)
+    GT.update_matrix(A, GT.laplacian(k2))
+    y2 = A @ x
+    yr = A.tocsr() @ x
+    assert np.abs(y2 - yr).max() <= 1e-13 * np.abs(yr).max()
+    assert np.abs(y2 - y1).max() > 1e-6 * np.abs(yr).max()
+    # a solve after the update uses the refreshed copy as well
+    b = np.ones(A.shape[0])
+    xs, info = GT.solve(A, b, rtol=1e-10, mode="fp64")
+    assert info["converged"]
+    assert np.abs(A.tocsr() @ xs - b).max() <= 1e-8 * np.abs(b).max()
