@@ -44,10 +44,10 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # tets), from ncu captures (summaries under profiles/): the element and
 # scatter kernels captured on 64^3 x 6 tets (1,572,864 cells) and scaled by
 # the cell ratio 3.375 (their traffic is proportional to the cells); the FP64
-# CG SpMV captured on the full workload
-TRAFFIC: dict = {"elements": (44.539136e6 + 192.030464e6) * 3.375,
-                 "scatter": (329.769472e6 + 26.009088e6) * 3.375,
-                 "spmv": 165.773568e6 + 5.912320e6}
+# SpMV (sliced-ELL copy) captured on the full workload
+TRAFFIC: dict = {"elements": (44.413440e6 + 191.132416e6) * 3.375,
+                 "scatter": (326.434560e6 + 25.815296e6) * 3.375,
+                 "spmv": 159.938048e6 + 5.819904e6}
 
 
 def parse():
