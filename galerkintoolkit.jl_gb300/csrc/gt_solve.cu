@@ -25,7 +25,8 @@ namespace gt {
 
 constexpr int RED_T = 256;  // threads per CTA of the reduction kernels
 constexpr int GROUP = 256;  // CTAs per first-level reduction group
-constexpr unsigned kOneLevel = 4096;  // grids up to this size reduce in one level
+constexpr unsigned kOneLevel = 2048;  // grids up to this size reduce in one level
+constexpr int64_t kLoopUpdate = int64_t(1) << 22;  // vector length of the looping update kernels
 constexpr int CHUNK = 16;   // CG iterations between host polls
 constexpr int CG_STALLED = 1;  // internal status: the FP32 iteration stalled
 constexpr int64_t kPersistentMaxRows = 262144;  // scalar rows solved by the persistent kernel
@@ -230,8 +231,7 @@ __global__ void __launch_bounds__(RED_T) k_cg_spmv(const int64_t* __restrict__ r
   pdl_wait();
   if (st->done) return;
   X v[1] = {(X)0};
-  // grid-stride with block-uniform trips (whole groups stay in the shuffles):
-  // a grid of one wave pays the reduction tail once per CTA
+  // grid-stride with block-uniform trips (whole groups stay in the shuffles)
   const int64_t ngroups = (nrows + RPG - 1) / RPG;
   for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x; t0 < ngroups * G; t0 += (int64_t)gridDim.x * blockDim.x) {
     const int64_t t = t0 + threadIdx.x;
@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(RED_T) k_cg_spmv(const int64_t* __restrict__ r
 // x += alpha p; r -= alpha q; z = Dinv r; r.z and r.r -> beta, convergence.
 // IPT elements per thread (coalesced, all loads issued before the math).
 constexpr int IPT = 4;
-template <class X>
+template <class X, bool LOOP>
 __global__ void __launch_bounds__(RED_T) k_cg_update(X* __restrict__ x, X* __restrict__ r, X* __restrict__ z,
                                                      const X* __restrict__ p, const X* __restrict__ q,
                                                      const X* __restrict__ dinv, int64_t n, CGState* st, RedBuf rb) {
@@ -271,8 +271,7 @@ __global__ void __launch_bounds__(RED_T) k_cg_update(X* __restrict__ x, X* __res
   if (st->done) return;
   const X alpha = (X)st->alpha;
   X v[2] = {(X)0, (X)0};
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x; base < n;
-       base += (int64_t)gridDim.x * blockDim.x * IPT) {
+  auto trip = [&](const int64_t base) {
     X rv[IPT], qv[IPT], pv[IPT], xv[IPT], dv[IPT];
 #pragma unroll
     for (int j = 0; j < IPT; j++) {
@@ -297,6 +296,14 @@ __global__ void __launch_bounds__(RED_T) k_cg_update(X* __restrict__ x, X* __res
       v[0] += ri * zi;
       v[1] += ri * ri;
     }
+  };
+  if constexpr (LOOP) {
+    // one wave of CTAs over the vector: fewer CTAs in the reduction
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x; base < n;
+         base += (int64_t)gridDim.x * blockDim.x * IPT)
+      trip(base);
+  } else {
+    trip((int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x);
   }
   pdl_release();
   if (reduce_last<2, X>(v, rb) && threadIdx.x == 0) {
@@ -794,8 +801,7 @@ struct Ops {
     unsigned grid = cg_spmv_grid(A);
     dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
-      launch_pdl(ctx, k_cg_spmv<BS, GG, V, X>, one_wave(ctx, k_cg_spmv<BS, GG, V, X>, grid), ctx->stream, A->rowptr,
-                 A->colind, val, p, q, A->nbrows, st, rb);
+      launch_pdl(ctx, k_cg_spmv<BS, GG, V, X>, grid, ctx->stream, A->rowptr, A->colind, val, p, q, A->nbrows, st, rb);
     });
     GT_LAUNCH(ctx, "k_cg_spmv");
     return GT_OK;
@@ -841,12 +847,18 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
   GT_LAUNCH(ctx, "k_cg_init");
   SellView<V> sell;
   GT_TRY(sell_prepare(A, val, &sell));
-  const unsigned gu = one_wave(ctx, k_cg_update<X>, gi);  // update kernel: one wave, grid-stride
+  // update kernel: up to kLoopUpdate elements, one wave of CTAs looping over
+  // the vector (measured faster on 0.86M rows); above, one trip per thread
+  // (the looping form holds twice the registers, which costs occupancy on
+  // long vectors: measured slower on 19M rows)
+  const bool uloop = n <= kLoopUpdate;
+  const unsigned gu = uloop ? one_wave(ctx, k_cg_update<X, true>, gi) : gi;
   CGState h{};
   for (int it = 0; it < maxit; it += CHUNK) {
     for (int k = 0; k < CHUNK; k++) {
       GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb, &sell)));
-      launch_pdl(ctx, k_cg_update<X>, gu, s, x, r, z, p, q, dinv, n, st, sc.rb);
+      if (uloop) launch_pdl(ctx, k_cg_update<X, true>, gu, s, x, r, z, p, q, dinv, n, st, sc.rb);
+      else launch_pdl(ctx, k_cg_update<X, false>, gu, s, x, r, z, p, q, dinv, n, st, sc.rb);
       launch_pdl(ctx, k_cg_pupdate<X>, gi, s, p, z, n, st);
     }
     GT_LAUNCH(ctx, "cg iteration");
@@ -879,7 +891,7 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
 // stays near that of FP64 CG, at the per-iteration cost of X.  Convergence
 // is declared on the FP64 true residual only.
 // ---------------------------------------------------------------------------
-template <class X>
+template <class X, bool LOOP>
 __global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __restrict__ r, X* __restrict__ z,
                                                      const X* __restrict__ p, const X* __restrict__ q,
                                                      const X* __restrict__ dinv, int64_t n, CGState* st, RedBuf rb) {
@@ -887,8 +899,7 @@ __global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __re
   if (st->done) return;
   const X alpha = (X)st->alpha;
   X v[2] = {(X)0, (X)0};
-  for (int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x; base < n;
-       base += (int64_t)gridDim.x * blockDim.x * IPT) {
+  auto trip = [&](const int64_t base) {
     X rv[IPT], qv[IPT], pv[IPT], xv[IPT], dv[IPT];
 #pragma unroll
     for (int j = 0; j < IPT; j++) {
@@ -913,6 +924,14 @@ __global__ void __launch_bounds__(RED_T) k_rl_update(X* __restrict__ xs, X* __re
       v[0] += ri * zi;
       v[1] += ri * ri;
     }
+  };
+  if constexpr (LOOP) {
+    // one wave of CTAs over the vector: fewer CTAs in the reduction
+    for (int64_t base = (int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x; base < n;
+         base += (int64_t)gridDim.x * blockDim.x * IPT)
+      trip(base);
+  } else {
+    trip((int64_t)blockIdx.x * blockDim.x * IPT + threadIdx.x);
   }
   pdl_release();
   if (reduce_last<2, X>(v, rb) && threadIdx.x == 0) {
@@ -1066,12 +1085,18 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
   GT_LAUNCH(ctx, "reliable CG start");
   SellView<V> sell;
   GT_TRY(sell_prepare(A, val, &sell));
-  const unsigned gu = one_wave(ctx, k_rl_update<X>, gi);  // update kernel: one wave, grid-stride
+  // update kernel: up to kLoopUpdate elements, one wave of CTAs looping over
+  // the vector (measured faster on 0.86M rows); above, one trip per thread
+  // (the looping form holds twice the registers, which costs occupancy on
+  // long vectors: measured slower on 19M rows)
+  const bool uloop = n <= kLoopUpdate;
+  const unsigned gu = uloop ? one_wave(ctx, k_rl_update<X, true>, gi) : gi;
   CGState h{};
   for (int it = 0; it < maxit + CHUNK; it += CHUNK) {
     for (int k = 0; k < CHUNK; k++) {
       GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb, &sell)));
-      launch_pdl(ctx, k_rl_update<X>, gu, s, xs, r, z, p, q, dinv, n, st, sc.rb);
+      if (uloop) launch_pdl(ctx, k_rl_update<X, true>, gu, s, xs, r, z, p, q, dinv, n, st, sc.rb);
+      else launch_pdl(ctx, k_rl_update<X, false>, gu, s, xs, r, z, p, q, dinv, n, st, sc.rb);
       launch_pdl(ctx, k_rl_xupdate<X>, resident_grid(ctx, gv), s, x, xs, n, st);
       resid();
       launch_pdl(ctx, k_cg_pupdate<X>, gi, s, p, z, n, st);
