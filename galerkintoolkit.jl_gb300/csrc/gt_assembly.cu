@@ -40,6 +40,7 @@ struct TabLayout {
   int D, nlv, nn, nq;
   int off_w, off_gg, off_sv, off_sg;
   int off_k;  // 32 doubles of per-reference-cell quadrature sums (P1 path)
+  int off_gv;  // geometry shape values at the points (nq x nlv), past the kernels' staged part
   int total;
 };
 inline TabLayout tab_layout(int ctype, int order) {
@@ -54,7 +55,8 @@ inline TabLayout tab_layout(int ctype, int order) {
   L.off_sv = L.off_gg + L.nq * L.nlv * L.D;
   L.off_sg = L.off_sv + L.nq * L.nn;
   L.off_k = L.off_sg + L.nq * L.nn * L.D;
-  L.total = L.off_k + 32;
+  L.off_gv = L.off_k + 32;
+  L.total = L.off_gv + L.nq * L.nlv;
   return L;
 }
 
@@ -103,11 +105,19 @@ __global__ void k_tabulate(int ctype, int order, TabLayout L, double* tab) {
         tab[L.off_sg + (q * 4 + n) * 3 + d] = gr[n][d];
       }
     double v[4] = {1.0 - x[0] - x[1] - x[2], x[0], x[1], x[2]};
-    for (int n = 0; n < 4; n++) tab[L.off_sv + q * 4 + n] = v[n];
+    for (int n = 0; n < 4; n++) {
+      tab[L.off_sv + q * 4 + n] = v[n];
+      tab[L.off_gv + q * 4 + n] = v[n];
+    }
     return;
   }
   double v1[3][3], d1[3][3];
   for (int d = 0; d < L.D; d++) lagrange1d(1, x[d], v1[d], d1[d]);
+  for (int n = 0; n < L.nlv; n++) {
+    double g = 1.0;
+    for (int e = 0; e < L.D; e++) g *= v1[e][(n >> e) & 1];
+    tab[L.off_gv + q * L.nlv + n] = g;
+  }
   for (int n = 0; n < L.nlv; n++)
     for (int d = 0; d < L.D; d++) {
       double g = 1.0;
@@ -908,6 +918,201 @@ int compute_elements(const Space* sp, int form, const double* d_coef, double nu,
     s = elements_T<double>(sp, form, d_coef, nu, tab, L, (double*)Ke, be, f, d_scoef, want_matrix);
   if (keep_tab) *keep_tab = tab;
   else dfree(ctx, tab);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// Integrals over the cells: GT.assemble_scalar (src/problems.jl:172-190) for
+// the fixed integrands the reference's tests integrate -- 1, a polynomial,
+// the discrete field, its square, and the squared L2 / H1-seminorm errors
+// against a polynomial (test/integration_tests.jl:68-77, the patch tests of
+// test/assembly_tests.jl:43-118).  Same quadrature as the assembly, dV =
+// |det J| w (src/quadrature.jl:4-6), grad u = J^-T grad u^ (src/accessors.jl:
+// 1365-1373).  One thread per cell; per-cell values summed in a fixed order.
+// ---------------------------------------------------------------------------
+// p(x) with coefficients of 1, x, y, z, x^2, y^2, z^2, xy, xz, yz, and its gradient
+__device__ __forceinline__ double poly_eval(const double* c, const double* x, double* g) {
+  const double X = x[0], Y = x[1], Z = x[2];
+  g[0] = c[1] + 2.0 * c[4] * X + c[7] * Y + c[8] * Z;
+  g[1] = c[2] + 2.0 * c[5] * Y + c[7] * X + c[9] * Z;
+  g[2] = c[3] + 2.0 * c[6] * Z + c[8] * X + c[9] * Y;
+  return c[0] + c[1] * X + c[2] * Y + c[3] * Z + c[4] * X * X + c[5] * Y * Y + c[6] * Z * Z + c[7] * X * Y +
+         c[8] * X * Z + c[9] * Y * Z;
+}
+
+constexpr int kPolyCoefs = 10;
+
+template <int D, int NLV, int NN>
+__global__ void __launch_bounds__(128) k_integrate(const double* __restrict__ coords, const int32_t* __restrict__ cell_nodes,
+                                                   const int32_t* __restrict__ cnd, const double* __restrict__ tab,
+                                                   TabLayout L, int64_t ncells, int ncomp, int kind,
+                                                   const double* __restrict__ uf, const double* __restrict__ ud,
+                                                   const double* __restrict__ poly, double* __restrict__ cell_val) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  double X[NLV][3];
+#pragma unroll
+  for (int v = 0; v < NLV; v++) {
+    const int64_t nd = cell_nodes[c * NLV + v];
+#pragma unroll
+    for (int d = 0; d < 3; d++) X[v][d] = d < D ? coords[nd * D + d] : 0.0;
+  }
+  const bool want_u = kind >= GT_INT_FIELD;
+  int32_t dof[NN];
+#pragma unroll
+  for (int n = 0; n < NN; n++) dof[n] = want_u ? cnd[c * NN + n] : 0;
+  double acc = 0.0;
+  for (int q = 0; q < L.nq; q++) {
+    double J[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}}, x[3] = {0, 0, 0};
+#pragma unroll
+    for (int i = 0; i < D; i++)
+#pragma unroll
+      for (int j = 0; j < D; j++) J[i][j] = 0.0;
+#pragma unroll
+    for (int v = 0; v < NLV; v++) {
+      const double gv = tab[L.off_gv + q * NLV + v];
+#pragma unroll
+      for (int i = 0; i < D; i++) {
+        x[i] += X[v][i] * gv;
+#pragma unroll
+        for (int j = 0; j < D; j++) J[i][j] += X[v][i] * tab[L.off_gg + (q * NLV + v) * D + j];
+      }
+    }
+    double det, inv[3][3];
+    if (D == 2) {
+      det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+      const double r = 1.0 / det;
+      inv[0][0] = J[1][1] * r; inv[0][1] = -J[0][1] * r; inv[1][0] = -J[1][0] * r; inv[1][1] = J[0][0] * r;
+    } else {
+      const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1], c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2],
+                   c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+      det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+      const double r = 1.0 / det;
+      inv[0][0] = c00 * r; inv[1][0] = c01 * r; inv[2][0] = c02 * r;
+      inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+      inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+      inv[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+      inv[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+      inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+      inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+    }
+    const double dv = fabs(det) * tab[L.off_w + q];
+    if (kind == GT_INT_VOLUME) {
+      acc += dv;
+      continue;
+    }
+    double pg[3];
+    if (kind == GT_INT_POLY) {
+      acc += dv * poly_eval(poly, x, pg);
+      continue;
+    }
+    double term = 0.0;
+    for (int k = 0; k < ncomp; k++) {
+      double u = 0.0, gr[3] = {0, 0, 0};
+#pragma unroll
+      for (int n = 0; n < NN; n++) {
+        const int32_t d = dof[n];
+        const double val = d > 0 ? uf[(int64_t)(d - 1) * ncomp + k] : (ud ? ud[(int64_t)(-d - 1) * ncomp + k] : 0.0);
+        u += val * tab[L.off_sv + q * NN + n];
+        if (kind == GT_INT_H1_ERROR2)
+#pragma unroll
+          for (int j = 0; j < D; j++) gr[j] += val * tab[L.off_sg + (q * NN + n) * D + j];
+      }
+      if (kind == GT_INT_FIELD) {
+        term += u;
+      } else if (kind == GT_INT_L2_NORM2) {
+        term += u * u;
+      } else {
+        const double p = poly_eval(poly + k * kPolyCoefs, x, pg);
+        if (kind == GT_INT_L2_ERROR2) {
+          term += (u - p) * (u - p);
+        } else {
+          // physical gradient: sum_j inv[j][i] * ref gradient j  (J^-T)
+#pragma unroll
+          for (int i = 0; i < D; i++) {
+            double g = 0.0;
+#pragma unroll
+            for (int j = 0; j < D; j++) g += inv[j][i] * gr[j];
+            term += (g - pg[i]) * (g - pg[i]);
+          }
+        }
+      }
+    }
+    acc += dv * term;
+  }
+  cell_val[c] = acc;
+}
+
+// fixed-order sums of 2048 consecutive values per CTA (strided per thread,
+// then a tree); the host adds the CTA sums in order
+__global__ void k_sum_fixed(const double* __restrict__ v, int64_t n, double* __restrict__ part) {
+  __shared__ double t[256];
+  const int64_t b0 = (int64_t)blockIdx.x * 2048;
+  double s = 0.0;
+  for (int k = 0; k < 8; k++) {
+    const int64_t i = b0 + (int64_t)k * 256 + threadIdx.x;
+    if (i < n) s += v[i];
+  }
+  t[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o; o >>= 1) {
+    if ((int)threadIdx.x < o) t[threadIdx.x] += t[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = t[0];
+}
+
+template <int D, int NLV, int NN>
+static void launch_integrate(const Space* sp, const double* tab, const TabLayout& L, int kind, const double* uf,
+                             const double* ud, const double* poly, double* cell_val) {
+  Ctx* ctx = ctx_of(sp);
+  const int64_t nc = sp->mesh->ncells;
+  k_integrate<D, NLV, NN><<<GT_KC(ctx, grid_for(nc, 128)), 128, 0, ctx->stream>>>(
+      sp->mesh->coords, sp->mesh->cell_nodes, sp->cell_ndofs, tab, L, nc, sp->ncomp, kind, uf, ud, poly, cell_val);
+}
+
+static int integrate(const Space* sp, int kind, const double* uf, const double* ud, const double* poly, double* out) {
+  Ctx* ctx = ctx_of(sp);
+  const int ct = sp->mesh->ctype, o = sp->order;
+  const int64_t nc = sp->mesh->ncells;
+  *out = 0.0;
+  if (nc == 0) return GT_OK;
+  mesh_wait_coords(sp->mesh);
+  double* tab = nullptr;
+  TabLayout L;
+  GT_TRY(get_tab(ctx, ct, o, &tab, &L));
+  double *cv = nullptr, *part = nullptr;
+  const int64_t nb = (nc + 2047) / 2048;
+  int s = dalloc(ctx, &cv, nc);
+  if (s == GT_OK) s = dalloc(ctx, &part, nb);
+  if (s == GT_OK) {
+    if (ct == GT_TET4) launch_integrate<3, 4, 4>(sp, tab, L, kind, uf, ud, poly, cv);
+    else if (ct == GT_QUAD4 && o == 1) launch_integrate<2, 4, 4>(sp, tab, L, kind, uf, ud, poly, cv);
+    else if (ct == GT_QUAD4) launch_integrate<2, 4, 9>(sp, tab, L, kind, uf, ud, poly, cv);
+    else if (o == 1) launch_integrate<3, 8, 8>(sp, tab, L, kind, uf, ud, poly, cv);
+    else launch_integrate<3, 8, 27>(sp, tab, L, kind, uf, ud, poly, cv);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) s = check_cuda(ctx, e, "k_integrate");
+  }
+  if (s == GT_OK) {
+    k_sum_fixed<<<GT_KC(ctx, (unsigned)nb), 256, 0, ctx->stream>>>(cv, nc, part);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) s = check_cuda(ctx, e, "k_sum_fixed");
+  }
+  std::vector<double> h((size_t)nb);
+  if (s == GT_OK) s = copy_out(ctx, h.data(), part, nb);
+  if (s == GT_OK) {
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) s = check_cuda(ctx, e, "integrate");
+  }
+  if (s == GT_OK) {
+    double t = 0.0;
+    for (int64_t i = 0; i < nb; i++) t += h[(size_t)i];
+    *out = t;
+  }
+  dfree(ctx, tab);
+  dfree(ctx, cv);
+  dfree(ctx, part);
   return s;
 }
 
@@ -2054,6 +2259,27 @@ int gt_assemble_vector(gt_space* sp, const double* f, const double* cell_coef, d
   if (s == GT_OK) s = device_status(ctx, "assemble_vector");
   if (!dev && bd) dfree(ctx, bd);
   dfree(ctx, be);
+  return s;
+}
+
+int gt_integrate(gt_space* sp, int kind, const double* u_free, const double* u_dirichlet, const double* poly,
+                 double* result) {
+  if (!sp || !result) return GT_ERR_INVALID;
+  Ctx* ctx = sp->mesh->ctx;
+  if (kind < GT_INT_VOLUME || kind > GT_INT_H1_ERROR2)
+    return set_error(ctx, GT_ERR_INVALID, "gt_integrate: unknown integrand kind");
+  const bool need_u = kind >= GT_INT_FIELD, need_p = kind == GT_INT_POLY || kind >= GT_INT_L2_ERROR2;
+  if (need_u && !u_free) return set_error(ctx, GT_ERR_INVALID, "gt_integrate: this integrand needs u_free");
+  if (need_p && !poly) return set_error(ctx, GT_ERR_INVALID, "gt_integrate: this integrand needs poly");
+  cudaSetDevice(ctx->device);
+  DevIn<double> uf, ud, pc;
+  GT_TRY(uf.init(ctx, need_u ? u_free : nullptr, sp->nfree_nodes * sp->ncomp));
+  GT_TRY(ud.init(ctx, need_u ? u_dirichlet : nullptr, sp->ndiri_nodes * sp->ncomp));
+  GT_TRY(pc.init(ctx, need_p ? poly : nullptr, (int64_t)kPolyCoefs * (kind == GT_INT_POLY ? 1 : sp->ncomp)));
+  double v = 0.0;
+  int s = integrate(sp, kind, uf.p, ud.p, pc.p, &v);
+  if (s == GT_OK) s = device_status(ctx, "integrate");
+  if (s == GT_OK) *result = v;
   return s;
 }
 

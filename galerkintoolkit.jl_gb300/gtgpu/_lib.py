@@ -22,6 +22,7 @@ GT_ERR_BUDGET = -7
 
 GT_QUAD4, GT_HEX8, GT_TET4 = 1, 2, 3
 GT_LAPLACE, GT_MASS, GT_ELASTICITY = 1, 2, 3
+GT_INT_VOLUME, GT_INT_POLY, GT_INT_FIELD, GT_INT_L2_NORM2, GT_INT_L2_ERROR2, GT_INT_H1_ERROR2 = 0, 1, 2, 3, 4, 5
 GT_FP64, GT_FP32, GT_MIXED = 0, 1, 2
 GT_SOLVE_FP64, GT_SOLVE_IR, GT_SOLVE_FP32 = 0, 1, 2
 
@@ -79,6 +80,7 @@ SIGNATURES = [
     ("gt_matrix_download_csr", I32, [P, P, P, P, P]),
     ("gt_matrix_destroy", I32, [P]),
     ("gt_assemble_vector", I32, [P, P, P, P]),
+    ("gt_integrate", I32, [P, I32, P, P, P, P]),
     ("gt_solve", I32, [P, P, P, DBL, I32, I32, C.POINTER(SolveInfo)]),
     ("gt_spmv", I32, [P, P, P]),
     ("gt_batch_create", I32, [P, I32, P, C.POINTER(P)]),

@@ -445,6 +445,65 @@ def interpolate_dirichlet(g, V: Space) -> np.ndarray:
     return np.ascontiguousarray(vals.reshape(-1))
 
 
+class Polynomial:
+    """A quadratic p(x) = c0 + cx x + cy y + cz z + cxx x^2 + cyy y^2 + czz z^2
+    + cxy xy + cxz xz + cyz yz: the exact solutions of the reference's patch
+    tests (u = x + y, test/assembly_tests.jl:43-118) and the integrands of its
+    integration tests.  Callable on an (n, D) array of points, so it also
+    serves as Dirichlet data for interpolate_dirichlet."""
+
+    NAMES = ("c0", "x", "y", "z", "xx", "yy", "zz", "xy", "xz", "yz")
+
+    def __init__(self, c0=0.0, x=0.0, y=0.0, z=0.0, xx=0.0, yy=0.0, zz=0.0, xy=0.0, xz=0.0, yz=0.0):
+        self.c = np.array([c0, x, y, z, xx, yy, zz, xy, xz, yz], np.float64)
+
+    def __call__(self, X):
+        X = np.asarray(X, np.float64)
+        P = np.zeros((X.shape[0], 3))
+        P[:, :X.shape[1]] = X
+        x, y, z = P[:, 0], P[:, 1], P[:, 2]
+        c = self.c
+        return (c[0] + c[1] * x + c[2] * y + c[3] * z + c[4] * x * x + c[5] * y * y + c[6] * z * z + c[7] * x * y
+                + c[8] * x * z + c[9] * y * z)
+
+
+_INT_KINDS = {"volume": _lib.GT_INT_VOLUME, "poly": _lib.GT_INT_POLY, "field": _lib.GT_INT_FIELD,
+              "l2_norm2": _lib.GT_INT_L2_NORM2, "l2_error2": _lib.GT_INT_L2_ERROR2, "h1_error2": _lib.GT_INT_H1_ERROR2}
+
+
+def integrate(V: Space, kind="volume", uh=None, exact=None, dirichlet_values=None) -> float:
+    """GT.assemble_scalar (src/problems.jl:172-190) for fixed integrands over
+    the cells of V's mesh: "volume" (int 1), "poly" (int p, exact a
+    Polynomial), "field" (int sum_k u_k), "l2_norm2" (int |u|^2),
+    "l2_error2" (int |u - p|^2) and "h1_error2" (int |grad u - grad p|^2).  uh:
+    the free DOF values (e.g. a solution); dirichlet_values: the Dirichlet DOF
+    values (default 0); exact: a Polynomial, or one per component."""
+    k = _INT_KINDS[kind]
+    uf = None if uh is None else np.ascontiguousarray(uh, np.float64)
+    if uf is not None and uf.size != V.num_free_dofs:
+        raise ValueError(f"uh has {uf.size} entries, the space has {V.num_free_dofs} free DOFs")
+    ud = None if dirichlet_values is None else np.ascontiguousarray(dirichlet_values, np.float64)
+    if ud is not None and ud.size != V.num_dirichlet_dofs:
+        raise ValueError(f"dirichlet_values has {ud.size} entries, the space has {V.num_dirichlet_dofs}")
+    pc = None
+    if exact is not None:
+        ps = exact if isinstance(exact, (list, tuple)) else [exact] * (1 if kind == "poly" else V.ncomp)
+        pc = np.ascontiguousarray(np.concatenate([p.c for p in ps]), np.float64)
+    out = C.c_double(0.0)
+    check(V.ctx.h, V.ctx.lib.gt_integrate(V.h, k, _ptr(uf), _ptr(ud), _ptr(pc), C.byref(out)))
+    return out.value
+
+
+def l2_error(V: Space, uh, exact, dirichlet_values=None) -> float:
+    """sqrt(int |u_h - u|^2) for a polynomial exact solution u"""
+    return float(np.sqrt(integrate(V, "l2_error2", uh, exact, dirichlet_values)))
+
+
+def h1_error(V: Space, uh, exact, dirichlet_values=None) -> float:
+    """sqrt(int |grad u_h - grad u|^2) for a polynomial exact solution u"""
+    return float(np.sqrt(integrate(V, "h1_error2", uh, exact, dirichlet_values)))
+
+
 def linear_problem(U: Space, a: Form, l: Source, T=np.float64, V=None, dirichlet_values=None) -> LinearProblem:
     """GT.PartitionedSolvers_linear_problem: A and b assembled on the GPU,
     x = 0.  With dirichlet_values (e.g. interpolate_dirichlet(g, U)) the

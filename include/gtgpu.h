@@ -203,6 +203,30 @@ int gt_matrix_download_csr(gt_matrix* matrix, int64_t* rowptr, int32_t* colind, 
                            float* values_f32);
 int gt_matrix_destroy(gt_matrix* matrix);
 
+/* ---- integrals ----------------------------------------------------------- */
+/* Replaces GT.assemble_scalar (src/problems.jl:172-190) for the integrands
+ * the reference's tests integrate: the sum over the cells of
+ *   GT_INT_VOLUME    int 1
+ *   GT_INT_POLY      int p(x)
+ *   GT_INT_FIELD     int sum_k u_k
+ *   GT_INT_L2_NORM2  int sum_k u_k^2
+ *   GT_INT_L2_ERROR2 int sum_k (u_k - p_k(x))^2
+ *   GT_INT_H1_ERROR2 int sum_k |grad u_k - grad p_k(x)|^2
+ * with the space's quadrature (degree 2 * order).  u: the discrete field,
+ * u_free (num_free_dofs values) and u_dirichlet (the Dirichlet DOF values,
+ * DOF -k -> u_dirichlet[k-1]; NULL = 0); p_k: a quadratic with 10
+ * coefficients (of 1, x, y, z, x^2, y^2, z^2, xy, xz, yz) per component
+ * (one set for GT_INT_POLY).  Host or device inputs; result on the host;
+ * the cell sums are added in a fixed order (bitwise reproducible). */
+#define GT_INT_VOLUME 0
+#define GT_INT_POLY 1
+#define GT_INT_FIELD 2
+#define GT_INT_L2_NORM2 3
+#define GT_INT_L2_ERROR2 4
+#define GT_INT_H1_ERROR2 5
+int gt_integrate(gt_space* space, int kind, const double* u_free, const double* u_dirichlet, const double* poly,
+                 double* result);
+
 /* ---- vector assembly ---------------------------------------------------- */
 /* Replaces GT.assemble_vector(v -> int f*v dOmega, T, V) (src/problems.jl:
  * 244-274, src/assembly.jl:27-73,558-569) with a constant source f (ncomp

@@ -766,7 +766,7 @@ static void elem_matrix(const elem_t* e, int form, double coef, double nu, const
 
 /* Element vector of int f v dOmega with a constant (vector) source f. */
 static void elem_vector(const elem_t* e, const double* f, double coef, const double* X, double* be) {
-  int D = e->D, nn = e->nn, nc = e->ncomp;
+  int nn = e->nn, nc = e->ncomp;
   memset(be, 0, sizeof(double) * e->nloc);
   for (int q = 0; q < e->nq; q++) {
     double invJ[9];
