@@ -220,18 +220,24 @@ __global__ void k_inc_sort(const int64_t* __restrict__ ptr, int32_t* __restrict_
 static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out);
 
 int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc, bool sort) {
+  return build_incidence_arr(ctx, sp->cell_ndofs, sp->mesh->ncells * sp->nn, sp->nfree_nodes, inc_ptr, inc, ninc, sort);
+}
+
+// the incidence lists of any array of n node-level DOF ids (>0 free): row r
+// lists the positions i with dofs[i] == r + 1
+int build_incidence_arr(Ctx* ctx, const int32_t* dofs, int64_t n, int64_t nrows, int64_t** inc_ptr, int32_t** inc,
+                        int64_t* ninc, bool sort) {
   cudaStream_t st = ctx->stream;
-  int64_t nrows = sp->nfree_nodes, n = sp->mesh->ncells * sp->nn;
   int32_t *cnt = nullptr, *rank = nullptr;
   GT_TRY(dalloc(ctx, &cnt, nrows + 1));
   GT_TRY(dalloc(ctx, &rank, n > 0 ? n : 1));
   GT_TRY(dalloc(ctx, inc_ptr, nrows + 1));
   GT_TRY(dalloc(ctx, inc, n));  // upper bound: every (cell, node) free
   GT_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), st));
-  if (n > 0) k_inc_count<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, cnt, rank);
+  if (n > 0) k_inc_count<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(dofs, n, cnt, rank);
   GT_LAUNCH(ctx, "k_inc_count");
   GT_TRY(exclusive_scan_i64(ctx, cnt, *inc_ptr, nrows));
-  if (n > 0) k_inc_fill<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, *inc_ptr, rank, *inc);
+  if (n > 0) k_inc_fill<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(dofs, n, *inc_ptr, rank, *inc);
   GT_LAUNCH(ctx, "k_inc_fill");
   *ninc = -1;  // not read back: the sparsity pass knows the row extents
   if (sort) {

@@ -235,6 +235,9 @@ void sell_release(Matrix* A);
 int number_dofs(Space* sp, int ngroups, const int32_t* groups);
 // incidence lists; sort = false leaves the order to the sparsity count pass
 int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int64_t* ninc, bool sort);
+// the same for any array of n node-level DOF ids (>0 free) over nrows rows
+int build_incidence_arr(Ctx* ctx, const int32_t* dofs, int64_t n, int64_t nrows, int64_t** inc_ptr, int32_t** inc,
+                        int64_t* ninc, bool sort);
 int build_pattern(Matrix* A);
 // keep_tab (optional): receives the tabulation buffer the kernels read
 // instead of freeing it (for launches on a stream other than the main one,

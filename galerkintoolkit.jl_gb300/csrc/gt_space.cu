@@ -530,6 +530,149 @@ __global__ void k_expand_cell_dofs(const int32_t* cnd, int64_t nc, int nn, int n
   out[i] = d > 0 ? (d - 1) * ncomp + k + 1 : -((-d - 1) * ncomp + k + 1);
 }
 
+// ---------------------------------------------------------------------------
+// Boundary integrals: GT.assemble_vector(v -> int g v dGamma) over boundary
+// faces of given groups (the Neumann term of docs/src/src_jl/
+// example_poisson_equation.jl:161-203; src/problems.jl:244-274 with a
+// boundary measure).  The selected boundary faces are found as local faces
+// of their cells (hash of the sorted node ids), listed in (cell, local face)
+// order; each gets its face vector over the closure nodes of the face
+// (Gauss points with order + 1 per direction on quadrilateral faces and
+// edges, the 3-point degree-2 rule on triangles; dGamma = |dx/ds| or
+// |dx/ds x dx/dt| dS); and every free DOF sums its face contributions in
+// that order (incidence lists, as for the cell scatter).
+// ---------------------------------------------------------------------------
+__global__ void k_insert_bfaces(Hash h, const int32_t* bfaces, const int32_t* bgroup, int64_t nb, int nbfv,
+                                const int32_t* groups, int ngroups, uint32_t* err) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= nb) return;
+  if (ngroups > 0) {
+    int k = 0;
+    for (int g = 0; g < ngroups; g++) k |= bgroup[i] == groups[g];
+    if (!k) return;
+  }
+  hash_insert(h, face_key(bfaces + i * nbfv, nbfv, err), err);
+}
+
+__global__ void k_flag_bfaces(Hash h, RefTables t, int64_t nc, const int32_t* cell_nodes, int32_t* flag, uint32_t* err) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nc * t.nlf) return;
+  const int64_t c = r / t.nlf;
+  const int f = (int)(r - c * t.nlf);
+  int32_t v[4];
+  for (int i = 0; i < t.nlfv; i++) v[i] = cell_nodes[c * t.nlv + t.lf_verts[f][i]];
+  flag[r] = hash_find(h, face_key(v, t.nlfv, err)) >= 0 ? 1 : 0;
+}
+
+__global__ void k_compact_bfaces(const int32_t* flag, const int32_t* pos, int64_t n, int32_t* list) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r < n && flag[r]) list[pos[r]] = (int32_t)r;
+}
+
+__device__ __forceinline__ double lagr(int order, int e, double x) {
+  if (order == 1) return e == 0 ? 1.0 - x : x;
+  return e == 0 ? 2.0 * (x - 0.5) * (x - 1.0) : (e == 1 ? -4.0 * x * (x - 1.0) : 2.0 * x * (x - 0.5));
+}
+
+// one thread per selected face: fe[(j * ncl + i) * ncomp + k] = g_k int phi_i
+// dGamma over the closure node i of face j; fdofs[j * ncl + i] its node DOF
+__global__ void k_face_vectors(const int32_t* list, int64_t nsel, RefTables t, int ctype, int order,
+                               const double* coords, const int32_t* cell_nodes, const int32_t* cnd, const double* g,
+                               int ncomp, double* fe, int32_t* fdofs) {
+  const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (j >= nsel) return;
+  const int64_t id = list[j], c = id / t.nlf;
+  const int f = (int)(id - c * t.nlf), D = t.D, ncl = t.nclosure;
+  double X[8][3];
+  for (int v = 0; v < t.nlv; v++)
+    for (int d = 0; d < 3; d++) X[v][d] = d < D ? coords[(int64_t)cell_nodes[c * t.nlv + v] * D + d] : 0.0;
+  double acc[9];
+  for (int i = 0; i < ncl; i++) {
+    acc[i] = 0.0;
+    fdofs[j * ncl + i] = cnd[c * t.nn + t.closure[f][i]];
+  }
+  if (ctype == GT_TET4) {
+    // P1 on a flat triangle: the 3-point rule at barycentric (2/3, 1/6, 1/6)
+    // and permutations, weights 1/6 on the unit right triangle
+    const int a0 = t.lf_verts[f][0], a1 = t.lf_verts[f][1], a2 = t.lf_verts[f][2];
+    double e1[3], e2[3], n[3];
+    for (int d = 0; d < 3; d++) { e1[d] = X[a1][d] - X[a0][d]; e2[d] = X[a2][d] - X[a0][d]; }
+    n[0] = e1[1] * e2[2] - e1[2] * e2[1];
+    n[1] = e1[2] * e2[0] - e1[0] * e2[2];
+    n[2] = e1[0] * e2[1] - e1[1] * e2[0];
+    const double jac = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int q = 0; q < 3; q++)
+      for (int i = 0; i < 3; i++) acc[i] += (1.0 / 6.0) * jac * (i == q ? 2.0 / 3.0 : 1.0 / 6.0);
+  } else {
+    const int dir = D == 2 ? (f < 2 ? 1 : 0) : 2 - f / 2, side = f & 1;
+    int fr[2], nfr = 0;
+    for (int d = 0; d < D; d++)
+      if (d != dir) fr[nfr++] = d;
+    const int n1 = order + 1, m = order + 1;
+    double gp[3], gw[3];
+    if (n1 == 2) {
+      const double s = 0.5 / sqrt(3.0);
+      gp[0] = 0.5 - s; gp[1] = 0.5 + s; gw[0] = gw[1] = 0.5;
+    } else {
+      const double s = 0.5 * sqrt(0.6);
+      gp[0] = 0.5 - s; gp[1] = 0.5; gp[2] = 0.5 + s;
+      gw[0] = 5.0 / 18.0; gw[1] = 8.0 / 18.0; gw[2] = 5.0 / 18.0;
+    }
+    const int nq = D == 2 ? n1 : n1 * n1;
+    for (int q = 0; q < nq; q++) {
+      double xi[3] = {0, 0, 0};
+      xi[dir] = (double)side;
+      xi[fr[0]] = gp[q % n1];
+      double w = gw[q % n1];
+      if (D == 3) {
+        xi[fr[1]] = gp[q / n1];
+        w *= gw[q / n1];
+      }
+      // tangents dx/dxi_a of the multilinear geometry map
+      double tg[2][3] = {{0, 0, 0}, {0, 0, 0}};
+      for (int v = 0; v < t.nlv; v++) {
+        for (int a = 0; a < nfr; a++) {
+          double dn = 1.0;
+          for (int d = 0; d < D; d++) {
+            const int bit = (v >> d) & 1;
+            dn *= d == fr[a] ? (bit ? 1.0 : -1.0) : (bit ? xi[d] : 1.0 - xi[d]);
+          }
+          for (int d = 0; d < D; d++) tg[a][d] += X[v][d] * dn;
+        }
+      }
+      double jac;
+      if (D == 2) {
+        jac = sqrt(tg[0][0] * tg[0][0] + tg[0][1] * tg[0][1]);
+      } else {
+        const double cx = tg[0][1] * tg[1][2] - tg[0][2] * tg[1][1], cy = tg[0][2] * tg[1][0] - tg[0][0] * tg[1][2],
+                     cz = tg[0][0] * tg[1][1] - tg[0][1] * tg[1][0];
+        jac = sqrt(cx * cx + cy * cy + cz * cz);
+      }
+      for (int i = 0; i < ncl; i++) {
+        const int k = t.closure[f][i];
+        const int e[3] = {k % m, (k / m) % m, k / (m * m)};
+        double phi = 1.0;
+        for (int d = 0; d < D; d++) phi *= lagr(order, e[d], xi[d]);
+        acc[i] += w * jac * phi;
+      }
+    }
+  }
+  for (int i = 0; i < ncl; i++)
+    for (int k = 0; k < ncomp; k++) fe[(j * ncl + i) * ncomp + k] = g[k] * acc[i];
+}
+
+// b[r] (+)= the face contributions of free node r, in (cell, local face) order
+__global__ void k_gather_bvec(const int64_t* inc_ptr, const int32_t* inc, int64_t nrows, const double* fe, int ncomp,
+                              double* b, int accumulate) {
+  const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (r >= nrows) return;
+  for (int k = 0; k < ncomp; k++) {
+    double s = 0.0;
+    for (int64_t e = inc_ptr[r]; e < inc_ptr[r + 1]; e++) s += fe[(int64_t)inc[e] * ncomp + k];
+    b[r * ncomp + k] = accumulate ? b[r * ncomp + k] + s : s;
+  }
+}
+
 }  // namespace gt
 
 using namespace gt;
@@ -668,6 +811,102 @@ int gt_space_cell_dofs(const gt_space* sp, int32_t* out) {
     if (e != cudaSuccess) s = check_cuda(ctx, e, "gt_space_cell_dofs");
   }
   dfree(ctx, tmp);
+  return s;
+}
+
+int gt_assemble_boundary_vector(gt_space* sp, int ngroups, const int32_t* groups, const double* g, double* b,
+                                int accumulate) {
+  if (!sp || !g || !b) return GT_ERR_INVALID;
+  Ctx* ctx = sp->mesh->ctx;
+  Mesh* M = sp->mesh;
+  cudaSetDevice(ctx->device);
+  cudaStream_t st = ctx->stream;
+  const RefTables t = make_ref_tables(M->ctype, sp->order);
+  const int64_t nc = M->ncells, nflag = nc * t.nlf, nb = sp->nfree_nodes * sp->ncomp;
+  const bool dev_b = [&] {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, b) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+  }();
+  double* bd = b;
+  if (!dev_b) {
+    GT_TRY(dalloc(ctx, &bd, nb > 0 ? nb : 1));
+    if (accumulate && nb > 0) GT_TRY(copy_in(ctx, bd, b, nb));
+  }
+  int32_t *dgroups = nullptr, *flag = nullptr, *pos = nullptr, *list = nullptr, *fdofs = nullptr, *inc = nullptr;
+  double *dg = nullptr, *fe = nullptr;
+  int64_t* inc_ptr = nullptr;
+  int64_t nsel = 0, ninc = 0;
+  const int ng = ngroups > 0 ? ngroups : 0;
+  mesh_wait_coords(M);
+  int s = dalloc(ctx, &dgroups, ng + 1);
+  if (s == GT_OK && ng > 0) s = copy_in(ctx, dgroups, groups, ng);
+  if (s == GT_OK) s = dalloc(ctx, &dg, sp->ncomp);
+  if (s == GT_OK) s = copy_in(ctx, dg, g, sp->ncomp);
+  if (s == GT_OK) s = dalloc(ctx, &flag, nflag + 1);
+  if (s == GT_OK) s = dalloc(ctx, &pos, nflag + 1);
+  if (s == GT_OK && M->nbfaces > 0 && nflag > 0) {
+    HashBuf hb;
+    s = hb.alloc(ctx, M->nbfaces);
+    if (s == GT_OK) {
+      k_insert_bfaces<<<GT_KC(ctx, grid_for(M->nbfaces, 256)), 256, 0, st>>>(hb.h, M->bfaces, M->bgroup, M->nbfaces,
+                                                                             M->nbfv, dgroups, ng, ctx->d_err);
+      k_flag_bfaces<<<GT_KC(ctx, grid_for(nflag, 256)), 256, 0, st>>>(hb.h, t, nc, M->cell_nodes, flag, ctx->d_err);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) s = check_cuda(ctx, e, "k_flag_bfaces");
+    }
+    if (s == GT_OK) s = exclusive_scan_i32(ctx, flag, pos, nflag);
+    if (s == GT_OK) {
+      int32_t tot = 0;
+      s = copy_out(ctx, &tot, pos + nflag, 1);
+      if (s == GT_OK) {
+        cudaError_t e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) s = check_cuda(ctx, e, "boundary faces");
+      }
+      nsel = tot;
+    }
+    hb.release(ctx);
+  }
+  if (s == GT_OK && nsel > 0) {
+    s = dalloc(ctx, &list, nsel);
+    if (s == GT_OK) s = dalloc(ctx, &fdofs, nsel * t.nclosure);
+    if (s == GT_OK) s = dalloc(ctx, &fe, nsel * t.nclosure * sp->ncomp);
+    if (s == GT_OK) {
+      k_compact_bfaces<<<GT_KC(ctx, grid_for(nflag, 256)), 256, 0, st>>>(flag, pos, nflag, list);
+      k_face_vectors<<<GT_KC(ctx, grid_for(nsel, 128)), 128, 0, st>>>(list, nsel, t, M->ctype, sp->order, M->coords,
+                                                                      M->cell_nodes, sp->cell_ndofs, dg, sp->ncomp, fe,
+                                                                      fdofs);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) s = check_cuda(ctx, e, "k_face_vectors");
+    }
+    if (s == GT_OK) s = build_incidence_arr(ctx, fdofs, nsel * t.nclosure, sp->nfree_nodes, &inc_ptr, &inc, &ninc, true);
+  }
+  if (s == GT_OK && sp->nfree_nodes > 0) {
+    if (nsel > 0) {
+      k_gather_bvec<<<GT_KC(ctx, grid_for(sp->nfree_nodes, 256)), 256, 0, st>>>(inc_ptr, inc, sp->nfree_nodes, fe,
+                                                                                sp->ncomp, bd, accumulate);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) s = check_cuda(ctx, e, "k_gather_bvec");
+    } else if (!accumulate) {
+      cudaError_t e = cudaMemsetAsync(bd, 0, sizeof(double) * nb, st);
+      if (e != cudaSuccess) s = check_cuda(ctx, e, "memset");
+    }
+  }
+  if (s == GT_OK && !dev_b && nb > 0) s = copy_out(ctx, b, bd, nb);
+  if (s == GT_OK) s = device_error_status(ctx, "assemble_boundary_vector");  // synchronises
+  if (!dev_b) dfree(ctx, bd);
+  dfree(ctx, dgroups);
+  dfree(ctx, dg);
+  dfree(ctx, flag);
+  dfree(ctx, pos);
+  dfree(ctx, list);
+  dfree(ctx, fdofs);
+  dfree(ctx, fe);
+  dfree(ctx, inc_ptr);
+  dfree(ctx, inc);
   return s;
 }
 

@@ -81,6 +81,7 @@ SIGNATURES = [
     ("gt_matrix_destroy", I32, [P]),
     ("gt_assemble_vector", I32, [P, P, P, P]),
     ("gt_integrate", I32, [P, I32, P, P, P, P]),
+    ("gt_assemble_boundary_vector", I32, [P, I32, P, P, P, I32]),
     ("gt_solve", I32, [P, P, P, DBL, I32, I32, C.POINTER(SolveInfo)]),
     ("gt_spmv", I32, [P, P, P]),
     ("gt_batch_create", I32, [P, I32, P, C.POINTER(P)]),

@@ -403,6 +403,20 @@ def assemble_vector(l: Source, T, V: Space, out=None):
     return b
 
 
+def assemble_boundary_vector(g, gamma: Domain, V: Space, out=None, accumulate=False):
+    """GT.assemble_vector(v -> int g v dGamma, T, V) over the boundary faces
+    of gamma (boundary(mesh, groups)): the Neumann term, g a constant (or
+    ncomp constants on a vector space).  With accumulate, adds to out."""
+    if gamma.dim != V.mesh.D - 1:
+        raise NotImplementedError("boundary integrals over the (D-1)-faces of the boundary only")
+    ng, groups = gamma.groups()
+    gv = np.ascontiguousarray(np.broadcast_to(np.asarray(g, np.float64), (V.ncomp,)))
+    b = out if out is not None else np.zeros(V.num_free_dofs, np.float64)
+    check(V.ctx.h, V.ctx.lib.gt_assemble_boundary_vector(V.h, ng, _ptr(groups), _ptr(gv), _ptr(b),
+                                                         1 if accumulate else 0))
+    return b
+
+
 def assemble_matrix_and_vector(a: Form, l: Source, T, U: Space, V: Space | None = None, out=None):
     """GT.assemble_matrix_and_vector(a, l, T, U, V) -> (A, b)."""
     _check_form(a)
@@ -504,11 +518,21 @@ def h1_error(V: Space, uh, exact, dirichlet_values=None) -> float:
     return float(np.sqrt(integrate(V, "h1_error2", uh, exact, dirichlet_values)))
 
 
-def linear_problem(U: Space, a: Form, l: Source, T=np.float64, V=None, dirichlet_values=None) -> LinearProblem:
+def linear_problem(U: Space, a: Form, l: Source, T=np.float64, V=None, dirichlet_values=None,
+                   neumann=None) -> LinearProblem:
     """GT.PartitionedSolvers_linear_problem: A and b assembled on the GPU,
     x = 0.  With dirichlet_values (e.g. interpolate_dirichlet(g, U)) the
     Dirichlet lift b -= Ad * xd is applied in the same pass
-    (src/problems.jl:439-453); without, homogeneous Dirichlet data."""
+    (src/problems.jl:439-453); without, homogeneous Dirichlet data.
+    neumann: (g, boundary(mesh, groups)) pairs whose boundary terms
+    int g v dGamma are added to b."""
+    lp = _linear_problem(U, a, l, T, V, dirichlet_values)
+    for g, gamma in (neumann or ()):
+        assemble_boundary_vector(g, gamma, U, out=lp.b, accumulate=True)
+    return lp
+
+
+def _linear_problem(U: Space, a: Form, l: Source, T, V, dirichlet_values) -> LinearProblem:
     if dirichlet_values is None:
         A, b = assemble_matrix_and_vector(a, l, T, U, V)
         return LinearProblem(A, b, np.zeros_like(b))

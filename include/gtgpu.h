@@ -232,6 +232,15 @@ int gt_integrate(gt_space* space, int kind, const double* u_free, const double* 
  * 244-274, src/assembly.jl:27-73,558-569) with a constant source f (ncomp
  * values) times an optional per-cell coefficient.  b: num_free_dofs FP64. */
 int gt_assemble_vector(gt_space* space, const double* f, const double* cell_coef, double* b);
+/* Replaces GT.assemble_vector(v -> int g v dGamma, T, V) over boundary faces
+ * (the Neumann term of docs/src/src_jl/example_poisson_equation.jl:161-203;
+ * src/problems.jl:244-274 with a boundary measure): a constant g (ncomp
+ * values) on the boundary faces of the groups (k of "(D-1)-face-k"; ngroups
+ * < 0: every boundary face).  b: num_free_dofs FP64 (host or device);
+ * accumulate != 0 adds to b.  Each DOF sums its faces in (cell, local face)
+ * order. */
+int gt_assemble_boundary_vector(gt_space* space, int ngroups, const int32_t* groups, const double* g, double* b,
+                                int accumulate);
 
 /* ---- solve -------------------------------------------------------------- */
 /* Replaces PS.solve(PS.LinearAlgebra_lu(GT.PartitionedSolvers_linear_problem
