@@ -49,7 +49,8 @@ inline TabLayout tab_layout(int ctype, int order) {
   L.nlv = ctype == GT_QUAD4 ? 4 : (ctype == GT_HEX8 ? 8 : 4);
   L.nn = space_nodes(ctype, order);
   int n1 = ctype == GT_TET4 ? 0 : order + 1;  // Gauss points per direction for degree 2*order
-  L.nq = ctype == GT_TET4 ? 4 : (L.D == 2 ? n1 * n1 : n1 * n1 * n1);
+  // tets: the 4-point degree-2 rule (P1) or the 11-point degree-4 rule (P2)
+  L.nq = ctype == GT_TET4 ? (order == 2 ? 11 : 4) : (L.D == 2 ? n1 * n1 : n1 * n1 * n1);
   L.off_w = 0;
   L.off_gg = L.nq;
   L.off_sv = L.off_gg + L.nq * L.nlv * L.D;
@@ -75,7 +76,19 @@ __global__ void k_tabulate(int ctype, int order, TabLayout L, double* tab) {
   int q = threadIdx.x;
   if (q >= L.nq) return;
   double x[3] = {0, 0, 0}, w;
-  if (ctype == GT_TET4) {
+  if (ctype == GT_TET4 && order == 2) {
+    // Keast's 11-point rule of degree 4 on the unit tetrahedron (the
+    // reference's strang_quadrature_4, src/quadrature.jl:554-590): the
+    // centroid (negative weight), the 4 points (11/14, 1/14, 1/14) and
+    // permutations plus (1/14,1/14,1/14), and the 6 points with two
+    // coordinates (1 + sqrt(5/14))/4 and one (1 - sqrt(5/14))/4 or the reverse
+    const double r = sqrt(5.0 / 14.0), a = 0.25 * (1.0 + r), b = 0.25 * (1.0 - r);
+    const double f = 11.0 / 14.0, g = 1.0 / 14.0;
+    const double P[11][3] = {{0.25, 0.25, 0.25}, {f, g, g}, {g, f, g}, {g, g, f}, {g, g, g}, {a, a, b},
+                             {a, b, a},          {a, b, b}, {b, a, a}, {b, a, b}, {b, b, a}};
+    for (int d = 0; d < 3; d++) x[d] = P[q][d];
+    w = q == 0 ? -74.0 / 5625.0 : (q < 5 ? 343.0 / 45000.0 : 56.0 / 2250.0);
+  } else if (ctype == GT_TET4) {
     const double a = 0.5854101966249685, b = 0.1381966011250105;
     x[0] = x[1] = x[2] = b;
     if (q > 0) x[q - 1] = a;
@@ -99,15 +112,35 @@ __global__ void k_tabulate(int ctype, int order, TabLayout L, double* tab) {
   // geometry map gradients (P1 / Q1)
   if (ctype == GT_TET4) {
     const double gr[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
-    for (int n = 0; n < 4; n++)
-      for (int d = 0; d < 3; d++) {
-        tab[L.off_gg + (q * 4 + n) * 3 + d] = gr[n][d];
-        tab[L.off_sg + (q * 4 + n) * 3 + d] = gr[n][d];
-      }
-    double v[4] = {1.0 - x[0] - x[1] - x[2], x[0], x[1], x[2]};
+    const double v[4] = {1.0 - x[0] - x[1] - x[2], x[0], x[1], x[2]};  // barycentric coordinates
     for (int n = 0; n < 4; n++) {
-      tab[L.off_sv + q * 4 + n] = v[n];
       tab[L.off_gv + q * 4 + n] = v[n];
+      for (int d = 0; d < 3; d++) tab[L.off_gg + (q * 4 + n) * 3 + d] = gr[n][d];
+    }
+    if (order == 1) {
+      for (int n = 0; n < 4; n++) {
+        tab[L.off_sv + q * 4 + n] = v[n];
+        for (int d = 0; d < 3; d++) tab[L.off_sg + (q * 4 + n) * 3 + d] = gr[n][d];
+      }
+      return;
+    }
+    // P2 in barycentric form: vertex i -> l_i (2 l_i - 1), edge (i, j) ->
+    // 4 l_i l_j, at the node order of the exponents (first index fastest)
+    const int vi[10] = {0, -1, 1, -1, -1, 2, -1, -1, -1, 3};
+    const int ei[10][2] = {{0, 0}, {0, 1}, {0, 0}, {0, 2}, {1, 2}, {0, 0}, {0, 3}, {1, 3}, {2, 3}, {0, 0}};
+    for (int n = 0; n < 10; n++) {
+      double val, g[3];
+      if (vi[n] >= 0) {
+        const int i = vi[n];
+        val = v[i] * (2.0 * v[i] - 1.0);
+        for (int d = 0; d < 3; d++) g[d] = (4.0 * v[i] - 1.0) * gr[i][d];
+      } else {
+        const int i = ei[n][0], j = ei[n][1];
+        val = 4.0 * v[i] * v[j];
+        for (int d = 0; d < 3; d++) g[d] = 4.0 * (v[j] * gr[i][d] + v[i] * gr[j][d]);
+      }
+      tab[L.off_sv + q * 10 + n] = val;
+      for (int d = 0; d < 3; d++) tab[L.off_sg + (q * 10 + n) * 3 + d] = g[d];
     }
     return;
   }
@@ -475,7 +508,7 @@ template <int NN>
 static int launch_pattern(Matrix* A, int maxinc) {
   // slot width of the count pass: P1/Q1/Q2-quad rows have <= 27 columns,
   // Q2-hex rows up to 125
-  constexpr int S = NN == 27 ? 128 : 32;
+  constexpr int S = NN >= 10 ? 128 : 32;  // P2-tet rows: up to ~70 columns
   const Space* sp = A->space;
   Ctx* ctx = sp->mesh->ctx;
   cudaStream_t st = ctx->stream;
@@ -548,6 +581,7 @@ int build_pattern(Matrix* A) {
     case 4: return launch_pattern<4>(A, maxinc);
     case 8: return launch_pattern<8>(A, maxinc);
     case 9: return launch_pattern<9>(A, maxinc);
+    case 10: return launch_pattern<10>(A, maxinc);
     case 27: return launch_pattern<27>(A, maxinc);
   }
   return set_error(ctx, GT_ERR_UNSUPPORTED, "element not supported");
@@ -884,7 +918,7 @@ template <class T>
 static int elements_T(const Space* sp, int form, const double* coef, double nu, const double* tab, const TabLayout& L,
                       T* Ke, double* be, const double* f, const double* scoef, int want_matrix) {
   int ct = sp->mesh->ctype, o = sp->order;
-  if (ct == GT_TET4 && sp->ncomp == 1 && (form == GT_LAPLACE || form == GT_MASS)) {
+  if (ct == GT_TET4 && o == 1 && sp->ncomp == 1 && (form == GT_LAPLACE || form == GT_MASS)) {
     Ctx* ctx = ctx_of(sp);
     int64_t nc = sp->mesh->ncells;
     double* consts = const_cast<double*>(tab) + L.off_k;  // inside the tabulation buffer: no allocation
@@ -899,6 +933,9 @@ static int elements_T(const Space* sp, int form, const double* coef, double nu, 
     GT_LAUNCH(ctx, "k_elements_p1");
     return GT_OK;
   }
+  // P2 tets: the map is affine but the shape gradients vary over the cell, so
+  // they are kept per quadrature point (the non-affine form of the kernel)
+  if (ct == GT_TET4 && o == 2) return dispatch_form<3, 4, 10, 11, 8, false, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
   if (ct == GT_TET4) return dispatch_form<3, 4, 4, 4, 128, true, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
   if (ct == GT_QUAD4 && o == 1) return dispatch_form<2, 4, 4, 4, 32, false, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
   if (ct == GT_QUAD4 && o == 2) return dispatch_form<2, 4, 9, 9, 8, false, T>(sp, form, coef, nu, tab, L, Ke, be, f, scoef, want_matrix);
@@ -1092,7 +1129,8 @@ static int integrate(const Space* sp, int kind, const double* uf, const double* 
   int s = dalloc(ctx, &cv, nc);
   if (s == GT_OK) s = dalloc(ctx, &part, nb);
   if (s == GT_OK) {
-    if (ct == GT_TET4) launch_integrate<3, 4, 4>(sp, tab, L, kind, uf, ud, poly, cv);
+    if (ct == GT_TET4 && o == 2) launch_integrate<3, 4, 10>(sp, tab, L, kind, uf, ud, poly, cv);
+    else if (ct == GT_TET4) launch_integrate<3, 4, 4>(sp, tab, L, kind, uf, ud, poly, cv);
     else if (ct == GT_QUAD4 && o == 1) launch_integrate<2, 4, 4>(sp, tab, L, kind, uf, ud, poly, cv);
     else if (ct == GT_QUAD4) launch_integrate<2, 4, 9>(sp, tab, L, kind, uf, ud, poly, cv);
     else if (o == 1) launch_integrate<3, 8, 8>(sp, tab, L, kind, uf, ud, poly, cv);

@@ -283,7 +283,7 @@ inline int grid_for(int64_t n, int block) {
 }
 
 inline int space_nodes(int ctype, int order) {
-  if (ctype == GT_TET4) return 4;
+  if (ctype == GT_TET4) return order == 2 ? 10 : 4;
   int D = ctype == GT_QUAD4 ? 2 : 3;
   int m = order + 1;
   return D == 2 ? m * m : m * m * m;

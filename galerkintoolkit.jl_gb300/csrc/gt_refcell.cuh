@@ -15,6 +15,7 @@ struct RefTables {
   int D, nlv, nn;          // dimension, vertices per cell, space nodes per cell
   int nle, nlf, nlfv;      // local edges, local (D-1)-faces, vertices per (D-1)-face
   int nclosure;            // space nodes on one (D-1)-face
+  int face_nodes, cell_node;  // order 2: nodes owned by 2-faces (hex: 1 each) / the cell (cubes: 1)
   int8_t vnode[8];         // space node of local vertex
   int8_t enode[12];        // space node at the midpoint of local edge (Q2)
   int8_t fnode[6];         // space node at the centre of local face (Q2 hex)
@@ -35,11 +36,39 @@ inline RefTables make_ref_tables(int ctype, int order) {
   static const int TE[6][2] = {{1, 2}, {1, 3}, {2, 3}, {1, 4}, {2, 4}, {3, 4}};
   RefTables t{};
   if (ctype == 3 /*TET4*/) {
-    t.D = 3; t.nlv = 4; t.nn = 4; t.nle = 6; t.nlf = 4; t.nlfv = 3; t.nclosure = 3;
-    for (int v = 0; v < 4; v++) t.vnode[v] = (int8_t)v;
+    t.D = 3; t.nlv = 4; t.nle = 6; t.nlf = 4; t.nlfv = 3;
     for (int e = 0; e < 6; e++) { t.le_verts[e][0] = TE[e][0] - 1; t.le_verts[e][1] = TE[e][1] - 1; }
     for (int f = 0; f < 4; f++)
-      for (int i = 0; i < 3; i++) { t.lf_verts[f][i] = TF[f][i] - 1; t.closure[f][i] = TF[f][i] - 1; }
+      for (int i = 0; i < 3; i++) t.lf_verts[f][i] = TF[f][i] - 1;
+    if (order == 1) {
+      t.nn = 4; t.nclosure = 3;
+      for (int v = 0; v < 4; v++) t.vnode[v] = (int8_t)v;
+      for (int f = 0; f < 4; f++)
+        for (int i = 0; i < 3; i++) t.closure[f][i] = TF[f][i] - 1;
+      return t;
+    }
+    // P2: nodes are the exponents (a, b, c), a + b + c <= 2, first index
+    // fastest: (000) (100) (200) (010) (110) (020) (001) (101) (011) (002)
+    // -- vertices at nodes 0, 2, 5, 9, the midpoints of the local edges at
+    // 1, 3, 4, 6, 7, 8 (edges 12, 13, 23, 14, 24, 34)
+    static const int PV[4] = {0, 2, 5, 9}, PE[6] = {1, 3, 4, 6, 7, 8};
+    t.nn = 10; t.nclosure = 6;
+    for (int v = 0; v < 4; v++) t.vnode[v] = (int8_t)PV[v];
+    for (int e = 0; e < 6; e++) t.enode[e] = (int8_t)PE[e];
+    for (int f = 0; f < 4; f++) {
+      // closure of face f: its 3 vertex nodes and the nodes of its 3 edges, ascending
+      int nodes[6], cnt = 0;
+      for (int i = 0; i < 3; i++) nodes[cnt++] = PV[TF[f][i] - 1];
+      for (int e = 0; e < 6; e++) {
+        int in = 0;
+        for (int i = 0; i < 3; i++) in += (TE[e][0] == TF[f][i]) + (TE[e][1] == TF[f][i]);
+        if (in == 2) nodes[cnt++] = PE[e];
+      }
+      for (int i = 0; i < 6; i++)
+        for (int j = i + 1; j < 6; j++)
+          if (nodes[j] < nodes[i]) { int tmp = nodes[i]; nodes[i] = nodes[j]; nodes[j] = tmp; }
+      for (int i = 0; i < 6; i++) t.closure[f][i] = (int8_t)nodes[i];
+    }
     return t;
   }
   int D = ctype == 1 ? 2 : 3, m = order + 1;
@@ -72,7 +101,11 @@ inline RefTables make_ref_tables(int ctype, int order) {
     }
     t.nclosure = cnt;
   }
-  if (order == 2) t.cnode = (int8_t)(D == 2 ? qn(1, 1, 0) : qn(1, 1, 1));
+  if (order == 2) {
+    t.cnode = (int8_t)(D == 2 ? qn(1, 1, 0) : qn(1, 1, 1));
+    t.face_nodes = D == 3 ? 1 : 0;
+    t.cell_node = 1;
+  }
   return t;
 }
 

@@ -306,9 +306,9 @@ __global__ void k_cell_node_dofs(RefTables t, int order, int64_t nc, const int32
   for (int v = 0; v < t.nlv; v++) o[t.vnode[v]] = cverts[c * t.nlv + v];
   if (order == 2) {
     for (int e = 0; e < t.nle; e++) o[t.enode[e]] = (int32_t)(nverts + cedges[c * t.nle + e]);
-    if (t.D == 3)
+    if (t.face_nodes)
       for (int f = 0; f < 6; f++) o[t.fnode[f]] = (int32_t)(nverts + nedges + cfaces[c * 6 + f]);
-    o[t.cnode] = (int32_t)(nverts + nedges + nfaces + c + 1);
+    if (t.cell_node) o[t.cnode] = (int32_t)(nverts + nedges + nfaces + c + 1);
   }
 }
 
@@ -429,6 +429,36 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
       s = number_faces(ctx, cverts, nc, 4, 4, 2, lq, pv, M->nbfaces, cedges, nullptr, &nedges);
       dfree(ctx, pv);
       GT_TRY(s);
+    } else if (M->ctype == GT_TET4) {
+      // P2 tets: triangles numbered over the tets (parents: the boundary
+      // triangles), edges over the triangles (parents: the boundary 1-faces),
+      // then each tet's 6 edges looked up (create_face_boundary!,
+      // src/topology.jl:1099-1125, generates d-faces from the (d+1)-faces)
+      LocalFaces ltf{}, ltri{}, lte{};
+      for (int f = 0; f < 4; f++)
+        for (int i = 0; i < 3; i++) ltf.v[f][i] = t.lf_verts[f][i];
+      static const int TRE[3][2] = {{0, 1}, {0, 2}, {1, 2}};  // edges of the unit triangle, src/domain.jl:413-424
+      for (int e = 0; e < 3; e++) { ltri.v[e][0] = TRE[e][0]; ltri.v[e][1] = TRE[e][1]; }
+      for (int e = 0; e < 6; e++) { lte.v[e][0] = t.le_verts[e][0]; lte.v[e][1] = t.le_verts[e][1]; }
+      int32_t *pf = nullptr, *pe = nullptr, *fverts = nullptr, *fedges = nullptr, *everts = nullptr;
+      GT_TRY(dalloc(ctx, &pf, M->nbfaces * 3 + 1));
+      GT_TRY(dalloc(ctx, &pe, M->nbedges * 2 + 1));
+      if (M->nbfaces > 0)
+        k_map_vertices<<<GT_KC(ctx, grid_for(M->nbfaces * 3, 256)), 256, 0, st>>>(M->bfaces, M->nbfaces * 3, node_vertex, pf);
+      if (M->nbedges > 0)
+        k_map_vertices<<<GT_KC(ctx, grid_for(M->nbedges * 2, 256)), 256, 0, st>>>(M->bedges, M->nbedges * 2, node_vertex, pe);
+      GT_LAUNCH(ctx, "k_map_vertices");
+      GT_TRY(dalloc(ctx, &cfaces, nc * 4));
+      GT_TRY(number_faces(ctx, cverts, nc, 4, 4, 3, ltf, pf, M->nbfaces, cfaces, &fverts, &nfaces));
+      GT_TRY(dalloc(ctx, &fedges, nfaces * 3));
+      GT_TRY(number_faces(ctx, fverts, nfaces, 3, 3, 2, ltri, pe, M->nbedges, fedges, &everts, &nedges));
+      GT_TRY(dalloc(ctx, &cedges, nc * 6));
+      GT_TRY(lookup_faces(ctx, everts, nedges, 2, cverts, nc, 4, 6, lte, cedges));
+      dfree(ctx, pf);
+      dfree(ctx, pe);
+      dfree(ctx, fverts);
+      dfree(ctx, fedges);
+      dfree(ctx, everts);
     } else {
       for (int f = 0; f < 6; f++)
         for (int i = 0; i < 4; i++) lh.v[f][i] = t.lf_verts[f][i];
@@ -456,7 +486,9 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
     }
   }
   // ---- node dofs before the split
-  int64_t nnodes_sp = nverts + (sp->order == 2 ? nedges + nfaces + nc : 0);
+  // node dofs: vertices, then (order 2) edges, 2-faces and cells that own a node
+  if (!t.face_nodes) nfaces = 0;
+  int64_t nnodes_sp = nverts + (sp->order == 2 ? nedges + nfaces + (t.cell_node ? nc : 0) : 0);
   GT_TRY(dalloc(ctx, &sp->cell_ndofs, nc * t.nn));
   k_cell_node_dofs<<<GT_KC(ctx, grid_for(nc, 128)), 128, 0, st>>>(t, sp->order, nc, cverts, cedges, cfaces, nverts, nedges, nfaces,
                                                        sp->cell_ndofs);
@@ -592,8 +624,11 @@ __global__ void k_face_vectors(const int32_t* list, int64_t nsel, RefTables t, i
     fdofs[j * ncl + i] = cnd[c * t.nn + t.closure[f][i]];
   }
   if (ctype == GT_TET4) {
-    // P1 on a flat triangle: the 3-point rule at barycentric (2/3, 1/6, 1/6)
-    // and permutations, weights 1/6 on the unit right triangle
+    // a flat triangle: the 3-point degree-2 rule at face-barycentric
+    // (2/3, 1/6, 1/6) and permutations, weights 1/6 on the unit right
+    // triangle; the cell's basis (P1: barycentric l_i; P2: l_i (2 l_i - 1) at
+    // the vertex nodes 0, 2, 5, 9 and 4 l_i l_j at the edge nodes) at the
+    // point's cell-barycentric coordinates
     const int a0 = t.lf_verts[f][0], a1 = t.lf_verts[f][1], a2 = t.lf_verts[f][2];
     double e1[3], e2[3], n[3];
     for (int d = 0; d < 3; d++) { e1[d] = X[a1][d] - X[a0][d]; e2[d] = X[a2][d] - X[a0][d]; }
@@ -601,8 +636,20 @@ __global__ void k_face_vectors(const int32_t* list, int64_t nsel, RefTables t, i
     n[1] = e1[2] * e2[0] - e1[0] * e2[2];
     n[2] = e1[0] * e2[1] - e1[1] * e2[0];
     const double jac = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-    for (int q = 0; q < 3; q++)
-      for (int i = 0; i < 3; i++) acc[i] += (1.0 / 6.0) * jac * (i == q ? 2.0 / 3.0 : 1.0 / 6.0);
+    for (int q = 0; q < 3; q++) {
+      double l[4] = {0, 0, 0, 0};
+      for (int i = 0; i < 3; i++) l[t.lf_verts[f][i]] = i == q ? 2.0 / 3.0 : 1.0 / 6.0;
+      double phi[10];
+      if (order == 1) {
+        for (int i = 0; i < 4; i++) phi[i] = l[i];
+      } else {
+        const int vi[4] = {0, 2, 5, 9};
+        const int ep[6][2] = {{0, 1}, {0, 2}, {1, 2}, {0, 3}, {1, 3}, {2, 3}}, en[6] = {1, 3, 4, 6, 7, 8};
+        for (int i = 0; i < 4; i++) phi[vi[i]] = l[i] * (2.0 * l[i] - 1.0);
+        for (int e = 0; e < 6; e++) phi[en[e]] = 4.0 * l[ep[e][0]] * l[ep[e][1]];
+      }
+      for (int i = 0; i < ncl; i++) acc[i] += (1.0 / 6.0) * jac * phi[t.closure[f][i]];
+    }
   } else {
     const int dir = D == 2 ? (f < 2 ? 1 : 0) : 2 - f / 2, side = f & 1;
     int fr[2], nfr = 0;
@@ -764,7 +811,6 @@ int gt_space_create(gt_mesh* M, int order, int ncomp, int ngroups, const int32_t
   *out = nullptr;
   Ctx* ctx = M->ctx;
   if (order != 1 && order != 2) return set_error(ctx, GT_ERR_UNSUPPORTED, "order must be 1 or 2");
-  if (M->ctype == GT_TET4 && order != 1) return set_error(ctx, GT_ERR_UNSUPPORTED, "TET4 supports P1 only");
   if (ncomp != 1 && ncomp != M->D) return set_error(ctx, GT_ERR_UNSUPPORTED, "ncomp must be 1 or the dimension");
   if (ngroups > 0 && !groups) return set_error(ctx, GT_ERR_INVALID, "groups is NULL");
   if (ngroups != 0 && M->nbfaces > 0 && M->ctype == GT_QUAD4 && !M->bgroup && ngroups > 0)

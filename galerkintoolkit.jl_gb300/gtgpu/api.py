@@ -204,10 +204,10 @@ class Space:
     def node_coordinates(self):
         """Physical coordinates of the space's nodes, ``(free, dirichlet)``
         arrays of shape (nodes, D) in the free and the Dirichlet node
-        numbering: the geometry map of each cell (P1: its vertices; QUAD4/HEX8:
-        multilinear) at the reference Lagrange nodes (lexicographic, spacing
-        1/order) -- the points at which the reference interpolates Dirichlet
-        data (src/space.jl:1127-1177)."""
+        numbering: the geometry map of each cell (tets: affine; QUAD4/HEX8:
+        multilinear) at the reference Lagrange nodes (exponents / order,
+        first index fastest; P: exponent sums <= order) -- the points at which
+        the reference interpolates Dirichlet data (src/space.jl:1127-1177)."""
         m, D, nc = self.mesh, self.mesh.D, self.ncomp
         cd = self.face_dofs()
         first = cd[:, ::nc]  # component 0 of every local node
@@ -215,7 +215,14 @@ class Space:
         nn = nd.shape[1]
         X = m.coords[m.cell_nodes.astype(np.int64) - 1]  # (cells, vertices, D)
         if m.cell_type == _lib.GT_TET4:
-            N = np.eye(4)
+            if self.order == 1:
+                N = np.eye(4)
+            else:
+                # P2 nodes: exponents (a, b, c), a + b + c <= 2, first index
+                # fastest; node at (a, b, c) / 2, barycentric weights of the vertices
+                ex = [(a, b, c) for c in range(3) for b in range(3) for a in range(3) if a + b + c <= 2]
+                P = np.array(ex, np.float64) / 2.0
+                N = np.column_stack([1.0 - P.sum(axis=1), P[:, 0], P[:, 1], P[:, 2]])  # (10, 4)
         else:
             k = self.order
             e = np.array(np.unravel_index(np.arange(nn), (k + 1,) * D, order="F")).T / k  # (nn, D)

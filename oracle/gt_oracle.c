@@ -416,7 +416,7 @@ void or_face_lookup(int64_t nc, int nlv, const int32_t* c_verts, int nld, int nd
 
 /* Number of local nodes of the space on a cell type. */
 static int space_nodes(int ctype, int order) {
-  if (ctype == OR_TET4) return 4;
+  if (ctype == OR_TET4) return order == 2 ? 10 : 4;
   int D = ctype == OR_QUAD4 ? 2 : 3;
   int m = order + 1;
   return D == 2 ? m * m : m * m * m;
@@ -429,7 +429,24 @@ static int qnode(int D, int order, const int* e) {
 }
 
 /* Q_k nodes of the closure of the local (D-1)-face lf; returns count. */
+/* P2 tetrahedron: nodes are the exponents (a,b,c), a+b+c <= 2, first index
+ * fastest (src/space.jl:1127-1146 with space_type :P): vertices at nodes
+ * 0, 2, 5, 9, midpoints of the local edges 12 13 23 14 24 34 at 1 3 4 6 7 8 */
+static const int P2_VERT[4] = {0, 2, 5, 9};
+static const int P2_EDGE[6] = {1, 3, 4, 6, 7, 8};
+static const int TET_EDGES[6][2] = {{1, 2}, {1, 3}, {2, 3}, {1, 4}, {2, 4}, {3, 4}};
+
 static int face_closure_nodes(int ctype, int order, int lf, int* out) {
+  if (ctype == OR_TET4 && order == 2) {
+    int cnt = 0;
+    for (int i = 0; i < 3; i++) out[cnt++] = P2_VERT[TET_FACES[lf][i] - 1];
+    for (int e = 0; e < 6; e++) {
+      int in = 0;
+      for (int i = 0; i < 3; i++) in += (TET_EDGES[e][0] == TET_FACES[lf][i]) + (TET_EDGES[e][1] == TET_FACES[lf][i]);
+      if (in == 2) out[cnt++] = P2_EDGE[e];
+    }
+    return cnt;
+  }
   if (ctype == OR_TET4) {
     for (int i = 0; i < 3; i++) out[i] = TET_FACES[lf][i] - 1;
     return 3;
@@ -465,6 +482,23 @@ static void lag1d(int order, double x, double* v, double* dv) {
 
 /* Shape values/gradients of a reference space at a point. */
 static void tabulate(int ctype, int order, const double* x, double* val, double* grad) {
+  if (ctype == OR_TET4 && order == 2) {
+    /* P2 Lagrange basis in barycentric form: l_i (2 l_i - 1) at vertex i,
+     * 4 l_i l_j at the midpoint of edge ij */
+    double l[4] = {1.0 - x[0] - x[1] - x[2], x[0], x[1], x[2]};
+    double gl[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    for (int i = 0; i < 4; i++) {
+      int n = P2_VERT[i];
+      val[n] = l[i] * (2.0 * l[i] - 1.0);
+      for (int d = 0; d < 3; d++) grad[n * 3 + d] = (4.0 * l[i] - 1.0) * gl[i][d];
+    }
+    for (int e = 0; e < 6; e++) {
+      int i = TET_EDGES[e][0] - 1, j = TET_EDGES[e][1] - 1, n = P2_EDGE[e];
+      val[n] = 4.0 * l[i] * l[j];
+      for (int d = 0; d < 3; d++) grad[n * 3 + d] = 4.0 * (l[j] * gl[i][d] + l[i] * gl[j][d]);
+    }
+    return;
+  }
   if (ctype == OR_TET4) {
     val[0] = 1.0 - x[0] - x[1] - x[2];
     val[1] = x[0]; val[2] = x[1]; val[3] = x[2];
@@ -493,8 +527,22 @@ static void tabulate(int ctype, int order, const double* x, double* val, double*
  * direction, first index fastest (src/quadrature.jl:78-106), or the 4-point
  * Strang rule on the tetrahedron (src/quadrature.jl:512-529).  Returns npts. */
 int or_quadrature(int ctype, int degree, double* x, double* w) {
+  if (ctype == OR_TET4 && degree > 2) {
+    /* degrees 3-4: the reference's strang_quadrature_4 (src/quadrature.jl:
+     * 554-590), Keast's 11-point rule: centroid, (11/14, 1/14, 1/14) and
+     * permutations with (1/14, 1/14, 1/14), the 6 points with coordinates
+     * (1 +- sqrt(5/14))/4 */
+    if (degree > 4) return -1;
+    double r = sqrt(5.0 / 14.0), a = 0.25 * (1.0 + r), b = 0.25 * (1.0 - r), f = 11.0 / 14.0, g = 1.0 / 14.0;
+    double p[11][3] = {{0.25, 0.25, 0.25}, {f, g, g}, {g, f, g}, {g, g, f}, {g, g, g}, {a, a, b},
+                       {a, b, a}, {a, b, b}, {b, a, a}, {b, a, b}, {b, b, a}};
+    for (int q = 0; q < 11; q++) {
+      for (int d = 0; d < 3; d++) x[3 * q + d] = p[q][d];
+      w[q] = q == 0 ? -74.0 / 5625.0 : (q < 5 ? 343.0 / 45000.0 : 56.0 / 2250.0);
+    }
+    return 11;
+  }
   if (ctype == OR_TET4) {
-    if (degree > 2) return -1;
     double a = 0.5854101966249685, b = 0.1381966011250105, c = 1.0 / 24.0;
     double p[4][3] = {{b, b, b}, {a, b, b}, {b, a, b}, {b, b, a}};
     for (int q = 0; q < 4; q++) {
@@ -565,18 +613,26 @@ int64_t or_dof_ids(int ctype, int order, int ncomp, int64_t nc, const int32_t* c
   int nloc = nn * ncomp;
   int nlf = ctype == OR_TET4 ? 4 : 2 * D;
   int nle = D == 2 ? 4 : 12;
+  /* P2 tets own dofs on vertices and edges only */
+  const int tet2 = ctype == OR_TET4 && order == 2;
   int64_t off_e = nverts * ncomp;
   int64_t off_f = off_e + (order == 2 ? nedges * ncomp : 0);
-  int64_t off_c = off_f + ((order == 2 && D == 3) ? nfaces * ncomp : 0);
-  int64_t ndofs = off_c + (order == 2 ? nc * ncomp : 0);
+  int64_t off_c = off_f + ((order == 2 && D == 3 && !tet2) ? nfaces * ncomp : 0);
+  int64_t ndofs = off_c + (order == 2 && !tet2 ? nc * ncomp : 0);
   for (int64_t c = 0; c < nc; c++) {
     int32_t* cd = cell_dofs + c * nloc;
     for (int lv = 0; lv < nlv; lv++) {
-      int node = (ctype == OR_TET4 || order == 1) ? lv : vertex_qnode(D, order, lv);
+      int node = tet2 ? P2_VERT[lv] : ((ctype == OR_TET4 || order == 1) ? lv : vertex_qnode(D, order, lv));
       int64_t v = c_verts[c * nlv + lv];
       for (int k = 0; k < ncomp; k++) cd[node * ncomp + k] = (int32_t)((v - 1) * ncomp + k + 1);
     }
-    if (order == 2) {
+    if (tet2) {
+      for (int le = 0; le < 6; le++) {
+        int64_t e = c_edges[c * 6 + le];
+        for (int k = 0; k < ncomp; k++)
+          cd[P2_EDGE[le] * ncomp + k] = (int32_t)(off_e + (e - 1) * ncomp + k + 1);
+      }
+    } else if (order == 2) {
       for (int le = 0; le < nle; le++) {
         const int* ev = D == 2 ? QUAD_EDGES[le] : HEX_EDGES[le];
         int node = centroid_qnode(D, ev, 2);

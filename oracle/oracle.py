@@ -36,6 +36,10 @@ HEX_EDGES = np.array([[1, 2], [3, 4], [1, 3], [2, 4], [5, 6], [7, 8],
                       [5, 7], [6, 8], [1, 5], [3, 7], [2, 6], [4, 8]], np.int32)
 HEX_FACES = np.array([[1, 2, 3, 4], [5, 6, 7, 8], [1, 2, 5, 6],
                       [3, 4, 7, 8], [1, 3, 5, 7], [2, 4, 6, 8]], np.int32)
+# unit simplex local faces, src/domain.jl:413-469
+TRI_EDGES = np.array([[1, 2], [1, 3], [2, 3]], np.int32)
+TET_EDGES = np.array([[1, 2], [1, 3], [2, 3], [1, 4], [2, 4], [3, 4]], np.int32)
+TET_FACES = np.array([[1, 2, 3], [1, 2, 4], [1, 3, 4], [2, 3, 4]], np.int32)
 
 _lock = threading.Lock()
 _lib = None
@@ -168,7 +172,26 @@ def lagrange_space(mesh, order, ncomp=1, dirichlet=None):
     c_verts = np.ascontiguousarray(node_vertex[cn - 1])
     c_edges = c_faces = None
     nedges = nfaces = 0
-    if order == 2:
+    if order == 2 and ctype == TET4:
+        # triangles over the tets (parents: boundary triangles), edges over the
+        # triangles (parents: boundary 1-faces), the tets' edges looked up
+        # (create_face_boundary!, src/topology.jl:1099-1125)
+        c_faces = np.zeros((nc, 4), np.int32)
+        par = np.ascontiguousarray(node_vertex[mesh["pf2"] - 1])
+        fv = np.zeros((par.shape[0] + nc * 4, 3), np.int32)
+        nfaces = L.or_face_boundary(nc, 4, _p(c_verts), 4, 3, _p(TET_FACES), par.shape[0], _p(par),
+                                    _p(c_faces), _p(fv))
+        fv = np.ascontiguousarray(fv[:nfaces])
+        f_edges = np.zeros((nfaces, 3), np.int32)
+        par1 = np.ascontiguousarray(node_vertex[mesh["pf1"] - 1])
+        ev = np.zeros((par1.shape[0] + nfaces * 3, 2), np.int32)
+        nedges = L.or_face_boundary(nfaces, 3, _p(fv), 3, 2, _p(TRI_EDGES), par1.shape[0], _p(par1),
+                                    _p(f_edges), _p(ev))
+        ev = np.ascontiguousarray(ev[:nedges])
+        c_edges = np.zeros((nc, 6), np.int32)
+        L.or_face_lookup(nc, 4, _p(c_verts), 6, 2, _p(TET_EDGES), nedges, _p(ev), _p(c_edges))
+        c_faces, nfaces = None, 0  # P2 has no face-interior nodes
+    elif order == 2:
         assert ctype in (QUAD4, HEX8)
         if D == 2:
             c_edges = np.zeros((nc, 4), np.int32)
@@ -196,7 +219,7 @@ def lagrange_space(mesh, order, ncomp=1, dirichlet=None):
     if dirichlet is not None:
         tf = np.ascontiguousarray(node_vertex[boundary_faces(mesh, dirichlet) - 1])
         L.or_tag_cell_faces(ctype, nc, _p(c_verts), tf.shape[0], _p(tf), _p(c_tagged))
-    nn = 4 if ctype == TET4 else (order + 1) ** D
+    nn = (10 if order == 2 else 4) if ctype == TET4 else (order + 1) ** D
     cell_dofs = np.zeros((nc, nn * ncomp), np.int32)
     ndiri = np.zeros(1, np.int64)
     nfree = L.or_dof_ids(ctype, order, ncomp, nc, _p(c_verts), nverts, _p(c_edges), nedges,

@@ -12,6 +12,7 @@ pytestmark = pytest.mark.gpu
 CASES = [
     # (id, box cells, simplex, order, jitter)
     ("p1tet", (4, 3, 5), True, 1, 0.2),
+    ("p2tet", (2, 3, 2), True, 2, 0.2),
     ("q1hex", (3, 4, 2), False, 1, 0.15),
     ("q2hex", (2, 3, 2), False, 2, 0.1),
     ("q1quad", (5, 4), False, 1, 0.2),

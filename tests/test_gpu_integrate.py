@@ -29,13 +29,13 @@ def _unit_cube_int(p):
     return c[0] + (c[1] + c[2] + c[3]) / 2 + (c[4] + c[5] + c[6]) / 3 + (c[7] + c[8] + c[9]) / 4
 
 
-@pytest.mark.parametrize("case", ["p1tet_jitter", "q2hex", "q1hex"])
+@pytest.mark.parametrize("case", ["p1tet_jitter", "p2tet_jitter", "q2hex", "q1hex"])
 def test_quadratic_exact_on_affine_cells(case):
     """a quadratic is integrated exactly on affine cells (degree-2 rules)"""
-    if case == "p1tet_jitter":
+    if case in ("p1tet_jitter", "p2tet_jitter"):
         m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (5, 4, 3), simplexify=True)
         GT.jitter_interior_nodes(m, 0.2, 3)
-        V = GT.lagrange_space(GT.interior(m), 1)
+        V = GT.lagrange_space(GT.interior(m), 1 if case == "p1tet_jitter" else 2)
     else:
         m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (3, 4, 2))
         V = GT.lagrange_space(GT.interior(m), 2 if case == "q2hex" else 1)
@@ -90,6 +90,14 @@ def test_patch_test_3d_tets_and_q2_quadratic():
     xd2 = GT.interpolate_dirichlet(q, V2)
     x2, _ = GT.solve(GT.linear_problem(V2, GT.laplacian(), GT.source(-2.0), dirichlet_values=xd2), rtol=1e-13)
     assert GT.l2_error(V2, x2, q, xd2) < 1e-10 and GT.h1_error(V2, x2, q, xd2) < 1e-9
+    # P2 tets reproduce a quadratic: u = x^2 + yz + z, -lap u = -2
+    m3 = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (3, 2, 2), simplexify=True)
+    GT.jitter_interior_nodes(m3, 0.2, 13)
+    V3 = GT.lagrange_space(GT.interior(m3), 2, dirichlet_boundary=GT.boundary(m3))
+    s3 = GT.Polynomial(z=1.0, xx=1.0, yz=1.0)
+    xd3 = GT.interpolate_dirichlet(s3, V3)
+    x3, _ = GT.solve(GT.linear_problem(V3, GT.laplacian(), GT.source(-2.0), dirichlet_values=xd3), rtol=1e-13)
+    assert GT.l2_error(V3, x3, s3, xd3) < 1e-10 and GT.h1_error(V3, x3, s3, xd3) < 1e-9
     # a P1 solution of the same quadratic problem is not exact: the error norm sees it
     V1 = GT.lagrange_space(GT.interior(m2), 1, dirichlet_boundary=GT.boundary(m2))
     xd1 = GT.interpolate_dirichlet(q, V1)

@@ -46,6 +46,10 @@ CASES = [
     ("q1quad_elast_affine", (5, 4), False, 1, 2, ["1-face-3"], O.ELASTICITY, 0.0, 0.5),
     ("q1quad_1x1_alldiri", (1, 1), False, 1, 1, "boundary", O.LAPLACE, 0.0, 0.0),
     ("q2quad_1x1", (1, 1), False, 2, 1, "boundary", O.LAPLACE, 0.0, 0.0),
+    ("p2tet_3x2x2_jitter", (3, 2, 2), True, 2, 1, "boundary", O.LAPLACE, 0.2, 1.0),
+    ("p2tet_mass_free", (2, 2, 2), True, 2, 1, None, O.MASS, 0.1, 0.5),
+    ("p2tet_elast_x0", (2, 2, 3), True, 2, 3, ["2-face-5"], O.ELASTICITY, 0.1, 0.5),
+    ("p2tet_1x1x1", (1, 1, 1), True, 2, 1, "boundary", O.LAPLACE, 0.0, 0.0),
 ]
 
 _KIND = {O.LAPLACE: GT.laplacian, O.MASS: GT.mass, O.ELASTICITY: GT.elasticity}
@@ -86,7 +90,10 @@ def test_matrix_pattern_and_fp64_values(case):
         assert np.abs(v - ov).max() <= TOL64 * scale
 
 
-@pytest.mark.parametrize("case", CASES[:8], ids=[c[0] for c in CASES[:8]])
+_FP32_CASES = CASES[:8] + [c for c in CASES if c[0] == "p2tet_3x2x2_jitter"]
+
+
+@pytest.mark.parametrize("case", _FP32_CASES, ids=[c[0] for c in _FP32_CASES])
 def test_fp32_and_mixed_values(case):
     m, V, ref, a, coef, form, order = _build(case)
     cp, rv, nz = O.assemble_matrix(ref, form, 2 * order, coef=coef, nu=0.3)
