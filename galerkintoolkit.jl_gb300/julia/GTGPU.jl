@@ -160,6 +160,38 @@ function assemble_vector(f::AbstractVector, ::Type{Float64}, V::Space; coef=noth
 end
 
 """
+    assemble_boundary_vector!(b, g::Vector{Float64} (ncomp), V, groups; accumulate=true)
+
+GT.assemble_vector(v -> ∫ g⋅v dΓ) over the boundary faces of the groups k of
+"(D-1)-face-k" (`groups === :boundary`: all of them), added to b.
+"""
+function assemble_boundary_vector!(b::Vector{Float64}, g::AbstractVector, V::Space, groups; accumulate=true)
+    ng, gs = groups === :boundary ? (Cint(-1), C_NULL) : (Cint(length(groups)), Int32.(groups))
+    check(V.ctx.h, ccall((:gt_assemble_boundary_vector, LIB), Cint,
+                         (Ptr{Cvoid}, Cint, Ptr{Int32}, Ptr{Float64}, Ptr{Float64}, Cint),
+                         V.h, ng, gs, collect(Float64, g), b, accumulate ? Cint(1) : Cint(0)))
+    b
+end
+
+const GT_INT_VOLUME, GT_INT_POLY, GT_INT_FIELD, GT_INT_L2_NORM2, GT_INT_L2_ERROR2, GT_INT_H1_ERROR2 = 0, 1, 2, 3, 4, 5
+
+"""
+    integrate(V, kind; u_free=nothing, u_dirichlet=nothing, poly=nothing) -> Float64
+
+GT.assemble_scalar for the fixed integrands of `gt_integrate` (e.g. the
+squared L2 error `kind = GT_INT_L2_ERROR2` against a quadratic with the 10
+coefficients of 1, x, y, z, x², y², z², xy, xz, yz per component).
+"""
+function integrate(V::Space, kind::Integer; u_free=nothing, u_dirichlet=nothing, poly=nothing)
+    r = Ref{Float64}(0.0)
+    check(V.ctx.h, ccall((:gt_integrate, LIB), Cint,
+                         (Ptr{Cvoid}, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ref{Float64}),
+                         V.h, kind, u_free === nothing ? C_NULL : u_free,
+                         u_dirichlet === nothing ? C_NULL : u_dirichlet, poly === nothing ? C_NULL : poly, r))
+    r[]
+end
+
+"""
     solve(dm::DeviceMatrix, b; rtol=1e-10, maxit=20000, mode=GT_SOLVE_FP64) -> x, SolveInfo
 """
 function solve(dm::DeviceMatrix, b::Vector{Float64}; rtol=1e-10, maxit=20000, mode=GT_SOLVE_FP64)

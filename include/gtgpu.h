@@ -125,7 +125,7 @@ int gt_mesh_destroy(gt_mesh* mesh);
 /* ---- space / DOF numbering ---------------------------------------------- */
 /* Replaces GT.lagrange_space(Omega, order; tensor_size, dirichlet_boundary)
  * (src/space.jl:1702-1735) and its generate_dof_ids (src/space.jl:299-535),
- * computed on the device.  order 1 or 2 (P1 on TET4), ncomp 1 or D.
+ * computed on the device.  order 1 or 2 (Q1/Q2 on QUAD4/HEX8, P1/P2 on TET4), ncomp 1 or D.
  * ngroups: -1 = Dirichlet on all boundary faces (GT.boundary(mesh)),
  * 0 = no Dirichlet, >0 = the groups listed in `groups` (values k of
  * "(D-1)-face-k").  Vector spaces are clamped on all components. */
