@@ -2047,6 +2047,7 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
   void* Ke = nullptr;
   double* be = nullptr;
   const bool pre = early && early->active;
+  bool b_copied = false;  // a host b already downloaded chunk by chunk
   if (pre) {
     // element stage already queued on the auxiliary stream: join it
     GT_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, early->done, 0));
@@ -2078,8 +2079,10 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
     if (s == GT_OK && hc && pat_down && A->bs == 1 && values_done) {
       // all chunks are queued first (the device never waits for the host),
       // then the host row pointers -- downloaded meanwhile -- give each
-      // chunk's range for its download behind the chunk's event
-      constexpr int NCH = 4;
+      // chunk's range for its download behind the chunk's event; a host b
+      // comes back chunk by chunk too, so only the last chunk's rows are left
+      // to copy after the last scatter
+      constexpr int NCH = 8;
       cudaEvent_t evs[NCH] = {};
       int nq = 0;
       for (int k = 0; k < NCH && s == GT_OK; k++, nq++) {
@@ -2094,20 +2097,35 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
         cudaError_t e = cudaEventSynchronize(pat_down);
         if (e != cudaSuccess) s = check_cuda(ctx, e, "pattern download");
       }
+      const bool b_side = b_out && !dev;
       for (int k = 0; k < NCH && s == GT_OK; k++) {
         const int64_t r0 = A->nbrows * k / NCH, r1 = A->nbrows * (k + 1) / NCH;
         const int64_t o0 = hc->rowptr[r0], o1 = hc->rowptr[r1];
-        if (o1 <= o0) continue;
         cudaStreamWaitEvent(ctx->side, evs[k], 0);
-        if (hc->v64 && A->val64)
+        if (o1 > o0 && hc->v64 && A->val64)
           cudaMemcpyAsync(hc->v64 + o0, A->val64 + o0, sizeof(double) * (o1 - o0), cudaMemcpyDefault, ctx->side);
-        if (hc->v32 && A->val32)
+        if (o1 > o0 && hc->v32 && A->val32)
           cudaMemcpyAsync(hc->v32 + o0, A->val32 + o0, sizeof(float) * (o1 - o0), cudaMemcpyDefault, ctx->side);
+        if (b_side && r1 > r0)  // scalar rows: b entries r0..r1
+          cudaMemcpyAsync(b_out + r0, bd + r0, sizeof(double) * (r1 - r0), cudaMemcpyDefault, ctx->side);
         cudaError_t ce = cudaGetLastError();
         if (ce != cudaSuccess) s = check_cuda(ctx, ce, "values download");
       }
       for (int k = 0; k < nq; k++)
         if (evs[k]) event_put(ctx, evs[k]);
+      if (s == GT_OK && b_side) {
+        // the staging block of b is freed below: later main-stream users of
+        // the block wait for the copies out of it
+        cudaEvent_t bev = event_get(ctx);
+        if (!bev) {
+          s = set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
+        } else {
+          cudaEventRecord(bev, ctx->side);
+          cudaStreamWaitEvent(ctx->stream, bev, 0);
+          event_put(ctx, bev);
+          b_copied = true;
+        }
+      }
       if (s == GT_OK) *values_done = true;
     } else if (s == GT_OK) {
       s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr);
@@ -2117,7 +2135,7 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
   // host b: the copy is queued here; the caller's device_status() call
   // synchronises the stream before returning (the freed staging block is only
   // reused by work queued after the copy)
-  if (s == GT_OK && b_out && !dev) s = copy_out(ctx, b_out, bd, nb);
+  if (s == GT_OK && b_out && !dev && !b_copied) s = copy_out(ctx, b_out, bd, nb);
   if (b_out && !dev) dfree(ctx, bd);
   if (Ke) pool_free(ctx, Ke);
   if (be) dfree(ctx, be);
