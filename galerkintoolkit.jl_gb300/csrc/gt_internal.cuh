@@ -96,6 +96,9 @@ struct Ctx {
   // element kernels on the auxiliary stream beside the sparsity kernels
   // (GTGPU_OVERLAP=0 at context creation: one stream, in order)
   bool overlap = true;
+  // lanes per row of the CSR row kernels: 0 = from the mean row length,
+  // else 1, 2, 4 or 8 (GTGPU_SPMV_LANES at context creation)
+  int spmv_lanes = 0;
   // phase profiling: CUDA events recorded on the stream between phases
   bool prof = false;
   std::vector<std::pair<std::string, cudaEvent_t>> marks;

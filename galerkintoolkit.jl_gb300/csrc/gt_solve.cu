@@ -423,11 +423,7 @@ __global__ void __launch_bounds__(TILE_T) k_cg_spmv_tiles(const int64_t* __restr
 // ---------------------------------------------------------------------------
 // lanes per block row (row_lanes, gt_rowdot.cuh)
 static int pick_group(const Matrix* A) {
-  const char* ov = getenv("GTGPU_SPMV_LANES");
-  if (ov) {
-    const int g = atoi(ov);
-    if (g == 1 || g == 2 || g == 4 || g == 8) return g;
-  }
+  if (A->ctx->spmv_lanes) return A->ctx->spmv_lanes;
   return row_lanes(A->nbrows > 0 ? (double)A->bnnz / (double)A->nbrows : 1.0);
 }
 static unsigned spmv_grid(const Matrix* A) {
