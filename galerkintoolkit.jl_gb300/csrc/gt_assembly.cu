@@ -72,6 +72,20 @@ __device__ void lagrange1d(int order, double x, double* v, double* dv) {
   }
 }
 
+// 1/d for d != 0 from the hardware reciprocal approximation (PTX
+// rcp.approx.ftz.f64) refined by two Newton-Raphson steps r <- r + r (1 - d r)
+// (each squares the relative error): within a few ulp of the rounded
+// quotient, in four FP64 FMAs instead of the correctly rounded division's
+// longer sequence -- the element kernels are bound by FP64 issue slots.
+__device__ __forceinline__ double recip_nr2(double d) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(d));
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
+}
+
 __global__ void k_tabulate(int ctype, int order, TabLayout L, double* tab) {
   int q = threadIdx.x;
   if (q >= L.nq) return;
@@ -646,7 +660,7 @@ __global__ void __launch_bounds__(128) k_elements(const double* __restrict__ coo
     double inv[D][D], det;
     if (D == 2) {
       det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-      double r = 1.0 / det;
+      double r = recip_nr2(det);
       inv[0][0] = J[1][1] * r; inv[0][1] = -J[0][1] * r;
       inv[1][0] = -J[1][0] * r; inv[1][1] = J[0][0] * r;
     } else {
@@ -654,7 +668,7 @@ __global__ void __launch_bounds__(128) k_elements(const double* __restrict__ coo
       double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
       double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
       det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-      double r = 1.0 / det;
+      double r = recip_nr2(det);
       inv[0][0] = c00 * r; inv[1][0] = c01 * r; inv[2][0] = c02 * r;
       inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
       inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
@@ -877,7 +891,7 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
         g[0][0] = (T)c10; g[0][1] = (T)c11; g[0][2] = (T)c12;
         g[1][0] = (T)c20; g[1][1] = (T)c21; g[1][2] = (T)c22;
         g[2][0] = (T)c30; g[2][1] = (T)c31; g[2][2] = (T)c32;
-        T s = (T)(cf * s_wsum / adet);
+        T s = (T)(cf * s_wsum * recip_nr2(adet));
         T k11 = s * (g[0][0] * g[0][0] + g[0][1] * g[0][1] + g[0][2] * g[0][2]);
         T k12 = s * (g[0][0] * g[1][0] + g[0][1] * g[1][1] + g[0][2] * g[1][2]);
         T k13 = s * (g[0][0] * g[2][0] + g[0][1] * g[2][1] + g[0][2] * g[2][2]);
@@ -1442,7 +1456,7 @@ __global__ void __launch_bounds__(256) k_geom_affine(const double* __restrict__ 
   double inv[D][D], det;
   if (D == 2) {
     det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-    double r = 1.0 / det;
+    double r = recip_nr2(det);
     inv[0][0] = J[1][1] * r; inv[0][1] = -J[0][1] * r;
     inv[1][0] = -J[1][0] * r; inv[1][1] = J[0][0] * r;
   } else {
@@ -1450,7 +1464,7 @@ __global__ void __launch_bounds__(256) k_geom_affine(const double* __restrict__ 
     double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
     double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
     det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
-    double r = 1.0 / det;
+    double r = recip_nr2(det);
     inv[0][0] = c00 * r; inv[1][0] = c01 * r; inv[2][0] = c02 * r;
     inv[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
     inv[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
