@@ -1969,6 +1969,15 @@ static int elements_early(const Space* sp, int form, const NumIn& in, double nu,
                           EarlyElems* E) {
   Ctx* ctx = ctx_of(sp);
   if (ctx->prof || !ctx->overlap || !ctx->aux || sp->mesh->ctype != GT_TET4) return GT_OK;
+  // only when the main stream outranks the auxiliary one (the context's own
+  // stream does; a caller's stream of default priority does not -- then the
+  // element blocks would hold the SMs ahead of the sparsity kernels)
+  int pm = 0, pa = 0;
+  if (cudaStreamGetPriority(ctx->stream, &pm) != cudaSuccess || cudaStreamGetPriority(ctx->aux, &pa) != cudaSuccess) {
+    cudaGetLastError();
+    return GT_OK;
+  }
+  if (!(pm < pa)) return GT_OK;
   if (form != GT_LAPLACE && form != GT_MASS && form != GT_ELASTICITY) return GT_OK;  // reported by numeric_in
   const int64_t nc = sp->mesh->ncells;
   const int kprec = precision == GT_FP32 ? GT_FP32 : GT_FP64;

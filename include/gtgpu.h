@@ -85,7 +85,10 @@ int gt_ctx_destroy(gt_ctx* ctx);
 const char* gt_last_error(const gt_ctx* ctx);
 int gt_ctx_synchronize(gt_ctx* ctx);
 /* Use an external stream (cudaStream_t passed as void*); NULL restores the
- * context's own stream. */
+ * context's own stream (created at the highest priority).  The context runs
+ * element kernels on a second, lowest-priority stream beside the sparsity
+ * kernels only when the main stream has a higher priority than that one;
+ * with a default-priority external stream the phases run in order. */
 int gt_ctx_set_stream(gt_ctx* ctx, void* stream);
 /* Bytes of device memory currently held by the context (live + pooled). */
 int gt_ctx_memory(gt_ctx* ctx, int64_t* live_bytes, int64_t* pooled_bytes);
