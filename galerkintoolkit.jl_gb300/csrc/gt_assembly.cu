@@ -469,6 +469,93 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
   }
 }
 
+// The count pass with one thread per block row, for rows of at most 32
+// incidences and 32 columns (P1 tetrahedra, Q1 quadrilaterals and hexahedra):
+// the thread sorts its incidences by insertion and builds its sorted column
+// list by binary search and insertion, both in shared memory interleaved
+// across the block's threads (element k of thread t at k * blockDim + t).
+// A warp then works on 32 rows at once instead of one, which cuts the warp
+// instructions per row several times over the warp-per-row kernel (whose
+// sorts, rounds and compaction are per-warp costs).  Same results: the
+// row's incidences ascending, its distinct free columns ascending.  A row
+// with more than 32 columns sets *redo and the warp kernel recounts.
+constexpr int kRowsMI = 32, kRowsS = 32;
+template <int NN>
+__global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict__ inc_ptr, int32_t* __restrict__ inc,
+                                                      const int32_t* __restrict__ cnd, int64_t nrows,
+                                                      int32_t* __restrict__ rowcnt, int32_t* __restrict__ slots,
+                                                      uint8_t* __restrict__ small, int32_t* maxrow, int32_t* redo) {
+  extern __shared__ int32_t s_rows[];
+  const int T = blockDim.x, tid = threadIdx.x;
+  int32_t* I = s_rows + tid;                 // incidences, I[k * T]
+  int32_t* Cl = s_rows + kRowsMI * T + tid;  // columns, Cl[k * T]
+  const int64_t r = blockIdx.x * (int64_t)T + tid;
+  if (r >= nrows) return;
+  const int64_t ib = inc_ptr[r];
+  const int ninc = min((int)(inc_ptr[r + 1] - ib), kRowsMI);  // the host checked the maximum
+  for (int k = 0; k < ninc; k++) {
+    const int32_t v = inc[ib + k];
+    int j = k;
+    while (j > 0 && I[(j - 1) * T] > v) {
+      I[j * T] = I[(j - 1) * T];
+      j--;
+    }
+    I[j * T] = v;
+  }
+  for (int k = 0; k < ninc; k++) inc[ib + k] = I[k * T];
+  int n = 0;
+  bool over = false;
+  if (ninc > 0) {
+    Cl[0] = (int32_t)r;  // the row's own DOF (block row r is node r + 1)
+    n = 1;
+  }
+  for (int k = 0; k < ninc; k++) {
+    const int32_t e = I[k * T];
+    const int32_t c = e / NN, self = e - c * NN;
+    int32_t d[NN];
+    if constexpr (NN == 4) {
+      const int4 q = __ldg(reinterpret_cast<const int4*>(cnd) + c);
+      d[0] = q.x; d[1] = q.y; d[2] = q.z; d[3] = q.w;
+    } else if constexpr (NN == 8) {
+      const int4 q0 = __ldg(reinterpret_cast<const int4*>(cnd) + 2 * (int64_t)c);
+      const int4 q1 = __ldg(reinterpret_cast<const int4*>(cnd) + 2 * (int64_t)c + 1);
+      d[0] = q0.x; d[1] = q0.y; d[2] = q0.z; d[3] = q0.w; d[4] = q1.x; d[5] = q1.y; d[6] = q1.z; d[7] = q1.w;
+    } else {
+#pragma unroll
+      for (int b = 0; b < NN; b++) d[b] = __ldg(cnd + (int64_t)c * NN + b);
+    }
+#pragma unroll
+    for (int b = 0; b < NN; b++) {
+      if (b == self || d[b] <= 0) continue;
+      const int32_t key = d[b] - 1;
+      int lo = 0, hi = n;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (Cl[mid * T] < key) lo = mid + 1;
+        else hi = mid;
+      }
+      if (lo < n && Cl[lo * T] == key) continue;
+      if (n == kRowsS) {
+        over = true;
+        continue;
+      }
+      for (int j = n; j > lo; j--) Cl[j * T] = Cl[(j - 1) * T];
+      Cl[lo * T] = key;
+      n++;
+    }
+  }
+  if (over) {
+    *redo = 1;
+    rowcnt[r] = 0;
+    small[r] = 0;
+    return;
+  }
+  rowcnt[r] = n;
+  small[r] = 1;
+  for (int k = 0; k < n; k++) slots[r * kRowsS + k] = Cl[k * T];
+  if (n > __ldcg(maxrow)) atomicMax(maxrow, n);
+}
+
 // colind of the rows whose sorted columns the count pass left in their slot
 // of S entries: four lanes per row, each copying a quarter of the row with
 // 16-byte slot loads (slots are 16-byte aligned), all loads in flight
@@ -545,23 +632,42 @@ static int launch_pattern(Matrix* A, int maxinc) {
   GT_TRY(dalloc(ctx, &slots, nrows * S));
   GT_TRY(dalloc(ctx, &small, nrows + 1));
   GT_TRY(dalloc(ctx, &A->rowptr, nrows + 1));
-  GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
   int grid = grid_for(nrows, warps);
-  if (nrows > 0)
-    k_pattern<NN, S, false><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, nrows,
-                                                                        hcap, icap, rowcnt, nullptr, nullptr, slots,
-                                                                        small, dmax, ctx->d_err);
-  GT_LAUNCH(ctx, "k_pattern<count>");
-  GT_TRY(exclusive_scan_i64(ctx, rowcnt, A->rowptr, nrows));
-  mark(ctx, "pattern_count");
-  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], A->rowptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
-  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[1], dmax, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  uint32_t bits = 0;
-  GT_TRY(take_device_error(ctx, &bits));  // synchronises
-  // bits of kernels on other streams (element checks) go back for the next take
-  const uint32_t own = DEV_ERR_ROW_CAP | DEV_ERR_HASH_FULL;
-  ctx->held_err |= bits & ~own;
-  if (bits & own) return set_error(ctx, GT_ERR_INVALID, "sparsity: row capacity exceeded");
+  // count pass: one thread per row where rows are short enough, else (or when
+  // a row turned out longer than 32 columns) one warp per row
+  bool rows_pass = NN <= 8 && S == kRowsS && maxinc <= kRowsMI && ctx->pattern_rows;
+  int32_t* dredo = nullptr;
+  GT_TRY(dalloc(ctx, &dredo, 1));
+  for (int attempt = 0; attempt < 2; attempt++) {
+    GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
+    GT_CUDA(ctx, cudaMemsetAsync(dredo, 0, sizeof(int32_t), st));
+    if (nrows > 0 && rows_pass) {
+      const size_t rsm = (size_t)128 * (kRowsMI + kRowsS) * sizeof(int32_t);
+      k_pattern_rows<NN><<<GT_KC(ctx, grid_for(nrows, 128)), 128, rsm, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs,
+                                                                             nrows, rowcnt, slots, small, dmax, dredo);
+    } else if (nrows > 0) {
+      k_pattern<NN, S, false><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, nrows,
+                                                                          hcap, icap, rowcnt, nullptr, nullptr, slots,
+                                                                          small, dmax, ctx->d_err);
+    }
+    GT_LAUNCH(ctx, "k_pattern<count>");
+    GT_TRY(exclusive_scan_i64(ctx, rowcnt, A->rowptr, nrows));
+    mark(ctx, "pattern_count");
+    GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], A->rowptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[1], dmax, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[2], dredo, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    uint32_t bits = 0;
+    GT_TRY(take_device_error(ctx, &bits));  // synchronises
+    // bits of kernels on other streams (element checks) go back for the next take
+    const uint32_t own = DEV_ERR_ROW_CAP | DEV_ERR_HASH_FULL;
+    ctx->held_err |= bits & ~own;
+    if (bits & own) return set_error(ctx, GT_ERR_INVALID, "sparsity: row capacity exceeded");
+    int32_t redo = 0;
+    memcpy(&redo, &ctx->h_scratch[2], sizeof(int32_t));
+    if (!rows_pass || !redo) break;
+    rows_pass = false;  // a row longer than 32 columns: count again, one warp per row
+  }
+  dfree(ctx, dredo);
   A->bnnz = ctx->h_scratch[0];
   int32_t mr = 0;
   memcpy(&mr, &ctx->h_scratch[1], sizeof(int32_t));

@@ -96,6 +96,9 @@ struct Ctx {
   // element kernels on the auxiliary stream beside the sparsity kernels
   // (GTGPU_OVERLAP=0 at context creation: one stream, in order)
   bool overlap = true;
+  // sparsity count pass with one thread per row where rows are short
+  // (GTGPU_PATTERN=warps at context creation: one warp per row always)
+  bool pattern_rows = true;
   // lanes per row of the CSR row kernels: 0 = from the mean row length,
   // else 1, 2, 4 or 8 (GTGPU_SPMV_LANES at context creation)
   int spmv_lanes = 0;
