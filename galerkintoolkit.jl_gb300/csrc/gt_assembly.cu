@@ -509,12 +509,17 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
     Cl[0] = (int32_t)r;  // the row's own DOF (block row r is node r + 1)
     n = 1;
   }
+  // the next incidence's node DOFs are loaded while the current ones are
+  // inserted (P1: one 16-byte load per incidence)
+  int4 nxt = make_int4(0, 0, 0, 0);
+  if (NN == 4 && ninc > 0) nxt = __ldg(reinterpret_cast<const int4*>(cnd) + I[0] / NN);
   for (int k = 0; k < ninc; k++) {
     const int32_t e = I[k * T];
     const int32_t c = e / NN, self = e - c * NN;
     int32_t d[NN];
     if constexpr (NN == 4) {
-      const int4 q = __ldg(reinterpret_cast<const int4*>(cnd) + c);
+      const int4 q = nxt;
+      if (k + 1 < ninc) nxt = __ldg(reinterpret_cast<const int4*>(cnd) + I[(k + 1) * T] / NN);
       d[0] = q.x; d[1] = q.y; d[2] = q.z; d[3] = q.w;
     } else if constexpr (NN == 8) {
       const int4 q0 = __ldg(reinterpret_cast<const int4*>(cnd) + 2 * (int64_t)c);
