@@ -474,11 +474,12 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
 // the thread sorts its incidences by insertion and builds its sorted column
 // list by binary search and insertion, both in shared memory interleaved
 // across the block's threads (element k of thread t at k * blockDim + t).
+// A row with more than 32 incidences or 32 columns sets *redo.
 // A warp then works on 32 rows at once instead of one, which cuts the warp
 // instructions per row several times over the warp-per-row kernel (whose
 // sorts, rounds and compaction are per-warp costs).  Same results: the
-// row's incidences ascending, its distinct free columns ascending.  A row
-// with more than 32 columns sets *redo and the warp kernel recounts.
+// row's incidences ascending, its distinct free columns ascending.  After a
+// *redo the warp kernel recounts every row.
 constexpr int kRowsMI = 32, kRowsS = 32;
 template <int NN>
 __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict__ inc_ptr, int32_t* __restrict__ inc,
@@ -492,7 +493,13 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
   const int64_t r = blockIdx.x * (int64_t)T + tid;
   if (r >= nrows) return;
   const int64_t ib = inc_ptr[r];
-  const int ninc = min((int)(inc_ptr[r + 1] - ib), kRowsMI);  // the host checked the maximum
+  const int ninc = (int)(inc_ptr[r + 1] - ib);
+  if (ninc > kRowsMI) {  // more incidences than the buffer: the warp kernel recounts
+    *redo = 1;
+    rowcnt[r] = 0;
+    small[r] = 0;
+    return;
+  }
   for (int k = 0; k < ninc; k++) {
     const int32_t v = inc[ib + k];
     int j = k;
@@ -611,7 +618,7 @@ static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out) {
 }
 
 template <int NN>
-static int launch_pattern(Matrix* A, int maxinc) {
+static int launch_pattern(Matrix* A, int32_t maxinc) {
   // slot width of the count pass: P1/Q1/Q2-quad rows have <= 27 columns,
   // Q2-hex rows up to 125
   constexpr int S = NN >= 10 ? 128 : 32;  // P2-tet rows: up to ~70 columns
@@ -621,15 +628,24 @@ static int launch_pattern(Matrix* A, int maxinc) {
   int64_t nrows = A->nbrows;
   // hash table: load factor <= 0.8 even if every candidate were distinct;
   // ibuf holds the row's incidences, then the compacted keys (<= candidates)
-  const int ncand_max = maxinc * NN;
-  int hcap = 32, icap = 32;
-  while (hcap < ncand_max + ncand_max / 4) hcap <<= 1;
-  while (icap < ncand_max) icap <<= 1;
-  if (hcap > 8192) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells for the sparsity kernel");
-  int warps = hcap >= 4096 ? 2 : (hcap >= 2048 ? 4 : 8);
-  size_t smem = (size_t)warps * (hcap + 2 * icap) * sizeof(int32_t);
-  cudaFuncSetAttribute(k_pattern<NN, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaFuncSetAttribute(k_pattern<NN, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // (the warp kernel's sizes need the longest incidence list, maxinc < 0:
+  // not known yet -- the row-per-thread pass does without it)
+  int hcap = 32, icap = 32, warps = 8;
+  size_t smem = 0;
+  auto setup_warp = [&]() -> int {
+    if (maxinc < 0) GT_TRY(max_diff(ctx, A->inc_ptr, nrows, &maxinc));
+    const int ncand_max = maxinc * NN;
+    hcap = 32;
+    icap = 32;
+    while (hcap < ncand_max + ncand_max / 4) hcap <<= 1;
+    while (icap < ncand_max) icap <<= 1;
+    if (hcap > 8192) return set_error(ctx, GT_ERR_UNSUPPORTED, "a DOF touches too many cells for the sparsity kernel");
+    warps = hcap >= 4096 ? 2 : (hcap >= 2048 ? 4 : 8);
+    smem = (size_t)warps * (hcap + 2 * icap) * sizeof(int32_t);
+    cudaFuncSetAttribute(k_pattern<NN, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_pattern<NN, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return GT_OK;
+  };
   int32_t *rowcnt = nullptr, *dmax = nullptr, *slots = nullptr;
   uint8_t* small = nullptr;
   GT_TRY(dalloc(ctx, &rowcnt, nrows + 1));
@@ -637,13 +653,14 @@ static int launch_pattern(Matrix* A, int maxinc) {
   GT_TRY(dalloc(ctx, &slots, nrows * S));
   GT_TRY(dalloc(ctx, &small, nrows + 1));
   GT_TRY(dalloc(ctx, &A->rowptr, nrows + 1));
-  int grid = grid_for(nrows, warps);
   // count pass: one thread per row where rows are short enough, else (or when
-  // a row turned out longer than 32 columns) one warp per row
-  bool rows_pass = NN <= 8 && S == kRowsS && maxinc <= kRowsMI && ctx->pattern_rows;
+  // a row turned out longer than 32 incidences or columns) one warp per row
+  bool rows_pass = NN <= 8 && S == kRowsS && ctx->pattern_rows;
+  if (!rows_pass) GT_TRY(setup_warp());
   int32_t* dredo = nullptr;
   GT_TRY(dalloc(ctx, &dredo, 1));
   for (int attempt = 0; attempt < 2; attempt++) {
+    const int grid = grid_for(nrows, warps);
     GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
     GT_CUDA(ctx, cudaMemsetAsync(dredo, 0, sizeof(int32_t), st));
     if (nrows > 0 && rows_pass) {
@@ -670,7 +687,8 @@ static int launch_pattern(Matrix* A, int maxinc) {
     int32_t redo = 0;
     memcpy(&redo, &ctx->h_scratch[2], sizeof(int32_t));
     if (!rows_pass || !redo) break;
-    rows_pass = false;  // a row longer than 32 columns: count again, one warp per row
+    rows_pass = false;  // a row beyond 32 incidences or columns: count again, one warp per row
+    GT_TRY(setup_warp());
   }
   dfree(ctx, dredo);
   A->bnnz = ctx->h_scratch[0];
@@ -683,6 +701,8 @@ static int launch_pattern(Matrix* A, int maxinc) {
     k_copy_slots<S><<<GT_KC(ctx, grid_for(nrows * 4, 256)), 256, 0, st>>>(A->rowptr, slots, nrows, A->colind);
     GT_LAUNCH(ctx, "k_copy_slots");
   } else if (nrows > 0) {
+    if (smem == 0) GT_TRY(setup_warp());
+    const int grid = grid_for(nrows, warps);
     k_pattern<NN, S, true><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, nrows,
                                                                        hcap, icap, nullptr, A->rowptr, A->colind,
                                                                        slots, small, dmax, ctx->d_err);
@@ -700,8 +720,7 @@ int build_pattern(Matrix* A) {
   const Space* sp = A->space;
   Ctx* ctx = sp->mesh->ctx;
   A->nbrows = sp->nfree_nodes;
-  int32_t maxinc = 0;
-  GT_TRY(max_diff(ctx, A->inc_ptr, A->nbrows, &maxinc));
+  const int32_t maxinc = -1;  // computed by launch_pattern if the warp kernel runs
   switch (sp->nn) {
     case 4: return launch_pattern<4>(A, maxinc);
     case 8: return launch_pattern<8>(A, maxinc);

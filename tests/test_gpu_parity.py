@@ -207,3 +207,39 @@ def test_spmv_copy_follows_value_updates():
     xs, info = GT.solve(A, b, rtol=1e-10, mode="fp64")
     assert info["converged"]
     assert np.abs(A.tocsr() @ xs - b).max() <= 1e-8 * np.abs(b).max()
+
+
+def _fan_mesh(n):
+    """A double pyramid over an n-gon: 2n tetrahedra around one centre node,
+    whose incidence list (2n cells) is longer than the row-per-thread
+    sparsity pass holds -- the warp kernel recounts."""
+    from gtgpu.mesh import Mesh
+    t = np.linspace(0.0, 2.0 * np.pi, n, endpoint=False)
+    ring = np.column_stack([np.cos(t), np.sin(t), np.zeros(n)])
+    coords = np.vstack([[0.0, 0.0, 0.0], [0.0, 0.0, 1.0], [0.0, 0.0, -1.0], ring])
+    cells, faces = [], []
+    for i in range(n):
+        a, b = 4 + i, 4 + (i + 1) % n  # 1-based ring nodes
+        cells += [[1, a, b, 2], [1, a, b, 3]]
+        faces += [[a, b, 2], [a, b, 3]]
+    faces = np.asarray(faces, np.int32)
+    return Mesh(D=3, cell_type=GT.api._lib.GT_TET4, coords=coords, cell_nodes=np.asarray(cells, np.int32),
+                corners=np.zeros(0, np.int32), bfaces=faces, bface_group=np.ones(len(faces), np.int32),
+                bedges=np.zeros((0, 2), np.int32))
+
+
+@pytest.mark.parametrize("dirichlet", [False, True])
+def test_pattern_rows_beyond_the_thread_pass(dirichlet):
+    m = _fan_mesh(20)  # 40 cells around node 1
+    diri = GT.boundary(m) if dirichlet else None
+    V = GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=diri)
+    A = GT.assemble_matrix(GT.laplacian(), np.float64, V, V)
+    rp, ci, v = A.csr()
+    om = dict(D=3, ctype=m.cell_type, coords=m.coords, cell_nodes=m.cell_nodes, pf0=m.corners, pf1=m.bedges,
+              pf1g=None, pf2=m.bfaces, pf2g=m.bface_group, cells=(), box=())
+    ref = O.lagrange_space(om, 1, dirichlet="boundary" if dirichlet else None)
+    assert np.array_equal(V.face_dofs(), ref["cell_dofs"])
+    cp, rv, nz = O.assemble_matrix(ref, O.LAPLACE, 2)
+    orp, oci, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    assert np.abs(v - ov).max() <= TOL64 * np.abs(ov).max()
