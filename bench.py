@@ -273,6 +273,41 @@ def wl_config(n, extra=None):
     return c
 
 
+class Replicas:
+    """The N > 1 layout of the benchmark: N independent replicas of the
+    step, one process per GPU (the path assembles one mesh per process and
+    has no data-path exchange).  The only collectives are the barriers around
+    the timed region and the max over ranks of the step time; the throughput
+    is the units all ranks processed divided by that time (weak scaling)."""
+
+    def __init__(self, backend="nccl"):
+        import torch.distributed as dist
+        self.dist = dist
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        if self.world > 1 and not dist.is_initialized():
+            dist.init_process_group(backend)
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max_ms(self, ms, device):
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        if self.world > 1:
+            self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def value(self, units_per_rank, ms):
+        return self.world * units_per_rank / (ms * 1e-3)
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
 def load_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
@@ -385,13 +420,9 @@ def main():
         {"elasticity": run_elasticity, "batched": run_batched, "serving": run_serving}[args.workload](args)
         return
     import torch
-    import torch.distributed as dist
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rep = Replicas("nccl")
+    world, rank, local = rep.world, rep.rank, rep.local
     torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl")
     import gtgpu as GT
 
     n = args.cells
@@ -422,8 +453,7 @@ def main():
     nnz = None
     times = []
     launches0 = ctx.launches()
-    if world > 1:
-        dist.barrier()
+    rep.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         t_wall = time.perf_counter()
@@ -439,15 +469,11 @@ def main():
             del A
         torch.cuda.synchronize()
         t_wall = time.perf_counter() - t_wall
-    if world > 1:
-        dist.barrier()
+    rep.barrier()
     launches = ctx.launches() - launches0
     ms = sum(times) / len(times)
-    tmax = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-    ms_max = float(tmax.item())
-    value = world * nnz / (ms_max * 1e-3)
+    ms_max = rep.max_ms(ms, "cuda")
+    value = rep.value(nnz, ms_max)
 
     # ---- phase profile of one extra step (dominant kernel + roofline)
     flush.fill_(1)
@@ -559,7 +585,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": wl_config(n, {"nnz": int(nnz), "free_dofs": int(nfree), "parallelism": f"replicas x{world}"}),
-            "e2e": {"value": world * nnz / (e2e_ms * 1e-3), "unit": "nnz/s", "ms_per_step": e2e_ms,
+            "e2e": {"value": rep.value(nnz, rep.max_ms(e2e_ms, "cuda")), "unit": "nnz/s", "ms_per_step": e2e_ms,
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "roofline": roof, "step_roofline": step_roof, "hbm_kernels": {**hbm, "spmv_fp64": spmv},
             "phases_ms": {k: round(v, 4) for k, v in phases},
@@ -567,8 +593,7 @@ def main():
             "gpu_launches": int(launches), "wall_s_timed": t_wall}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    rep.close()
 
 
 if __name__ == "__main__":
