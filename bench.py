@@ -491,9 +491,10 @@ def main():
     ph = {k: v for k, v in phases}
     # algorithmic bytes per launch of the phases (stated in the design doc)
     alg = {
-        "elements": nc * (4 * 4 + 8) + m.num_nodes * 24 + nc * 16 * 8 + nc * 4 * 8,  # reads + Ke/be writes
+        # reads + Ke/be writes (Ke: the 10 entries of the packed symmetric 4 x 4 block)
+        "elements": nc * (4 * 4 + 8) + m.num_nodes * 24 + nc * 10 * 8 + nc * 4 * 8,
         # Ke, be, incidences, cell dofs, rowptr, colind + values, load vector
-        "scatter": nc * 16 * 8 + nc * 4 * 8 + nc * 4 * 4 + nc * 4 * 4 + nfree * 8 + nnz * (4 + 8) + nfree * 8,
+        "scatter": nc * 10 * 8 + nc * 4 * 8 + nc * 4 * 4 + nc * 4 * 4 + nfree * 8 + nnz * (4 + 8) + nfree * 8,
     }
     # FP64 flops per P1 tetrahedron (FMA = 2, the division = 1): J 9, cofactors
     # 27, det 5, scale 2, six vertex-1..3 entries 36, vertex-0 entries 8, load 6

@@ -520,6 +520,17 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
   // inserted (P1: one 16-byte load per incidence)
   int4 nxt = make_int4(0, 0, 0, 0);
   if (NN == 4 && ninc > 0) nxt = __ldg(reinterpret_cast<const int4*>(cnd) + I[0] / NN);
+  // the node DOFs of the previous PV incidences (all already in the list):
+  // a candidate equal to one of them is a known duplicate and skips the
+  // search.  Incidences are visited by ascending cell, and neighbouring cells
+  // share most of their nodes (on the P1 benchmark mesh this filter takes out
+  // about half of the searches)
+  constexpr int PV = NN <= 4 ? 2 : (NN <= 8 ? 1 : 0);
+  int32_t prev[PV > 0 ? PV : 1][NN];
+#pragma unroll
+  for (int u = 0; u < PV; u++)
+#pragma unroll
+    for (int b = 0; b < NN; b++) prev[u][b] = 0;
   for (int k = 0; k < ninc; k++) {
     const int32_t e = I[k * T];
     const int32_t c = e / NN, self = e - c * NN;
@@ -539,6 +550,12 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
 #pragma unroll
     for (int b = 0; b < NN; b++) {
       if (b == self || d[b] <= 0) continue;
+      bool known = false;
+#pragma unroll
+      for (int u = 0; u < PV; u++)
+#pragma unroll
+        for (int q = 0; q < NN; q++) known |= prev[u][q] == d[b];
+      if (known) continue;
       const int32_t key = d[b] - 1;
       int lo = 0, hi = n;
       while (lo < hi) {
@@ -554,6 +571,14 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
       for (int j = n; j > lo; j--) Cl[j * T] = Cl[(j - 1) * T];
       Cl[lo * T] = key;
       n++;
+    }
+    if constexpr (PV > 0) {
+#pragma unroll
+      for (int u = PV - 1; u > 0; u--)
+#pragma unroll
+        for (int b = 0; b < NN; b++) prev[u][b] = prev[u - 1][b];
+#pragma unroll
+      for (int b = 0; b < NN; b++) prev[0][b] = d[b];
     }
   }
   if (over) {
@@ -1042,12 +1067,10 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
   #pragma unroll
           for (int m = n; m < 4; m++) k[e++] = s * (T)__ldg(s_mass + n * 4 + m);
       }
-      T* K = Ke + 16 * c;
-      const int up[4][4] = {{0, 1, 2, 3}, {1, 4, 5, 6}, {2, 5, 7, 8}, {3, 6, 8, 9}};
+      // packed upper triangle (the matrix is symmetric): 10 entries per cell
+      T* K = Ke + 10 * c;
   #pragma unroll
-      for (int n = 0; n < 4; n++)
-  #pragma unroll
-        for (int m = 0; m < 4; m++) K[n * 4 + m] = k[up[n][m]];
+      for (int e = 0; e < 10; e++) K[e] = k[e];
     }
     if (be) {
       double sc = (scoef ? scoef[c] : 1.0) * fsrc[0] * adet;
@@ -1339,18 +1362,62 @@ __device__ __forceinline__ int find_col(const int32_t* cols, int L, int32_t j) {
   return lo;
 }
 
-// With be != nullptr the group's lane 0 also sums the element vectors of the
-// row's incidences, in the same ascending order as k_scatter_vec (so the
-// load vector is bitwise the one of the separate pass), and writes bvec.
-template <int BS, int G, class TK, class TA>
+// Load-vector entries of a block row: the element vectors of the row's
+// incidences summed in one fixed order, shared by every kernel that sums
+// them (k_scatter, k_scatter_kron, k_scatter_vec), so the load vector of
+// assemble_vector is bitwise the one of assemble_matrix_and_vector: four
+// partial sums s_j over the incidences ib + j, ib + j + 4, ... (ascending),
+// combined as (s0 + s1) + (s2 + s3).
+// s[cc] = s_j of components cc < BS of the element vectors (be: bs
+// components per local node)
+template <int BS>
+__device__ __forceinline__ void load_partial(const int64_t ib, int64_t ie, int j, const int32_t* __restrict__ inc,
+                                             int nn, int bs, const double* __restrict__ be, double* s) {
+#pragma unroll
+  for (int cc = 0; cc < BS; cc++) s[cc] = 0.0;
+  for (int64_t k = ib + j; k < ie; k += 4) {
+    int32_t cb = __ldg(inc + k);
+    int32_t c = cb / nn, a = cb - c * nn;
+#pragma unroll
+    for (int cc = 0; cc < BS; cc++) s[cc] += __ldg(be + ((int64_t)c * nn + a) * bs + cc);
+  }
+}
+
+// The same sum by lanes 0..3 of a row's group of G >= 4 lanes (lane j forms
+// s_j; two butterfly steps combine them): one FP64 add per lane per four
+// incidences, where a single lane summing in sequence would issue a warp
+// FP64 instruction per incidence.  Every lane of the group gets the sums.
+template <int BS>
+__device__ __forceinline__ void row_load_sum(const int64_t ib, int64_t ie, const int32_t* __restrict__ inc, int nn,
+                                             const double* __restrict__ be, int gl, unsigned gmask, double* out) {
+  double s[BS];
+  load_partial<BS>(ib, gl < 4 ? ie : ib, gl, inc, nn, BS, be, s);
+#pragma unroll
+  for (int cc = 0; cc < BS; cc++) {
+    s[cc] += __shfl_xor_sync(gmask, s[cc], 1);
+    s[cc] += __shfl_xor_sync(gmask, s[cc], 2);
+    out[cc] = s[cc];
+  }
+}
+
+// With be != nullptr the group also sums the element vectors of the row's
+// incidences (row_load_sum), then lane 0 subtracts the Dirichlet lift of
+// each incidence in ascending order (when xd), and writes bvec.
+// PK: element matrices stored packed (the upper triangle of a symmetric
+// 4 x 4 block per cell, scalar P1 tetrahedra); entry (a, b) is read from
+// (min, max) of the pair.
+template <int BS, int G, class TK, class TA, bool PK>
 __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                           const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
-                          const int32_t* __restrict__ cnd, int nn, int64_t row_begin, int64_t row_end, int lmax,
-                          const TK* __restrict__ Ke, double* __restrict__ v64, float* __restrict__ v32,
+                          const int32_t* __restrict__ cnd, int nn_arg, int64_t row_begin, int64_t row_end,
+                          int lmax, const TK* __restrict__ Ke, double* __restrict__ v64, float* __restrict__ v32,
                           const double* __restrict__ be, double* __restrict__ bvec,
                           const double* __restrict__ xd) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   constexpr int RPW = 32 / G;  // rows per warp
+  // packed blocks are P1 tetrahedra: 4 nodes per cell, known at compile time
+  // (the incidence decode cell = e / nn, node = e % nn is then a shift)
+  const int nn = PK ? 4 : nn_arg;
   const int nloc = nn * BS;
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int sub = lane / G, gl = lane - sub * G;
@@ -1378,9 +1445,13 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
     const int b = gl;
     const bool vec = be != nullptr && gl == 0;
     double bsum[BS];
-#pragma unroll
-    for (int cc = 0; cc < BS; cc++) bsum[cc] = 0.0;
     int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+    if (be != nullptr) {
+      row_load_sum<BS>(ib, ie, inc, nn, be, gl, gmask, bsum);
+    } else {
+#pragma unroll
+      for (int cc = 0; cc < BS; cc++) bsum[cc] = 0.0;
+    }
     for (int64_t k0 = ib; k0 < ie; k0 += U) {
       int32_t jj[U];
       TA kv[U][BS * BS];
@@ -1391,11 +1462,14 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
         if (k < ie && b < nn) {
           int32_t cb = __ldg(inc + k);
           int32_t c = cb / nn, a = cb - c * nn;
-          if (vec)
-#pragma unroll
-            for (int cc = 0; cc < BS; cc++) bsum[cc] += __ldg(be + (int64_t)c * nloc + a * BS + cc);
           jj[u] = __ldg(cnd + (int64_t)c * nn + b);
-          const TK* Krow = Ke + (int64_t)c * nloc * nloc + (int64_t)(a * BS) * nloc + b * BS;
+          const TK* Krow;
+          if constexpr (PK) {
+            const int lo = a < b ? a : b, hi = a ^ b ^ lo;
+            Krow = Ke + (int64_t)c * 10 + (lo * 4 - ((lo * (lo - 1)) >> 1)) + (hi - lo);
+          } else {
+            Krow = Ke + (int64_t)c * nloc * nloc + (int64_t)(a * BS) * nloc + b * BS;
+          }
 #pragma unroll
           for (int cc = 0; cc < BS; cc++)
 #pragma unroll
@@ -1458,11 +1532,21 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
     while (warps > 1 && (size_t)warps * RPW * per_row > 96 * 1024) warps >>= 1;
     size_t smem = (size_t)warps * RPW * per_row;
     if (smem > 200 * 1024) return set_error(ctx, GT_ERR_UNSUPPORTED, "sparsity row too wide for the scatter kernel");
-    cudaFuncSetAttribute(k_scatter<BS, G, TK, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int64_t rows_per_block = (int64_t)warps * RPW;
     int64_t grid = (r1 - r0 + rows_per_block - 1) / rows_per_block;
-    k_scatter<BS, G, TK, TA><<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
-        A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, r0, r1, lmax, Ke, v64, v32, be, bvec, xd);
+    auto launch = [&](auto kern) {
+      cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      kern<<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
+          A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, nn, r0, r1, lmax, Ke, v64, v32, be, bvec, xd);
+    };
+    bool done = false;
+    if constexpr (BS == 1 && G == 4) {
+      if (ke_packed(sp)) {
+        launch(k_scatter<1, 4, TK, TA, true>);
+        done = true;
+      }
+    }
+    if (!done) launch(k_scatter<BS, G, TK, TA, false>);
     GT_LAUNCH(ctx, "k_scatter");
     return GT_OK;
   };
@@ -1757,20 +1841,21 @@ __global__ void k_scatter_kron(const int64_t* __restrict__ rowptr, const int32_t
   if (active) {
     const int b = gl;
     int nbi[3] = {b % M1, (b / M1) % M1, b / (M1 * M1)};
-    // with be: the group's lane 0 also sums the load vector of the row (same
-    // incidence order as k_scatter_vec), minus the Dirichlet lift when xd
+    // with be: the group also sums the load vector of the row (row_load_sum),
+    // and lane 0 subtracts the Dirichlet lift when xd
     const bool vec = be != nullptr && gl == 0;
     const bool lift = be != nullptr && xd != nullptr;
     double bsum[BS];
-#pragma unroll
-    for (int cc = 0; cc < BS; cc++) bsum[cc] = 0.0;
     int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+    if (be != nullptr) {
+      row_load_sum<BS>(ib, ie, inc, NN, be, gl, gmask, bsum);
+    } else {
+#pragma unroll
+      for (int cc = 0; cc < BS; cc++) bsum[cc] = 0.0;
+    }
     for (int64_t k = ib; k < ie; k++) {
       int32_t cb = __ldg(inc + k);
       int32_t c = cb / NN, a = cb - c * NN;
-      if (vec)
-#pragma unroll
-        for (int cc = 0; cc < BS; cc++) bsum[cc] += __ldg(be + (int64_t)c * NN * BS + a * BS + cc);
       double lv[BS];
 #pragma unroll
       for (int cc = 0; cc < BS; cc++) lv[cc] = 0.0;
@@ -1922,21 +2007,20 @@ static int kron_numeric(Matrix* A, int form, const double* coef, double nu, cons
   return s;
 }
 
-// vector scatter: each (row, component) sums its cells in ascending order
+// vector scatter: each (row, component) sums its cells in the order of
+// row_load_sum
 __global__ void k_scatter_vec(const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, int nn, int bs,
                               int64_t nrows, const double* __restrict__ be, double* __restrict__ b) {
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= nrows * bs) return;
   int64_t r = t / bs;
   int k = (int)(t - r * bs);
-  int nloc = nn * bs;
-  double s = 0.0;
-  for (int64_t i = inc_ptr[r]; i < inc_ptr[r + 1]; i++) {
-    int32_t cb = inc[i];
-    int32_t c = cb / nn, a = cb - c * nn;
-    s += be[(int64_t)c * nloc + a * bs + k];
-  }
-  b[t] = s;
+  // the order of row_load_sum, one thread per (row, component)
+  const int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+  double s[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) load_partial<1>(ib, ie, j, inc, nn, bs, be + k, &s[j]);
+  b[t] = (s[0] + s[1]) + (s[2] + s[3]);
 }
 
 int scatter_vector(const Space* sp, const int64_t* inc_ptr, const int32_t* inc, const double* be, double* b) {
@@ -2123,7 +2207,7 @@ static int elements_early(const Space* sp, int form, const NumIn& in, double nu,
   in.wait_on(ctx->aux);
   mesh_wait_coords_on(sp->mesh, ctx->aux);
   if (want_b) GT_TRY(dalloc(ctx, &E->be, nc * sp->nloc));
-  GT_TRY(dalloc(ctx, (unsigned char**)&E->Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz)));
+  GT_TRY(dalloc(ctx, (unsigned char**)&E->Ke, (int64_t)(nc * ke_per_cell(sp) * esz)));
   cudaStream_t main_stream = ctx->stream;
   ctx->stream = ctx->aux;
   int s = compute_elements(sp, form, in.coef.p, nu, precision, in.f.p, in.scoef.p, E->Ke, E->be, 1, &E->tab);
@@ -2224,7 +2308,7 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
                              &used_kron);
   if (s == GT_OK && !used_kron) {
     if (!pre) {
-      s = dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * sp->nloc * sp->nloc * esz));
+      s = dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * ke_per_cell(sp) * esz));
       if (s == GT_OK) s = compute_elements(sp, form, coef.p, nu, A->precision, f.p, scoef.p, Ke, be, 1);
     }
     mark(ctx, "elements");

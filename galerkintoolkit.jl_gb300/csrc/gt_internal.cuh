@@ -245,6 +245,15 @@ int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc,
 int build_incidence_arr(Ctx* ctx, const int32_t* dofs, int64_t n, int64_t nrows, int64_t** inc_ptr, int32_t** inc,
                         int64_t* ninc, bool sort);
 int build_pattern(Matrix* A);
+// Element matrices of scalar P1 tetrahedra (Laplacian, mass) are symmetric
+// and stored packed: the 10 entries of the upper triangle per cell, row by
+// row ({00,01,02,03,11,12,13,22,23,33}); every other space stores the full
+// nloc x nloc row-major block per cell.
+inline bool ke_packed(const Space* sp) {
+  return sp->mesh->ctype == GT_TET4 && sp->order == 1 && sp->ncomp == 1;
+}
+// entries of the element-matrix buffer per cell
+inline int64_t ke_per_cell(const Space* sp) { return ke_packed(sp) ? 10 : (int64_t)sp->nloc * sp->nloc; }
 // keep_tab (optional): receives the tabulation buffer the kernels read
 // instead of freeing it (for launches on a stream other than the main one,
 // whose reuse of the block must wait for them)

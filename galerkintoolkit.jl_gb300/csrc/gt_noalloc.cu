@@ -80,7 +80,7 @@ int gt_update_matrix_noalloc(gt_matrix* A, int form, const double* cell_coef, do
   int kprec = A->precision == GT_FP32 ? GT_FP32 : GT_FP64;
   size_t esz = kprec == GT_FP32 ? sizeof(float) : sizeof(double);
   size_t tab_bytes = ((size_t)tabulation_doubles(sp) * sizeof(double) + 255) & ~size_t(255);
-  size_t ke_bytes = (size_t)sp->mesh->ncells * sp->nloc * sp->nloc * esz;
+  size_t ke_bytes = (size_t)sp->mesh->ncells * ke_per_cell(sp) * esz;
   if (tab_bytes + ke_bytes > kNoAllocScratchBytes)
     return set_error(ctx, GT_ERR_INVALID,
                      "gt_update_matrix_noalloc: needs " + std::to_string(tab_bytes + ke_bytes) +

@@ -131,6 +131,18 @@ def test_assembly_is_deterministic():
     assert np.array_equal(A1.csr()[2], A2.csr()[2])
 
 
+@pytest.mark.parametrize("ci", [1, 3, 15])
+def test_fused_load_vector_is_bitwise_the_separate_pass(ci):
+    # P1 tets (packed element matrices), non-affine Q1 hexes, P2 tets: the
+    # element vectors come from the same kernel either way, and the fused
+    # scatter sums them in the order of the separate vector pass
+    m, V, ref, a, coef, form, order = _build(CASES[ci])
+    l = GT.source(1.0, coef)
+    b1 = GT.assemble_vector(l, np.float64, V)
+    _, b2 = GT.assemble_matrix_and_vector(a, l, np.float64, V)
+    assert np.array_equal(b1, b2)
+
+
 def test_update_matrix_equals_fresh_assembly():
     m, V, ref, a, coef, form, order = _build(CASES[1])
     A = GT.assemble_matrix(a, np.float64, V, V)

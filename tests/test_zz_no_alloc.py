@@ -68,7 +68,8 @@ def test_noalloc_refill_matches_update_matrix_q2_elasticity_fp32():
 
 def test_noalloc_refuses_oversize_and_host_memory():
     torch = pytest.importorskip("torch")
-    m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (62, 62, 62), simplexify=True)  # 1.43M cells x 16 x 8 B > 128 MiB
+    # 2.06M cells x 10 packed entries x 8 B > 128 MiB
+    m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (70, 70, 70), simplexify=True)
     V = GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m))
     A = GT.assemble_matrix(GT.laplacian(), np.float64, V, V)
     assert _refill_noalloc(A, _lib.GT_LAPLACE, None) == _lib.GT_ERR_INVALID
