@@ -45,8 +45,8 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # scatter kernels captured on 64^3 x 6 tets (1,572,864 cells) and scaled by
 # the cell ratio 3.375 (their traffic is proportional to the cells); the FP64
 # SpMV (sliced-ELL copy) captured on the full workload
-TRAFFIC: dict = {"elements": (44.413440e6 + 191.132416e6) * 3.375,
-                 "scatter": (326.434560e6 + 25.815296e6) * 3.375,
+TRAFFIC: dict = {"elements": (44.357120e6 + 114.737920e6) * 3.375,
+                 "scatter": (244.073472e6 + 24.874752e6) * 3.375,
                  "spmv": 159.938048e6 + 5.819904e6}
 
 
