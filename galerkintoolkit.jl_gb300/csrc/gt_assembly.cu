@@ -229,6 +229,31 @@ __global__ void k_inc_fill(const int32_t* __restrict__ cnd, int64_t n, const int
     if (d > 0) inc[__ldg(ptr + d - 1) + __ldg(rank + i)] = (int32_t)i;  // cell * nn + local node
   }
 }
+// The incidence of a matrix whose rows the row-per-thread count pass takes
+// (P1/Q1, at most kIncBucket incidences per row), in one pass: every entry
+// takes its position among its node's entries as in k_inc_count and is
+// written straight into its row's bucket of kIncBucket slots, so neither
+// the ranks nor a fill pass are needed.  Entries beyond a bucket are only
+// counted; the count pass then finds the row too long, and the incidence is
+// rebuilt by k_inc_count + k_inc_fill for the warp-per-row kernel.
+constexpr int kIncBucket = 32;
+__global__ void k_inc_place(const int32_t* __restrict__ cnd, int64_t n, int32_t* __restrict__ cnt,
+                            int32_t* __restrict__ bucket) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); i0 < n; i0 += stride) {
+    const int64_t i = i0 + lane;
+    const int32_t d = i < n ? __ldg(cnd + i) : 0;
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const int leader = __ffs(peers) - 1;
+    int32_t base = 0;
+    if (lane == leader && d > 0) base = atomicAdd(&cnt[d - 1], __popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    const int32_t pos = base + __popc(peers & ((1u << lane) - 1u));
+    if (d > 0 && pos < kIncBucket) bucket[(int64_t)(d - 1) * kIncBucket + pos] = (int32_t)i;
+  }
+}
+
 // sort each row's incidences ascending (= by cell): one warp per row,
 // bitonic sort in shared memory (icap slots per warp)
 // ascending bitonic sort of buf[0..P) (P a power of two >= 32) by one warp
@@ -474,18 +499,22 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
 // the thread sorts its incidences by insertion and builds its sorted column
 // list by binary search and insertion, both in shared memory interleaved
 // across the block's threads (element k of thread t at k * blockDim + t).
-// A row with more than 32 incidences or 32 columns sets *redo.
+// A row with more than 32 incidences or 32 columns sets *redo.  With bucket
+// the incidences are read from the row's bucket (k_inc_place) and the
+// sorted list is written to the row's CSR range.
 // A warp then works on 32 rows at once instead of one, which cuts the warp
 // instructions per row several times over the warp-per-row kernel (whose
 // sorts, rounds and compaction are per-warp costs).  Same results: the
 // row's incidences ascending, its distinct free columns ascending.  After a
 // *redo the warp kernel recounts every row.
 constexpr int kRowsMI = 32, kRowsS = 32;
+static_assert(kIncBucket == kRowsMI, "a bucket holds the incidences the row-per-thread pass takes");
 template <int NN>
 __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict__ inc_ptr, int32_t* __restrict__ inc,
                                                       const int32_t* __restrict__ cnd, int64_t nrows,
                                                       int32_t* __restrict__ rowcnt, int32_t* __restrict__ slots,
-                                                      uint8_t* __restrict__ small, int32_t* maxrow, int32_t* redo) {
+                                                      uint8_t* __restrict__ small, int32_t* maxrow, int32_t* redo,
+                                                      const int32_t* __restrict__ bucket) {
   extern __shared__ int32_t s_rows[];
   const int T = blockDim.x, tid = threadIdx.x;
   int32_t* I = s_rows + tid;                 // incidences, I[k * T]
@@ -500,8 +529,10 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
     small[r] = 0;
     return;
   }
+  // the row's incidences: from its bucket (k_inc_place) or its CSR list
+  const int32_t* src = bucket ? bucket + r * kIncBucket : inc + ib;
   for (int k = 0; k < ninc; k++) {
-    const int32_t v = inc[ib + k];
+    const int32_t v = src[k];
     int j = k;
     while (j > 0 && I[(j - 1) * T] > v) {
       I[j * T] = I[(j - 1) * T];
@@ -642,8 +673,10 @@ static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out) {
   return GT_OK;
 }
 
+// bucket (optional): the incidences were placed by k_inc_place (row r's in
+// bucket[r * kIncBucket ...]); A->inc then only receives the sorted lists
 template <int NN>
-static int launch_pattern(Matrix* A, int32_t maxinc) {
+static int launch_pattern(Matrix* A, int32_t maxinc, const int32_t* bucket) {
   // slot width of the count pass: P1/Q1/Q2-quad rows have <= 27 columns,
   // Q2-hex rows up to 125
   constexpr int S = NN >= 10 ? 128 : 32;  // P2-tet rows: up to ~70 columns
@@ -690,8 +723,8 @@ static int launch_pattern(Matrix* A, int32_t maxinc) {
     GT_CUDA(ctx, cudaMemsetAsync(dredo, 0, sizeof(int32_t), st));
     if (nrows > 0 && rows_pass) {
       const size_t rsm = (size_t)128 * (kRowsMI + kRowsS) * sizeof(int32_t);
-      k_pattern_rows<NN><<<GT_KC(ctx, grid_for(nrows, 128)), 128, rsm, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs,
-                                                                             nrows, rowcnt, slots, small, dmax, dredo);
+      k_pattern_rows<NN><<<GT_KC(ctx, grid_for(nrows, 128)), 128, rsm, st>>>(
+          A->inc_ptr, A->inc, sp->cell_ndofs, nrows, rowcnt, slots, small, dmax, dredo, bucket);
     } else if (nrows > 0) {
       k_pattern<NN, S, false><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, nrows,
                                                                           hcap, icap, rowcnt, nullptr, nullptr, slots,
@@ -713,6 +746,13 @@ static int launch_pattern(Matrix* A, int32_t maxinc) {
     memcpy(&redo, &ctx->h_scratch[2], sizeof(int32_t));
     if (!rows_pass || !redo) break;
     rows_pass = false;  // a row beyond 32 incidences or columns: count again, one warp per row
+    if (bucket) {
+      // the buckets kept only the first kIncBucket incidences of each row:
+      // the whole incidence again, by count + fill (the stream is idle here)
+      dfree(ctx, A->inc_ptr);
+      dfree(ctx, A->inc);
+      GT_TRY(build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc, false));
+    }
     GT_TRY(setup_warp());
   }
   dfree(ctx, dredo);
@@ -741,19 +781,50 @@ static int launch_pattern(Matrix* A, int32_t maxinc) {
   return GT_OK;
 }
 
+// incidence in one pass into row buckets (k_inc_place): row pointers from
+// the counts, the lists themselves left to the count pass
+static int build_incidence_bucket(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc, int32_t** bucket) {
+  cudaStream_t st = ctx->stream;
+  const int64_t n = sp->mesh->ncells * sp->nn, nrows = sp->nfree_nodes;
+  int32_t* cnt = nullptr;
+  GT_TRY(dalloc(ctx, &cnt, nrows + 1));
+  GT_TRY(dalloc(ctx, bucket, nrows > 0 ? nrows * kIncBucket : 1));
+  GT_TRY(dalloc(ctx, inc_ptr, nrows + 1));
+  GT_TRY(dalloc(ctx, inc, n > 0 ? n : 1));
+  GT_CUDA(ctx, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * (nrows + 1), st));
+  if (n > 0) k_inc_place<<<GT_KC(ctx, grid_for(n, 256)), 256, 0, st>>>(sp->cell_ndofs, n, cnt, *bucket);
+  GT_LAUNCH(ctx, "k_inc_place");
+  GT_TRY(exclusive_scan_i64(ctx, cnt, *inc_ptr, nrows));
+  dfree(ctx, cnt);
+  return GT_OK;
+}
+
 int build_pattern(Matrix* A) {
   const Space* sp = A->space;
   Ctx* ctx = sp->mesh->ctx;
   A->nbrows = sp->nfree_nodes;
-  const int32_t maxinc = -1;  // computed by launch_pattern if the warp kernel runs
-  switch (sp->nn) {
-    case 4: return launch_pattern<4>(A, maxinc);
-    case 8: return launch_pattern<8>(A, maxinc);
-    case 9: return launch_pattern<9>(A, maxinc);
-    case 10: return launch_pattern<10>(A, maxinc);
-    case 27: return launch_pattern<27>(A, maxinc);
+  // P1/Q1 rows go through the row-per-thread count pass, whose incidence
+  // comes in one pass through row buckets
+  int32_t* bucket = nullptr;
+  if ((sp->nn == 4 || sp->nn == 8) && ctx->pattern_rows) {
+    GT_TRY(build_incidence_bucket(ctx, sp, &A->inc_ptr, &A->inc, &bucket));
+    A->ninc = -1;
+  } else {
+    GT_TRY(build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc, false));
   }
-  return set_error(ctx, GT_ERR_UNSUPPORTED, "element not supported");
+  mark(ctx, "incidence");
+  const int32_t maxinc = -1;  // computed by launch_pattern if the warp kernel runs
+  int s = GT_OK;
+  switch (sp->nn) {
+    case 4: s = launch_pattern<4>(A, maxinc, bucket); break;
+    case 8: s = launch_pattern<8>(A, maxinc, bucket); break;
+    case 9: s = launch_pattern<9>(A, maxinc, nullptr); break;
+    case 10: s = launch_pattern<10>(A, maxinc, nullptr); break;
+    case 27: s = launch_pattern<27>(A, maxinc, nullptr); break;
+    default: s = set_error(ctx, GT_ERR_UNSUPPORTED, "element not supported");
+  }
+  if (bucket) dfree(ctx, bucket);
+  return s;
 }
 
 // ---------------------------------------------------------------------------
@@ -2462,9 +2533,7 @@ static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double n
   // element kernels on the auxiliary stream, beside the sparsity kernels
   EarlyElems early;
   if (s == GT_OK) s = elements_early(sp, form, in, nu, precision, b != nullptr, &early);
-  if (s == GT_OK) s = build_incidence(ctx, sp, &A->inc_ptr, &A->inc, &A->ninc, false);
-  mark(ctx, "incidence");
-  if (s == GT_OK) s = build_pattern(A);
+  if (s == GT_OK) s = build_pattern(A);  // incidence + sparsity
   cudaEvent_t side_done = nullptr;
   const int bs = A->bs;
   const int64_t nscal = A->nbrows * bs, nnz = A->bnnz * bs * bs;

@@ -244,6 +244,8 @@ int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc,
 // the same for any array of n node-level DOF ids (>0 free) over nrows rows
 int build_incidence_arr(Ctx* ctx, const int32_t* dofs, int64_t n, int64_t nrows, int64_t** inc_ptr, int32_t** inc,
                         int64_t* ninc, bool sort);
+// the matrix's incidence (A->inc_ptr, A->inc: every row's list ascending) and
+// its sparsity (rowptr, colind, max_row)
 int build_pattern(Matrix* A);
 // Element matrices of scalar P1 tetrahedra (Laplacian, mass) are symmetric
 // and stored packed: the 10 entries of the upper triangle per cell, row by
