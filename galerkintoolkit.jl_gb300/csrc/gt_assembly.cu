@@ -529,16 +529,42 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
     small[r] = 0;
     return;
   }
-  // the row's incidences: from its bucket (k_inc_place) or its CSR list
-  const int32_t* src = bucket ? bucket + r * kIncBucket : inc + ib;
-  for (int k = 0; k < ninc; k++) {
-    const int32_t v = src[k];
-    int j = k;
-    while (j > 0 && I[(j - 1) * T] > v) {
-      I[j * T] = I[(j - 1) * T];
-      j--;
+  // the row's incidences, sorted by insertion in I: from its bucket
+  // (k_inc_place; 16-byte aligned, so all of it is loaded at once into I and
+  // sorted in place) or from its CSR list
+  if (bucket) {
+    const int4* b4 = reinterpret_cast<const int4*>(bucket + r * kIncBucket);
+    int4 v[kIncBucket / 4];
+#pragma unroll
+    for (int q = 0; q < kIncBucket / 4; q++)
+      if (4 * q < ninc) v[q] = __ldg(b4 + q);
+#pragma unroll
+    for (int q = 0; q < kIncBucket / 4; q++)
+      if (4 * q < ninc) {
+        I[(4 * q) * T] = v[q].x;
+        I[(4 * q + 1) * T] = v[q].y;
+        I[(4 * q + 2) * T] = v[q].z;
+        I[(4 * q + 3) * T] = v[q].w;
+      }
+    for (int k = 1; k < ninc; k++) {
+      const int32_t x = I[k * T];
+      int j = k;
+      while (j > 0 && I[(j - 1) * T] > x) {
+        I[j * T] = I[(j - 1) * T];
+        j--;
+      }
+      I[j * T] = x;
     }
-    I[j * T] = v;
+  } else {
+    for (int k = 0; k < ninc; k++) {
+      const int32_t x = inc[ib + k];
+      int j = k;
+      while (j > 0 && I[(j - 1) * T] > x) {
+        I[j * T] = I[(j - 1) * T];
+        j--;
+      }
+      I[j * T] = x;
+    }
   }
   for (int k = 0; k < ninc; k++) inc[ib + k] = I[k * T];
   int n = 0;
@@ -1060,7 +1086,8 @@ static int dispatch_form(const Space* sp, int form, const double* coef, double n
 // cofactors and det stay FP64 in every precision; in FP32 mode the cofactor
 // columns are rounded to FP32 for the entries.
 // the quadrature sums of the P1 reference cell, once per assembly:
-// k[0] = sum_q w_q, k[1..4] = sum_q w_q phi_n(q), k[5..20] = sum_q w_q phi_n phi_m
+// k[0] = sum_q w_q, k[1..4] = sum_q w_q phi_n(q), k[5..20] = sum_q w_q phi_n phi_m,
+// k[21] = 1 when k[1..4] are bitwise equal (a symmetric rule), else 0
 __global__ void k_p1_consts(const double* __restrict__ tab, TabLayout L, double* __restrict__ k) {
   const int t = threadIdx.x;
   double s = 0.0;
@@ -1073,6 +1100,10 @@ __global__ void k_p1_consts(const double* __restrict__ tab, TabLayout L, double*
     for (int q = 0; q < 4; q++) s += tab[L.off_w + q] * tab[L.off_sv + q * 4 + n] * tab[L.off_sv + q * 4 + m];
   }
   if (t < 21) k[t] = s;
+  long long b[4];
+#pragma unroll
+  for (int n = 0; n < 4; n++) b[n] = __double_as_longlong(__shfl_sync(0xffffffffu, s, n + 1));
+  if (t == 21) k[t] = (b[0] == b[1] && b[0] == b[2] && b[0] == b[3]) ? 1.0 : 0.0;
 }
 
 template <int FORM, class T>
@@ -1086,6 +1117,10 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
   const double* s_load = consts + 1;
   const double* s_mass = consts + 5;
   const double s_wsum = __ldg(consts);
+  // uniform over the launch: one load entry for all four nodes, and the
+  // source value without a cell coefficient (1 * f is f)
+  const bool load_equal = __double_as_longlong(__ldg(consts + 21)) != 0;
+  const double f0 = fsrc ? __ldg(fsrc) : 0.0;
   // grid-stride over the cells (one thread per cell)
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
     int4 nd = *reinterpret_cast<const int4*>(cell_nodes + 4 * c);
@@ -1103,7 +1138,8 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
     double c20 = d1 * a2 - d2 * a1, c21 = d2 * a0 - d0 * a2, c22 = d0 * a1 - d1 * a0;  // column 1
     double c30 = a1 * b2 - a2 * b1, c31 = a2 * b0 - a0 * b2, c32 = a0 * b1 - a1 * b0;  // column 2
     double det = a0 * c10 + a1 * c11 + a2 * c12;
-    if (!(det != 0.0)) atomicOr(err, DEV_ERR_DEGENERATE);
+    // det == +-0 tested on its bits: integer instructions, not an FP64 compare
+    if ((__double_as_longlong(det) << 1) == 0) atomicOr(err, DEV_ERR_DEGENERATE);
     double adet = fabs(det);
     double cf = coef ? coef[c] : 1.0;
     if (want_matrix) {
@@ -1144,9 +1180,16 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
       for (int e = 0; e < 10; e++) K[e] = k[e];
     }
     if (be) {
-      double sc = (scoef ? scoef[c] : 1.0) * fsrc[0] * adet;
+      const double sc = (scoef ? scoef[c] * f0 : f0) * adet;
+      if (load_equal) {
+        const double v = sc * __ldg(s_load);
+        double2* b2 = reinterpret_cast<double2*>(be + 4 * c);  // 32-byte records of a pool block
+        b2[0] = make_double2(v, v);
+        b2[1] = make_double2(v, v);
+      } else {
   #pragma unroll
-      for (int n = 0; n < 4; n++) be[4 * c + n] = sc * __ldg(s_load + n);
+        for (int n = 0; n < 4; n++) be[4 * c + n] = sc * __ldg(s_load + n);
+      }
     }
   }
 }
