@@ -699,6 +699,38 @@ static int max_diff(Ctx* ctx, const int64_t* ptr, int64_t n, int32_t* out) {
   return GT_OK;
 }
 
+// The last cell among the incidences of each row chunk (rows
+// nrows*k/K .. nrows*(k+1)/K, K = kRowChunks): after the count pass every
+// row's list is sorted, so a row's last incidence holds its last cell.  Per
+// warp, one max reduction and one atomicMax for each chunk its rows touch.
+__global__ void k_chunk_last(const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc, int64_t nrows,
+                             int nn, int32_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r0 = blockIdx.x * (int64_t)blockDim.x + (threadIdx.x & ~31); r0 < nrows; r0 += stride) {
+    const int64_t r = r0 + lane;
+    const bool in = r < nrows;
+    int32_t v = -1;
+    int k = 0;
+    if (in) {
+      const int64_t b = inc_ptr[r], e = inc_ptr[r + 1];
+      if (e > b) v = inc[e - 1] / nn;
+      k = (int)(((r + 1) * kRowChunks - 1) / nrows);  // the chunk whose range holds r
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, in);
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      const int kk = __shfl_sync(0xffffffffu, k, src);
+      const bool mine = in && k == kk;
+      int32_t m = mine ? v : -1;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+      if (lane == src && m >= 0) atomicMax(out + kk, m);
+      todo &= ~__ballot_sync(0xffffffffu, mine);
+    }
+  }
+}
+
 // bucket (optional): the incidences were placed by k_inc_place (row r's in
 // bucket[r * kIncBucket ...]); A->inc then only receives the sorted lists
 template <int NN>
@@ -743,6 +775,8 @@ static int launch_pattern(Matrix* A, int32_t maxinc, const int32_t* bucket) {
   if (!rows_pass) GT_TRY(setup_warp());
   int32_t* dredo = nullptr;
   GT_TRY(dalloc(ctx, &dredo, 1));
+  int32_t* dlast = nullptr;
+  GT_TRY(dalloc(ctx, &dlast, kRowChunks));
   for (int attempt = 0; attempt < 2; attempt++) {
     const int grid = grid_for(nrows, warps);
     GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
@@ -758,7 +792,12 @@ static int launch_pattern(Matrix* A, int32_t maxinc, const int32_t* bucket) {
     }
     GT_LAUNCH(ctx, "k_pattern<count>");
     GT_TRY(exclusive_scan_i64(ctx, rowcnt, A->rowptr, nrows));
+    GT_CUDA(ctx, cudaMemsetAsync(dlast, 0xff, sizeof(int32_t) * kRowChunks, st));
+    if (nrows > 0)
+      k_chunk_last<<<GT_KC(ctx, grid_for(nrows, 256)), 256, 0, st>>>(A->inc_ptr, A->inc, nrows, sp->nn, dlast);
+    GT_LAUNCH(ctx, "k_chunk_last");
     mark(ctx, "pattern_count");
+    GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[16], dlast, sizeof(int32_t) * kRowChunks, cudaMemcpyDeviceToHost, st));
     GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], A->rowptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[1], dmax, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[2], dredo, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -782,6 +821,9 @@ static int launch_pattern(Matrix* A, int32_t maxinc, const int32_t* bucket) {
     GT_TRY(setup_warp());
   }
   dfree(ctx, dredo);
+  dfree(ctx, dlast);
+  memcpy(A->chunk_last, &ctx->h_scratch[16], sizeof(int32_t) * kRowChunks);
+  A->chunk_last_ok = true;
   A->bnnz = ctx->h_scratch[0];
   int32_t mr = 0;
   memcpy(&mr, &ctx->h_scratch[1], sizeof(int32_t));
@@ -1110,8 +1152,8 @@ template <int FORM, class T>
 __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ coords,
                                                      const int32_t* __restrict__ cell_nodes,
                                                      const double* __restrict__ coef,
-                                                     const double* __restrict__ consts, int64_t ncells,
-                                                     T* __restrict__ Ke, double* __restrict__ be,
+                                                     const double* __restrict__ consts, int64_t c_begin,
+                                                     int64_t ncells, T* __restrict__ Ke, double* __restrict__ be,
                                                      const double* __restrict__ fsrc,
                                                      const double* __restrict__ scoef, int want_matrix, uint32_t* err) {
   const double* s_load = consts + 1;
@@ -1121,8 +1163,9 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
   // source value without a cell coefficient (1 * f is f)
   const bool load_equal = __double_as_longlong(__ldg(consts + 21)) != 0;
   const double f0 = fsrc ? __ldg(fsrc) : 0.0;
-  // grid-stride over the cells (one thread per cell)
-  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells; c += (int64_t)gridDim.x * blockDim.x) {
+  // grid-stride over the cells [c_begin, ncells) (one thread per cell)
+  for (int64_t c = c_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells;
+       c += (int64_t)gridDim.x * blockDim.x) {
     int4 nd = *reinterpret_cast<const int4*>(cell_nodes + 4 * c);
     const double* p0 = coords + 3 * (int64_t)nd.x;
     const double* p1 = coords + 3 * (int64_t)nd.y;
@@ -1197,21 +1240,32 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
 // element kernels per cell type / order; returns GT_OK or an error
 template <class T>
 static int elements_T(const Space* sp, int form, const double* coef, double nu, const double* tab, const TabLayout& L,
-                      T* Ke, double* be, const double* f, const double* scoef, int want_matrix) {
+                      T* Ke, double* be, const double* f, const double* scoef, int want_matrix,
+                      ElemChunks* chunks = nullptr) {
+  if (chunks && !(sp->mesh->ctype == GT_TET4 && sp->order == 1 && sp->ncomp == 1)) chunks->n = 0;
   int ct = sp->mesh->ctype, o = sp->order;
   if (ct == GT_TET4 && o == 1 && sp->ncomp == 1 && (form == GT_LAPLACE || form == GT_MASS)) {
     Ctx* ctx = ctx_of(sp);
     int64_t nc = sp->mesh->ncells;
     double* consts = const_cast<double*>(tab) + L.off_k;  // inside the tabulation buffer: no allocation
     k_p1_consts<<<GT_KC(ctx, 1), 32, 0, ctx->stream>>>(tab, L, consts);
-    const int grid = grid_for(nc, 256);
-    if (form == GT_LAPLACE)
-      k_elements_p1<GT_LAPLACE, T><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
-          sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
-    else
-      k_elements_p1<GT_MASS, T><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
-          sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, nc, Ke, be, f, scoef, want_matrix, ctx->d_err);
-    GT_LAUNCH(ctx, "k_elements_p1");
+    // one launch, or one per cell chunk with the chunk's event behind it
+    const int nch = chunks ? chunks->n : 1;
+    for (int i = 0; i < nch; i++) {
+      const int64_t c0 = nc * i / nch, c1 = nc * (i + 1) / nch;
+      const int grid = grid_for(c1 - c0 > 0 ? c1 - c0 : 1, 256);
+      if (form == GT_LAPLACE)
+        k_elements_p1<GT_LAPLACE, T><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
+            sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, c0, c1, Ke, be, f, scoef, want_matrix, ctx->d_err);
+      else
+        k_elements_p1<GT_MASS, T><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
+            sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, c0, c1, Ke, be, f, scoef, want_matrix, ctx->d_err);
+      GT_LAUNCH(ctx, "k_elements_p1");
+      if (chunks) {
+        chunks->end[i] = c1;
+        GT_CUDA(ctx, cudaEventRecord(chunks->ev[i], ctx->stream));
+      }
+    }
     return GT_OK;
   }
   // P2 tets: the map is affine but the shape gradients vary over the cell, so
@@ -1226,7 +1280,8 @@ static int elements_T(const Space* sp, int form, const double* coef, double nu, 
 }
 
 int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision, const double* f,
-                     const double* d_scoef, void* Ke, double* be, int want_matrix, double** keep_tab) {
+                     const double* d_scoef, void* Ke, double* be, int want_matrix, double** keep_tab,
+                     ElemChunks* chunks) {
   Ctx* ctx = ctx_of(sp);
   if (form != GT_LAPLACE && form != GT_MASS && form != GT_ELASTICITY)
     return set_error(ctx, GT_ERR_UNSUPPORTED, "weak form not supported (Laplacian, mass, linear elasticity only)");
@@ -1237,9 +1292,9 @@ int compute_elements(const Space* sp, int form, const double* d_coef, double nu,
   GT_TRY(get_tab(ctx, sp->mesh->ctype, sp->order, &tab, &L));
   int s;
   if (precision == GT_FP32)
-    s = elements_T<float>(sp, form, d_coef, nu, tab, L, (float*)Ke, be, f, d_scoef, want_matrix);
+    s = elements_T<float>(sp, form, d_coef, nu, tab, L, (float*)Ke, be, f, d_scoef, want_matrix, chunks);
   else
-    s = elements_T<double>(sp, form, d_coef, nu, tab, L, (double*)Ke, be, f, d_scoef, want_matrix);
+    s = elements_T<double>(sp, form, d_coef, nu, tab, L, (double*)Ke, be, f, d_scoef, want_matrix, chunks);
   if (keep_tab) *keep_tab = tab;
   else dfree(ctx, tab);
   return s;
@@ -2291,10 +2346,17 @@ struct EarlyElems {
   double* be = nullptr;
   double* tab = nullptr;
   cudaEvent_t done = nullptr;
+  ElemChunks chunks;  // chunked launches (P1): the event of each cell chunk
 };
 
+static void early_put_chunk_events(Ctx* ctx, EarlyElems* E) {
+  for (int i = 0; i < kRowChunks; i++)
+    if (E->chunks.ev[i]) event_put(ctx, E->chunks.ev[i]);
+  E->chunks = ElemChunks{};
+}
+
 static int elements_early(const Space* sp, int form, const NumIn& in, double nu, int precision, bool want_b,
-                          EarlyElems* E) {
+                          bool chunked, EarlyElems* E) {
   Ctx* ctx = ctx_of(sp);
   if (ctx->prof || !ctx->overlap || !ctx->aux || sp->mesh->ctype != GT_TET4) return GT_OK;
   // only when the main stream outranks the auxiliary one (the context's own
@@ -2313,6 +2375,17 @@ static int elements_early(const Space* sp, int form, const NumIn& in, double nu,
   cudaEvent_t start = event_get(ctx);
   E->done = event_get(ctx);
   if (!start || !E->done) return set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
+  E->chunks.n = chunked ? kRowChunks : 0;
+  for (int i = 0; i < E->chunks.n; i++) {
+    E->chunks.ev[i] = event_get(ctx);
+    if (!E->chunks.ev[i]) {
+      event_put(ctx, start);
+      event_put(ctx, E->done);
+      early_put_chunk_events(ctx, E);
+      *E = EarlyElems{};
+      return set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
+    }
+  }
   // the auxiliary stream starts after all work queued so far (mesh, space,
   // and every block the pool may hand out below) and after the uploads
   GT_CUDA(ctx, cudaEventRecord(start, ctx->stream));
@@ -2324,7 +2397,8 @@ static int elements_early(const Space* sp, int form, const NumIn& in, double nu,
   GT_TRY(dalloc(ctx, (unsigned char**)&E->Ke, (int64_t)(nc * ke_per_cell(sp) * esz)));
   cudaStream_t main_stream = ctx->stream;
   ctx->stream = ctx->aux;
-  int s = compute_elements(sp, form, in.coef.p, nu, precision, in.f.p, in.scoef.p, E->Ke, E->be, 1, &E->tab);
+  int s = compute_elements(sp, form, in.coef.p, nu, precision, in.f.p, in.scoef.p, E->Ke, E->be, 1, &E->tab,
+                           chunked ? &E->chunks : nullptr);
   if (s == GT_OK && cudaEventRecord(E->done, ctx->aux) != cudaSuccess) s = check_cuda(ctx, cudaGetLastError(), "event");
   ctx->stream = main_stream;
   if (s != GT_OK) {
@@ -2334,10 +2408,29 @@ static int elements_early(const Space* sp, int form, const NumIn& in, double nu,
     if (E->Ke) pool_free(ctx, E->Ke);
     if (E->be) dfree(ctx, E->be);
     event_put(ctx, E->done);
+    early_put_chunk_events(ctx, E);
     *E = EarlyElems{};
     return s;
   }
   E->active = true;
+  return GT_OK;
+}
+
+// the main stream waits for the whole element stage; its events and its
+// tabulation block go back to the context
+static int join_stage(Ctx* ctx, EarlyElems* E) {
+  if (!E->active) return GT_OK;
+  E->active = false;
+  cudaError_t e = cudaStreamWaitEvent(ctx->stream, E->done, 0);
+  event_put(ctx, E->done);
+  E->done = nullptr;
+  early_put_chunk_events(ctx, E);
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(ctx->aux);
+    dfree(ctx, E->tab);
+    return check_cuda(ctx, e, "join of the element stage");
+  }
+  dfree(ctx, E->tab);  // later users of the block are ordered after the join
   return GT_OK;
 }
 
@@ -2349,6 +2442,7 @@ static void early_release(Ctx* ctx, EarlyElems* E) {
   pool_free(ctx, E->Ke);
   if (E->be) dfree(ctx, E->be);
   event_put(ctx, E->done);
+  early_put_chunk_events(ctx, E);
   *E = EarlyElems{};
 }
 
@@ -2399,27 +2493,44 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
   double* be = nullptr;
   const bool pre = early && early->active;
   bool b_copied = false;  // a host b already downloaded chunk by chunk
+  // element stage already queued on the auxiliary stream: taken over here.
+  // When the values go to host buffers chunk by chunk and the stage was
+  // launched in cell chunks (P1), it is pipelined with the scatter: each row
+  // chunk's scatter waits only for the element chunks up to its rows' last
+  // cell, so the downloads start while elements are still computed, and the
+  // whole stage is joined after the last chunk.  Otherwise it is joined
+  // before the scatter (on device buffers that is faster: scatter blocks
+  // beside FP64-bound element blocks run slower than after them)
+  EarlyElems stage;
+  const bool host_chunks = hc && pat_down && A->bs == 1 && values_done;
+  const bool piped = host_chunks && pre && early->chunks.n == kRowChunks && A->chunk_last_ok;
   if (pre) {
-    // element stage already queued on the auxiliary stream: join it
-    GT_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, early->done, 0));
-    event_put(ctx, early->done);
-    Ke = early->Ke;
-    be = early->be;
-    dfree(ctx, early->tab);  // later users of the block are ordered after the join
+    stage = *early;
     *early = EarlyElems{};
+    Ke = stage.Ke;
+    be = stage.be;
+    if (!piped) GT_TRY(join_stage(ctx, &stage));
   } else if (b_out) {
     GT_TRY(dalloc(ctx, &be, nc * sp->nloc));
   }
+  // the main stream waits for the element chunks that hold row chunk k's cells
+  auto wait_rows = [&](int k) -> int {
+    const int32_t last = A->chunk_last[k];
+    int j = 0;
+    while (j < stage.chunks.n - 1 && stage.chunks.end[j] <= last) j++;
+    GT_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, stage.chunks.ev[j], 0));
+    return GT_OK;
+  };
   const bool dev = b_out && is_device_ptr(b_out);
   double* bd = b_out;
   const int64_t nb = sp->nfree_nodes * sp->ncomp;
-  if (b_out && !dev) GT_TRY(dalloc(ctx, &bd, nb));
+  int s = GT_OK;
+  if (b_out && !dev) s = dalloc(ctx, &bd, nb);  // errors fall through to the stage release below
   int used_kron = 0;
   // the load vector (and the Dirichlet lift) is summed inside the matrix
   // scatter, over the same incidences
-  int s = pre ? GT_OK
-              : kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr,
-                             &used_kron);
+  if (s == GT_OK && !pre)
+    s = kron_numeric(A, form, coef.p, nu, f.p, scoef.p, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr, &used_kron);
   if (s == GT_OK && !used_kron) {
     if (!pre) {
       s = dalloc(ctx, (unsigned char**)&Ke, (int64_t)(nc * ke_per_cell(sp) * esz));
@@ -2427,18 +2538,20 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
     }
     mark(ctx, "elements");
     if (s == GT_OK) s = alloc_values(A);
-    if (s == GT_OK && hc && pat_down && A->bs == 1 && values_done) {
+    if (s == GT_OK && host_chunks) {
       // all chunks are queued first (the device never waits for the host),
       // then the host row pointers -- downloaded meanwhile -- give each
       // chunk's range for its download behind the chunk's event; a host b
       // comes back chunk by chunk too, so only the last chunk's rows are left
       // to copy after the last scatter
-      constexpr int NCH = 8;
+      constexpr int NCH = kRowChunks;
       cudaEvent_t evs[NCH] = {};
       int nq = 0;
       for (int k = 0; k < NCH && s == GT_OK; k++, nq++) {
         const int64_t r0 = A->nbrows * k / NCH, r1 = A->nbrows * (k + 1) / NCH;
-        s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr, r0, r1);
+        if (piped) s = wait_rows(k);
+        if (s == GT_OK)
+          s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr, r0, r1);
         evs[k] = event_get(ctx);
         if (s == GT_OK && !evs[k]) s = set_error(ctx, GT_ERR_CUDA, "cudaEventCreate failed");
         if (s == GT_OK && cudaEventRecord(evs[k], ctx->stream) != cudaSuccess)
@@ -2482,6 +2595,18 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
       s = scatter_matrix(A, Ke, kprec, A->precision, be, b_out ? bd : nullptr, b_out ? xd.p : nullptr);
     }
     mark(ctx, "scatter");
+  }
+  if (stage.active) {
+    if (s == GT_OK) {
+      s = join_stage(ctx, &stage);
+    } else {
+      // nothing of the stage may be reused before the auxiliary stream drains
+      cudaStreamSynchronize(ctx->aux);
+      event_put(ctx, stage.done);
+      early_put_chunk_events(ctx, &stage);
+      dfree(ctx, stage.tab);
+      stage.active = false;
+    }
   }
   // host b: the copy is queued here; the caller's device_status() call
   // synchronises the stream before returning (the freed staging block is only
@@ -2575,7 +2700,9 @@ static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double n
   int s = in.init(sp, cell_coef, f, source_coef, b ? xd : nullptr, true);
   // element kernels on the auxiliary stream, beside the sparsity kernels
   EarlyElems early;
-  if (s == GT_OK) s = elements_early(sp, form, in, nu, precision, b != nullptr, &early);
+  // (in cell chunks when the values go to host buffers: the scatter and the
+  // downloads then start on the first chunks)
+  if (s == GT_OK) s = elements_early(sp, form, in, nu, precision, b != nullptr, hc != nullptr, &early);
   if (s == GT_OK) s = build_pattern(A);  // incidence + sparsity
   cudaEvent_t side_done = nullptr;
   const int bs = A->bs;

@@ -201,6 +201,9 @@ struct Space {
   int64_t ninc = 0;
 };
 
+// row chunks of the pipelined scatter (and of its downloads to host buffers)
+constexpr int kRowChunks = 8;
+
 struct Matrix {
   Ctx* ctx = nullptr;  // owning context
   Space* space = nullptr;
@@ -225,6 +228,11 @@ struct Matrix {
   double* sell_v64 = nullptr;
   float* sell_v32 = nullptr;
   bool sell_cur64 = false, sell_cur32 = false;  // values match val64 / val32
+  // the last cell among the incidences of each row chunk (rows nbrows*k/K ..
+  // nbrows*(k+1)/K, K = kRowChunks; -1: no incidence), from the count pass:
+  // the scatter of a chunk waits only for the element chunks up to that cell
+  int32_t chunk_last[kRowChunks] = {};
+  bool chunk_last_ok = false;
 };
 
 // called by every kernel launch that rewrites a matrix's values
@@ -259,9 +267,17 @@ inline int64_t ke_per_cell(const Space* sp) { return ke_packed(sp) ? 10 : (int64
 // keep_tab (optional): receives the tabulation buffer the kernels read
 // instead of freeing it (for launches on a stream other than the main one,
 // whose reuse of the block must wait for them)
+// Element kernels launched over cell chunks, each followed by its event (so
+// a consumer can start on the first chunks): n events in, n chunks out; a
+// path without chunked launches sets n = 0.
+struct ElemChunks {
+  int n = 0;
+  int64_t end[kRowChunks] = {};  // chunk i covers cells [end[i-1], end[i])
+  cudaEvent_t ev[kRowChunks] = {};
+};
 int compute_elements(const Space* sp, int form, const double* d_coef, double nu, int precision,
                      const double* f, const double* d_scoef, void* Ke, double* be, int want_matrix,
-                     double** keep_tab = nullptr);
+                     double** keep_tab = nullptr, ElemChunks* chunks = nullptr);
 // be/bvec (optional): element vectors and the load vector summed in the same
 // pass; xd: Dirichlet values (lift); [r0, r1): block rows (r1 < 0: all)
 int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precision, const double* be = nullptr,
