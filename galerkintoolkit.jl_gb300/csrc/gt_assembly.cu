@@ -733,8 +733,9 @@ __global__ void k_chunk_last(const int64_t* __restrict__ inc_ptr, const int32_t*
 
 // bucket (optional): the incidences were placed by k_inc_place (row r's in
 // bucket[r * kIncBucket ...]); A->inc then only receives the sorted lists
+// want_last: also find each row chunk's last cell (A->chunk_last)
 template <int NN>
-static int launch_pattern(Matrix* A, int32_t maxinc, const int32_t* bucket) {
+static int launch_pattern(Matrix* A, int32_t maxinc, const int32_t* bucket, bool want_last) {
   // slot width of the count pass: P1/Q1/Q2-quad rows have <= 27 columns,
   // Q2-hex rows up to 125
   constexpr int S = NN >= 10 ? 128 : 32;  // P2-tet rows: up to ~70 columns
@@ -792,12 +793,14 @@ static int launch_pattern(Matrix* A, int32_t maxinc, const int32_t* bucket) {
     }
     GT_LAUNCH(ctx, "k_pattern<count>");
     GT_TRY(exclusive_scan_i64(ctx, rowcnt, A->rowptr, nrows));
-    GT_CUDA(ctx, cudaMemsetAsync(dlast, 0xff, sizeof(int32_t) * kRowChunks, st));
-    if (nrows > 0)
-      k_chunk_last<<<GT_KC(ctx, grid_for(nrows, 256)), 256, 0, st>>>(A->inc_ptr, A->inc, nrows, sp->nn, dlast);
-    GT_LAUNCH(ctx, "k_chunk_last");
+    if (want_last) {
+      GT_CUDA(ctx, cudaMemsetAsync(dlast, 0xff, sizeof(int32_t) * kRowChunks, st));
+      if (nrows > 0)
+        k_chunk_last<<<GT_KC(ctx, grid_for(nrows, 256)), 256, 0, st>>>(A->inc_ptr, A->inc, nrows, sp->nn, dlast);
+      GT_LAUNCH(ctx, "k_chunk_last");
+      GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[16], dlast, sizeof(int32_t) * kRowChunks, cudaMemcpyDeviceToHost, st));
+    }
     mark(ctx, "pattern_count");
-    GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[16], dlast, sizeof(int32_t) * kRowChunks, cudaMemcpyDeviceToHost, st));
     GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], A->rowptr + nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
     GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[1], dmax, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[2], dredo, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
@@ -822,8 +825,10 @@ static int launch_pattern(Matrix* A, int32_t maxinc, const int32_t* bucket) {
   }
   dfree(ctx, dredo);
   dfree(ctx, dlast);
-  memcpy(A->chunk_last, &ctx->h_scratch[16], sizeof(int32_t) * kRowChunks);
-  A->chunk_last_ok = true;
+  if (want_last) {
+    memcpy(A->chunk_last, &ctx->h_scratch[16], sizeof(int32_t) * kRowChunks);
+    A->chunk_last_ok = true;
+  }
   A->bnnz = ctx->h_scratch[0];
   int32_t mr = 0;
   memcpy(&mr, &ctx->h_scratch[1], sizeof(int32_t));
@@ -867,7 +872,7 @@ static int build_incidence_bucket(Ctx* ctx, const Space* sp, int64_t** inc_ptr, 
   return GT_OK;
 }
 
-int build_pattern(Matrix* A) {
+int build_pattern(Matrix* A, bool chunk_last) {
   const Space* sp = A->space;
   Ctx* ctx = sp->mesh->ctx;
   A->nbrows = sp->nfree_nodes;
@@ -884,11 +889,11 @@ int build_pattern(Matrix* A) {
   const int32_t maxinc = -1;  // computed by launch_pattern if the warp kernel runs
   int s = GT_OK;
   switch (sp->nn) {
-    case 4: s = launch_pattern<4>(A, maxinc, bucket); break;
-    case 8: s = launch_pattern<8>(A, maxinc, bucket); break;
-    case 9: s = launch_pattern<9>(A, maxinc, nullptr); break;
-    case 10: s = launch_pattern<10>(A, maxinc, nullptr); break;
-    case 27: s = launch_pattern<27>(A, maxinc, nullptr); break;
+    case 4: s = launch_pattern<4>(A, maxinc, bucket, chunk_last); break;
+    case 8: s = launch_pattern<8>(A, maxinc, bucket, chunk_last); break;
+    case 9: s = launch_pattern<9>(A, maxinc, nullptr, chunk_last); break;
+    case 10: s = launch_pattern<10>(A, maxinc, nullptr, chunk_last); break;
+    case 27: s = launch_pattern<27>(A, maxinc, nullptr, chunk_last); break;
     default: s = set_error(ctx, GT_ERR_UNSUPPORTED, "element not supported");
   }
   if (bucket) dfree(ctx, bucket);
@@ -2703,7 +2708,9 @@ static int assemble_mv(gt_space* sp, int form, const double* cell_coef, double n
   // (in cell chunks when the values go to host buffers: the scatter and the
   // downloads then start on the first chunks)
   if (s == GT_OK) s = elements_early(sp, form, in, nu, precision, b != nullptr, hc != nullptr, &early);
-  if (s == GT_OK) s = build_pattern(A);  // incidence + sparsity
+  // incidence + sparsity (+ each row chunk's last cell for the pipelined
+  // scatter into host buffers)
+  if (s == GT_OK) s = build_pattern(A, hc != nullptr);
   cudaEvent_t side_done = nullptr;
   const int bs = A->bs;
   const int64_t nscal = A->nbrows * bs, nnz = A->bnnz * bs * bs;

@@ -253,8 +253,9 @@ int build_incidence(Ctx* ctx, const Space* sp, int64_t** inc_ptr, int32_t** inc,
 int build_incidence_arr(Ctx* ctx, const int32_t* dofs, int64_t n, int64_t nrows, int64_t** inc_ptr, int32_t** inc,
                         int64_t* ninc, bool sort);
 // the matrix's incidence (A->inc_ptr, A->inc: every row's list ascending) and
-// its sparsity (rowptr, colind, max_row)
-int build_pattern(Matrix* A);
+// its sparsity (rowptr, colind, max_row); chunk_last: also each row chunk's
+// last cell (Matrix::chunk_last)
+int build_pattern(Matrix* A, bool chunk_last = false);
 // Element matrices of scalar P1 tetrahedra (Laplacian, mass) are symmetric
 // and stored packed: the 10 entries of the upper triangle per cell, row by
 // row ({00,01,02,03,11,12,13,22,23,33}); every other space stores the full
