@@ -387,6 +387,12 @@ int gt_ctx_launch_count(gt_ctx* c, int64_t* launches) {
   return GT_OK;
 }
 
+int gt_ctx_graph_launch_count(gt_ctx* c, int64_t* launches) {
+  if (!c || !launches) return GT_ERR_INVALID;
+  *launches = c->graph_launches;
+  return GT_OK;
+}
+
 int gt_ctx_profile_begin(gt_ctx* c) {
   if (!c) return GT_ERR_INVALID;
   for (auto& m : c->marks) c->spare_events.push_back(m.second);

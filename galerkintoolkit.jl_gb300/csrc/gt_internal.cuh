@@ -87,6 +87,7 @@ struct Ctx {
   int64_t* h_scratch = nullptr;    // pinned small readbacks (64 words)
   double* h_dscratch = nullptr;    // pinned small FP64 readbacks (64 words)
   int64_t launches = 0;            // kernels launched by this context
+  int64_t graph_launches = 0;      // CUDA-graph launches (replayed CG chunks)
   // PCG path: 0 = by size (persistent kernel for small systems, separate
   // launches per phase for large ones), 1 = always launches, 2 = always
   // persistent (environment GTGPU_PCG=launches|persistent at context creation)

@@ -56,6 +56,43 @@ static void launch_pdl(Ctx* ctx, void (*kern)(KArgs...), unsigned grid, cudaStre
   cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
 }
 
+// CHUNK iterations of a CG loop, captured once into a CUDA graph and
+// replayed for every chunk: one graph launch instead of about five kernel
+// launches per iteration (the programmatic-launch edges between the kernels
+// are kept by the capture; every launch argument is a device pointer or a
+// size fixed for the solve).  When the capture or the instantiation fails
+// (e.g. on the legacy default stream), the chunk runs as direct launches.
+struct ChunkGraph {
+  cudaGraphExec_t exec = nullptr;
+  bool tried = false;
+  ChunkGraph() = default;
+  ChunkGraph(const ChunkGraph&) = delete;
+  ChunkGraph& operator=(const ChunkGraph&) = delete;
+  ~ChunkGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+  template <class F>
+  int run(Ctx* ctx, cudaStream_t s, F&& body) {
+    if (!tried) {
+      tried = true;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const int rc = body();
+        const cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (rc == GT_OK && e == cudaSuccess && g && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) exec = nullptr;
+        if (g) cudaGraphDestroy(g);
+      }
+      cudaGetLastError();  // a failed capture leaves its error here; the direct path follows
+    }
+    if (exec) {
+      GT_CUDA(ctx, cudaGraphLaunch(exec, s));
+      ctx->graph_launches++;
+      return GT_OK;
+    }
+    return body();
+  }
+};
+
 // device-resident CG state (one per solve)
 struct CGState {
   double rz, pq, rr, bb, alpha, beta;
@@ -850,7 +887,8 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
   const bool uloop = n <= kLoopUpdate;
   const unsigned gu = uloop ? one_wave(ctx, k_cg_update<X, true>, gi) : gi;
   CGState h{};
-  for (int it = 0; it < maxit; it += CHUNK) {
+  ChunkGraph graph;
+  auto chunk = [&]() -> int {
     for (int k = 0; k < CHUNK; k++) {
       GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb, &sell)));
       if (uloop) launch_pdl(ctx, k_cg_update<X, true>, gu, s, x, r, z, p, q, dinv, n, st, sc.rb);
@@ -858,6 +896,10 @@ static int pcg(Matrix* A, const V* val, const X* b, X* x, double rtol, int maxit
       launch_pdl(ctx, k_cg_pupdate<X>, gi, s, p, z, n, st);
     }
     GT_LAUNCH(ctx, "cg iteration");
+    return GT_OK;
+  };
+  for (int it = 0; it < maxit; it += CHUNK) {
+    GT_TRY(graph.run(ctx, s, chunk));
     GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
     GT_CUDA(ctx, cudaStreamSynchronize(s));
     memcpy(&h, ctx->h_dscratch, sizeof(CGState));
@@ -1088,7 +1130,8 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
   const bool uloop = n <= kLoopUpdate;
   const unsigned gu = uloop ? one_wave(ctx, k_rl_update<X, true>, gi) : gi;
   CGState h{};
-  for (int it = 0; it < maxit + CHUNK; it += CHUNK) {
+  ChunkGraph graph;
+  auto chunk = [&]() -> int {
     for (int k = 0; k < CHUNK; k++) {
       GT_TRY((Ops<V, X>::cg_spmv(ctx, A, val, p, q, st, sc.rb, &sell)));
       if (uloop) launch_pdl(ctx, k_rl_update<X, true>, gu, s, xs, r, z, p, q, dinv, n, st, sc.rb);
@@ -1098,6 +1141,10 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
       launch_pdl(ctx, k_cg_pupdate<X>, gi, s, p, z, n, st);
     }
     GT_LAUNCH(ctx, "reliable CG iteration");
+    return GT_OK;
+  };
+  for (int it = 0; it < maxit + CHUNK; it += CHUNK) {
+    GT_TRY(graph.run(ctx, s, chunk));
     GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, st, sizeof(CGState), cudaMemcpyDeviceToHost, s));
     GT_CUDA(ctx, cudaStreamSynchronize(s));
     memcpy(&h, ctx->h_dscratch, sizeof(CGState));

@@ -60,6 +60,12 @@ class Context:
         check(self.h, self.lib.gt_ctx_launch_count(self.h, C.byref(n)))
         return n.value
 
+    def graph_launches(self) -> int:
+        """CUDA-graph launches so far (each replays a chunk of CG iterations)."""
+        n = C.c_int64()
+        check(self.h, self.lib.gt_ctx_graph_launch_count(self.h, C.byref(n)))
+        return n.value
+
     def fma_rate(self, fp64=True) -> float:
         """Measured FMA throughput (TFLOP/s) of FP64 or FP32 on this device."""
         t = C.c_double()

@@ -99,6 +99,9 @@ int gt_ctx_trim(gt_ctx* ctx);
 int gt_ctx_fma_rate(gt_ctx* ctx, int precision, double* tflops);
 /* Number of kernels the context has launched so far. */
 int gt_ctx_launch_count(gt_ctx* ctx, int64_t* launches);
+/* Number of CUDA-graph launches the context has made so far (the solver
+ * replays each chunk of CG iterations as one captured graph). */
+int gt_ctx_graph_launch_count(gt_ctx* ctx, int64_t* launches);
 /* Phase timing with CUDA events on the context's stream: begin, run calls,
  * end.  end() returns up to max phases: names (32 chars each) and device
  * milliseconds between consecutive phase boundaries. */
