@@ -67,18 +67,17 @@ def _node_grid(cells):
 
 
 def _hex_cells(cells):
+    """(cell nodes 0-based, ncells x 2^D; cell coordinates, D x ncells)."""
     D = len(cells)
     np_ = [c + 1 for c in cells]
     ci = np.indices(cells[::-1]).reshape(D, -1)[::-1]  # cell coords, x-fastest
     strides = np.cumprod([1] + np_[:-1])
     nlv = 1 << D
-    out = np.zeros((ci.shape[1], nlv), np.int64)
-    for lv in range(nlv):
-        node = np.zeros(ci.shape[1], np.int64)
-        for d in range(D):
-            node += (ci[d] + ((lv >> d) & 1)) * strides[d]
-        out[:, lv] = node
-    return out  # 0-based
+    base = np.zeros(ci.shape[1], np.int64)
+    for d in range(D):
+        base += ci[d] * strides[d]
+    off = np.array([sum(((lv >> d) & 1) * strides[d] for d in range(D)) for lv in range(nlv)], np.int64)
+    return base[:, None] + off[None, :], ci
 
 
 def _cube_face_triangles():
@@ -116,19 +115,26 @@ def cartesian_mesh(domain, cells, simplexify=False):
     hi = np.array(domain[1::2], np.float64)
     h = (hi - lo) / np.array(cells, np.float64)
     coords = np.ascontiguousarray((lo[:, None] + h[:, None] * idx).T)
-    hexes = _hex_cells(cells)
+    hexes, cidx = _hex_cells(cells)
     # number of hex cells around each node
     cnt = np.ones(coords.shape[0], np.int64)
     for d in range(D):
         cnt *= np.where((idx[d] == 0) | (idx[d] == cells[d]), 1, 2)
-    cc = cnt[hexes]  # (nhex, nlv)
+    # boundary entities lie in boundary cells only: the scans below run over
+    # those (ascending, so every list keeps the order of a scan over all cells)
+    onb = np.zeros(hexes.shape[0], bool)
+    for d in range(D):
+        onb |= (cidx[d] == 0) | (cidx[d] == cells[d] - 1)
+    bcell = np.nonzero(onb)[0]
+    hb = hexes[bcell]
+    cc = cnt[hb]  # (boundary cells, nlv)
     # d = 0: corners, in cell order
-    corners = hexes[cc <= 1]
+    corners = hb[cc <= 1]
     # parent 1-faces
     ledges = QUAD_EDGES if D == 2 else HEX_EDGES
     e_ok = (cc[:, ledges[:, 0]] <= 2) & (cc[:, ledges[:, 1]] <= 2)
     ci, le = np.nonzero(e_ok)
-    edges = np.stack([hexes[ci, ledges[le, 0]], hexes[ci, ledges[le, 1]]], 1)
+    edges = np.stack([hb[ci, ledges[le, 0]], hb[ci, ledges[le, 1]]], 1)
     egroup = le + 1
     if D == 2:
         bfaces, bgroup, bedges = edges, egroup, np.zeros((0, 2), np.int64)
@@ -139,7 +145,7 @@ def cartesian_mesh(domain, cells, simplexify=False):
         ci, lf = np.nonzero(f_ok)
         bedges = edges
         if not simplexify:
-            bfaces = hexes[ci[:, None], HEX_FACES[lf]]
+            bfaces = hb[ci[:, None], HEX_FACES[lf]]
             bgroup = lf + 1
             ctype = HEX8
             cell_nodes = hexes
@@ -151,7 +157,7 @@ def cartesian_mesh(domain, cells, simplexify=False):
             lf2 = np.repeat(lf, rep)
             sub = np.concatenate([np.arange(r) for r in rep]) if rep.size else np.zeros(0, np.int64)
             tri_arr = np.array(tri)  # (6, 2, 3)
-            bfaces = hexes[ci2[:, None], tri_arr[lf2, sub]]
+            bfaces = hb[ci2[:, None], tri_arr[lf2, sub]]
             bgroup = lf2 + 1
             ctype = TET4
             cell_nodes = hexes[:, CUBE_TETS].reshape(-1, 4)
