@@ -127,7 +127,10 @@ def run_batched(args):
     reliable updates, instances up to 32768 rows one per CTA in one
     persistent launch) against the plain FP64 path (one instance at a time,
     FP64 assembly and FP64 PCG).  The lanes autotuner runs once before the
-    timed region (its choice is cached by batch shape)."""
+    timed region (its choice is cached by batch shape).  The host inputs
+    (meshes and seeded coefficients) are generated before the timed region;
+    both paths time the upload, the space, the assembly and the solve of
+    every instance."""
     import gtgpu as GT
     from gtgpu import batch as GB
     specs = GB.batch_workload(args.instances, seed=404)
@@ -151,13 +154,18 @@ def run_batched(args):
     tune = GB.autotune_lanes(B, np.concatenate([bb for _, _, _, bb in inst]), iters=32)
     del B, inst
     ctx.trim()
+    host = {s.index: GB.instance_inputs(s, seed=404) for s in specs}  # untimed: the inputs
+
+    def release(s):  # the mesh's device copy goes with its instance
+        host[s.index][0]._device.clear()
+
     ctx.synchronize()
     t_all = time.perf_counter()
     iters, fp64_its, worst = [], [], 0.0
     t_asm = t_solve = t_small = t_large = 0.0
     for w in waves:
         t0 = time.perf_counter()
-        inst = [GB.assemble_instance(s, seed=404, T="mixed", ctx=ctx) for s in w]
+        inst = [GB.assemble_instance(s, seed=404, T="mixed", ctx=ctx, inputs=host[s.index]) for s in w]
         B = GB.Batch([A for _, _, A, _ in inst])
         b = np.concatenate([bb for _, _, _, bb in inst])
         t1 = time.perf_counter()
@@ -173,6 +181,8 @@ def run_batched(args):
         fp64_its += [i["fp64_iterations"] for i in infos]
         worst = max(worst, max(i["rel_residual"] for i in infos))
         del B, inst
+        for s in w:
+            release(s)
         ctx.trim()
     ctx.synchronize()
     t_batched = time.perf_counter() - t_all
@@ -183,7 +193,7 @@ def run_batched(args):
     its64 = []
     for s in specs:
         ta = time.perf_counter()
-        m, V, A, b = GB.assemble_instance(s, seed=404, T=np.float64, ctx=ctx)
+        m, V, A, b = GB.assemble_instance(s, seed=404, T=np.float64, ctx=ctx, inputs=host[s.index])
         tb = time.perf_counter()
         x, info = GT.solve(A, b, rtol=1e-8, maxit=100000, mode="fp64", raise_on_fail=False)
         p_asm += tb - ta
@@ -191,6 +201,7 @@ def run_batched(args):
         its64.append(info["iterations"])
         worst64 = max(worst64, info["rel_residual"])
         del A, V
+        release(s)
         if ctx.memory()[1] > 20e9:
             ctx.trim()
     t_plain = time.perf_counter() - t0

@@ -155,12 +155,22 @@ def estimate_bytes(spec: InstanceSpec, precision="mixed"):
     return int(nnz * per_nnz + dofs * 120 + (spec.cells_per_dir ** spec.dim) * 200)
 
 
-def assemble_instance(spec: InstanceSpec, seed=404, T="mixed", ctx=None):
-    """Mesh, space, matrix and load vector of one batch instance."""
-    ctx = ctx or default_context()
+def instance_inputs(spec: InstanceSpec, seed=404):
+    """Host inputs of one batch instance: its mesh and its seeded cell
+    coefficient."""
     box = tuple(x for _ in range(spec.dim) for x in (0.0, 1.0))
     m = cartesian_mesh(box, (spec.cells_per_dir,) * spec.dim)
-    V = lagrange_space(interior(m), spec.order, dirichlet_boundary=boundary(m), ctx=ctx)
     kappa = lognormal_cells(m.num_cells, 0.5, seed * 1000003 + spec.index)
+    return m, kappa
+
+
+def assemble_instance(spec: InstanceSpec, seed=404, T="mixed", ctx=None, inputs=None):
+    """Mesh, space, matrix and load vector of one batch instance (from
+    inputs = instance_inputs(spec, seed) when given; the mesh's device copy
+    is made here, and dropped with mesh._device.clear() by a caller that
+    keeps the host mesh)."""
+    ctx = ctx or default_context()
+    m, kappa = inputs if inputs is not None else instance_inputs(spec, seed)
+    V = lagrange_space(interior(m), spec.order, dirichlet_boundary=boundary(m), ctx=ctx)
     A, b = assemble_matrix_and_vector(laplacian(kappa), source(1.0), T, V)
     return m, V, A, b
