@@ -57,6 +57,37 @@ def test_assemble_csr_matches_separate_calls(kind, pinned):
     assert np.array_equal(v_h.numpy(), v) and np.array_equal(b_h.numpy(), b)
 
 
+@pytest.mark.parametrize("prec", ["fp32", "mixed"])
+def test_assemble_csr_fp32_and_mixed_values(prec):
+    """The pipelined host-buffer path (element chunks, row-chunk scatter,
+    chunked downloads) with FP32 values (FP32) or both copies (mixed): the
+    values of the separate assembly, bitwise."""
+    m, V, form, f = _space("p1tet_large")
+    kappa = GT.lognormal_cells(m.num_cells, 0.5, 21)
+    a = form(kappa)
+    T = np.float32 if prec == "fp32" else "mixed"
+    A, b = GT.assemble_matrix_and_vector(a, GT.source(f), T, V)
+    rp, ci, _ = A.csr()
+    v32 = A.values32()
+    n, nnz = rp.size - 1, ci.size
+    pin = lambda t, d: torch.empty(t, dtype=d).pin_memory()
+    rp_h, ci_h, b_h = pin(n + 1, torch.int64), pin(nnz, torch.int32), pin(n, torch.float64)
+    v32_h = pin(nnz, torch.float32)
+    v64_h = pin(nnz, torch.float64) if prec == "mixed" else None
+    kap = torch.from_numpy(kappa).pin_memory()
+    fv = np.ones(1)
+    h = C.c_void_p()
+    lib = V.ctx.lib
+    p = _lib.GT_FP32 if prec == "fp32" else _lib.GT_MIXED
+    _lib.check(V.ctx.h, lib.gt_assemble_csr(V.h, a.kind, _ptr(kap), a.nu, p, _ptr(fv), None, _ptr(b_h), nnz,
+                                            _ptr(rp_h), _ptr(ci_h), _ptr(v64_h), _ptr(v32_h), C.byref(h)))
+    lib.gt_matrix_destroy(h)
+    assert np.array_equal(rp_h.numpy(), rp) and np.array_equal(ci_h.numpy(), ci)
+    assert np.array_equal(v32_h.numpy(), v32) and np.array_equal(b_h.numpy(), b)
+    if prec == "mixed":
+        assert np.array_equal(v64_h.numpy(), A.csr()[2])
+
+
 def test_assemble_csr_capacity_too_small():
     m, V, form, f = _space("q1quad")
     A = GT.assemble_matrix(form(None), np.float64, V, V)
