@@ -39,6 +39,8 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "galerkintoolkit.jl_gb300"))
 
 METRIC = "nnz/s assembled (assemble_matrix + assemble_vector, plain FP64)"
+SOLVE_RTOL = 1e-10   # relative residual of the headline solves (FP64 and mixed)
+SOLVE_SAMPLES = 100  # timed solves per mode (p50 / p99 latency)
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # DRAM bytes (read + write) per launch on the default workload (96^3 x 6 P1
 # tets), from ncu captures (summaries under profiles/): the element and
@@ -393,23 +395,43 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # CPU side: the oracle restatement of the reference algorithm
 # ---------------------------------------------------------------------------
-def cpu_assembly(m, kappa, reps=1, threads=None):
-    """Times count pass + COO + COO->CSC + assemble_vector of the oracle."""
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
     import oracle as O
+    return O
+
+
+def oracle_space(m):
+    """The oracle's space of the benchmark mesh (DOF numbering; not timed:
+    the GPU step also starts from the space)."""
+    O = _oracle()
     om = dict(D=3, ctype=O.TET4, coords=m.coords, cell_nodes=m.cell_nodes, pf0=m.corners, pf1=m.bedges,
               pf2=m.bfaces, pf2g=m.bface_group)
-    V = O.lagrange_space(om, 1, dirichlet="boundary")
-    times, nnz = [], 0
+    return O.lagrange_space(om, 1, dirichlet="boundary")
+
+
+def cpu_assembly(m, kappa, reps=1, threads=None, space=None):
+    """Times the oracle's assemble_matrix (counting pass + COO append +
+    COO->CSC) + assemble_vector on the host's cores (threads: OpenMP
+    threads, 1 = the reference's single-threaded path).  Returns nnz, the
+    times, the threads used and the last (colptr, rowval, nzval, b)."""
+    O = _oracle()
+    O.set_threads(threads or os.cpu_count())
+    V = space if space is not None else oracle_space(m)
+    times, out = [], None
     for _ in range(reps):
         t = time.perf_counter()
         cp, rv, nz = O.assemble_matrix(V, O.LAPLACE, 2, coef=kappa)
-        O.assemble_vector(V, 2, 1.0)
+        b = O.assemble_vector(V, 2, 1.0)
         times.append(time.perf_counter() - t)
-        nnz = rv.size
-    return nnz, times, O.num_threads()
+        out = (cp, rv, nz, b)
+    return out[1].size, times, O.num_threads(), out
+
+
+def _relerr(a, ref):
+    ref = np.asarray(ref)
+    scale = float(np.abs(ref).max()) if ref.size else 0.0
+    return float(np.abs(np.asarray(a) - ref).max() / scale) if scale > 0 else 0.0
 
 
 def run_reference(args):
@@ -419,8 +441,8 @@ def run_reference(args):
     n = args.cells
     m, kappa = workload(n)
     ncores = os.cpu_count()
-    nnz, times, used = cpu_assembly(m, kappa, reps=max(1, args.warmup + args.steps if args.steps <= 2 else 2),
-                                    threads=ncores)
+    nnz, times, used, _ = cpu_assembly(m, kappa, reps=max(1, args.warmup + args.steps if args.steps <= 2 else 2),
+                                       threads=ncores)
     t = min(times)
     v = nnz / t
     line = {"metric": METRIC, "value": v, "unit": "nnz/s", "impl": "reference", "n_gpus": args.gpus,
@@ -507,6 +529,10 @@ def main():
     ctx.profile_begin()
     A = step()
     phases = ctx.profile_end()
+    # the step's CSR and load vector (bitwise those of every timed step) for
+    # the parity check against the oracle
+    g_rp, g_ci, g_v = A.csr()
+    g_b = bdev.cpu().numpy()
     spmv = spmv_roofline(A, flush, stream)
     del A
     peaks, peaks_kind = load_peaks()
@@ -516,7 +542,7 @@ def main():
     nc, nn = m.num_cells, 4
     nfree = V.num_free_dofs
     ph = {k: v for k, v in phases}
-    # algorithmic bytes per launch of the phases (stated in the design doc)
+    # algorithmic bytes per launch of the phases
     alg = {
         # reads + Ke/be writes (Ke: the 10 entries of the packed symmetric 4 x 4 block)
         "elements": nc * (4 * 4 + 8) + m.num_nodes * 24 + nc * 10 * 8 + nc * 4 * 8,
@@ -528,24 +554,38 @@ def main():
     flops_el = nc * 93.0
     dom = max((k for k in ph if k in ("elements", "scatter", "pattern_count", "pattern_fill", "incidence")),
               key=lambda k: ph[k])
+    # B_asm: the per-matrix algorithmic bytes of the assembly (CSR values
+    # written once, cell DOFs, node coordinates once per node, the per-cell
+    # coefficient); element matrices are not counted (they would stay on chip)
+    b_asm = nnz * 8 + nc * 4 * 4 + m.num_nodes * 24 + nc * 8
     hbm = {}
     for k in ("scatter", "elements"):
         if k in ph:
             gbs = alg[k] / (ph[k] * 1e-3) / 1e9
             hbm[k] = {"achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
-                      "algorithmic_bytes": alg[k], "ms": ph[k], "traffic": TRAFFIC.get(k)}
+                      "algorithmic_bytes": alg[k], "ms": ph[k], "traffic": TRAFFIC.get(k),
+                      "bytes_counted": "this kernel's reads and writes, the materialised element matrices included"}
+    if "scatter" in ph:
+        g = b_asm / (ph["scatter"] * 1e-3) / 1e9
+        hbm["scatter"]["b_asm"] = {"algorithmic_bytes": b_asm, "achieved": g, "frac": g / peaks["hbm_gbs"]}
+    if "scatter" in ph and "elements" in ph:
+        t = ph["scatter"] + ph["elements"]
+        g = b_asm / (t * 1e-3) / 1e9
+        hbm["elements_plus_scatter_b_asm"] = {"algorithmic_bytes": b_asm, "ms": t, "achieved": g, "unit": "GB/s",
+                                              "frac": g / peaks["hbm_gbs"]}
     if dom == "elements":
         achieved = flops_el / (ph[dom] * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": "k_elements_p1<Laplacian, double>", "achieved": achieved,
                 "peak": fp64_tf, "unit": "TFLOP/s", "frac": achieved / fp64_tf,
                 "peak_source": "measured FP64 FMA rate of this device (gt_ctx_fma_rate); FP64 units, not tensor",
+                "peak_method": "gt_ctx_fma_rate: 8 CTAs/SM x 256 threads, 8 independent FMA chains per thread, "
+                               "2048 iterations, CUDA events after a warm-up launch (FMA = 2 flops)",
                 "algorithmic_flops": flops_el, "traffic": TRAFFIC.get("elements")}
     else:
         bytes_dom = alg.get(dom, nnz * 12)
         achieved = bytes_dom / (ph[dom] * 1e-3) / 1e9
         roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks_kind, "traffic": TRAFFIC.get(dom)}
-    b_asm = nnz * 8 + nc * 4 * 4 + m.num_nodes * 24 + nc * 8
     step_roof = {"algorithmic_bytes": b_asm, "GB/s": b_asm / (ms * 1e-3) / 1e9,
                  "frac_of_hbm": b_asm / (ms * 1e-3) / 1e9 / peaks["hbm_gbs"]}
 
@@ -580,44 +620,77 @@ def main():
     h2d = m.coords.nbytes + kappa.nbytes
     d2h = rp_h.numel() * 8 + nnz * 4 + nnz * 8 + nfree * 8
 
-    # ---- solve: plain FP64 PCG vs FP64 refinement around FP32 PCG
+    # ---- solve: plain FP64 PCG vs FP32 PCG with FP64 reliable updates,
+    # latency over SOLVE_SAMPLES timed solves each
     solve = None
+    xs = {}
     if not args.no_solve:
         Am, bm = GT.assemble_matrix_and_vector(a, l, "mixed", V)
         res = {}
-        xs = {}
         for mode in ("fp64", "ir"):
             lat = []
-            for r in range(3):
+            GT.solve(Am, bm, rtol=SOLVE_RTOL, mode=mode)  # warm-up (sliced-ELL copy, graphs)
+            for r in range(SOLVE_SAMPLES):
                 t0 = time.perf_counter()
-                x, info = GT.solve(Am, bm, rtol=1e-10, mode=mode)
+                x, info = GT.solve(Am, bm, rtol=SOLVE_RTOL, mode=mode)
                 lat.append(time.perf_counter() - t0)
             xs[mode] = x
-            lat.sort()
-            res[mode] = {"solves_per_s": 1.0 / statistics.mean(lat), "p50_ms": 1e3 * lat[len(lat) // 2],
-                         "p99_ms": 1e3 * lat[-1], "iterations": info["iterations"],
+            lat = np.array(lat)
+            res[mode] = {"solves_per_s": 1.0 / float(lat.mean()), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                         "p99_ms": 1e3 * float(np.percentile(lat, 99)), "samples": int(lat.size),
+                         "iterations": info["iterations"], "fp64_iterations": info["fp64_iterations"],
                          "true_residual_updates": info["outer_iterations"], "rel_residual": info["rel_residual"],
-                         "ms_per_iteration": 1e3 * lat[0] / max(1, info["iterations"])}
-        res["ir_vs_fp64_rel_err"] = float(np.abs(xs["ir"] - xs["fp64"]).max() / np.abs(xs["fp64"]).max())
-        res["rtol"] = 1e-10
+                         "ms_per_iteration": 1e3 * float(lat.min()) / max(1, info["iterations"])}
+        res["ir_vs_fp64_rel_err"] = _relerr(xs["ir"], xs["fp64"])
+        res["mixed_vs_fp64_speedup"] = res["ir"]["solves_per_s"] / res["fp64"]["solves_per_s"]
+        res["rtol"] = SOLVE_RTOL
         solve = res
+        del Am
 
-    cpu = None
+    # ---- CPU: the oracle (C restatement of the reference) on the same
+    # workload, single-threaded like the reference and on all host cores;
+    # its CSR, load vector and FP64 solution are the parity references
+    cpu, parity = None, None
     if rank == 0 and not args.no_cpu:
+        O = _oracle()
+        osp = oracle_space(m)
+        cnnz, t1, _, _ = cpu_assembly(m, kappa, reps=1, threads=1, space=osp)
         ncores = os.cpu_count()
-        cnnz, ctimes, used = cpu_assembly(m, kappa, reps=1, threads=ncores)
-        cpu = {"value": cnnz / min(ctimes), "unit": "nnz/s", "cores": used, "kind": "port",
-               "sample": "full workload, 1 repetition (C restatement of the reference, OpenMP)"}
+        cnnz, tn, used, (cp, rv, nz, ob) = cpu_assembly(m, kappa, reps=1, threads=ncores, space=osp)
+        orp, oci, ov = O.csc_to_csr(cp, rv, nz, osp["nfree"])
+        t0 = time.perf_counter()
+        _, cg_it, cg_rr = O.pcg(orp, oci, ov, ob, rtol=SOLVE_RTOL)
+        cg_s = time.perf_counter() - t0
+        cpu = {"value": cnnz / min(tn), "unit": "nnz/s", "cores": used, "kind": "port",
+               "sample": f"full workload, 1 repetition (C restatement of the reference, OpenMP {used} threads)",
+               "single_thread": {"value": cnnz / min(t1), "unit": "nnz/s", "cores": 1, "seconds": min(t1),
+                                 "sample": "full workload, 1 repetition, 1 thread (the reference is single-threaded)"},
+               "solve": {"seconds": cg_s, "solves_per_s": 1.0 / cg_s, "iterations": cg_it, "rel_residual": cg_rr,
+                         "rtol": SOLVE_RTOL, "threads": 1,
+                         "kind": "oracle FP64 Jacobi-PCG on the oracle's CSR (the reference solves with a direct "
+                                 "LU; it has no CG)"}}
+        parity = {"oracle": "oracle/gt_oracle.c (C restatement of the reference), same seeded mesh and kappa",
+                  "pattern_equal": bool(np.array_equal(g_rp, orp) and np.array_equal(g_ci, oci)),
+                  "values_max_rel_err": _relerr(g_v, ov) if g_v.size == ov.size else None,
+                  "load_vector_max_rel_err": _relerr(g_b, ob),
+                  "tolerance": {"values": 1e-12, "load_vector": 1e-12, "solution": 1e-8},
+                  "error_scale": "max |gpu - oracle| / max |oracle|"}
+        if xs:
+            xo, o_it, o_rr = O.pcg(orp, oci, ov, ob, rtol=1e-12)
+            parity["solution_ref"] = f"oracle FP64 PCG to rel. residual {o_rr:.1e} ({o_it} iterations)"
+            parity["solution_max_rel_err"] = {k: _relerr(v, xo) for k, v in xs.items()}
 
     line = {"metric": METRIC, "value": value, "unit": "nnz/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
             "config": wl_config(n, {"nnz": int(nnz), "free_dofs": int(nfree), "parallelism": f"replicas x{world}"}),
             "e2e": {"value": rep.value(nnz, rep.max_ms(e2e_ms, "cuda")), "unit": "nnz/s", "ms_per_step": e2e_ms,
-                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "resident": "the space (cell DOF ids, free-first numbering) stays on the device; coordinates "
+                                "and kappa are uploaded and the CSR + load vector downloaded every step"},
             "roofline": roof, "step_roofline": step_roof, "hbm_kernels": {**hbm, "spmv_fp64": spmv},
             "phases_ms": {k: round(v, 4) for k, v in phases},
-            "cpu_baseline": cpu, "solve": solve, "clocks": clocks.summary(),
+            "cpu_baseline": cpu, "parity": parity, "solve": solve, "clocks": clocks.summary(),
             "gpu_launches": int(launches), "wall_s_timed": t_wall}
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -2278,6 +2278,8 @@ struct DevIn {
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, src) == cudaSuccess &&
         (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged)) {
+      if (at.type == cudaMemoryTypeDevice && at.device != c->device)
+        return set_error(c, GT_ERR_INVALID, "input array is memory of another device");
       p = src;
       return GT_OK;
     }

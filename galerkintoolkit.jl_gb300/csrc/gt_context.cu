@@ -381,6 +381,12 @@ int gt_ctx_fma_rate(gt_ctx* c, int precision, double* tflops) {
   return set_error(c, GT_ERR_INVALID, "precision must be GT_FP64 or GT_FP32");
 }
 
+int gt_ctx_barrier_probe(gt_ctx* c, int ctas, int missing, int64_t timeout_ns) {
+  if (!c) return GT_ERR_INVALID;
+  cudaSetDevice(c->device);
+  return barrier_probe(c, ctas, missing, timeout_ns);
+}
+
 int gt_ctx_launch_count(gt_ctx* c, int64_t* launches) {
   if (!c || !launches) return GT_ERR_INVALID;
   *launches = c->launches;

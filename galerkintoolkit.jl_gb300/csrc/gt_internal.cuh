@@ -305,6 +305,9 @@ constexpr int kSlowCycle = 1000;
 int pcg_persistent(Matrix* A, int mode, const double* b, double* x, double rtol, int maxit, int32_t* iters,
                    int32_t* nupd, int32_t* iters64, double* relres);
 int spmv64(Matrix* A, const double* x, double* y);
+// the persistent solver's grid barrier run alone (gt_pcg.cu): ctas CTAs wait
+// for ctas + missing arrivals with the given time limit
+int barrier_probe(Ctx* ctx, int ctas, int missing, int64_t timeout_ns);
 
 // device scans (exclusive prefix sum; out has n+1 entries, out[n] = total)
 int exclusive_scan_i64(Ctx* ctx, const int32_t* in, int64_t* out, int64_t n);

@@ -26,8 +26,11 @@
 //     (two streams or two contexts at once) race on the array -- serialise
 //     them;
 //   * the first call on a device looks up the array's device address
-//     (cudaGetSymbolAddress with that device current); make that first call
-//     before any stream capture.
+//     (cudaGetSymbolAddress with that device current, the caller's current
+//     device restored afterwards); make that first call before any stream
+//     capture;
+//   * every call waits for the context's stream before it returns (it reads
+//     the kernels' error word).
 #include <mutex>
 
 #include "gt_internal.cuh"
@@ -47,9 +50,12 @@ static int scratch_address(Ctx* ctx, void** out) {
   if (ctx->device < 0 || ctx->device >= kMaxDevices) return set_error(ctx, GT_ERR_INVALID, "device id out of range");
   std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (!g_scratch_addr[ctx->device]) {
+    int prev = 0;
+    GT_CUDA(ctx, cudaGetDevice(&prev));
     GT_CUDA(ctx, cudaSetDevice(ctx->device));
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress((void**)&p, g_refill_scratch);
+    cudaSetDevice(prev);
     if (e != cudaSuccess || !p) return check_cuda(ctx, e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress");
     g_scratch_addr[ctx->device] = p;
   }
@@ -76,6 +82,8 @@ int gt_update_matrix_noalloc(gt_matrix* A, int form, const double* cell_coef, do
       cudaGetLastError();
       return set_error(ctx, GT_ERR_INVALID, "gt_update_matrix_noalloc: cell_coef must be device memory (or NULL)");
     }
+    if (at.type == cudaMemoryTypeDevice && at.device != ctx->device)
+      return set_error(ctx, GT_ERR_INVALID, "gt_update_matrix_noalloc: cell_coef is memory of another device");
   }
   int kprec = A->precision == GT_FP32 ? GT_FP32 : GT_FP64;
   size_t esz = kprec == GT_FP32 ? sizeof(float) : sizeof(double);

@@ -86,14 +86,16 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
 }
 
 // grid-wide barrier number `target / gridDim.x`; false when it timed out
-__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, int32_t* err, int* s_abort) {
+// (no arrival for timeout_ns: the error word is set and every CTA returns)
+__device__ __forceinline__ bool grid_sync(uint32_t* bar, uint32_t target, int32_t* err, int* s_abort,
+                                          uint64_t timeout_ns = BAR_TIMEOUT_NS) {
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
     atomicAdd(bar, 1u);
     uint64_t t0 = global_ns();
     while (ld_acquire(bar) < target) {
-      if (global_ns() - t0 > BAR_TIMEOUT_NS) {
+      if (global_ns() - t0 > timeout_ns) {
         atomicExch(err, 1);
         *s_abort = 1;
         break;
@@ -549,7 +551,46 @@ int run_dispatch(Matrix* A, const V* val, const double* b, double* x, double rto
   return set_error(A->ctx, GT_ERR_UNSUPPORTED, "persistent PCG: unsupported block size");
 }
 
+// The solver's grid barrier run alone: `ctas` co-resident CTAs wait for
+// ctas + missing arrivals.  With missing > 0 the barrier can never complete,
+// so each CTA gives up after timeout_ns and sets the error word.
+__global__ void __launch_bounds__(PT) k_barrier_probe(uint32_t* bar, uint32_t target, int32_t* err,
+                                                      uint64_t timeout_ns) {
+  __shared__ int s_abort;
+  if (threadIdx.x == 0) s_abort = 0;
+  grid_sync(bar, target, err, &s_abort, timeout_ns);
+}
+
 }  // namespace
+
+int barrier_probe(Ctx* ctx, int ctas, int missing, int64_t timeout_ns) {
+  if (ctas < 1 || missing < 0 || timeout_ns <= 0 || timeout_ns > 2000000000ll)
+    return set_error(ctx, GT_ERR_INVALID, "barrier probe: 1 <= ctas, 0 <= missing, 0 < timeout <= 2 s");
+  int dev = 0, nsm = 0, per_sm = 0;
+  GT_CUDA(ctx, cudaGetDevice(&dev));
+  GT_CUDA(ctx, cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  GT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_barrier_probe, PT, 0));
+  if ((int64_t)ctas > (int64_t)nsm * per_sm) return set_error(ctx, GT_ERR_INVALID, "barrier probe: more CTAs than fit");
+  cudaStream_t s = ctx->stream;
+  uint32_t* bar = nullptr;
+  int32_t* err = nullptr;
+  GT_TRY(dalloc(ctx, &bar, 2));
+  GT_TRY(dalloc(ctx, &err, 2));
+  GT_CUDA(ctx, cudaMemsetAsync(bar, 0, 2 * sizeof(uint32_t), s));
+  GT_CUDA(ctx, cudaMemsetAsync(err, 0, 2 * sizeof(int32_t), s));
+  uint32_t target = (uint32_t)(ctas + missing);
+  uint64_t tns = (uint64_t)timeout_ns;
+  void* kargs[] = {&bar, &target, &err, &tns};
+  ctx->launches++;
+  GT_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(ctas), dim3(PT), kargs, 0, s));
+  GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_scratch, err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  GT_CUDA(ctx, cudaStreamSynchronize(s));
+  int32_t e = 0;
+  memcpy(&e, ctx->h_scratch, sizeof(int32_t));
+  dfree(ctx, bar);
+  dfree(ctx, err);
+  return e ? set_error(ctx, GT_ERR_TIMEOUT, "barrier probe: the grid barrier timed out") : GT_OK;
+}
 
 int pcg_persistent(Matrix* A, int mode, const double* b, double* x, double rtol, int maxit, int32_t* iters,
                    int32_t* nupd, int32_t* iters64, double* relres) {

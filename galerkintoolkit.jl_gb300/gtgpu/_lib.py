@@ -58,6 +58,7 @@ SIGNATURES = [
     ("gt_ctx_set_stream", I32, [P, P]),
     ("gt_ctx_memory", I32, [P, P, P]),
     ("gt_ctx_trim", I32, [P]),
+    ("gt_ctx_barrier_probe", I32, [P, I32, I32, I64]),
     ("gt_ctx_launch_count", I32, [P, P]),
     ("gt_ctx_graph_launch_count", I32, [P, P]),
     ("gt_ctx_fma_rate", I32, [P, I32, P]),

@@ -494,6 +494,69 @@ class Polynomial:
                 + c[8] * x * z + c[9] * y * z)
 
 
+class DiscreteField:
+    """GT.DiscreteField of a Lagrange space (src/field.jl): the free DOF
+    values and the Dirichlet DOF values (DOF -k -> dirichlet_values[k-1]).
+    ``integrate`` / ``l2_error`` / ``h1_error`` take one in place of the
+    (uh, dirichlet_values) pair."""
+
+    def __init__(self, space: Space, free_values, dirichlet_values):
+        fv = np.ascontiguousarray(free_values, np.float64)
+        dv = np.ascontiguousarray(dirichlet_values, np.float64)
+        if fv.size != space.num_free_dofs:
+            raise ValueError(f"{fv.size} free values, the space has {space.num_free_dofs} free DOFs")
+        if dv.size != space.num_dirichlet_dofs:
+            raise ValueError(f"{dv.size} Dirichlet values, the space has {space.num_dirichlet_dofs} Dirichlet DOFs")
+        self.space, self.free_values, self.dirichlet_values = space, fv, dv
+
+    def dof_values(self) -> np.ndarray:
+        """Values per cell and local DOF, (ncells, nloc): free DOF d > 0 takes
+        free_values[d-1], Dirichlet DOF -k takes dirichlet_values[k-1]."""
+        cd = self.space.face_dofs().astype(np.int64)
+        out = np.empty(cd.shape, np.float64)
+        f = cd > 0
+        out[f] = self.free_values[cd[f] - 1]
+        out[~f] = self.dirichlet_values[-cd[~f] - 1]
+        return out
+
+
+def zero_dirichlet_field(U: Space) -> DiscreteField:
+    """GT.zero_dirichlet_field(T, U): zero free and Dirichlet values."""
+    return DiscreteField(U, np.zeros(U.num_free_dofs), np.zeros(U.num_dirichlet_dofs))
+
+
+def dirichlet_field(U: Space, g=None) -> DiscreteField:
+    """The Dirichlet field uhd of GT.interpolate_dirichlet!(g, uhd)
+    (src/field.jl:364-367): zero free values, Dirichlet values of g at the
+    Dirichlet nodes (zero without g)."""
+    xd = np.zeros(U.num_dirichlet_dofs) if g is None else interpolate_dirichlet(g, U)
+    return DiscreteField(U, np.zeros(U.num_free_dofs), xd)
+
+
+def solution_field(U, x) -> DiscreteField:
+    """GT.solution_field (src/problems.jl:501-516): the discrete field with
+    free values x (a vector, or the solution of a LinearProblem) and the
+    Dirichlet values of uhd -- ``solution_field(uhd, x)`` -- or zero Dirichlet
+    values -- ``solution_field(U, x)``."""
+    if isinstance(x, LinearProblem):
+        x = x.x
+    if isinstance(U, DiscreteField):
+        return DiscreteField(U.space, np.array(x, np.float64, copy=True), U.dirichlet_values.copy())
+    return DiscreteField(U, np.array(x, np.float64, copy=True), np.zeros(U.num_dirichlet_dofs))
+
+
+def solution_field_inplace(uh: DiscreteField, x) -> DiscreteField:
+    """GT.solution_field!(uh, x) (src/problems.jl:518-526): new free values,
+    the Dirichlet values kept."""
+    if isinstance(x, LinearProblem):
+        x = x.x
+    x = np.asarray(x, np.float64)
+    if x.size != uh.free_values.size:
+        raise ValueError(f"{x.size} values, the field has {uh.free_values.size} free DOFs")
+    uh.free_values[...] = x
+    return uh
+
+
 _INT_KINDS = {"volume": _lib.GT_INT_VOLUME, "poly": _lib.GT_INT_POLY, "field": _lib.GT_INT_FIELD,
               "l2_norm2": _lib.GT_INT_L2_NORM2, "l2_error2": _lib.GT_INT_L2_ERROR2, "h1_error2": _lib.GT_INT_H1_ERROR2}
 
@@ -503,9 +566,12 @@ def integrate(V: Space, kind="volume", uh=None, exact=None, dirichlet_values=Non
     the cells of V's mesh: "volume" (int 1), "poly" (int p, exact a
     Polynomial), "field" (int sum_k u_k), "l2_norm2" (int |u|^2),
     "l2_error2" (int |u - p|^2) and "h1_error2" (int |grad u - grad p|^2).  uh:
-    the free DOF values (e.g. a solution); dirichlet_values: the Dirichlet DOF
-    values (default 0); exact: a Polynomial, or one per component."""
+    a DiscreteField, or the free DOF values (e.g. a solution) with
+    dirichlet_values the Dirichlet DOF values (default 0); exact: a
+    Polynomial, or one per component."""
     k = _INT_KINDS[kind]
+    if isinstance(uh, DiscreteField):
+        uh, dirichlet_values = uh.free_values, uh.dirichlet_values
     uf = None if uh is None else np.ascontiguousarray(uh, np.float64)
     if uf is not None and uf.size != V.num_free_dofs:
         raise ValueError(f"uh has {uf.size} entries, the space has {V.num_free_dofs} free DOFs")
@@ -522,23 +588,28 @@ def integrate(V: Space, kind="volume", uh=None, exact=None, dirichlet_values=Non
 
 
 def l2_error(V: Space, uh, exact, dirichlet_values=None) -> float:
-    """sqrt(int |u_h - u|^2) for a polynomial exact solution u"""
+    """sqrt(int |u_h - u|^2) for a polynomial exact solution u (uh: a
+    DiscreteField or the free values)"""
     return float(np.sqrt(integrate(V, "l2_error2", uh, exact, dirichlet_values)))
 
 
 def h1_error(V: Space, uh, exact, dirichlet_values=None) -> float:
-    """sqrt(int |grad u_h - grad u|^2) for a polynomial exact solution u"""
+    """sqrt(int |grad u_h - grad u|^2) for a polynomial exact solution u (uh:
+    a DiscreteField or the free values)"""
     return float(np.sqrt(integrate(V, "h1_error2", uh, exact, dirichlet_values)))
 
 
 def linear_problem(U: Space, a: Form, l: Source, T=np.float64, V=None, dirichlet_values=None,
                    neumann=None) -> LinearProblem:
     """GT.PartitionedSolvers_linear_problem: A and b assembled on the GPU,
-    x = 0.  With dirichlet_values (e.g. interpolate_dirichlet(g, U)) the
+    x = 0.  With dirichlet_values (the Dirichlet field uhd of
+    dirichlet_field(U, g), or its values interpolate_dirichlet(g, U)) the
     Dirichlet lift b -= Ad * xd is applied in the same pass
     (src/problems.jl:439-453); without, homogeneous Dirichlet data.
     neumann: (g, boundary(mesh, groups)) pairs whose boundary terms
     int g v dGamma are added to b."""
+    if isinstance(dirichlet_values, DiscreteField):
+        dirichlet_values = dirichlet_values.dirichlet_values
     lp = _linear_problem(U, a, l, T, V, dirichlet_values)
     for g, gamma in (neumann or ()):
         assemble_boundary_vector(g, gamma, U, out=lp.b, accumulate=True)

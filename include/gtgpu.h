@@ -97,6 +97,14 @@ int gt_ctx_trim(gt_ctx* ctx);
 /* Measured FMA throughput of the device in TFLOP/s (GT_FP64 or GT_FP32);
  * the roofline of the integration kernels.  No reference counterpart. */
 int gt_ctx_fma_rate(gt_ctx* ctx, int precision, double* tflops);
+/* Failure-detection check of the persistent solver's grid barrier, no
+ * reference counterpart: `ctas` co-resident CTAs run the barrier the
+ * persistent PCG uses between its phases, waiting for ctas + missing
+ * arrivals with a time limit of timeout_ns (at most 2 s).  missing = 0
+ * completes (GT_OK); missing > 0 can never complete, so every CTA gives up
+ * after the limit and the call returns GT_ERR_TIMEOUT with the context still
+ * usable -- the path a solve takes when a barrier does not complete. */
+int gt_ctx_barrier_probe(gt_ctx* ctx, int ctas, int missing, int64_t timeout_ns);
 /* Number of kernels the context has launched so far. */
 int gt_ctx_launch_count(gt_ctx* ctx, int64_t* launches);
 /* Number of CUDA-graph launches the context has made so far (the solver
@@ -193,9 +201,11 @@ int gt_update_matrix(gt_matrix* matrix, int form, const double* cell_coef, doubl
  * assembled matrix using one static 128 MiB device array as scratch;
  * cell_coef must be device memory or NULL; a refill needing more scratch
  * than 128 MiB (tabulation + ncells*nloc^2 values) returns GT_ERR_INVALID.
- * The first call on a device looks up the array's address (do it before any
- * stream capture).  All calls share the array: calls that overlap on the
- * GPU race. */
+ * The first call on a device looks up the array's address (make it before
+ * any stream capture); every call waits for the context's stream before it
+ * returns.  All calls on a device share the one array, which keeps the last
+ * call's contents: calls that overlap on the GPU (two streams, contexts or
+ * threads at once) race on it, so callers serialise them. */
 int gt_update_matrix_noalloc(gt_matrix* matrix, int form, const double* cell_coef, double nu);
 /* Replaces GT.update_matrix_and_vector! (src/problems.jl:409-414). */
 int gt_update_matrix_and_vector(gt_matrix* matrix, int form, const double* cell_coef, double nu,

@@ -977,6 +977,147 @@ void or_assemble_vector(int ctype, int order, int ncomp, int degree, const doubl
   }
 }
 
+/* Neumann term int g . v dGamma over tagged boundary faces, the loop of
+ * assemble_in_Γn! (docs/src/src_jl/example_poisson_equation.jl:161-203)
+ * with a constant g (ncomp values):
+ *  - faces are visited in the order of the tagged-face list (the faces of
+ *    the boundary domain); each one is found among the cells' local faces by
+ *    its vertex set (fill_face_boundary_mesh_topology!, src/topology.jl:
+ *    515-591), which gives its cell c and local face lf;
+ *  - the face's reference quadrature of the given degree: tensor
+ *    Gauss-Legendre on a segment or square (src/quadrature.jl:78-106); on a
+ *    triangle the reference uses the collapsed (Duffy) rule of
+ *    src/quadrature.jl:121-153 -- restated here as Gauss-Legendre in both
+ *    collapsed coordinates with the collapse factor (1 - u) in the weight,
+ *    exact like the reference's rule for the polynomial integrands of this
+ *    term (degree <= order on a flat face), so the two agree to rounding;
+ *  - the face point mapped into the cell's reference coordinates, the cell's
+ *    shape values there, dGamma = sqrt(det(T^T T)) w with T the tangents
+ *    J dxi/ds of the geometry map (change_of_measure, src/quadrature.jl:4-6);
+ *  - contribute! of the face-closure DOFs, skipping Dirichlet DOFs
+ *    (src/assembly.jl:27-73): b[dof] += be in face order.
+ * t_verts: nt tagged faces as vertex ids (ndv each); c_verts: cells' vertex
+ * ids.  b (nfree) is accumulated into. */
+void or_assemble_boundary_vector(int ctype, int order, int ncomp, int degree, const double* g, int64_t nc,
+                                 const int32_t* cell_nodes, const double* coords, const int32_t* cell_dofs,
+                                 const int32_t* c_verts, int64_t nt, const int32_t* t_verts, double* b) {
+  const int D = ctype == OR_QUAD4 ? 2 : 3;
+  const int nlv = ctype == OR_TET4 ? 4 : (1 << D);
+  const int nlf = ctype == OR_TET4 ? 4 : 2 * D;
+  const int ndv = ctype == OR_TET4 ? 3 : (D == 2 ? 2 : 4);
+  const int nn = space_nodes(ctype, order), nloc = nn * ncomp;
+  /* reference coordinates of the cell's vertices */
+  double xv[8][3];
+  for (int v = 0; v < nlv; v++)
+    for (int d = 0; d < 3; d++)
+      xv[v][d] = ctype == OR_TET4 ? (v == d + 1 ? 1.0 : 0.0) : (d < D ? (double)((v >> d) & 1) : 0.0);
+  /* 1-D Gauss-Legendre on [0,1] with n points (n = 1..4) */
+  double gp[4], gw[4];
+  int n1 = (degree + 2) / 2;
+  if (ctype == OR_TET4) n1 = n1 + 1; /* one more point for the (1 - u) factor */
+  if (n1 > 4) n1 = 4;
+  if (n1 == 1) { gp[0] = 0.5; gw[0] = 1.0; }
+  else if (n1 == 2) { double s = 0.5 / sqrt(3.0); gp[0] = 0.5 - s; gp[1] = 0.5 + s; gw[0] = gw[1] = 0.5; }
+  else if (n1 == 3) {
+    double s = 0.5 * sqrt(0.6);
+    gp[0] = 0.5 - s; gp[1] = 0.5; gp[2] = 0.5 + s;
+    gw[0] = gw[2] = 5.0 / 18.0; gw[1] = 8.0 / 18.0;
+  } else {
+    double a = sqrt(3.0 / 7.0 - 2.0 / 7.0 * sqrt(1.2)), c = sqrt(3.0 / 7.0 + 2.0 / 7.0 * sqrt(1.2));
+    double wa = (18.0 + sqrt(30.0)) / 36.0, wc = (18.0 - sqrt(30.0)) / 36.0;
+    gp[0] = 0.5 - 0.5 * c; gp[1] = 0.5 - 0.5 * a; gp[2] = 0.5 + 0.5 * a; gp[3] = 0.5 + 0.5 * c;
+    gw[0] = gw[3] = 0.5 * wc; gw[1] = gw[2] = 0.5 * wa;
+  }
+  /* cells' local faces by vertex set */
+  omap m;
+  omap_init(&m, nc * nlf);
+  int found;
+  int32_t v[4];
+  for (int64_t c = 0; c < nc; c++)
+    for (int lf = 0; lf < nlf; lf++) {
+      for (int i = 0; i < ndv; i++) {
+        int lv = ctype == OR_TET4 ? TET_FACES[lf][i] : (D == 2 ? QUAD_EDGES[lf][i] : HEX_FACES[lf][i]);
+        v[i] = c_verts[c * nlv + lv - 1];
+      }
+      int32_t* s = omap_slot(&m, v, ndv, &found);
+      if (!found) *s = (int32_t)(c * nlf + lf + 1);
+    }
+  double val[27], grad[27 * 3], gv[8], gg[8 * 3], be[81];
+  int clos[27];
+  for (int64_t t = 0; t < nt; t++) {
+    int32_t* s = omap_slot(&m, t_verts + t * ndv, ndv, &found);
+    if (!found) continue; /* not a face of this mesh */
+    const int64_t c = (*s - 1) / nlf;
+    const int lf = (int)((*s - 1) % nlf);
+    int lvs[4];
+    for (int i = 0; i < ndv; i++)
+      lvs[i] = (ctype == OR_TET4 ? TET_FACES[lf][i] : (D == 2 ? QUAD_EDGES[lf][i] : HEX_FACES[lf][i])) - 1;
+    double X[8 * 3];
+    for (int n = 0; n < nlv; n++)
+      for (int d = 0; d < D; d++) X[n * D + d] = coords[(int64_t)(cell_nodes[c * nlv + n] - 1) * D + d];
+    const int ncl = face_closure_nodes(ctype, order, lf, clos);
+    for (int i = 0; i < nloc; i++) be[i] = 0.0;
+    const int nq = D == 2 ? n1 : n1 * n1;
+    for (int q = 0; q < nq; q++) {
+      const double s1 = gp[q % n1], s2 = D == 3 ? gp[q / n1] : 0.0;
+      double w = gw[q % n1] * (D == 3 ? gw[q / n1] : 1.0);
+      /* reference point xi(s) and its derivatives dxi/ds_a on the face */
+      double xi[3] = {0, 0, 0}, dxi[2][3] = {{0, 0, 0}, {0, 0, 0}};
+      if (D == 2) {
+        for (int d = 0; d < 2; d++) {
+          xi[d] = (1.0 - s1) * xv[lvs[0]][d] + s1 * xv[lvs[1]][d];
+          dxi[0][d] = xv[lvs[1]][d] - xv[lvs[0]][d];
+        }
+      } else if (ctype == OR_TET4) {
+        const double u = s1, t2 = s2 * (1.0 - s1); /* collapsed coordinates */
+        w *= (1.0 - s1);
+        for (int d = 0; d < 3; d++) {
+          xi[d] = xv[lvs[0]][d] + u * (xv[lvs[1]][d] - xv[lvs[0]][d]) + t2 * (xv[lvs[2]][d] - xv[lvs[0]][d]);
+          dxi[0][d] = xv[lvs[1]][d] - xv[lvs[0]][d];
+          dxi[1][d] = xv[lvs[2]][d] - xv[lvs[0]][d];
+        }
+      } else {
+        /* square face: its vertices at (0,0), (1,0), (0,1), (1,1) */
+        const double N[4] = {(1 - s1) * (1 - s2), s1 * (1 - s2), (1 - s1) * s2, s1 * s2};
+        const double dN0[4] = {-(1 - s2), 1 - s2, -s2, s2}, dN1[4] = {-(1 - s1), -s1, 1 - s1, s1};
+        for (int d = 0; d < 3; d++)
+          for (int i = 0; i < 4; i++) {
+            xi[d] += N[i] * xv[lvs[i]][d];
+            dxi[0][d] += dN0[i] * xv[lvs[i]][d];
+            dxi[1][d] += dN1[i] * xv[lvs[i]][d];
+          }
+      }
+      /* geometry Jacobian at xi, physical tangents T_a = J dxi_a */
+      tabulate(ctype, 1, xi, gv, gg);
+      double J[9] = {0};
+      for (int n = 0; n < nlv; n++)
+        for (int i = 0; i < D; i++)
+          for (int j = 0; j < D; j++) J[i * D + j] += X[n * D + i] * gg[n * D + j];
+      double T[2][3] = {{0, 0, 0}, {0, 0, 0}};
+      for (int a = 0; a < D - 1; a++)
+        for (int i = 0; i < D; i++)
+          for (int j = 0; j < D; j++) T[a][i] += J[i * D + j] * dxi[a][j];
+      double meas;
+      if (D == 2) {
+        meas = sqrt(T[0][0] * T[0][0] + T[0][1] * T[0][1]);
+      } else {
+        double g11 = 0, g12 = 0, g22 = 0;
+        for (int i = 0; i < 3; i++) { g11 += T[0][i] * T[0][i]; g12 += T[0][i] * T[1][i]; g22 += T[1][i] * T[1][i]; }
+        meas = sqrt(g11 * g22 - g12 * g12);
+      }
+      tabulate(ctype, order, xi, val, grad);
+      for (int i = 0; i < ncl; i++)
+        for (int k = 0; k < ncomp; k++) be[clos[i] * ncomp + k] += g[k] * val[clos[i]] * (meas * w);
+    }
+    for (int i = 0; i < ncl; i++)
+      for (int k = 0; k < ncomp; k++) {
+        int32_t dof = cell_dofs[c * nloc + clos[i] * ncomp + k];
+        if (dof > 0) b[dof - 1] += be[clos[i] * ncomp + k];
+      }
+  }
+  omap_free(&m);
+}
+
 /* Element matrix of one cell (diagnostics / small tests). */
 void or_element_matrix(int ctype, int order, int ncomp, int degree, int form, double nu,
                        double coef, const double* X, double* Ke) {
@@ -1047,5 +1188,14 @@ int or_num_threads(void) {
   return omp_get_max_threads();
 #else
   return 1;
+#endif
+}
+
+/* Threads of the OpenMP loops (1 = the reference's single-threaded path). */
+void or_set_num_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+#else
+  (void)n;
 #endif
 }

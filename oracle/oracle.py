@@ -87,6 +87,8 @@ def lib():
             L.or_pcg.argtypes = [i64, P, P, P, P, P, dbl, i32, P]
             L.or_pcg.restype = i32
             L.or_num_threads.restype = i32
+            L.or_set_num_threads.argtypes = [i32]
+            L.or_assemble_boundary_vector.argtypes = [i32, i32, i32, i32, P, i64, P, P, P, P, i64, P, P]
             _lib = L
     return _lib
 
@@ -314,3 +316,27 @@ def pcg(rowptr, colind, vals, b, rtol=1e-12, maxit=10000):
 
 def num_threads():
     return int(lib().or_num_threads())
+
+
+def set_threads(n):
+    """Threads of the oracle's OpenMP loops (1: the reference's
+    single-threaded path)."""
+    lib().or_set_num_threads(int(n))
+
+
+def assemble_boundary_vector(space, degree, g, groups=None):
+    """The Neumann term int g . v dGamma (constant g, ncomp values) over the
+    boundary faces of the named groups (None / "boundary": all), the loop of
+    assemble_in_Γn! (docs/src/src_jl/example_poisson_equation.jl:161-203);
+    free DOFs only."""
+    mesh = space["mesh"]
+    cd = space["cell_dofs"]
+    nv = space["node_vertex"]
+    c_verts = np.ascontiguousarray(nv[mesh["cell_nodes"] - 1])
+    tf = np.ascontiguousarray(nv[boundary_faces(mesh, groups) - 1])
+    fv = np.ascontiguousarray(np.broadcast_to(np.asarray(g, np.float64), (space["ncomp"],)))
+    b = np.zeros(space["nfree"], np.float64)
+    lib().or_assemble_boundary_vector(mesh["ctype"], space["order"], space["ncomp"], int(degree), _p(fv),
+                                      cd.shape[0], _p(mesh["cell_nodes"]), _p(mesh["coords"]), _p(cd),
+                                      _p(c_verts), tf.shape[0], _p(tf), _p(b))
+    return b

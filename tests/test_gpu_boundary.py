@@ -89,3 +89,46 @@ def test_vector_traction():
     g = np.array([0.5, -1.0, 2.0])
     b = GT.assemble_boundary_vector(g, GT.boundary(m, ["2-face-2"]), V)  # z = 1, area 1
     assert np.allclose(b.reshape(-1, 3).sum(axis=0), g, rtol=0, atol=1e-12)
+
+
+def _oracle_space(m, order, ncomp, groups):
+    import oracle as O
+    om = dict(D=m.D, ctype=m.cell_type, coords=m.coords, cell_nodes=m.cell_nodes, pf0=m.corners,
+              cells=m.cells_per_dir, box=m.domain)
+    if m.D == 2:
+        om["pf1"], om["pf1g"] = m.bfaces, m.bface_group
+    else:
+        om["pf1"], om["pf2"], om["pf2g"] = m.bedges, m.bfaces, m.bface_group
+    return O.lagrange_space(om, order, ncomp=ncomp, dirichlet=groups)
+
+
+ORACLE_CASES = [
+    # (id, cells, simplex, order, ncomp, jitter, Dirichlet groups, Neumann groups, g)
+    ("p1tet_x1", (4, 3, 5), True, 1, 1, 0.2, ["2-face-1", "2-face-2"], ["2-face-6"], 1.0),
+    ("p1tet_sides", (4, 3, 5), True, 1, 1, 0.2, ["2-face-5"], ["2-face-6", "2-face-1"], -0.75),
+    ("p2tet_all", (2, 3, 2), True, 2, 1, 0.2, None, None, 1.5),
+    ("q1hex_z1", (3, 4, 2), False, 1, 1, 0.15, ["2-face-5"], ["2-face-2"], 2.0),
+    ("q2hex_vec", (2, 3, 2), False, 2, 3, 0.1, ["2-face-5"], ["2-face-6", "2-face-3"], [0.5, -1.0, 2.0]),
+    ("q1quad_all", (5, 4), False, 1, 1, 0.2, ["1-face-3"], None, 1.25),
+    ("q2quad_vec", (3, 2), False, 2, 2, 0.0, ["1-face-1"], ["1-face-4"], [1.0, -2.0]),
+]
+
+
+@pytest.mark.parametrize("case", ORACLE_CASES, ids=[c[0] for c in ORACLE_CASES])
+def test_boundary_vector_matches_oracle(case):
+    """gt_assemble_boundary_vector entry by entry against the oracle's
+    restatement of assemble_in_Γn! (same faces, same free DOFs; the two sum
+    each DOF's faces in different orders and use different exact triangle
+    rules, so they agree to rounding: 1e-12 of the largest entry)."""
+    import oracle as O
+    cid, cells, simplex, order, ncomp, jit, diri, neu, g = case
+    m = _mesh(cells, simplex, jit)
+    V = GT.lagrange_space(GT.interior(m), order, tensor_size=(ncomp,) if ncomp > 1 else None,
+                          dirichlet_boundary=None if diri is None else GT.boundary(m, None if diri == "boundary" else diri))
+    ref = _oracle_space(m, order, ncomp, diri)
+    assert np.array_equal(V.face_dofs(), ref["cell_dofs"])
+    b = GT.assemble_boundary_vector(g, GT.boundary(m, neu), V)
+    ob = O.assemble_boundary_vector(ref, 2 * order, g, neu)
+    assert b.shape == ob.shape
+    if ob.size:
+        assert np.abs(b - ob).max() <= 1e-12 * np.abs(ob).max()

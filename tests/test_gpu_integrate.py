@@ -112,3 +112,34 @@ def test_integrate_rejects_bad_arguments():
         GT.integrate(V, "l2_error2", np.zeros(V.num_free_dofs))  # no exact solution
     with pytest.raises(ValueError):
         GT.integrate(V, "field", np.zeros(3))
+
+
+def test_solution_field():
+    """GT.solution_field (src/problems.jl:501-526): the solved free values
+    plus the Dirichlet field's values make the discrete field whose error
+    norms the reference's tests check; solution_field(U, x) has zero
+    Dirichlet values; solution_field! replaces the free values in place."""
+    m = GT.cartesian_mesh((0, 1, 0, 1), (6, 5))
+    GT.jitter_interior_nodes(m, 0.2, 3)
+    V = GT.lagrange_space(GT.interior(m), 2, dirichlet_boundary=GT.boundary(m))
+    p = GT.Polynomial(x=1.0, y=1.0)
+    uhd = GT.dirichlet_field(V, p)
+    assert np.array_equal(uhd.dirichlet_values, GT.interpolate_dirichlet(p, V))
+    lp = GT.linear_problem(V, GT.laplacian(), GT.source(0.0), dirichlet_values=uhd)
+    GT.solve(lp, rtol=1e-13)
+    uh = GT.solution_field(uhd, lp)
+    assert GT.l2_error(V, uh, p) < 1e-10 and GT.h1_error(V, uh, p) < 1e-10
+    # the same field through the (free values, Dirichlet values) pair
+    assert GT.l2_error(V, uh, p) == GT.l2_error(V, lp.x, p, uhd.dirichlet_values)
+    # per-cell values: Dirichlet DOFs carry the interpolated data
+    cd = V.face_dofs()
+    dv = uh.dof_values()
+    assert np.array_equal(dv[cd < 0], uhd.dirichlet_values[-cd[cd < 0] - 1])
+    # zero Dirichlet values: the boundary data is missing, so the error is not small
+    u0 = GT.solution_field(V, lp.x)
+    assert not u0.dirichlet_values.any() and GT.l2_error(V, u0, p) > 1e-2
+    # in place
+    GT.solution_field_inplace(u0, np.zeros(V.num_free_dofs))
+    assert GT.integrate(V, "l2_norm2", u0) == 0.0
+    with pytest.raises(ValueError):
+        GT.solution_field_inplace(u0, np.zeros(3))

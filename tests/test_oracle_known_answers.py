@@ -102,3 +102,52 @@ def test_oracle_pcg_matches_direct():
     x, it, rr = O.pcg(rp, ci, vv, b, rtol=1e-13)
     xd = sla.spsolve(sp.csc_matrix((nz, rv, cp), shape=(V["nfree"],) * 2), b)
     assert rr < 1e-13 and np.abs(x - xd).max() / np.abs(xd).max() < 1e-11
+
+
+# ---------------------------------------------------------------------------
+# the oracle's Neumann term (assemble_in_Γn!, docs/src/src_jl/
+# example_poisson_equation.jl:161-203): boundary measures, first moments and
+# a Neumann patch test
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("cells,simplex,order,measure", [
+    ((5, 4), False, 1, 8.0), ((3, 5), False, 2, 8.0), ((3, 2, 4), False, 1, 24.0), ((2, 3, 2), False, 2, 24.0),
+    ((3, 2, 2), True, 1, 24.0), ((2, 2, 3), True, 2, 24.0)])
+def test_neumann_term_sums_to_the_boundary_measure(cells, simplex, order, measure):
+    # box [0,2]^D: perimeter 8, surface 24; interior nodes jittered
+    m = O.cartesian_mesh(tuple(x for _ in cells for x in (0.0, 2.0)), cells, simplexify=simplex)
+    O.jitter(m, 0.2, 5)
+    V = O.lagrange_space(m, order)
+    b = O.assemble_boundary_vector(V, 2 * order, 1.0)
+    assert abs(b.sum() - measure) < 1e-12
+    # one side only: x = 0 ("(D-1)-face-3" in 2-D, "(D-1)-face-5" in 3-D) has measure 2^(D-1)
+    side = "1-face-3" if len(cells) == 2 else "2-face-5"
+    bs = O.assemble_boundary_vector(V, 2 * order, 1.0, [side])
+    assert abs(bs.sum() - 2.0 ** (len(cells) - 1)) < 1e-12
+
+
+def test_neumann_term_first_moment():
+    # Q1 reproduces u = x, so sum_i x_i b_i = int_dOmega x dGamma = 2 on the unit square
+    m = O.cartesian_mesh((0, 1, 0, 1), (4, 3))
+    V = O.lagrange_space(m, 1)
+    b = O.assemble_boundary_vector(V, 2, 1.0)
+    xf, _ = _dof_values(m, V, lambda x: x[0])
+    assert abs(xf @ b - 2.0) < 1e-13
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_neumann_patch_test(order):
+    # -Laplace(u) = 0, u = x + y: Dirichlet on x = 0 (1-face-3), du/dn = 1 on
+    # x = 1 (1-face-4) and y = 1 (1-face-2), du/dn = -1 on y = 0 (1-face-1)
+    m = O.cartesian_mesh((0, 1, 0, 1), (4, 3))
+    O.jitter(m, 0.15, 9)
+    V = O.lagrange_space(m, order, dirichlet=["1-face-3"])
+    deg = 2 * order
+    cp, rv, nz = O.assemble_matrix(V, O.LAPLACE, deg)
+    cpd, rvd, nzd = O.assemble_matrix(V, O.LAPLACE, deg, dirichlet_cols=True)
+    A = sp.csc_matrix((nz, rv, cp), shape=(V["nfree"], V["nfree"]))
+    Ad = sp.csc_matrix((nzd, rvd, cpd), shape=(V["nfree"], V["ndiri"]))
+    uf, ud = _dof_values(m, V, lambda x: x.sum())
+    b = (O.assemble_boundary_vector(V, deg, 1.0, ["1-face-4", "1-face-2"])
+         + O.assemble_boundary_vector(V, deg, -1.0, ["1-face-1"]) - Ad @ ud)
+    x = sla.spsolve(A, b)
+    assert np.abs(x - uf).max() < 1e-10

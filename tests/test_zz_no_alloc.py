@@ -6,9 +6,11 @@ latency-critical refill loop where cudaMalloc/cudaFree would synchronise the
 device -- refill an assembled matrix through this entry point, which takes
 its scratch from one static 128 MiB device array.  This file checks it,
 through the C ABI, against the allocating gt_update_matrix on two calls in a
-row (the shared array keeps the previous call's contents), and checks that an
-oversize refill and a host-memory coefficient are refused.  The file sorts
-last so that a run stopping at the first failure has run every other test.
+row (the shared array keeps the previous call's contents), checks that those
+calls take no device memory from the library's pool (its live and pooled
+bytes stay the same across them), and checks that an oversize refill and a
+host-memory coefficient are refused.  The file sorts last so that a run
+stopping at the first failure has run every other test.
 """
 import ctypes as C
 
@@ -44,11 +46,15 @@ def test_noalloc_refill_matches_update_matrix_p1():
     k0 = GT.lognormal_cells(m.num_cells, 1.0, 1)
     A = GT.assemble_matrix(GT.laplacian(k0), np.float64, V, V)
     B = GT.assemble_matrix(GT.laplacian(k0), np.float64, V, V)
-    for seed in (21, 22):  # two calls in a row
-        k = GT.lognormal_cells(m.num_cells, 1.0, seed)
-        GT.update_matrix(A, GT.laplacian(k))
-        st = _refill_noalloc(B, _lib.GT_LAPLACE, torch.from_numpy(k).cuda())
-        assert st == 0, GT.default_context().lib.gt_last_error(GT.default_context().h)
+    ctx = B.ctx
+    coefs = [torch.from_numpy(GT.lognormal_cells(m.num_cells, 1.0, seed)).cuda() for seed in (21, 22)]
+    ctx.synchronize()
+    for k in coefs:  # two calls in a row
+        held = ctx.memory()  # (live, pooled) bytes of the library's pool
+        st = _refill_noalloc(B, _lib.GT_LAPLACE, k)
+        assert st == 0, ctx.lib.gt_last_error(ctx.h)
+        assert ctx.memory() == held, "the refill took device memory from the pool"
+        GT.update_matrix(A, GT.laplacian(k.cpu().numpy()))
         _compare(A, B)
 
 
