@@ -1794,22 +1794,13 @@ __device__ void lagrange_table_1d(int order, double* M, double* Dm, double* Kd, 
   }
 }
 
+// geometry record of one affine QUAD4/HEX8 cell: J^-1 (elasticity) or the
+// metric J^-1 J^-T (Laplacian) in gv[0..D*D), |det J| and det J; false when
+// some node is off the affine map x0 + sum_d bit_d(n) J[:, d]
 template <int D, int NV>
-__global__ void __launch_bounds__(256) k_geom_affine(const double* __restrict__ coords,
-                                                     const int32_t* __restrict__ cell_nodes,
-                                                     const double* __restrict__ coef, int form, int order,
-                                                     int64_t ncells, int nn, int bs, void* __restrict__ Gout, int g64,
-                                                     double* __restrict__ be, const double* __restrict__ fsrc,
-                                                     const double* __restrict__ scoef, uint32_t* nonaffine,
-                                                     uint32_t* err) {
-  __shared__ double s_m1[3];
-  if (threadIdx.x == 0) {
-    double M[9], Dm[9], Kd[9];
-    lagrange_table_1d(order, M, Dm, Kd, s_m1);
-  }
-  __syncthreads();
-  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (c >= ncells) return;
+__device__ __forceinline__ bool affine_record(const double* __restrict__ coords, const int32_t* __restrict__ cell_nodes,
+                                              int64_t c, int form, double (&gv)[GSTRIDE], double& adet,
+                                              double& det) {
   double x[NV][D];
 #pragma unroll
   for (int n = 0; n < NV; n++) {
@@ -1817,12 +1808,11 @@ __global__ void __launch_bounds__(256) k_geom_affine(const double* __restrict__ 
 #pragma unroll
     for (int d = 0; d < D; d++) x[n][d] = p[d];
   }
-  double J[D][D], scale = 0.0;
+  double J[D][D];
 #pragma unroll
   for (int i = 0; i < D; i++)
 #pragma unroll
     for (int d = 0; d < D; d++) J[i][d] = x[1 << d][i] - x[0][i];
-  // affine iff every node is x0 + sum_d bit_d(n) J[:, d]
   double hmax = 0.0;
 #pragma unroll
   for (int i = 0; i < D; i++)
@@ -1840,8 +1830,7 @@ __global__ void __launch_bounds__(256) k_geom_affine(const double* __restrict__ 
       if (fabs(x[n][i] - pred) > 1e-13 * hmax) affine = false;
     }
   }
-  if (!affine) atomicOr(nonaffine, 1u);
-  double inv[D][D], det;
+  double inv[D][D];
   if (D == 2) {
     det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
     double r = recip_nr2(det);
@@ -1861,9 +1850,7 @@ __global__ void __launch_bounds__(256) k_geom_affine(const double* __restrict__ 
     inv[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
     inv[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
   }
-  if (!(det != 0.0)) atomicOr(err, DEV_ERR_DEGENERATE);
-  double adet = fabs(det);
-  double gv[GSTRIDE];
+  adet = fabs(det);
 #pragma unroll
   for (int i = 0; i < GSTRIDE; i++) gv[i] = 0.0;
   if (form == GT_LAPLACE) {
@@ -1883,7 +1870,56 @@ __global__ void __launch_bounds__(256) k_geom_affine(const double* __restrict__ 
 #pragma unroll
       for (int l = 0; l < D; l++) gv[k * D + l] = inv[k][l];
   }
-  scale = adet * (coef ? coef[c] : 1.0);
+  return affine;
+}
+
+// the record of cell 0: the reference of the uniformity test
+// (gref[0..GSTRIDE-1) the record, gref[GSTRIDE-1] |det J|)
+template <int D, int NV>
+__global__ void k_geom_ref(const double* __restrict__ coords, const int32_t* __restrict__ cell_nodes, int form,
+                           double* __restrict__ gref) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  double gv[GSTRIDE], adet, det;
+  affine_record<D, NV>(coords, cell_nodes, 0, form, gv, adet, det);
+  gv[GSTRIDE - 1] = adet;
+#pragma unroll
+  for (int i = 0; i < GSTRIDE; i++) gref[i] = gv[i];
+}
+
+// per-cell records G[c] = {record, scale = |det J| coef_c} (+ the load
+// vector), affinity check, and -- with gref -- the uniformity test: a cell
+// whose record and |det J| differ from cell 0's by more than 1e-13 of the
+// largest record entry (of |det J|) sets *nonuniform
+template <int D, int NV>
+__global__ void __launch_bounds__(256) k_geom_affine(const double* __restrict__ coords,
+                                                     const int32_t* __restrict__ cell_nodes,
+                                                     const double* __restrict__ coef, int form, int order,
+                                                     int64_t ncells, int nn, int bs, void* __restrict__ Gout, int g64,
+                                                     double* __restrict__ be, const double* __restrict__ fsrc,
+                                                     const double* __restrict__ scoef, uint32_t* nonaffine,
+                                                     uint32_t* err, const double* __restrict__ gref,
+                                                     uint32_t* nonuniform) {
+  __shared__ double s_m1[3];
+  if (threadIdx.x == 0) {
+    double M[9], Dm[9], Kd[9];
+    lagrange_table_1d(order, M, Dm, Kd, s_m1);
+  }
+  __syncthreads();
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= ncells) return;
+  double gv[GSTRIDE], adet, det;
+  if (!affine_record<D, NV>(coords, cell_nodes, c, form, gv, adet, det)) atomicOr(nonaffine, 1u);
+  if (!(det != 0.0)) atomicOr(err, DEV_ERR_DEGENERATE);
+  if (gref) {
+    double gm = 0.0;
+#pragma unroll
+    for (int i = 0; i < D * D; i++) gm = fmax(gm, fabs(gref[i]));
+    bool same = fabs(adet - gref[GSTRIDE - 1]) <= 1e-13 * gref[GSTRIDE - 1];
+#pragma unroll
+    for (int i = 0; i < D * D; i++) same = same && fabs(gv[i] - gref[i]) <= 1e-13 * gm;
+    if (!same) atomicOr(nonuniform, 1u);
+  }
+  const double scale = adet * (coef ? coef[c] : 1.0);
   gv[GSTRIDE - 1] = scale;
   if (g64) {
     double* G = (double*)Gout + c * GSTRIDE;
@@ -2077,6 +2113,175 @@ __global__ void k_scatter_kron(const int64_t* __restrict__ rowptr, const int32_t
   }
 }
 
+// Uniform geometry: every cell has the reference record (cell 0's), so an
+// element block is scale_c x Kref[a][b] with Kref the unit-scale block of
+// the reference record, computed once per CTA into shared memory by
+// kron_block (FP64 for FP64 values, FP32 for FP32 values) and scale_c =
+// |det J| coef_c -- the per-(row, cell, column node) work is BS*BS
+// multiply-adds instead of a kron_block.  Otherwise as k_scatter_kron (row
+// owner, incidences in ascending cell order, load vector and Dirichlet lift
+// in the same pass).
+template <int D, int ORDER, int BS, int FORM, int G, class T>
+__global__ void k_scatter_uniform(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                                  const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                  const int32_t* __restrict__ cnd, int64_t nrows, int lmax,
+                                  const double* __restrict__ gref, const double* __restrict__ coef, T lamf, T muf,
+                                  double* __restrict__ v64, float* __restrict__ v32, const double* __restrict__ be,
+                                  double* __restrict__ bvec, const double* __restrict__ xd) {
+  constexpr int M1 = ORDER + 1;
+  constexpr int NN = D == 2 ? M1 * M1 : M1 * M1 * M1;
+  constexpr int RPW = 32 / G;
+  constexpr int KB = BS * BS;
+  constexpr size_t KREF_BYTES = ((size_t)NN * NN * KB * sizeof(T) + 15) & ~size_t(15);
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  __shared__ T s_M[9], s_D[9], s_K[9];
+  T* s_ref = (T*)s_raw;
+  if (threadIdx.x == 0) {
+    double M[9], Dm[9], Kd[9], m1[3];
+    lagrange_table_1d(ORDER, M, Dm, Kd, m1);
+    for (int i = 0; i < 9; i++) { s_M[i] = (T)M[i]; s_D[i] = (T)Dm[i]; s_K[i] = (T)Kd[i]; }
+  }
+  __syncthreads();
+  {
+    T g[GSTRIDE];
+#pragma unroll
+    for (int i = 0; i < GSTRIDE - 1; i++) g[i] = (T)__ldg(gref + i);
+    g[GSTRIDE - 1] = (T)1;
+    for (int ab = threadIdx.x; ab < NN * NN; ab += blockDim.x) {
+      const int a = ab / NN, b = ab - (ab / NN) * NN;
+      int na[3] = {a % M1, (a / M1) % M1, a / (M1 * M1)};
+      int nb[3] = {b % M1, (b / M1) % M1, b / (M1 * M1)};
+      T blk[BS][BS];
+      kron_block<D, BS, FORM, T>(na, nb, g, s_M, s_D, s_K, lamf, muf, blk);
+#pragma unroll
+      for (int cc = 0; cc < BS; cc++)
+#pragma unroll
+        for (int dd = 0; dd < BS; dd++) s_ref[(size_t)ab * KB + cc * BS + dd] = blk[cc][dd];
+    }
+  }
+  __syncthreads();
+  const double adet = __ldg(gref + GSTRIDE - 1);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int sub = lane / G, gl = lane - sub * G;
+  int slot = w * RPW + sub;
+  T* acc = (T*)(s_raw + KREF_BYTES) + (size_t)slot * lmax * KB;
+  int32_t* cols = (int32_t*)((T*)(s_raw + KREF_BYTES) + (size_t)(blockDim.x / G) * lmax * KB) + (size_t)slot * lmax;
+  int64_t r = ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * RPW + sub;
+  bool active = r < nrows;
+  unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
+  int64_t rb = 0;
+  int L = 0;
+  if (active) {
+    rb = rowptr[r];
+    L = (int)(rowptr[r + 1] - rb);
+    for (int i = gl; i < L; i += G) cols[i] = colind[rb + i];
+    for (int i = gl; i < L * KB; i += G) acc[i] = (T)0;
+  }
+  __syncwarp(gmask);
+  if (active) {
+    const int b = gl;
+    const bool vec = be != nullptr && gl == 0;
+    const bool lift = be != nullptr && xd != nullptr;
+    double bsum[BS];
+    int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+    if (be != nullptr) {
+      row_load_sum<BS>(ib, ie, inc, NN, be, gl, gmask, bsum);
+    } else {
+#pragma unroll
+      for (int cc = 0; cc < BS; cc++) bsum[cc] = 0.0;
+    }
+    for (int64_t k = ib; k < ie; k++) {
+      int32_t cb = __ldg(inc + k);
+      int32_t c = cb / NN, a = cb - c * NN;
+      double lv[BS];
+#pragma unroll
+      for (int cc = 0; cc < BS; cc++) lv[cc] = 0.0;
+      if (b < NN) {
+        int32_t j = __ldg(cnd + (int64_t)c * NN + b);
+        if (j > 0 || (j < 0 && lift)) {
+          const T sc = (T)(adet * (coef ? __ldg(coef + c) : 1.0));
+          const T* kr = s_ref + (size_t)(a * NN + b) * KB;
+          if (j > 0) {
+            int p = find_col(cols, L, j - 1);
+#pragma unroll
+            for (int e = 0; e < KB; e++) acc[p * KB + e] += sc * kr[e];
+          } else {
+#pragma unroll
+            for (int cc = 0; cc < BS; cc++)
+#pragma unroll
+              for (int dd = 0; dd < BS; dd++)
+                lv[cc] += (double)(sc * kr[cc * BS + dd]) * __ldg(xd + (int64_t)(-j - 1) * BS + dd);
+          }
+        }
+      }
+      if (lift)
+#pragma unroll
+        for (int cc = 0; cc < BS; cc++) {
+#pragma unroll
+          for (int o = G >> 1; o; o >>= 1) lv[cc] += __shfl_xor_sync(gmask, lv[cc], o);
+          if (gl == 0) bsum[cc] -= lv[cc];
+        }
+      __syncwarp(gmask);
+    }
+    int64_t ob = rb * KB;
+    for (int i = gl; i < L * KB; i += G) {
+      T v = acc[i];
+      if (v64) v64[ob + i] = (double)v;
+      if (v32) v32[ob + i] = (float)v;
+    }
+    if (vec)
+#pragma unroll
+      for (int cc = 0; cc < BS; cc++) bvec[r * BS + cc] = bsum[cc];
+  }
+}
+
+// launches k_scatter_uniform; GT_ERR_UNSUPPORTED (nothing launched) when
+// the reference block and the row slots do not fit in shared memory
+template <int D, int ORDER, int BS, int FORM, class T>
+static int launch_uniform(Matrix* A, const double* gref, const double* coef, double nu, const double* be,
+                          double* bvec, const double* xd) {
+  const Space* sp = A->space;
+  Ctx* ctx = ctx_of(sp);
+  constexpr int M1 = ORDER + 1;
+  constexpr int NN = D == 2 ? M1 * M1 : M1 * M1 * M1;
+  constexpr int G = NN <= 4 ? 4 : (NN <= 8 ? 8 : (NN <= 16 ? 16 : 32));
+  constexpr int RPW = 32 / G;
+  constexpr size_t KREF_BYTES = ((size_t)NN * NN * BS * BS * sizeof(T) + 15) & ~size_t(15);
+  int lmax = A->max_row > 0 ? A->max_row : 1;
+  double* v64 = A->precision != GT_FP32 ? A->val64 : nullptr;
+  float* v32 = A->precision != GT_FP64 ? A->val32 : nullptr;
+  int warps = 4;
+  size_t per_row = (size_t)lmax * (BS * BS * sizeof(T) + sizeof(int32_t));
+  while (warps > 1 && KREF_BYTES + (size_t)warps * RPW * per_row > 112 * 1024) warps >>= 1;
+  size_t smem = KREF_BYTES + (size_t)warps * RPW * per_row;
+  if (smem > 200 * 1024) return GT_ERR_UNSUPPORTED;
+  auto kern = k_scatter_uniform<D, ORDER, BS, FORM, G, T>;
+  GT_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  matrix_values_changed(A);
+  int64_t rows_per_block = (int64_t)warps * RPW;
+  int64_t grid = (A->nbrows + rows_per_block - 1) / rows_per_block;
+  T lamf = (T)(nu / ((1.0 + nu) * (1.0 - 2.0 * nu))), muf = (T)(1.0 / (2.0 * (1.0 + nu)));
+  kern<<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
+      A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, A->nbrows, lmax, gref, coef, lamf, muf, v64, v32, be,
+      bvec, xd);
+  GT_LAUNCH(ctx, "k_scatter_uniform");
+  return GT_OK;
+}
+
+template <int D, int ORDER, class T>
+static int dispatch_uniform(Matrix* A, int form, const double* gref, const double* coef, double nu, const double* be,
+                            double* bvec, const double* xd) {
+  if (A->bs == 1) {
+    if (form == GT_LAPLACE) return launch_uniform<D, ORDER, 1, GT_LAPLACE, T>(A, gref, coef, nu, be, bvec, xd);
+    if (form == GT_MASS) return launch_uniform<D, ORDER, 1, GT_MASS, T>(A, gref, coef, nu, be, bvec, xd);
+  } else {
+    if (form == GT_LAPLACE) return launch_uniform<D, ORDER, D, GT_LAPLACE, T>(A, gref, coef, nu, be, bvec, xd);
+    if (form == GT_MASS) return launch_uniform<D, ORDER, D, GT_MASS, T>(A, gref, coef, nu, be, bvec, xd);
+    if (form == GT_ELASTICITY) return launch_uniform<D, ORDER, D, GT_ELASTICITY, T>(A, gref, coef, nu, be, bvec, xd);
+  }
+  return set_error(ctx_of(A->space), GT_ERR_UNSUPPORTED, "weak form not supported on this space");
+}
+
 template <int D, int ORDER, int BS, int FORM, class T>
 static int launch_kron(Matrix* A, const T* Gc, double nu, const double* be, double* bvec, const double* xd) {
   const Space* sp = A->space;
@@ -2137,28 +2342,48 @@ static int kron_numeric(Matrix* A, int form, const double* coef, double nu, cons
   bool g64 = A->precision != GT_FP32;
   void* Gc = nullptr;
   uint32_t* flag = nullptr;
+  double* gref = nullptr;
   GT_TRY(dalloc(ctx, (unsigned char**)&Gc, nc * GSTRIDE * (int64_t)(g64 ? sizeof(double) : sizeof(float))));
-  GT_TRY(dalloc(ctx, &flag, 1));
-  GT_CUDA(ctx, cudaMemsetAsync(flag, 0, sizeof(uint32_t), ctx->stream));
-  if (ct == GT_QUAD4)
+  GT_TRY(dalloc(ctx, &flag, 2));
+  GT_TRY(dalloc(ctx, &gref, GSTRIDE));
+  GT_CUDA(ctx, cudaMemsetAsync(flag, 0, 2 * sizeof(uint32_t), ctx->stream));
+  double* gr = ctx->uniform_geom ? gref : nullptr;
+  if (ct == GT_QUAD4) {
+    if (gr) k_geom_ref<2, 4><<<GT_KC(ctx, 1), 32, 0, ctx->stream>>>(sp->mesh->coords, sp->mesh->cell_nodes, form, gr);
     k_geom_affine<2, 4><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
         sp->mesh->coords, sp->mesh->cell_nodes, coef, form, sp->order, nc, sp->nn, sp->ncomp, Gc, g64, be, f, scoef,
-        flag, ctx->d_err);
-  else
+        flag, ctx->d_err, gr, flag + 1);
+  } else {
+    if (gr) k_geom_ref<3, 8><<<GT_KC(ctx, 1), 32, 0, ctx->stream>>>(sp->mesh->coords, sp->mesh->cell_nodes, form, gr);
     k_geom_affine<3, 8><<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, ctx->stream>>>(
         sp->mesh->coords, sp->mesh->cell_nodes, coef, form, sp->order, nc, sp->nn, sp->ncomp, Gc, g64, be, f, scoef,
-        flag, ctx->d_err);
+        flag, ctx->d_err, gr, flag + 1);
+  }
   GT_LAUNCH(ctx, "k_geom_affine");
-  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[2], flag, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[2], flag, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-  uint32_t nonaffine = 0;
-  memcpy(&nonaffine, &ctx->h_scratch[2], sizeof(uint32_t));
+  uint32_t flags[2] = {0, 0};
+  memcpy(flags, &ctx->h_scratch[2], 2 * sizeof(uint32_t));
+  const uint32_t nonaffine = flags[0];
+  const bool uniform = gr && !flags[1];
   mark(ctx, "elements");
   int s = GT_OK;
   if (!nonaffine) {
     s = alloc_values(A);
     int D = sp->mesh->D, o = sp->order;
-    if (s == GT_OK) {
+    int us = GT_ERR_UNSUPPORTED;  // uniform path taken: GT_OK
+    if (s == GT_OK && uniform) {
+      us = g64 ? (D == 2 ? (o == 1 ? dispatch_uniform<2, 1, double>(A, form, gr, coef, nu, be, bvec, xd)
+                                   : dispatch_uniform<2, 2, double>(A, form, gr, coef, nu, be, bvec, xd))
+                         : (o == 1 ? dispatch_uniform<3, 1, double>(A, form, gr, coef, nu, be, bvec, xd)
+                                   : dispatch_uniform<3, 2, double>(A, form, gr, coef, nu, be, bvec, xd)))
+               : (D == 2 ? (o == 1 ? dispatch_uniform<2, 1, float>(A, form, gr, coef, nu, be, bvec, xd)
+                                   : dispatch_uniform<2, 2, float>(A, form, gr, coef, nu, be, bvec, xd))
+                         : (o == 1 ? dispatch_uniform<3, 1, float>(A, form, gr, coef, nu, be, bvec, xd)
+                                   : dispatch_uniform<3, 2, float>(A, form, gr, coef, nu, be, bvec, xd)));
+      if (us != GT_OK && us != GT_ERR_UNSUPPORTED) s = us;
+    }
+    if (s == GT_OK && us == GT_ERR_UNSUPPORTED) {
       if (g64) {
         const double* G = (const double*)Gc;
         s = D == 2 ? (o == 1 ? dispatch_kron<2, 1, double>(A, form, G, nu, be, bvec, xd)
@@ -2178,6 +2403,7 @@ static int kron_numeric(Matrix* A, int form, const double* coef, double nu, cons
   }
   pool_free(ctx, Gc);
   dfree(ctx, flag);
+  dfree(ctx, gref);
   return s;
 }
 
@@ -2486,8 +2712,8 @@ struct HostCsr {
 // downloaded on the copy stream (pat_down: its event); the values are then
 // scattered in row chunks, each chunk's download overlapping the next chunk's
 // scatter (*values_done set when that happened).
-static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, const HostCsr* hc = nullptr,
-                      cudaEvent_t pat_down = nullptr, bool* values_done = nullptr, EarlyElems* early = nullptr) {
+static int numeric_pass(Matrix* A, int form, NumIn& in, double nu, double* b_out, const HostCsr* hc,
+                        cudaEvent_t pat_down, bool* values_done, EarlyElems* early) {
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   int64_t nc = sp->mesh->ncells;
@@ -2622,6 +2848,40 @@ static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, 
   if (b_out && !dev) dfree(ctx, bd);
   if (Ke) pool_free(ctx, Ke);
   if (be) dfree(ctx, be);
+  return s;
+}
+
+// FP32 values of a GT_MIXED matrix integrated in FP32 (FP64 Jacobian, its
+// inverse and determinant; FP32 element blocks and FP32 accumulation), on the
+// pattern the FP64 pass built
+static int fp32_values_pass(Matrix* A, int form, NumIn& in, double nu) {
+  const Space* sp = A->space;
+  Ctx* ctx = ctx_of(sp);
+  int used = 0;
+  GT_TRY(kron_numeric(A, form, in.coef.p, nu, nullptr, nullptr, nullptr, nullptr, nullptr, &used));
+  if (used) return GT_OK;
+  void* Ke = nullptr;
+  GT_TRY(dalloc(ctx, (unsigned char**)&Ke, (int64_t)(sp->mesh->ncells * ke_per_cell(sp) * sizeof(float))));
+  int s = compute_elements(sp, form, in.coef.p, nu, GT_FP32, nullptr, nullptr, Ke, nullptr, 1);
+  if (s == GT_OK) s = alloc_values(A);
+  if (s == GT_OK) s = scatter_matrix(A, Ke, GT_FP32, GT_FP32, nullptr, nullptr, nullptr);
+  pool_free(ctx, Ke);
+  return s;
+}
+
+// element matrices + scatter on the existing pattern (and optionally b).  A
+// GT_MIXED matrix takes two passes: FP64 integration into the FP64 values
+// (and b), then FP32 integration into the FP32 values
+static int numeric_in(Matrix* A, int form, NumIn& in, double nu, double* b_out, const HostCsr* hc = nullptr,
+                      cudaEvent_t pat_down = nullptr, bool* values_done = nullptr, EarlyElems* early = nullptr) {
+  if (A->precision != GT_MIXED) return numeric_pass(A, form, in, nu, b_out, hc, pat_down, values_done, early);
+  A->precision = GT_FP64;
+  int s = numeric_pass(A, form, in, nu, b_out, hc, pat_down, values_done, early);
+  A->precision = GT_FP32;
+  if (s == GT_OK) s = fp32_values_pass(A, form, in, nu);
+  A->precision = GT_MIXED;
+  if (s == GT_OK && hc && values_done && *values_done && hc->v32 && A->bs == 1 && A->bnnz > 0)
+    s = copy_out(ctx_of(A->space), hc->v32, A->val32, A->bnnz);
   return s;
 }
 

@@ -326,6 +326,8 @@ int gt_ctx_create(int device, gt_ctx** out) {
   c->overlap = !(ov && strcmp(ov, "0") == 0);
   const char* pt = getenv("GTGPU_PATTERN");
   c->pattern_rows = !(pt && strcmp(pt, "warps") == 0);
+  const char* un = getenv("GTGPU_UNIFORM");
+  c->uniform_geom = !(un && strcmp(un, "0") == 0);
   const char* ln = getenv("GTGPU_SPMV_LANES");
   const int lanes = ln ? atoi(ln) : 0;
   c->spmv_lanes = (lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8) ? lanes : 0;

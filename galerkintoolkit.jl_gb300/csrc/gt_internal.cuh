@@ -100,6 +100,10 @@ struct Ctx {
   // sparsity count pass with one thread per row where rows are short
   // (GTGPU_PATTERN=warps at context creation: one warp per row always)
   bool pattern_rows = true;
+  // affine QUAD4/HEX8 meshes whose cells all share one geometry record (to
+  // 1e-13 relative) scatter scale_c x one reference element block
+  // (GTGPU_UNIFORM=0 at context creation: always the per-cell records)
+  bool uniform_geom = true;
   // lanes per row of the CSR row kernels: 0 = from the mean row length,
   // else 1, 2, 4 or 8 (GTGPU_SPMV_LANES at context creation)
   int spmv_lanes = 0;

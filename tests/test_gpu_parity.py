@@ -104,8 +104,10 @@ def test_fp32_and_mixed_values(case):
     assert np.abs(v32 - ov).max() <= TOL32 * scale
     Am = GT.assemble_matrix(a, "mixed", V, V)
     _, _, v64 = Am.csr()
+    # mixed: FP64-integrated FP64 values, FP32-integrated FP32 values (the
+    # same FP32 pass as the FP32 assembly)
     assert np.abs(v64 - ov).max() <= TOL64 * scale
-    assert np.array_equal(Am.values32(), v64.astype(np.float32))
+    assert np.array_equal(Am.values32(), v32)
 
 
 @pytest.mark.parametrize("case", CASES, ids=[c[0] for c in CASES])
@@ -274,3 +276,77 @@ def test_pattern_rows_beyond_the_thread_pass(dirichlet):
     orp, oci, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
     assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
     assert np.abs(v - ov).max() <= TOL64 * np.abs(ov).max()
+
+
+def _graded(cells, order, ncomp, groups, form, sig):
+    """A Cartesian mesh with x -> x^2 (and y -> y^1.5): every cell stays an
+    axis-aligned box (affine), but cell sizes differ, so the sum-factorised
+    path uses per-cell geometry records instead of one shared record."""
+    D = len(cells)
+    m = GT.cartesian_mesh(tuple(x for _ in cells for x in (0.0, 1.0)), cells)
+    m.coords[:, 0] = m.coords[:, 0] ** 2
+    m.coords[:, 1] = m.coords[:, 1] ** 1.5
+    coef = GT.lognormal_cells(m.num_cells, sig, 11) if sig else None
+    diri = None if groups is None else GT.boundary(m, None if groups == "boundary" else groups)
+    V = GT.lagrange_space(GT.interior(m), order, tensor_size=(ncomp,) if ncomp > 1 else None, dirichlet_boundary=diri)
+    ref, om = _oracle_space(m, order, ncomp, groups)
+    a = _KIND[form](coef) if form != O.ELASTICITY else GT.elasticity(coef, 0.3)
+    return m, V, ref, a, coef
+
+
+GRADED = [((5, 4), 2, 1, "boundary", O.LAPLACE, 1.0), ((3, 4, 3), 2, 3, ["2-face-5"], O.ELASTICITY, 0.5),
+          ((4, 3, 3), 1, 1, "boundary", O.MASS, 0.5), ((4, 5), 1, 2, ["1-face-3"], O.ELASTICITY, 0.0)]
+
+
+@pytest.mark.parametrize("case", GRADED, ids=lambda c: f"{len(c[0])}d_q{c[1]}_bs{c[2]}_f{c[4]}")
+def test_graded_affine_mesh(case):
+    """affine, non-uniform cells: FP64, FP32 and mixed values and the load
+    vector against the oracle"""
+    cells, order, ncomp, groups, form, sig = case
+    m, V, ref, a, coef = _graded(cells, order, ncomp, groups, form, sig)
+    assert np.array_equal(V.face_dofs(), ref["cell_dofs"])
+    cp, rv, nz = O.assemble_matrix(ref, form, 2 * order, coef=coef, nu=0.3)
+    orp, oci, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
+    f = np.array([0.0, 0.0, -1.0])[-ncomp:] if ncomp > 1 else 1.0
+    A, b = GT.assemble_matrix_and_vector(a, GT.source(f, coef), np.float64, V)
+    rp, ci, v = A.csr()
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    scale = np.abs(ov).max()
+    assert np.abs(v - ov).max() <= TOL64 * scale
+    ob = O.assemble_vector(ref, 2 * order, f, coef=coef)
+    assert np.abs(b - ob).max() <= TOL64 * np.abs(ob).max()
+    v32 = GT.assemble_matrix(a, np.float32, V).values32()
+    assert np.abs(v32 - ov).max() <= TOL32 * scale
+    Am = GT.assemble_matrix(a, "mixed", V)
+    assert np.abs(Am.csr()[2] - ov).max() <= TOL64 * scale
+    assert np.array_equal(Am.values32(), v32)
+
+
+_AFFINE = [c for c in CASES if c[7] == 0.0 and not c[2] and c[1] != (1, 1)]
+
+
+@pytest.mark.parametrize("case", _AFFINE, ids=[c[0] for c in _AFFINE])
+def test_uniform_geometry_path_matches_per_cell_records(case, monkeypatch):
+    """Uniform Cartesian meshes take the shared-record path (one reference
+    block scaled per cell); a context created with GTGPU_UNIFORM=0 takes the
+    per-cell records.  Both agree with each other and with the oracle."""
+    m, V, ref, a, coef, form, order = _build(case)
+    A = GT.assemble_matrix(a, np.float64, V, V)
+    monkeypatch.setenv("GTGPU_UNIFORM", "0")
+    ctx2 = GT.Context(0)
+    monkeypatch.delenv("GTGPU_UNIFORM")
+    V2 = GT.lagrange_space(GT.interior(m), order, tensor_size=(V.ncomp,) if V.ncomp > 1 else None,
+                           dirichlet_boundary=None if case[5] is None else
+                           GT.boundary(m, None if case[5] == "boundary" else case[5]), ctx=ctx2)
+    B = GT.assemble_matrix(a, np.float64, V2, V2)
+    _, _, va = A.csr()
+    _, _, vb = B.csr()
+    cp, rv, nz = O.assemble_matrix(ref, form, 2 * order, coef=coef, nu=0.3)
+    _, _, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
+    if ov.size:
+        scale = np.abs(ov).max()
+        assert np.abs(va - ov).max() <= TOL64 * scale and np.abs(vb - ov).max() <= TOL64 * scale
+        assert np.abs(va - vb).max() <= 1e-13 * scale
+    del B, V2
+    m._device.pop(id(ctx2), None)
+    ctx2.close()
