@@ -124,100 +124,92 @@ def run_elasticity(args):
 def run_batched(args):
     """512 independent Poisson instances (dim 2|3, order 1|2, cells
     log-uniform 16^2..96^3, kappa lognormal(0,0.5), Dirichlet boundary),
-    solved to 1e-8: batched mixed path (HBM-budgeted waves; each wave
-    assembled in mixed precision, then solved as one batch: FP32 PCG with FP64
-    reliable updates, instances up to 32768 rows one per CTA in one
-    persistent launch) against the plain FP64 path (one instance at a time,
-    FP64 assembly and FP64 PCG).  The lanes autotuner runs once before the
-    timed region (its choice is cached by batch shape).  The host inputs
-    (meshes and seeded coefficients) are generated before the timed region;
-    both paths time the upload, the space, the assembly and the solve of
-    every instance."""
+    each assembled and solved to a 1e-10 relative residual (the tolerance at
+    which the solutions stay within 1e-8 of the oracle's).  Three arms time
+    the upload, DOF numbering, assembly and solve of every instance (the host
+    meshes and seeded coefficients are generated before the timed region):
+      mixed_batched  gtgpu.batch.run_batch, mixed precision (FP32-integrated
+                     FP32 values + FP64 values; FP32 CG with FP64 reliable
+                     updates): worker contexts assembling concurrently, large
+                     instances solved on the workers' streams, the small ones
+                     in one persistent launch
+      fp64_batched   the same runner in plain FP64
+      plain_fp64     one instance at a time on one context, FP64 assembly and
+                     FP64 CG
+    The worker count and the small tier's SpMV lanes come from
+    autotune_batch (untimed, cached).  Solutions of a seeded sample of the
+    instances are compared with the oracle's FP64 solve."""
     import gtgpu as GT
     from gtgpu import batch as GB
+    rtol = 1e-10
     specs = GB.batch_workload(args.instances, seed=404)
     budget = args.budget_gb * 1e9
     ctx = GT.default_context()
-    # waves: largest first, greedy under the budget
-    order = sorted(specs, key=lambda s: -GB.estimate_bytes(s))
-    waves, cur, used = [], [], 0
-    for s in order:
-        e = GB.estimate_bytes(s)
-        if cur and used + e > budget:
-            waves.append(cur)
-            cur, used = [], 0
-        cur.append(s)
-        used += e
-    if cur:
-        waves.append(cur)
-    # autotune the per-CTA SpMV lanes on the smallest wave (untimed, cached)
-    inst = [GB.assemble_instance(s, seed=404, T="mixed", ctx=ctx) for s in waves[-1]]
-    B = GB.Batch([A for _, _, A, _ in inst])
-    tune = GB.autotune_lanes(B, np.concatenate([bb for _, _, _, bb in inst]), iters=32)
-    del B, inst
-    ctx.trim()
     host = {s.index: GB.instance_inputs(s, seed=404) for s in specs}  # untimed: the inputs
-
-    def release(s):  # the mesh's device copy goes with its instance
-        host[s.index][0]._device.clear()
-
-    ctx.synchronize()
-    t_all = time.perf_counter()
-    iters, fp64_its, worst = [], [], 0.0
-    t_asm = t_solve = t_small = t_large = 0.0
-    for w in waves:
-        t0 = time.perf_counter()
-        inst = [GB.assemble_instance(s, seed=404, T="mixed", ctx=ctx, inputs=host[s.index]) for s in w]
-        B = GB.Batch([A for _, _, A, _ in inst])
-        b = np.concatenate([bb for _, _, _, bb in inst])
-        t1 = time.perf_counter()
-        B.set_lanes(tune["lanes"])
-        ctx.profile_begin()
-        x, infos = B.solve(b, rtol=1e-8, maxit=100000, mode="ir", raise_on_fail=False)
-        ph = dict(ctx.profile_end())
-        t_small += ph.get("batch_small", 0.0) * 1e-3
-        t_large += ph.get("batch_large", 0.0) * 1e-3
-        t_asm += t1 - t0
-        t_solve += time.perf_counter() - t1
-        iters += [i["iterations"] for i in infos]
-        fp64_its += [i["fp64_iterations"] for i in infos]
-        worst = max(worst, max(i["rel_residual"] for i in infos))
-        del B, inst
-        for s in w:
-            release(s)
+    tune = GB.autotune_batch(specs, host, "mixed", rtol=rtol)
+    ctx.trim()
+    runs = {}
+    for name, prec in (("mixed_batched", "mixed"), ("fp64_batched", "fp64")):
+        r = GB.run_batch(specs, host, prec, rtol=rtol, workers=tune["workers"], lanes=tune["lanes"],
+                         budget_bytes=budget)
+        its = [i["iterations"] for i in r.infos.values()]
+        runs[name] = {"solves_per_s": len(specs) / r.seconds, "seconds": r.seconds, "waves": r.waves,
+                      "small_tier": r.small, "large_tier": r.large,
+                      "worst_rel_residual": max(i["rel_residual"] for i in r.infos.values()),
+                      "iterations_sum": int(sum(its)),
+                      "fp64_iterations_sum": int(sum(i.get("fp64_iterations", 0) for i in r.infos.values())),
+                      "instances_handed_to_fp64": int(sum(1 for i in r.infos.values()
+                                                          if prec == "mixed" and i.get("fp64_iterations", 0) > 0))}
+        runs[name]["_sol"] = r.solutions
         ctx.trim()
-    ctx.synchronize()
-    t_batched = time.perf_counter() - t_all
     # plain FP64 path, one instance at a time
     t0 = time.perf_counter()
-    worst64 = 0.0
-    p_asm = p_solve = 0.0
-    its64 = []
+    worst64, its64, plain_sol = 0.0, [], {}
     for s in specs:
-        ta = time.perf_counter()
         m, V, A, b = GB.assemble_instance(s, seed=404, T=np.float64, ctx=ctx, inputs=host[s.index])
-        tb = time.perf_counter()
-        x, info = GT.solve(A, b, rtol=1e-8, maxit=100000, mode="fp64", raise_on_fail=False)
-        p_asm += tb - ta
-        p_solve += time.perf_counter() - tb
+        x, info = GT.solve(A, b, rtol=rtol, maxit=100000, mode="fp64", raise_on_fail=False)
         its64.append(info["iterations"])
         worst64 = max(worst64, info["rel_residual"])
+        plain_sol[s.index] = x
         del A, V
-        release(s)
+        host[s.index][0]._device.clear()
         if ctx.memory()[1] > 20e9:
             ctx.trim()
     t_plain = time.perf_counter() - t0
-    out = {"metric": "batched solves/s (assemble + solve to 1e-8), mixed batched vs plain FP64", "n_gpus": 1,
+    runs["plain_fp64"] = {"solves_per_s": len(specs) / t_plain, "seconds": t_plain, "worst_rel_residual": worst64,
+                          "iterations_sum": int(sum(its64)), "_sol": plain_sol}
+    # oracle check on a seeded sample (instances the oracle solves in seconds)
+    O = _oracle()
+    rows = {s.index: (s.order * s.cells_per_dir - 1) ** s.dim for s in specs}
+    cand = [s for s in specs if rows[s.index] <= 40000]
+    pick = np.linspace(0, len(cand) - 1, min(24, len(cand))).round().astype(int)
+    errs = {k: 0.0 for k in runs}
+    for i in sorted(set(pick.tolist())):
+        s = cand[i]
+        m, kappa = host[s.index]
+        om = dict(D=m.D, ctype=m.cell_type, coords=m.coords, cell_nodes=m.cell_nodes, pf0=m.corners)
+        if m.D == 2:
+            om["pf1"], om["pf1g"] = m.bfaces, m.bface_group
+        else:
+            om["pf1"], om["pf2"], om["pf2g"] = m.bedges, m.bfaces, m.bface_group
+        ref = O.lagrange_space(om, s.order, dirichlet="boundary")
+        cp, rv, nz = O.assemble_matrix(ref, O.LAPLACE, 2 * s.order, coef=kappa)
+        orp, oci, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
+        xo, _, _ = O.pcg(orp, oci, ov, O.assemble_vector(ref, 2 * s.order, 1.0), rtol=1e-13, maxit=200000)
+        for k in runs:
+            errs[k] = max(errs[k], _relerr(runs[k]["_sol"][s.index], xo))
+    for k in runs:
+        del runs[k]["_sol"]
+    out = {"metric": "batched solves/s (assemble + solve to 1e-10), mixed batched vs plain FP64", "n_gpus": 1,
            "config": {"workload": f"{args.instances} Poisson instances, dim 2|3, Q1|Q2, cells log-uniform 16^2..96^3",
-                      "waves": len(waves), "budget_gb": args.budget_gb, "lanes": tune["lanes"]},
-           "batched": {"solves_per_s": len(specs) / t_batched, "seconds": t_batched, "assemble_s": t_asm,
-                       "solve_s": t_solve, "solve_small_tier_s": t_small, "solve_large_tier_s": t_large,
-                       "worst_rel_residual": worst, "iterations_max": int(max(iters)),
-                       "iterations_sum": int(sum(iters)), "fp64_iterations_sum": int(sum(fp64_its)),
-                       "instances_handed_to_fp64": int(sum(1 for v in fp64_its if v > 0))},
-           "plain_fp64": {"solves_per_s": len(specs) / t_plain, "seconds": t_plain, "assemble_s": p_asm,
-                          "solve_s": p_solve, "worst_rel_residual": worst64, "iterations_sum": int(sum(its64))},
-           "speedup": t_plain / t_batched, "data": "synthetic (seeded)"}
+                      "budget_gb": args.budget_gb, "rtol": rtol, "tuning": tune},
+           **runs,
+           "speedup_vs_plain_fp64": runs["plain_fp64"]["seconds"] / runs["mixed_batched"]["seconds"],
+           "speedup_vs_fp64_batched": runs["fp64_batched"]["seconds"] / runs["mixed_batched"]["seconds"],
+           "oracle_check": {"instances": int(len(set(pick.tolist()))), "max_rel_err": errs,
+                            "reference": "oracle assembly + oracle FP64 PCG to 1e-13",
+                            "error_scale": "max |gpu - oracle| / max |oracle|"},
+           "data": "synthetic (seeded)"}
     print(json.dumps(out), flush=True)
 
 

@@ -2115,94 +2115,131 @@ __global__ void k_scatter_kron(const int64_t* __restrict__ rowptr, const int32_t
 
 // Uniform geometry: every cell has the reference record (cell 0's), so an
 // element block is scale_c x Kref[a][b] with Kref the unit-scale block of
-// the reference record, computed once per CTA into shared memory by
-// kron_block (FP64 for FP64 values, FP32 for FP32 values) and scale_c =
-// |det J| coef_c -- the per-(row, cell, column node) work is BS*BS
-// multiply-adds instead of a kron_block.  Otherwise as k_scatter_kron (row
-// owner, incidences in ascending cell order, load vector and Dirichlet lift
-// in the same pass).
-template <int D, int ORDER, int BS, int FORM, int G, class T>
-__global__ void k_scatter_uniform(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
-                                  const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
-                                  const int32_t* __restrict__ cnd, int64_t nrows, int lmax,
-                                  const double* __restrict__ gref, const double* __restrict__ coef, T lamf, T muf,
-                                  double* __restrict__ v64, float* __restrict__ v32, const double* __restrict__ be,
-                                  double* __restrict__ bvec, const double* __restrict__ xd) {
+// the reference record and scale_c = |det J| coef_c.  k_kref computes Kref
+// once (kron_block: FP64 for FP64 values, FP32 for FP32 values) into global
+// memory; k_scatter_uniform is persistent: each CTA copies Kref into shared
+// memory once and then loops over row groups, so the per-(row, cell, column
+// node) work is BS*BS multiply-adds instead of a kron_block.  Otherwise as
+// k_scatter_kron (row owner, incidences in ascending cell order, load vector
+// and Dirichlet lift in the same pass).
+template <int D, int ORDER, int BS, int FORM, class T>
+__global__ void k_kref(const double* __restrict__ gref, T lamf, T muf, T* __restrict__ kref) {
   constexpr int M1 = ORDER + 1;
   constexpr int NN = D == 2 ? M1 * M1 : M1 * M1 * M1;
-  constexpr int RPW = 32 / G;
-  constexpr int KB = BS * BS;
-  constexpr size_t KREF_BYTES = ((size_t)NN * NN * KB * sizeof(T) + 15) & ~size_t(15);
-  extern __shared__ __align__(16) unsigned char s_raw[];
   __shared__ T s_M[9], s_D[9], s_K[9];
-  T* s_ref = (T*)s_raw;
   if (threadIdx.x == 0) {
     double M[9], Dm[9], Kd[9], m1[3];
     lagrange_table_1d(ORDER, M, Dm, Kd, m1);
     for (int i = 0; i < 9; i++) { s_M[i] = (T)M[i]; s_D[i] = (T)Dm[i]; s_K[i] = (T)Kd[i]; }
   }
   __syncthreads();
-  {
-    T g[GSTRIDE];
+  const int ab = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ab >= NN * NN) return;
+  T g[GSTRIDE];
 #pragma unroll
-    for (int i = 0; i < GSTRIDE - 1; i++) g[i] = (T)__ldg(gref + i);
-    g[GSTRIDE - 1] = (T)1;
-    for (int ab = threadIdx.x; ab < NN * NN; ab += blockDim.x) {
-      const int a = ab / NN, b = ab - (ab / NN) * NN;
-      int na[3] = {a % M1, (a / M1) % M1, a / (M1 * M1)};
-      int nb[3] = {b % M1, (b / M1) % M1, b / (M1 * M1)};
-      T blk[BS][BS];
-      kron_block<D, BS, FORM, T>(na, nb, g, s_M, s_D, s_K, lamf, muf, blk);
+  for (int i = 0; i < GSTRIDE - 1; i++) g[i] = (T)gref[i];
+  g[GSTRIDE - 1] = (T)1;
+  const int a = ab / NN, b = ab - (ab / NN) * NN;
+  int na[3] = {a % M1, (a / M1) % M1, a / (M1 * M1)};
+  int nb[3] = {b % M1, (b / M1) % M1, b / (M1 * M1)};
+  T blk[BS][BS];
+  kron_block<D, BS, FORM, T>(na, nb, g, s_M, s_D, s_K, lamf, muf, blk);
 #pragma unroll
-      for (int cc = 0; cc < BS; cc++)
+  for (int cc = 0; cc < BS; cc++)
 #pragma unroll
-        for (int dd = 0; dd < BS; dd++) s_ref[(size_t)ab * KB + cc * BS + dd] = blk[cc][dd];
-    }
-  }
+    for (int dd = 0; dd < BS; dd++) kref[(size_t)ab * BS * BS + cc * BS + dd] = blk[cc][dd];
+}
+
+template <int D, int ORDER, int BS, int G, class T>
+__global__ void k_scatter_uniform(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
+                                  const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
+                                  const int32_t* __restrict__ cnd, int64_t nrows, int lmax,
+                                  const T* __restrict__ kref, const double* __restrict__ gref,
+                                  const double* __restrict__ coef, double* __restrict__ v64, float* __restrict__ v32,
+                                  const double* __restrict__ be, double* __restrict__ bvec,
+                                  const double* __restrict__ xd) {
+  constexpr int M1 = ORDER + 1;
+  constexpr int NN = D == 2 ? M1 * M1 : M1 * M1 * M1;
+  constexpr int RPW = 32 / G;
+  constexpr int KB = BS * BS;
+  constexpr int KREF_N = NN * NN * KB;
+  constexpr size_t KREF_BYTES = ((size_t)KREF_N * sizeof(T) + 15) & ~size_t(15);
+  constexpr int PF = G < 8 ? G : 8;  // incidences fetched ahead per row
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  T* s_ref = (T*)s_raw;
+  for (int i = threadIdx.x; i < KREF_N; i += blockDim.x) s_ref[i] = __ldg(kref + i);
   __syncthreads();
   const double adet = __ldg(gref + GSTRIDE - 1);
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  int sub = lane / G, gl = lane - sub * G;
-  int slot = w * RPW + sub;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int sub = lane / G, gl = lane - sub * G;
+  const int slot = w * RPW + sub;
   T* acc = (T*)(s_raw + KREF_BYTES) + (size_t)slot * lmax * KB;
   int32_t* cols = (int32_t*)((T*)(s_raw + KREF_BYTES) + (size_t)(blockDim.x / G) * lmax * KB) + (size_t)slot * lmax;
-  int64_t r = ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * RPW + sub;
-  bool active = r < nrows;
-  unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
-  int64_t rb = 0;
-  int L = 0;
-  if (active) {
-    rb = rowptr[r];
-    L = (int)(rowptr[r + 1] - rb);
+  const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
+  const bool vec = be != nullptr && gl == 0;
+  const bool lift = be != nullptr && xd != nullptr;
+  const int b = gl;
+  const int64_t nblk = (nrows + (int64_t)nw * RPW - 1) / ((int64_t)nw * RPW);
+  for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
+    const int64_t r = (blk * nw + w) * RPW + sub;
+    if (r >= nrows) continue;  // the group's lanes all skip together
+    const int64_t rb = rowptr[r];
+    const int L = (int)(rowptr[r + 1] - rb);
     for (int i = gl; i < L; i += G) cols[i] = colind[rb + i];
     for (int i = gl; i < L * KB; i += G) acc[i] = (T)0;
-  }
-  __syncwarp(gmask);
-  if (active) {
-    const int b = gl;
-    const bool vec = be != nullptr && gl == 0;
-    const bool lift = be != nullptr && xd != nullptr;
+    __syncwarp(gmask);
     double bsum[BS];
-    int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+    const int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
     if (be != nullptr) {
       row_load_sum<BS>(ib, ie, inc, NN, be, gl, gmask, bsum);
     } else {
 #pragma unroll
       for (int cc = 0; cc < BS; cc++) bsum[cc] = 0.0;
     }
-    for (int64_t k = ib; k < ie; k++) {
-      int32_t cb = __ldg(inc + k);
-      int32_t c = cb / NN, a = cb - c * NN;
+    // the row's first PF incidences (at most 2^D on a structured mesh) are
+    // fetched up front: their cells, each lane's column DOF and the cells'
+    // scales are loads in flight together, and the column positions are
+    // independent searches, so the summation loop below waits on no global
+    // load; later incidences (a node in more than PF cells) load in the loop
+    const int nin = (int)(ie - ib);
+    const int32_t my_cb = gl < nin ? __ldg(inc + ib + gl) : 0;
+    int32_t cbk[PF], jk[PF], pk[PF];
+    T sck[PF];
+#pragma unroll
+    for (int k = 0; k < PF; k++) {
+      cbk[k] = __shfl_sync(gmask, my_cb, k, G);
+      const int32_t c = cbk[k] / NN;
+      jk[k] = (k < nin && b < NN) ? __ldg(cnd + (int64_t)c * NN + b) : 0;
+      sck[k] = (T)(adet * ((coef && k < nin) ? __ldg(coef + c) : 1.0));
+    }
+#pragma unroll
+    for (int k = 0; k < PF; k++) pk[k] = jk[k] > 0 ? find_col(cols, L, jk[k] - 1) : -1;
+    for (int k = 0; k < nin; k++) {
+      int32_t cb, j, p;
+      T sc;
+      if (k < PF) {
+        cb = cbk[0];
+        j = jk[0];
+        p = pk[0];
+        sc = sck[0];
+#pragma unroll
+        for (int u = 1; u < PF; u++)
+          if (k == u) { cb = cbk[u]; j = jk[u]; p = pk[u]; sc = sck[u]; }
+      } else {
+        cb = __ldg(inc + ib + k);
+        const int32_t c = cb / NN;
+        j = b < NN ? __ldg(cnd + (int64_t)c * NN + b) : 0;
+        p = j > 0 ? find_col(cols, L, j - 1) : -1;
+        sc = (T)(adet * (coef ? __ldg(coef + c) : 1.0));
+      }
+      const int32_t a = cb - (cb / NN) * NN;
       double lv[BS];
 #pragma unroll
       for (int cc = 0; cc < BS; cc++) lv[cc] = 0.0;
       if (b < NN) {
-        int32_t j = __ldg(cnd + (int64_t)c * NN + b);
         if (j > 0 || (j < 0 && lift)) {
-          const T sc = (T)(adet * (coef ? __ldg(coef + c) : 1.0));
           const T* kr = s_ref + (size_t)(a * NN + b) * KB;
           if (j > 0) {
-            int p = find_col(cols, L, j - 1);
 #pragma unroll
             for (int e = 0; e < KB; e++) acc[p * KB + e] += sc * kr[e];
           } else {
@@ -2223,20 +2260,22 @@ __global__ void k_scatter_uniform(const int64_t* __restrict__ rowptr, const int3
         }
       __syncwarp(gmask);
     }
-    int64_t ob = rb * KB;
+    const int64_t ob = rb * KB;
     for (int i = gl; i < L * KB; i += G) {
-      T v = acc[i];
+      const T v = acc[i];
       if (v64) v64[ob + i] = (double)v;
       if (v32) v32[ob + i] = (float)v;
     }
     if (vec)
 #pragma unroll
       for (int cc = 0; cc < BS; cc++) bvec[r * BS + cc] = bsum[cc];
+    __syncwarp(gmask);  // the row slot is reused by the group's next row
   }
 }
 
-// launches k_scatter_uniform; GT_ERR_UNSUPPORTED (nothing launched) when
-// the reference block and the row slots do not fit in shared memory
+// launches k_kref + k_scatter_uniform; GT_ERR_UNSUPPORTED (nothing
+// launched) when the reference block and the row slots do not fit in
+// shared memory
 template <int D, int ORDER, int BS, int FORM, class T>
 static int launch_uniform(Matrix* A, const double* gref, const double* coef, double nu, const double* be,
                           double* bvec, const double* xd) {
@@ -2246,25 +2285,38 @@ static int launch_uniform(Matrix* A, const double* gref, const double* coef, dou
   constexpr int NN = D == 2 ? M1 * M1 : M1 * M1 * M1;
   constexpr int G = NN <= 4 ? 4 : (NN <= 8 ? 8 : (NN <= 16 ? 16 : 32));
   constexpr int RPW = 32 / G;
-  constexpr size_t KREF_BYTES = ((size_t)NN * NN * BS * BS * sizeof(T) + 15) & ~size_t(15);
+  constexpr int KREF_N = NN * NN * BS * BS;
+  constexpr size_t KREF_BYTES = ((size_t)KREF_N * sizeof(T) + 15) & ~size_t(15);
   int lmax = A->max_row > 0 ? A->max_row : 1;
   double* v64 = A->precision != GT_FP32 ? A->val64 : nullptr;
   float* v32 = A->precision != GT_FP64 ? A->val32 : nullptr;
-  int warps = 4;
+  // up to 16 warps per CTA where the row slots fit beside the reference
+  // block (the loop is latency-bound: warps per SM decide its rate)
+  int warps = 16;
   size_t per_row = (size_t)lmax * (BS * BS * sizeof(T) + sizeof(int32_t));
-  while (warps > 1 && KREF_BYTES + (size_t)warps * RPW * per_row > 112 * 1024) warps >>= 1;
+  while (warps > 1 && KREF_BYTES + (size_t)warps * RPW * per_row > 210 * 1024) warps >>= 1;
   size_t smem = KREF_BYTES + (size_t)warps * RPW * per_row;
-  if (smem > 200 * 1024) return GT_ERR_UNSUPPORTED;
-  auto kern = k_scatter_uniform<D, ORDER, BS, FORM, G, T>;
+  if (smem > 210 * 1024) return GT_ERR_UNSUPPORTED;
+  auto kern = k_scatter_uniform<D, ORDER, BS, G, T>;
   GT_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  GT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));
+  if (per_sm < 1) return GT_ERR_UNSUPPORTED;
+  T* kref = nullptr;
+  GT_TRY(dalloc(ctx, &kref, KREF_N));
   matrix_values_changed(A);
-  int64_t rows_per_block = (int64_t)warps * RPW;
-  int64_t grid = (A->nbrows + rows_per_block - 1) / rows_per_block;
   T lamf = (T)(nu / ((1.0 + nu) * (1.0 - 2.0 * nu))), muf = (T)(1.0 / (2.0 * (1.0 + nu)));
-  kern<<<GT_KC(ctx, (unsigned)(grid > 0 ? grid : 1)), warps * 32, smem, ctx->stream>>>(
-      A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs, A->nbrows, lmax, gref, coef, lamf, muf, v64, v32, be,
-      bvec, xd);
-  GT_LAUNCH(ctx, "k_scatter_uniform");
+  k_kref<D, ORDER, BS, FORM, T><<<GT_KC(ctx, (NN * NN + 127) / 128), 128, 0, ctx->stream>>>(gref, lamf, muf, kref);
+  GT_LAUNCH(ctx, "k_kref");
+  const int64_t rows_per_block = (int64_t)warps * RPW;
+  const int64_t nblk = (A->nbrows + rows_per_block - 1) / rows_per_block;
+  const int64_t cap = (int64_t)per_sm * ctx->num_sms;
+  const int grid = (int)std::max<int64_t>(1, std::min(nblk, cap));
+  kern<<<GT_KC(ctx, grid), warps * 32, smem, ctx->stream>>>(A->rowptr, A->colind, A->inc_ptr, A->inc, sp->cell_ndofs,
+                                                             A->nbrows, lmax, kref, gref, coef, v64, v32, be, bvec, xd);
+  cudaError_t e = cudaGetLastError();
+  dfree(ctx, kref);  // stream-ordered: the pool hands the block out again only to later work
+  if (e != cudaSuccess) return check_cuda(ctx, e, "k_scatter_uniform");
   return GT_OK;
 }
 

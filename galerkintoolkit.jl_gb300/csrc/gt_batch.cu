@@ -95,7 +95,7 @@ template <int G, class V, class X, bool REL>
 __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, const int32_t* __restrict__ queue,
                                              int nq, int32_t* head, const double* __restrict__ b, double* x, X* xs,
                                              X* r, X* z, X* p, X* q, X* dinv, BRes* res, double rtol2, double delta2,
-                                             int maxit, int from_x) {
+                                             int maxit, int from_x, double stall_ratio, int stall_count) {
   __shared__ double s_red[2][3 * BNW];
   __shared__ int s_k;
   constexpr int NG = BT / G;
@@ -242,8 +242,8 @@ __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, co
           nupd++;
           done = rr <= tol2 || iters >= maxit || !(rr == rr);
           if (sizeof(X) < sizeof(double) && !done) {
-            stall = rr > 0.25 * prev ? stall + 1 : 0;
-            if (stall >= 3 || slow) {
+            stall = rr > stall_ratio * prev ? stall + 1 : 0;
+            if (stall >= stall_count || slow) {
               done = true;
               status = 2;
             }
@@ -311,7 +311,8 @@ static int launch_small_g(gt_batch* B, int G, const std::vector<int>& ids, const
     int64_t cap = (int64_t)std::max(per_sm, 1) * ctx->num_sms;
     int grid = (int)std::min<int64_t>(cap, (int64_t)ids.size());
     kern<<<GT_KC(ctx, grid), BT, 0, s>>>(B->d_inst, queue, (int)ids.size(), head, b, x, xs, r, z, p, q, dinv, res,
-                                         rtol * rtol, delta * delta, maxit, from_x);
+                                         rtol * rtol, delta * delta, maxit, from_x, ctx->ir_stall_ratio,
+                                         ctx->ir_stall_count);
     GT_LAUNCH(ctx, "k_bpcg");
     return GT_OK;
   };
@@ -381,7 +382,7 @@ static int batch_solve(gt_batch* B, const double* b, double* x, double rtol, int
   } else if (mode == GT_SOLVE_FP32) {
     GT_TRY((launch_small<float, float, false>(B, B->small, b, x, rtol, maxit, 0.0, 0, hres)));
   } else {
-    GT_TRY((launch_small<float, float, true>(B, B->small, b, x, rtol, maxit, 0.1, 0, hres)));
+    GT_TRY((launch_small<float, float, true>(B, B->small, b, x, rtol, maxit, ctx->ir_delta, 0, hres)));
     std::vector<int> stalled;
     for (int i : B->small)
       if (hres[i].status == 2) stalled.push_back(i);
@@ -412,6 +413,9 @@ static int batch_solve(gt_batch* B, const double* b, double* x, double rtol, int
     Matrix* A = B->mats[i];
     const int64_t off = B->h_inst[i].off;
     GT_CUDA(ctx, cudaMemsetAsync(x + off, 0, sizeof(double) * A->nbrows, ctx->stream));
+    // a matrix of another context solves on that context's stream: b and x
+    // (written on this one) are complete first; solve() returns synchronised
+    if (A->ctx != ctx) GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     int s = solve(A, b + off, x + off, rtol, maxit, mode, &info[i]);
     if (s != GT_OK && s != GT_ERR_NOT_CONVERGED) return s;
     if (s == GT_ERR_NOT_CONVERGED) status = s;
@@ -439,11 +443,15 @@ int gt_batch_create(gt_ctx* ctx, int n, gt_matrix* const* mats, gt_batch** out) 
   int64_t off = 0;
   for (int i = 0; i < n; i++) {
     Matrix* A = mats[i];
-    if (!A || A->ctx != ctx || A->bs != 1) {
+    if (!A || A->ctx->device != ctx->device || A->bs != 1) {
       delete B;
-      return set_error(ctx, GT_ERR_INVALID, "batch: matrices must be scalar (block size 1) and of this context");
+      return set_error(ctx, GT_ERR_INVALID, "batch: matrices must be scalar (block size 1) and on this context's device");
     }
     int s = find_diag(A);
+    // a matrix of another context (assembled on another stream): its
+    // diagonal positions are complete before this context's kernels read them
+    if (s == GT_OK && A->ctx != ctx && cudaStreamSynchronize(A->ctx->stream) != cudaSuccess)
+      s = set_error(ctx, GT_ERR_CUDA, "batch: synchronising a matrix's context failed");
     if (s != GT_OK) {
       delete B;
       return s;

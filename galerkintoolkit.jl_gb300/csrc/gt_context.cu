@@ -328,6 +328,20 @@ int gt_ctx_create(int device, gt_ctx** out) {
   c->pattern_rows = !(pt && strcmp(pt, "warps") == 0);
   const char* un = getenv("GTGPU_UNIFORM");
   c->uniform_geom = !(un && strcmp(un, "0") == 0);
+  const char* irs = getenv("GTGPU_IR_STALL");
+  if (irs) {
+    double ratio = 0.0;
+    int count = 0;
+    if (sscanf(irs, "%lf,%d", &ratio, &count) == 2 && ratio > 0.0 && ratio < 1.0 && count >= 1 && count <= 100) {
+      c->ir_stall_ratio = ratio;
+      c->ir_stall_count = count;
+    }
+  }
+  const char* ird = getenv("GTGPU_IR_DELTA");
+  if (ird) {
+    const double d = atof(ird);
+    if (d > 1e-6 && d < 1.0) c->ir_delta = d;
+  }
   const char* ln = getenv("GTGPU_SPMV_LANES");
   const int lanes = ln ? atoi(ln) : 0;
   c->spmv_lanes = (lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8) ? lanes : 0;

@@ -104,6 +104,18 @@ struct Ctx {
   // 1e-13 relative) scatter scale_c x one reference element block
   // (GTGPU_UNIFORM=0 at context creation: always the per-cell records)
   bool uniform_geom = true;
+  // mixed-precision hand-over: an FP32 cycle (between two reliable updates)
+  // whose FP64 true residual norm^2 did not fall below ir_stall_ratio x its
+  // value at the cycle start counts as stalled; ir_stall_count stalled cycles
+  // in a row continue the solve in FP64 (GTGPU_IR_STALL="ratio,count" at
+  // context creation)
+  double ir_stall_ratio = 0.25;
+  int ir_stall_count = 3;
+  // reliable update when the FP32 recurrence residual norm fell by this
+  // factor since the last one (GTGPU_IR_DELTA at context creation).  0.3
+  // measured: Q2 elasticity 64^3 5244 FP32 iterations (0.1: 7049), the P1
+  // Poisson 96^3 x 6 solve 2% slower (20 updates instead of 11)
+  double ir_delta = 0.3;
   // lanes per row of the CSR row kernels: 0 = from the mean row length,
   // else 1, 2, 4 or 8 (GTGPU_SPMV_LANES at context creation)
   int spmv_lanes = 0;

@@ -71,6 +71,8 @@ struct PArgs {
   PState* st;
   double rtol2, delta2;
   int maxit;
+  double stall_ratio;  // hand-over rule (Ctx::ir_stall_ratio / ir_stall_count)
+  int stall_count;
 };
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -375,8 +377,8 @@ __global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
         if (sizeof(X) < sizeof(double) && !S.done) {
           // the recurrence fell by delta but the true residual did not halve:
           // the FP32 operator no longer resolves the error (eps32 * cond ~ 1)
-          S.stall = s_tot[1] > 0.25 * prev ? S.stall + 1 : 0;
-          if (S.stall >= 3 || slow) S.done = 2;
+          S.stall = s_tot[1] > a.stall_ratio * prev ? S.stall + 1 : 0;
+          if (S.stall >= a.stall_count || slow) S.done = 2;
         }
         if (cyc > S.max_cyc) S.max_cyc = cyc;
         S.it_upd = S.iters;
@@ -489,6 +491,8 @@ int run_typed(Matrix* A, const V* val, const double* b, double* x, double rtol, 
   args.rtol2 = rtol * rtol;
   args.delta2 = delta * delta;
   args.maxit = maxit;
+  args.stall_ratio = ctx->ir_stall_ratio;
+  args.stall_count = ctx->ir_stall_count;
   PState h{};
   int status = GT_OK;
   int chunk = 32, done_iters = from ? from->st.iters : 0;
@@ -601,7 +605,7 @@ int pcg_persistent(Matrix* A, int mode, const double* b, double* x, double rtol,
     s = run_dispatch<double, double, true>(A, A->val64, b, x, rtol, maxit, 0.0, nullptr, &run);
     *iters64 = run.st.iters;
   } else if (mode == GT_SOLVE_IR) {
-    s = run_dispatch<float, float, true>(A, A->val32, b, x, rtol, maxit, 0.1, nullptr, &run);
+    s = run_dispatch<float, float, true>(A, A->val32, b, x, rtol, maxit, A->ctx->ir_delta, nullptr, &run);
     if (s == PCG_STALLED) {
       // the FP32 iteration stalled or lost its rate (eps32 * cond(A) too
       // large): the same Krylov iteration goes on in FP64 from the current

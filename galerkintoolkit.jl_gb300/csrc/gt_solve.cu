@@ -103,6 +103,8 @@ struct CGState {
   int32_t done;   // 1 converged or maxit, 2 FP32 iteration stalled or slowed down
   int32_t iters, maxit, upd, nupd;
   int32_t it_upd, max_cyc, stall, slow;  // reliable-update cycle bookkeeping
+  double stall_ratio;   // hand-over rule (Ctx::ir_stall_ratio / ir_stall_count)
+  int32_t stall_count, pad_;
 };
 
 // reduction scratch sized for the largest grid of a solve
@@ -1048,8 +1050,8 @@ __global__ void __launch_bounds__(RED_T) k_rl_resid(const int64_t* __restrict__ 
     if (sizeof(X) < sizeof(double) && !st->done && st->nupd > 1) {
       // the recurrence fell by delta but the true residual did not halve,
       // three times running, or the cycle slowed down: continue in FP64
-      st->stall = v[1] > 0.25 * prev ? st->stall + 1 : 0;
-      if (st->stall >= 3 || st->slow) st->done = 2;
+      st->stall = v[1] > st->stall_ratio * prev ? st->stall + 1 : 0;
+      if (st->stall >= st->stall_count || st->slow) st->done = 2;
     }
     const int cyc = st->iters - st->it_upd;
     if (st->nupd > 1 && cyc > st->max_cyc) st->max_cyc = cyc;
@@ -1065,7 +1067,10 @@ __global__ void k_copy_vec(const X* __restrict__ a, X* __restrict__ out, int64_t
   if (i < n) out[i] = a[i];
 }
 
-__global__ void k_rl_setup(CGState* st, const double* bb, double rtol2, double delta2, int maxit) {
+__global__ void k_rl_setup(CGState* st, const double* bb, double rtol2, double delta2, int maxit, double stall_ratio,
+                           int stall_count) {
+  st->stall_ratio = stall_ratio;
+  st->stall_count = stall_count;
   st->bb = *bb;
   st->tol2 = rtol2 * (*bb);
   st->delta2 = delta2;
@@ -1110,7 +1115,8 @@ static int pcg_reliable(Matrix* A, const V* val, const double* b, double* x, dou
   else k_dinv<3, double, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, A->val64, A->nbrows, dinv);
   GT_LAUNCH(ctx, "k_dinv");
   GT_TRY(norm2(ctx, b, n, bb, sc.rb));
-  k_rl_setup<<<GT_KC(ctx, 1), 1, 0, s>>>(st, bb, rtol * rtol, delta * delta, maxit);
+  k_rl_setup<<<GT_KC(ctx, 1), 1, 0, s>>>(st, bb, rtol * rtol, delta * delta, maxit, ctx->ir_stall_ratio,
+                                         ctx->ir_stall_count);
   auto resid = [&]() {
     Ops<double, double>::dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
@@ -1273,7 +1279,7 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
     // FP32 CG (FP32 values, vectors and inner sums) with an FP64 true
     // residual and solution update each time the residual fell tenfold
     int32_t it = 0, nupd = 0;
-    status = pcg_reliable<float, float>(A, A->val32, b, x, rtol, maxit, 0.1, &it, &nupd, &inf.rel_residual);
+    status = pcg_reliable<float, float>(A, A->val32, b, x, rtol, maxit, A->ctx->ir_delta, &it, &nupd, &inf.rel_residual);
     if (status == CG_STALLED) {
       // eps32 * cond(A) too large for the FP32 iteration: FP64 CG from the
       // current FP64 solution

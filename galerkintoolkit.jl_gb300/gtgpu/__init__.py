@@ -6,6 +6,6 @@ from .api import (Context, DiscreteField, Domain, Form, LinearProblem, Matrix, P
                   assemble_boundary_vector, assemble_matrix, assemble_matrix_and_vector, assemble_vector, boundary,
                   default_context, device_mesh, elasticity, h1_error, integrate, interior, interpolate_dirichlet,
                   l2_error, lagrange_space, laplacian, linear_problem, mass, num_dirichlet_dofs, num_free_dofs, solve,
-                  source, update_matrix, dirichlet_field, solution_field, solution_field_inplace,
+                  source, update_matrix, update_matrix_and_vector, dirichlet_field, solution_field, solution_field_inplace,
                   zero_dirichlet_field)
 from .mesh import Mesh, cartesian_mesh, jitter_interior_nodes, keyed_uniform, lognormal_cells  # noqa: F401

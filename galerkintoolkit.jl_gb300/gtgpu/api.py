@@ -7,6 +7,7 @@ Mirrors the problem-level entry points of GalerkinToolkit.jl v0.6.3:
   GT.assemble_matrix / update_matrix!  src/problems.jl:319-361
   GT.assemble_vector                   src/problems.jl:244-274
   GT.assemble_matrix_and_vector        src/problems.jl:391-414
+  GT.update_matrix_and_vector!         src/problems.jl:409-414
   GT.PartitionedSolvers_linear_problem src/problems.jl:439-462 (+ PS.solve)
 
 Weak forms are passed as explicit tags (``laplacian``, ``mass``,
@@ -403,6 +404,23 @@ def update_matrix(A: Matrix, a: Form | None = None):
     check(A.ctx.h, A.ctx.lib.gt_update_matrix(A.h, a.kind, _ptr(coef), a.nu))
     A.form = a
     return A
+
+
+def update_matrix_and_vector(A: Matrix, a: Form, l: Source, out=None):
+    """GT.update_matrix_and_vector! (src/problems.jl:409-414): new matrix
+    values and load vector on A's sparsity, bitwise what a fresh
+    assemble_matrix_and_vector of the same forms gives."""
+    _check_form(a)
+    if not isinstance(l, Source):
+        raise NotImplementedError("only source terms int coef*f*v are supported")
+    V = A.space
+    b = out if out is not None else np.zeros(V.num_free_dofs, np.float64)
+    coef = a.cell_coef(V.mesh.num_cells)
+    scoef = None if l.coef is None else (np.full(V.mesh.num_cells, float(l.coef)) if np.isscalar(l.coef) else l.coef)
+    fv = l.fvec(V.ncomp)  # kept alive across the call (ctypes releases the GIL)
+    check(A.ctx.h, A.ctx.lib.gt_update_matrix_and_vector(A.h, a.kind, _ptr(coef), a.nu, _ptr(fv), _ptr(scoef), _ptr(b)))
+    A.form = a
+    return A, b
 
 
 def assemble_vector(l: Source, T, V: Space, out=None):

@@ -3,12 +3,15 @@
 ``Batch`` wraps ``gt_batch_*``: the small instances (up to 32768 rows) are
 solved by one persistent launch in which every CTA takes instances from a
 queue (largest first) and runs each one's whole Jacobi-PCG alone; the large
-instances, which fill the GPU by themselves, run one after the other through
-the persistent cooperative solver.  Each instance keeps its own CG scalars
-and a summation order that depends only on the instance.
+instances run through the single-system solver.  Each instance keeps its own
+CG scalars and a summation order that depends only on the instance.
+``run_batch`` drives a whole batch: HBM-budgeted waves, several worker
+contexts assembling instances concurrently and solving the large ones on
+their own streams while the small ones gather for the one-launch tier.
 ``autotune_lanes`` picks the lanes per matrix row of the per-CTA SpMV by
-timing the candidates on the batch itself and caches the choice in a JSON
-file keyed by the batch's shape.
+timing the candidates on the batch itself, ``autotune_batch`` the number of
+worker contexts (and the lanes) on a sample of a workload; both cache the
+choice in a JSON file keyed by the batch's shape.
 
 ``batch_workload`` draws the seeded instance list of the batched benchmark:
 independent Poisson problems on unit boxes, dimension 2 or 3 and order 1 or 2
@@ -27,8 +30,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib
-from .api import (Matrix, _ptr, assemble_matrix_and_vector, boundary, default_context, interior, lagrange_space,
-                  laplacian, source)
+from .api import (Context, Matrix, _ptr, assemble_matrix_and_vector, boundary, default_context, interior,
+                  lagrange_space, laplacian, solve, source)
 from ._lib import check
 from .mesh import cartesian_mesh, keyed_uniform, lognormal_cells
 
@@ -36,11 +39,14 @@ _MODES = {"fp64": _lib.GT_SOLVE_FP64, "ir": _lib.GT_SOLVE_IR, "mixed": _lib.GT_S
 
 
 class Batch:
-    def __init__(self, matrices, lanes: int | None = None):
+    """gt_batch over assembled scalar matrices of one device (they may come
+    from several contexts); solved on ``ctx`` (default: the first matrix's)."""
+
+    def __init__(self, matrices, lanes: int | None = None, ctx=None):
         if not matrices:
             raise ValueError("empty batch")
         self.mats = list(matrices)
-        self.ctx = self.mats[0].ctx
+        self.ctx = ctx or self.mats[0].ctx
         arr = (C.c_void_p * len(self.mats))(*[m.h.value for m in self.mats])
         h = C.c_void_p()
         check(self.ctx.h, self.ctx.lib.gt_batch_create(self.ctx.h, len(self.mats), arr, C.byref(h)))
@@ -174,3 +180,187 @@ def assemble_instance(spec: InstanceSpec, seed=404, T="mixed", ctx=None, inputs=
     V = lagrange_space(interior(m), spec.order, dirichlet_boundary=boundary(m), ctx=ctx)
     A, b = assemble_matrix_and_vector(laplacian(kappa), source(1.0), T, V)
     return m, V, A, b
+
+
+# ---------------------------------------------------------------------------
+# concurrent batched assembly + solve
+# ---------------------------------------------------------------------------
+@dataclass
+class BatchRun:
+    """Outcome of run_batch: per-instance solutions (by instance index) and
+    solve infos, plus the timings of the run."""
+    solutions: dict
+    infos: dict
+    seconds: float
+    waves: int
+    small: int
+    large: int
+
+
+def waves_by_budget(specs, budget_bytes, precision="mixed"):
+    """Instances largest first, greedily grouped so that each wave's estimated
+    device bytes stay under the budget (an instance alone above it still
+    forms a wave of its own)."""
+    order = sorted(specs, key=lambda s: -estimate_bytes(s, precision))
+    waves, cur, used = [], [], 0
+    for s in order:
+        e = estimate_bytes(s, precision)
+        if cur and used + e > budget_bytes:
+            waves.append(cur)
+            cur, used = [], 0
+        cur.append(s)
+        used += e
+    if cur:
+        waves.append(cur)
+    return waves
+
+
+def run_batch(specs, inputs, precision="mixed", rtol=1e-10, maxit=100000, workers=4, small_rows=32768, lanes=None,
+              budget_bytes=150e9, contexts=None, keep_solutions=True, ctx=None):
+    """Batched assembly + solve of many independent instances.
+
+    The instances go in HBM-budgeted waves (largest first).  In a wave,
+    ``workers`` threads, each with its own context (its own CUDA streams and
+    buffer pool), take instances from a largest-first queue and assemble them
+    -- mesh upload, DOF numbering, sparsity, values (mixed: FP64-integrated
+    FP64 values and FP32-integrated FP32 values) and load vector -- so the
+    device overlaps the assembly of several instances.  An instance with more
+    than ``small_rows`` rows is solved at once by its worker through the
+    single-system solver on the worker's stream, so several such solves and
+    the other workers' assembly run on the device together; the smaller
+    instances wait for the wave's small tier: one gt_batch over all of them,
+    solved by one persistent launch in which each CTA runs whole instances
+    from a largest-first queue.  Every instance's arithmetic depends only on
+    the instance, so its result is bitwise the same whatever the batch.
+
+    inputs: {index: (mesh, kappa)} (instance_inputs).  precision "mixed"
+    solves with FP32 CG + FP64 reliable updates (mode "ir"), float64 with
+    FP64 CG.  Returns a BatchRun."""
+    import threading
+
+    T = "mixed" if precision == "mixed" else np.float64
+    mode = "ir" if precision == "mixed" else "fp64"
+    ctx = ctx or default_context()
+    ctxs = list(contexts) if contexts else [Context(ctx.device) for _ in range(max(1, workers))]
+    sols, infos = {}, {}
+    n_small = n_large = 0
+    t0 = time.perf_counter()
+    waves = waves_by_budget(specs, budget_bytes, "mixed" if precision == "mixed" else "fp64")
+    for wave in waves:
+        queue = list(wave)  # largest first
+        qlock = threading.Lock()
+        small = []          # (spec, mesh, V, A, b) waiting for the small tier
+        errors = []
+
+        def work(wctx):
+            while True:
+                with qlock:
+                    if not queue:
+                        return
+                    s = queue.pop(0)
+                try:
+                    m, kappa = inputs[s.index]
+                    m_, V, A, b = assemble_instance(s, T=T, ctx=wctx, inputs=(m, kappa))
+                    if A.shape[0] > small_rows:
+                        x, info = solve(A, b, rtol=rtol, maxit=maxit, mode=mode, raise_on_fail=False)
+                        with qlock:
+                            sols[s.index] = x if keep_solutions else None
+                            infos[s.index] = info
+                        del A, V
+                        m._device.pop(id(wctx), None)
+                        if wctx.memory()[1] > budget_bytes / (4 * len(ctxs)):
+                            wctx.trim()
+                    else:
+                        with qlock:
+                            small.append((s, m, V, A, b))
+                except Exception as e:  # reported after the wave
+                    with qlock:
+                        errors.append((s.index, e))
+
+        threads = [threading.Thread(target=work, args=(c,)) for c in ctxs]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        if errors:
+            raise errors[0][1]
+        n_large += len(wave) - len(small)
+        n_small += len(small)
+        if small:
+            small.sort(key=lambda t: t[0].index)
+            B = Batch([A for _, _, _, A, _ in small], ctx=ctx)
+            if lanes:
+                B.set_lanes(lanes)
+            x, binfo = B.solve([b for *_, b in small], rtol=rtol, maxit=maxit, mode=mode, raise_on_fail=False)
+            for (s, m, V, A, b), xi, info in zip(small, B.split(x), binfo):
+                sols[s.index] = xi.copy() if keep_solutions else None
+                infos[s.index] = dict(info, converged=info["rel_residual"] <= rtol)
+            del B
+            for s, m, V, A, b in small:
+                for c in ctxs:
+                    m._device.pop(id(c), None)
+            small.clear()
+        for c in ctxs:
+            c.trim()
+    ctx.synchronize()
+    seconds = time.perf_counter() - t0
+    if not contexts:
+        for c in ctxs:
+            c.close()
+    return BatchRun(sols, infos, seconds, len(waves), n_small, n_large)
+
+
+def autotune_batch(specs, inputs, precision="mixed", rtol=1e-10, workers=(1, 2, 4, 8), sample=48, max_rows=2_000_000,
+                   cache=None, use_cache=True, seed=0):
+    """Pick run_batch's concurrency (worker contexts) and the small tier's
+    SpMV lanes for a workload: run_batch is timed on a seeded sample of the
+    instances (at most ``sample``, each under ``max_rows`` rows, spread over
+    the size range) once per worker count, then autotune_lanes times the
+    lane candidates on the sample's small tier.  The choice is cached in the
+    autotune JSON file under the workload's signature."""
+    path = _cache_path(cache)
+    sig = hashlib.sha1(repr(sorted((s.dim, s.order, s.cells_per_dir) for s in specs)).encode()).hexdigest()[:16]
+    key = f"batch:{precision}:{sig}"
+    table = {}
+    if use_cache and os.path.exists(path):
+        try:
+            table = json.load(open(path))
+        except Exception:
+            table = {}
+    if key in table:
+        return table[key]
+    rows = {s.index: (s.order * s.cells_per_dir - 1) ** s.dim for s in specs}
+    pool = sorted([s for s in specs if rows[s.index] <= max_rows], key=lambda s: rows[s.index])
+    if len(pool) > sample:
+        pick = np.linspace(0, len(pool) - 1, sample).round().astype(int)
+        pool = [pool[i] for i in sorted(set(pick.tolist()))]
+    sub = {s.index: inputs[s.index] for s in pool}
+    run_batch(pool[:4], sub, precision, rtol=rtol, workers=1)  # warm-up (module load, pools)
+    times = {}
+    for w in workers:
+        times[w] = run_batch(pool, sub, precision, rtol=rtol, workers=w, keep_solutions=False).seconds
+    best_w = min(times, key=times.get)
+    ctx = default_context()
+    T = "mixed" if precision == "mixed" else np.float64
+    small = [s for s in pool if rows[s.index] <= 32768]
+    lanes = 0
+    if small:
+        inst = [assemble_instance(s, T=T, ctx=ctx, inputs=sub[s.index]) for s in small]
+        B = Batch([A for _, _, A, _ in inst])
+        lanes = autotune_lanes(B, np.concatenate([b for *_, b in inst]), iters=32, cache=cache, use_cache=use_cache)["lanes"]
+        del B, inst
+    entry = {"workers": int(best_w), "lanes": int(lanes), "seconds": {str(k): v for k, v in times.items()},
+             "sample": len(pool)}
+    table = {}
+    if os.path.exists(path):
+        try:
+            table = json.load(open(path))
+        except Exception:
+            table = {}
+    table[key] = entry
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        json.dump(table, open(path, "w"), indent=1)
+    except OSError:
+        pass
+    return entry

@@ -270,8 +270,9 @@ int gt_spmv(gt_matrix* matrix, const double* x, double* y);
 
 /* ---- batched solves ----------------------------------------------------- */
 /* No counterpart in the reference (which solves one problem per call).
- * A batch of n assembled scalar matrices (block size 1) of one context,
- * solved together: instances of up to 32768 rows in one persistent launch
+ * A batch of n assembled scalar matrices (block size 1) on the device of
+ * ctx (they may come from other contexts of that device, e.g. assembled
+ * concurrently on several streams), solved together on ctx's stream: instances of up to 32768 rows in one persistent launch
  * in which each CTA takes instances from a queue (largest first) and runs
  * each one's whole PCG alone; larger instances one after the other through
  * the single-system solver.  An instance's result does not depend on the

@@ -68,3 +68,20 @@ def test_batch_with_large_instance_matches_alone():
             assert infos[k]["rel_residual"] <= 1e-9
             alone, _ = GB.Batch([mats[k]]).solve([bs[k]], rtol=1e-9, mode=mode)
             assert np.array_equal(alone, parts[k])
+
+
+def test_run_batch_concurrent_workers_bitwise_and_converged():
+    """run_batch with several worker contexts (concurrent assembly, large
+    instances solved on the workers' streams, the small ones in one launch)
+    gives bitwise the results of one worker, in mixed and plain FP64."""
+    specs = [GB.InstanceSpec(0, 2, 1, 9), GB.InstanceSpec(1, 2, 2, 30), GB.InstanceSpec(2, 3, 1, 12),
+             GB.InstanceSpec(3, 3, 2, 5), GB.InstanceSpec(4, 2, 1, 120), GB.InstanceSpec(5, 3, 1, 7),
+             GB.InstanceSpec(6, 2, 2, 3), GB.InstanceSpec(7, 3, 2, 9)]
+    inputs = {s.index: GB.instance_inputs(s, seed=21) for s in specs}
+    for prec in ("mixed", "fp64"):
+        one = GB.run_batch(specs, inputs, prec, rtol=1e-10, workers=1, small_rows=2000)
+        three = GB.run_batch(specs, inputs, prec, rtol=1e-10, workers=3, small_rows=2000)
+        assert one.small + one.large == len(specs) and one.large >= 3 and one.small >= 3
+        for s in specs:
+            assert three.infos[s.index]["rel_residual"] <= 1e-10
+            assert np.array_equal(one.solutions[s.index], three.solutions[s.index])
