@@ -64,7 +64,8 @@ def parse():
     p.add_argument("--workload", default="tets", choices=["tets", "elasticity", "batched", "serving"],
                    help="tets: the headline workload; the others measure the remaining configurations")
     p.add_argument("--instances", type=int, default=512, help="batched: number of instances")
-    p.add_argument("--requests", type=int, default=48, help="serving: number of requests")
+    p.add_argument("--serve-seconds", type=float, default=30.0, help="serving: length of the request stream")
+    p.add_argument("--slots", type=int, default=4, help="serving: concurrent request slots")
     p.add_argument("--budget-gb", type=float, default=150.0, help="batched/serving: HBM admission budget")
     return p.parse_args()
 
@@ -214,21 +215,38 @@ def run_batched(args):
 
 
 def run_serving(args):
-    """Poisson-process stream (mean 2000 req/s) of assemble+solve requests:
-    Poisson or elasticity, Q1|Q2 hexahedra, cells log-uniform 1e3..2e6,
-    seeded coefficients, HBM admission budget; mixed path with 4 slots vs the
-    plain FP64 path with one slot.  p50/p99 latency = arrival -> result."""
-    from gtgpu.server import Server, request_stream
+    """Open-loop Poisson-process stream (mean 2000 req/s) of assemble+solve
+    requests: Poisson or elasticity, Q1|Q2 hexahedra, cells log-uniform
+    1e3..2e6, seeded coefficients, HBM admission budget 150 GB, solved to a
+    1e-10 relative residual.  The stream runs for --serve-seconds: requests
+    arriving in that window are fed at their arrival times, none starts after
+    it, and those still waiting then are reported as pending (the offered
+    load is far above what one GPU completes, so the window, not a request
+    count, bounds the run).  Arms: mixed precision and plain FP64 with the
+    same slot count, and plain FP64 with one slot.  Each slot keeps its
+    geometries resident (mesh, space, pattern) and refills values on a
+    repeat; host meshes come from a library built before the stream.
+    p50/p99 latency = arrival -> result, over the completed requests."""
+    from gtgpu.server import MeshLibrary, Server, request_stream
+    rate, dur = 2000.0, args.serve_seconds
+    n = int(rate * dur * 1.2) + 16
+    reqs0 = [r for r in request_stream(n, rate=rate, seed=505) if r.arrival < dur]
+    lib = MeshLibrary(r.cells_per_dir for r in reqs0)  # untimed: the pre-built meshes
     res = {}
-    for name, slots, prec in (("mixed_served", 4, "mixed"), ("plain_fp64", 1, "fp64")):
-        reqs = request_stream(args.requests, rate=2000.0, seed=505)
-        srv = Server(slots=slots, budget_bytes=args.budget_gb * 1e9, precision=prec, rtol=1e-8,
-                     keep_solutions=False)
-        res[name] = srv.serve(reqs, realtime=True)
-    out = {"metric": "serving: solves/s and p50/p99 latency, mixed served vs plain FP64", "n_gpus": 1,
-           "config": {"workload": f"{args.requests} requests, Poisson arrivals 2000/s, cells log-uniform 1e3..2e6",
-                      "budget_gb": args.budget_gb},
-           **res, "speedup": res["mixed_served"]["solves_per_s"] / max(res["plain_fp64"]["solves_per_s"], 1e-12),
+    for name, slots, prec in (("mixed", args.slots, "mixed"), ("fp64", args.slots, "fp64"), ("fp64_1slot", 1, "fp64")):
+        reqs = request_stream(n, rate=rate, seed=505)
+        srv = Server(slots=slots, budget_bytes=args.budget_gb * 1e9, precision=prec, rtol=1e-10,
+                     keep_solutions=False, library=lib)
+        res[name] = srv.serve(reqs, realtime=True, duration=dur)
+        srv.close()
+    out = {"metric": "serving: solves/s and p50/p99 latency, mixed vs plain FP64 (same slots) and 1-slot FP64",
+           "n_gpus": 1,
+           "config": {"workload": f"Poisson arrivals 2000/s for {dur:g} s ({len(reqs0)} requests), cells log-uniform "
+                                  f"1e3..2e6, Poisson|elasticity x Q1|Q2", "budget_gb": args.budget_gb,
+                      "rtol": 1e-10, "policy": "shortest estimated work first", "slots": args.slots},
+           **res,
+           "speedup_vs_fp64_same_slots": res["mixed"]["solves_per_s"] / max(res["fp64"]["solves_per_s"], 1e-12),
+           "speedup_vs_fp64_1slot": res["mixed"]["solves_per_s"] / max(res["fp64_1slot"]["solves_per_s"], 1e-12),
            "data": "synthetic (seeded)"}
     print(json.dumps(out), flush=True)
 

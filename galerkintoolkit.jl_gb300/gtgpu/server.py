@@ -1,13 +1,27 @@
 """Request serving: assemble + solve requests with continuous batching.
 
 A ``Server`` runs ``slots`` workers, each with its own context (its own CUDA
-stream and buffer pool), so the device overlaps the work of concurrent
-requests.  Requests arriving while others run are admitted as soon as a slot
-is free and the HBM budget (sum of the admitted requests' estimated device
-bytes) has room; a request whose estimate alone exceeds the budget is refused
-with ``GT_ERR_BUDGET`` and counted.  Mesh, space and matrix stay on the
-device for the life of a request.  Every kernel reduces in a fixed order per
-request, so a request's result is bitwise the same alone and in any mix.
+streams and buffer pool), so the device overlaps the work of concurrent
+requests.  Requests arriving while others run wait in a pending set and are
+admitted as soon as a slot is free and the HBM budget has room for their
+estimated device bytes; a request whose estimate alone exceeds the budget is
+refused with ``GT_ERR_BUDGET`` and counted.  The policy picks the next
+pending request: ``"sjf"`` the smallest estimated work (the default: under a
+stream the device cannot keep up with it completes the most requests),
+``"fifo"`` the earliest arrival.  The next request waits until the budget
+has room for it.
+
+State stays on the device across requests: every slot keeps a cache of
+resident geometries keyed by (form, order, mesh) -- the mesh's device copy,
+the space (DOF numbering) and the assembled matrix (sparsity and value
+arrays) -- up to its share of the budget, least recently used out first.  A
+request for a cached geometry only refills the values and the load vector
+(GT.update_matrix_and_vector!, src/problems.jl:409-414) before its solve; a
+miss builds mesh, space and pattern and caches them.  Host meshes come from
+a ``MeshLibrary`` of pre-built meshes, so no mesh is generated inside a
+request's latency.  Every kernel reduces in a fixed order per request, and a
+refill gives bitwise the values of a fresh assembly, so a request's result
+is bitwise the same alone, in any mix, hit or miss.
 
 ``request_stream`` draws the seeded request mix of the serving benchmark:
 Poisson arrivals, each request Poisson or linear elasticity on Q1 or Q2
@@ -15,16 +29,17 @@ hexahedra, cell count log-uniform in a range, seeded per-cell coefficients.
 """
 from __future__ import annotations
 
-import queue
+import heapq
 import threading
 import time
+from collections import OrderedDict, deque
 from dataclasses import dataclass, field
 
 import numpy as np
 
 from . import _lib
 from .api import (Context, assemble_matrix_and_vector, boundary, elasticity, interior, lagrange_space, laplacian,
-                  solve, source)
+                  solve, source, update_matrix_and_vector)
 from .mesh import cartesian_mesh, keyed_uniform, lognormal_cells
 
 
@@ -42,19 +57,36 @@ class Request:
     finished: float = 0.0
     iterations: int = 0
     rel_residual: float = 0.0
+    cache_hit: bool = False
     solution: np.ndarray | None = field(default=None, repr=False)
 
     @property
     def cells(self):
         return self.cells_per_dir ** 3
 
+    @property
+    def key(self):
+        return (self.form, self.order, self.cells_per_dir)
+
+    @property
+    def ncomp(self):
+        return 3 if self.form == "elasticity" else 1
+
     def est_bytes(self, precision="mixed"):
         m = self.order * self.cells_per_dir + 1
         nodes = m ** 3
-        ncomp = 3 if self.form == "elasticity" else 1
+        ncomp = self.ncomp
         nnz = nodes * (2 * self.order + 1) ** 3 * ncomp * ncomp
         per = {"mixed": 16, "fp64": 12, "fp32": 8}[precision]
         return int(nnz * per + nodes * ncomp * 120 + self.cells * (24 + 8 + 4 * 27 * 3))
+
+    def est_work(self):
+        """Relative cost of the solve: matrix entries x a CG iteration count
+        growing with the nodes per direction (x4 for elasticity's ratio of
+        iterations)."""
+        m = self.order * self.cells_per_dir + 1
+        nnz = m ** 3 * (2 * self.order + 1) ** 3 * self.ncomp ** 2
+        return nnz * m * (4.0 if self.form == "elasticity" else 1.0)
 
 
 def request_stream(n, rate=2000.0, seed=505, min_cells=1e3, max_cells=2e6):
@@ -70,46 +102,144 @@ def request_stream(n, rate=2000.0, seed=505, min_cells=1e3, max_cells=2e6):
     return [Request(i, float(t[i]), str(form[i]), int(order[i]), int(k[i]), seed * 1000003 + i) for i in range(n)]
 
 
-def run_request(req: Request, ctx: Context, precision="mixed", rtol=1e-8, keep_solution=True):
-    """Assemble and solve one request on ctx (mesh, space, matrix on the device)."""
-    k = req.cells_per_dir
-    m = cartesian_mesh((0, 1, 0, 1, 0, 1), (k, k, k))
-    coef = lognormal_cells(m.num_cells, 0.5, req.seed)
+class MeshLibrary:
+    """Pre-built host meshes of the unit cube, one per cells-per-direction
+    (built once, shared read-only by every slot)."""
+
+    def __init__(self, ks=()):
+        self.meshes = {}
+        self.lock = threading.Lock()
+        for k in sorted(set(ks)):
+            self.get(k)
+
+    def get(self, k):
+        with self.lock:
+            m = self.meshes.get(k)
+            if m is None:
+                m = cartesian_mesh((0, 1, 0, 1, 0, 1), (k, k, k))
+                self.meshes[k] = m
+        return m
+
+
+@dataclass
+class _Entry:
+    V: object
+    A: object
+    bytes: int
+
+
+class GeometryCache:
+    """One slot's resident geometries: key -> (space, matrix), least recently
+    used out first when the cached bytes pass the capacity."""
+
+    def __init__(self, ctx, capacity_bytes):
+        self.ctx = ctx
+        self.capacity = float(capacity_bytes)
+        self.entries: OrderedDict = OrderedDict()
+        self.bytes = 0
+        self.hits = 0
+        self.misses = 0
+
+    def get(self, key):
+        e = self.entries.get(key)
+        if e is not None:
+            self.entries.move_to_end(key)
+            self.hits += 1
+        return e
+
+    def put(self, key, V, A, nbytes, library):
+        self.misses += 1
+        if nbytes > self.capacity:
+            return False
+        while self.entries and self.bytes + nbytes > self.capacity:
+            self._evict(library)
+        self.entries[key] = _Entry(V, A, nbytes)
+        self.bytes += nbytes
+        return True
+
+    def uses_mesh(self, k):
+        return any(key[2] == k for key in self.entries)
+
+    def _evict(self, library):
+        key, e = self.entries.popitem(last=False)
+        self.bytes -= e.bytes
+        del e
+        if not self.uses_mesh(key[2]):  # the mesh's device copy goes with its last entry
+            library.get(key[2])._device.pop(id(self.ctx), None)
+
+    def clear(self, library):
+        while self.entries:
+            self._evict(library)
+
+
+def _forms(req, coef):
     if req.form == "poisson":
-        V = lagrange_space(interior(m), req.order, dirichlet_boundary=boundary(m), ctx=ctx)
-        a, l = laplacian(coef), source(1.0)
-    else:
-        V = lagrange_space(interior(m), req.order, tensor_size=(3,), dirichlet_boundary=boundary(m, ["2-face-5"]),
-                           ctx=ctx)
-        a, l = elasticity(coef, 0.3), source([0.0, 0.0, -1.0])
+        return laplacian(coef), source(1.0)
+    return elasticity(coef, 0.3), source([0.0, 0.0, -1.0])
+
+
+def run_request(req: Request, ctx: Context, precision="mixed", rtol=1e-8, keep_solution=True, cache=None,
+                library=None):
+    """Assemble and solve one request on ctx: from the slot's cache when its
+    geometry is resident (values and load vector refilled), else mesh upload,
+    space and assembly (then cached when it fits the slot's share)."""
+    library = library or MeshLibrary()
+    m = library.get(req.cells_per_dir)
+    coef = lognormal_cells(m.num_cells, 0.5, req.seed)
+    a, l = _forms(req, coef)
     T = "mixed" if precision == "mixed" else np.float64
-    A, b = assemble_matrix_and_vector(a, l, T, V)
-    x, info = solve(A, b, rtol=rtol, mode="ir" if precision == "mixed" else "fp64", raise_on_fail=False)
+    e = cache.get(req.key) if cache is not None else None
+    if e is not None:
+        A, b = update_matrix_and_vector(e.A, a, l)
+        req.cache_hit = True
+    else:
+        if req.form == "poisson":
+            V = lagrange_space(interior(m), req.order, dirichlet_boundary=boundary(m), ctx=ctx)
+        else:
+            V = lagrange_space(interior(m), req.order, tensor_size=(3,), dirichlet_boundary=boundary(m, ["2-face-5"]),
+                               ctx=ctx)
+        A, b = assemble_matrix_and_vector(a, l, T, V)
+        if cache is None or not cache.put(req.key, V, A, req.est_bytes(precision), library):
+            del V
+    x, info = solve(A, b, rtol=rtol, maxit=200000, mode="ir" if precision == "mixed" else "fp64",
+                    raise_on_fail=False)
     req.iterations = info["iterations"]
     req.rel_residual = info["rel_residual"]
     req.status = 0 if info["converged"] else _lib.GT_ERR_NOT_CONVERGED
     if keep_solution:
         req.solution = x
-    del A, V
+    del A
+    if cache is None or (e is None and not cache.uses_mesh(req.cells_per_dir)):
+        m._device.pop(id(ctx), None)  # nothing resident keeps this mesh's device copy
     return req
 
 
 class Server:
     def __init__(self, slots=4, budget_bytes=150e9, precision="mixed", rtol=1e-8, device=0, keep_solutions=True,
-                 ctx_factory=None, runner=None):
+                 ctx_factory=None, runner=None, policy="sjf", cache_fraction=0.1, library=None):
         self.slots = slots
         self.runner = runner or run_request
         self.budget = float(budget_bytes)
         self.precision = precision
         self.rtol = rtol
         self.keep = keep_solutions
+        self.policy = policy
+        self.library = library or MeshLibrary()
         self.ctxs = [(ctx_factory or (lambda: Context(device)))() for _ in range(slots)]
-        self.pending: list[Request] = []
+        # each slot caches geometries up to its share of cache_fraction of the
+        # budget; that share is reserved, so admission counts it as in use
+        cached = runner is None
+        share = self.budget * cache_fraction / max(1, slots)
+        self.caches = [GeometryCache(c, share) if cached else None for c in self.ctxs]
+        self.reserved = share * slots if cached else 0.0
+        # pending requests: a heap by estimated work (sjf) or arrival order (fifo)
+        self.pending = [] if policy == "sjf" else deque()
         self.lock = threading.Condition()
         self.in_use = 0.0
         self.done: list[Request] = []
         self.refused: list[Request] = []
         self.closed = False
+        self.deadline = None
         self.t0 = None
         self.errors = []
         self.workers = [threading.Thread(target=self._work, args=(i,), daemon=True) for i in range(slots)]
@@ -119,37 +249,54 @@ class Server:
 
     def submit(self, req: Request):
         with self.lock:
-            if req.est_bytes(self.precision) > self.budget:
+            if req.est_bytes(self.precision) > self.budget - self.reserved:
                 req.status = _lib.GT_ERR_BUDGET
                 req.admitted = req.finished = self._now()
                 self.refused.append(req)
                 return
-            self.pending.append(req)
+            if self.policy == "sjf":
+                heapq.heappush(self.pending, (req.est_work(), req.arrival, req.rid, req))
+            else:
+                self.pending.append(req)
             self.lock.notify_all()
 
     def _take(self):
         with self.lock:
             while True:
-                # first pending request that fits in the remaining budget
-                for i, r in enumerate(self.pending):
+                if self.deadline is not None and self._now() >= self.deadline:
+                    return None, 0
+                # the next request by the policy, admitted once the budget has
+                # room for it (else wait for running requests to finish)
+                r = None
+                if self.pending:
+                    r = self.pending[0][3] if self.policy == "sjf" else self.pending[0]
+                    if self.in_use + self.reserved + r.est_bytes(self.precision) > self.budget:
+                        r = None
+                if r is not None:
+                    if self.policy == "sjf":
+                        heapq.heappop(self.pending)
+                    else:
+                        self.pending.popleft()
                     need = r.est_bytes(self.precision)
-                    if self.in_use + need <= self.budget:
-                        self.pending.pop(i)
-                        self.in_use += need
-                        r.admitted = self._now()
-                        return r, need
+                    self.in_use += need
+                    r.admitted = self._now()
+                    return r, need
                 if self.closed and not self.pending:
                     return None, 0
-                self.lock.wait(0.05)
+                self.lock.wait(0.01)
 
     def _work(self, slot):
         ctx = self.ctxs[slot]
+        cache = self.caches[slot]
         while True:
             req, need = self._take()
             if req is None:
                 return
             try:
-                self.runner(req, ctx, self.precision, self.rtol, self.keep)
+                if cache is not None:
+                    self.runner(req, ctx, self.precision, self.rtol, self.keep, cache=cache, library=self.library)
+                else:
+                    self.runner(req, ctx, self.precision, self.rtol, self.keep)
             except Exception as e:  # a failed request is reported, the server continues
                 req.status = getattr(e, "code", _lib.GT_ERR_CUDA)
                 self.errors.append((req.rid, repr(e)))
@@ -163,12 +310,18 @@ class Server:
                 self.done.append(req)
                 self.lock.notify_all()
 
-    def serve(self, requests, realtime=True):
-        """Feed requests at their arrival times; returns when all finished."""
+    def serve(self, requests, realtime=True, duration=None):
+        """Feed requests at their arrival times (realtime) and serve them.
+        duration (seconds from the start): requests arriving later are not
+        fed and no request starts after it; those still waiting then are
+        reported as pending.  Returns the report."""
         self.t0 = time.perf_counter()
+        self.deadline = duration
         for w in self.workers:
             w.start()
         for r in sorted(requests, key=lambda r: r.arrival):
+            if duration is not None and r.arrival >= duration:
+                break
             if realtime:
                 dt = r.arrival - self._now()
                 if dt > 0:
@@ -181,11 +334,21 @@ class Server:
             w.join()
         return self.report()
 
+    def close(self):
+        """Drops the cached geometries and the slots' contexts."""
+        for c in self.caches:
+            if c is not None:
+                c.clear(self.library)
+        for c in self.ctxs:
+            if hasattr(c, "close"):
+                c.close()
+
     def report(self):
         done = [r for r in self.done if r.status == 0]
         lat = np.array([r.finished - r.arrival for r in done]) if done else np.array([0.0])
         span = max((r.finished for r in self.done), default=0.0)
         return {"completed": len(done), "failed": len(self.done) - len(done), "refused_budget": len(self.refused),
-                "solves_per_s": len(done) / span if span > 0 else 0.0, "p50_ms": 1e3 * float(np.percentile(lat, 50)),
-                "p99_ms": 1e3 * float(np.percentile(lat, 99)), "makespan_s": span,
-                "errors": self.errors[:5]}
+                "pending_at_end": len(self.pending), "solves_per_s": len(done) / span if span > 0 else 0.0,
+                "p50_ms": 1e3 * float(np.percentile(lat, 50)), "p99_ms": 1e3 * float(np.percentile(lat, 99)),
+                "makespan_s": span, "cache_hits": sum(1 for r in done if r.cache_hit), "policy": self.policy,
+                "slots": self.slots, "errors": self.errors[:5]}

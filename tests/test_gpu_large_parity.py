@@ -116,6 +116,7 @@ def test_served_solutions_against_oracle():
     reqs = request_stream(6, rate=2000.0, seed=17, min_cells=300, max_cells=3000)
     srv = Server(slots=3, budget_bytes=150e9, precision="mixed", rtol=RTOL)
     rep = srv.serve(reqs, realtime=True)
+    srv.close()
     assert rep["completed"] == len(reqs)
     from gtgpu.mesh import cartesian_mesh, lognormal_cells
     for r in reqs:

@@ -11,9 +11,44 @@ pytestmark = pytest.mark.gpu
 def test_results_same_alone_and_in_the_mix():
     reqs_a = request_stream(8, rate=2000.0, seed=11, min_cells=500, max_cells=8000)
     reqs_b = request_stream(8, rate=2000.0, seed=11, min_cells=500, max_cells=8000)
-    alone = Server(slots=1, budget_bytes=150e9).serve(reqs_a, realtime=False)
-    mixed = Server(slots=4, budget_bytes=150e9).serve(reqs_b, realtime=True)
+    s1, s4 = Server(slots=1, budget_bytes=150e9), Server(slots=4, budget_bytes=150e9)
+    alone = s1.serve(reqs_a, realtime=False)
+    mixed = s4.serve(reqs_b, realtime=True)
+    s1.close()
+    s4.close()
     assert alone["completed"] == 8 and mixed["completed"] == 8
     for ra, rb in zip(sorted(reqs_a, key=lambda r: r.rid), sorted(reqs_b, key=lambda r: r.rid)):
         assert ra.rel_residual <= 1e-8
         assert np.array_equal(ra.solution, rb.solution)
+
+
+def test_cached_geometry_refill_is_bitwise_a_fresh_assembly():
+    """A slot keeps a served request's geometry (mesh, space, pattern) on the
+    device; a later request on the same geometry only refills the values and
+    the load vector, and its solution is bitwise that of a slot that builds
+    everything afresh."""
+    from gtgpu.server import Request
+    reqs = [Request(0, 0.0, "poisson", 2, 7, 101), Request(1, 0.0, "elasticity", 1, 6, 102),
+            Request(2, 0.0, "poisson", 2, 7, 103), Request(3, 0.0, "elasticity", 1, 6, 104)]
+    warm = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo")
+    warm.serve(reqs, realtime=False)
+    assert [r.cache_hit for r in sorted(reqs, key=lambda r: r.rid)] == [False, False, True, True]
+    fresh = [Request(r.rid, 0.0, r.form, r.order, r.cells_per_dir, r.seed) for r in reqs[2:]]
+    cold = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo", cache_fraction=1e-9)
+    cold.serve(fresh, realtime=False)
+    for a, b in zip(sorted(reqs[2:], key=lambda r: r.rid), sorted(fresh, key=lambda r: r.rid)):
+        assert not b.cache_hit and a.rel_residual <= 1e-10
+        assert np.array_equal(a.solution, b.solution)
+    warm.close()
+    cold.close()
+
+
+def test_serving_window_reports_pending():
+    """duration: no request starts after the window; those left are pending"""
+    reqs = request_stream(200, rate=2000.0, seed=5, min_cells=20000, max_cells=60000)
+    srv = Server(slots=2, budget_bytes=150e9, rtol=1e-8, keep_solutions=False)
+    rep = srv.serve(reqs, realtime=True, duration=0.05)
+    srv.close()
+    fed = sum(1 for r in reqs if r.arrival < 0.05)
+    assert rep["completed"] + rep["pending_at_end"] + rep["failed"] + rep["refused_budget"] == fed
+    assert rep["pending_at_end"] > 0
