@@ -320,8 +320,6 @@ int gt_ctx_create(int device, gt_ctx** out) {
   c->stream = c->own_stream;
   const char* pcg = getenv("GTGPU_PCG");
   c->pcg_path = !pcg ? 0 : strcmp(pcg, "launches") == 0 ? 1 : strcmp(pcg, "persistent") == 0 ? 2 : 0;
-  const char* sp = getenv("GTGPU_SPMV");
-  c->tiles_spmv = sp && strcmp(sp, "tiles") == 0;
   const char* ov = getenv("GTGPU_OVERLAP");
   c->overlap = !(ov && strcmp(ov, "0") == 0);
   const char* pt = getenv("GTGPU_PATTERN");

@@ -92,8 +92,6 @@ struct Ctx {
   // launches per phase for large ones), 1 = always launches, 2 = always
   // persistent (environment GTGPU_PCG=launches|persistent at context creation)
   int pcg_path = 0;
-  // bulk-copied row tiles instead of the row-group SpMV (GTGPU_SPMV=tiles)
-  bool tiles_spmv = false;
   // element kernels on the auxiliary stream beside the sparsity kernels
   // (GTGPU_OVERLAP=0 at context creation: one stream, in order)
   bool overlap = true;

@@ -19,7 +19,6 @@
 
 #include "gt_internal.cuh"
 #include "gt_rowdot.cuh"
-#include "gt_tiles.cuh"
 
 namespace gt {
 
@@ -429,33 +428,6 @@ __global__ void k_copy_f32_to_f64(const float* a, int64_t n, double* out) {
   if (i < n) out[i] = (double)a[i];
 }
 
-// scalar CSR SpMV over bulk-copied row tiles (gt_tiles.cuh): y = A x or
-// y = bsub - A x
-template <int G, class V, class X>
-__global__ void __launch_bounds__(TILE_T) k_spmv_tiles(const int64_t* __restrict__ rowptr,
-                                                       const int32_t* __restrict__ colind, const V* __restrict__ val,
-                                                       const X* __restrict__ x, int64_t nrows,
-                                                       const X* __restrict__ bsub, X* __restrict__ y, uint32_t* err) {
-  extern __shared__ __align__(128) unsigned char tsm[];
-  spmv_tiles<G, V, X, false>(rowptr, colind, val, x, bsub, y, nrows, tsm, err, nullptr);
-}
-
-// q = A p and p.q over bulk-copied row tiles; the last CTA sets alpha
-template <int G, class V, class X>
-__global__ void __launch_bounds__(TILE_T) k_cg_spmv_tiles(const int64_t* __restrict__ rowptr,
-                                                          const int32_t* __restrict__ colind, const V* __restrict__ val,
-                                                          const X* __restrict__ p, X* __restrict__ q, int64_t nrows,
-                                                          CGState* st, RedBuf rb, uint32_t* err) {
-  extern __shared__ __align__(128) unsigned char tsm[];
-  if (st->done) return;
-  X dot = (X)0;
-  spmv_tiles<G, V, X, true>(rowptr, colind, val, p, nullptr, q, nrows, tsm, err, &dot);
-  X v[1] = {dot};
-  if (reduce_last<1, X>(v, rb) && threadIdx.x == 0) {
-    st->pq = (double)v[0];
-    st->alpha = st->rz / (double)v[0];
-  }
-}
 
 // ---------------------------------------------------------------------------
 // host side
@@ -648,7 +620,7 @@ template <class V>
 static int sell_prepare(Matrix* A, const V* val, SellView<V>* view) {
   *view = SellView<V>{};
   Ctx* ctx = A->ctx;
-  if (A->bs != 1 || A->nbrows == 0 || A->bnnz == 0 || A->sell_state < 0 || ctx->tiles_spmv || !val) return GT_OK;
+  if (A->bs != 1 || A->nbrows == 0 || A->bnnz == 0 || A->sell_state < 0 || !val) return GT_OK;
   const int64_t nrows = A->nbrows, ns = (nrows + SELL_C - 1) / SELL_C;
   const unsigned g = (unsigned)((ns * 32 + 255) / 256);
   if (A->sell_state == 0) {
@@ -762,48 +734,7 @@ struct Ops {
     else if (bs == 2) byg(I2());
     else byg(I3());
   }
-  // lanes per row of the tiled SpMV (R = 256 / G rows per tile, at most
-  // TILE_CAP entries per tile); 0 when the tiled kernel does not apply
-  static int tile_lanes(const Matrix* A) {
-    if (A->bs != 1 || !A->ctx->tiles_spmv) return 0;
-    for (int g = 1; g <= 32; g *= 2)
-      if ((int64_t)(TILE_T / g) * A->max_row <= TILE_CAP) return g;
-    return 0;
-  }
-  template <class F>
-  static void by_lanes(int g, F&& go) {
-    switch (g) {
-      case 1: go(std::integral_constant<int, 1>()); break;
-      case 2: go(std::integral_constant<int, 2>()); break;
-      case 4: go(std::integral_constant<int, 4>()); break;
-      case 8: go(std::integral_constant<int, 8>()); break;
-      case 16: go(std::integral_constant<int, 16>()); break;
-      default: go(std::integral_constant<int, 32>()); break;
-    }
-  }
-  // persistent grid of the tiled kernels: every resident CTA walks tiles
-  template <class K>
-  static unsigned tiles_grid(Ctx* ctx, const Matrix* A, int g, K kern) {
-    const size_t smem = tiles_smem_bytes<V>();
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TILE_T, smem);
-    int64_t ntiles = (A->nbrows + TILE_T / g - 1) / (TILE_T / g);
-    int64_t cap = (int64_t)(per_sm > 0 ? per_sm : 1) * ctx->num_sms;
-    return (unsigned)(ntiles < cap ? (ntiles > 0 ? ntiles : 1) : cap);
-  }
   static int spmv(Ctx* ctx, const Matrix* A, const V* val, const X* x, const X* bsub, X* y) {
-    if (int tg = tile_lanes(A)) {
-      by_lanes(tg, [&](auto g_t) {
-        constexpr int GG = decltype(g_t)::value;
-        auto kern = k_spmv_tiles<GG, V, X>;
-        unsigned grid = tiles_grid(ctx, A, GG, kern);
-        kern<<<GT_KC(ctx, grid), TILE_T, tiles_smem_bytes<V>(), ctx->stream>>>(A->rowptr, A->colind, val, x, A->nbrows,
-                                                                               bsub, y, ctx->d_err);
-      });
-      GT_LAUNCH(ctx, "k_spmv_tiles");
-      return GT_OK;
-    }
     unsigned grid = spmv_grid(A);
     dispatch(A->bs, pick_group(A), [&](auto bs_t, auto g_t) {
       constexpr int BS = decltype(bs_t)::value, GG = decltype(g_t)::value;
@@ -820,17 +751,6 @@ struct Ops {
       launch_pdl(ctx, kern, g, ctx->stream, sell->ptr, sell->len, sell->col, sell->val, p, q, A->nbrows,
                  sell->nslices, st, rb);
       GT_LAUNCH(ctx, "k_cg_spmv_sell");
-      return GT_OK;
-    }
-    if (int tg = tile_lanes(A)) {
-      by_lanes(tg, [&](auto g_t) {
-        constexpr int GG = decltype(g_t)::value;
-        auto kern = k_cg_spmv_tiles<GG, V, X>;
-        unsigned grid = tiles_grid(ctx, A, GG, kern);
-        kern<<<GT_KC(ctx, grid), TILE_T, tiles_smem_bytes<V>(), ctx->stream>>>(A->rowptr, A->colind, val, p, q,
-                                                                               A->nbrows, st, rb, ctx->d_err);
-      });
-      GT_LAUNCH(ctx, "k_cg_spmv_tiles");
       return GT_OK;
     }
     unsigned grid = cg_spmv_grid(A);
@@ -1297,7 +1217,6 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
   if (info) *info = inf;
   uint32_t bits = 0;
   GT_TRY(take_device_error(ctx, &bits));
-  if (bits & DEV_ERR_TIMEOUT) return set_error(ctx, GT_ERR_TIMEOUT, "solve: a tile copy did not complete");
   if (status == GT_ERR_NOT_CONVERGED) set_error(ctx, status, "solver did not reach the tolerance within maxit");
   return status;
 }
@@ -1359,7 +1278,6 @@ int gt_spmv(gt_matrix* A, const double* x, double* y) {
   if (s == GT_OK && e != cudaSuccess) s = check_cuda(ctx, e, "gt_spmv");
   uint32_t bits = 0;
   if (s == GT_OK) s = take_device_error(ctx, &bits);
-  if (s == GT_OK && (bits & DEV_ERR_TIMEOUT)) s = set_error(ctx, GT_ERR_TIMEOUT, "gt_spmv: a tile copy did not complete");
   if (!xdev) dfree(ctx, xd);
   if (!ydev) dfree(ctx, yd);
   return s;
