@@ -22,6 +22,7 @@
 #include <type_traits>
 
 #include "gt_internal.cuh"
+#include "gt_dfloat.cuh"
 #include "gt_refcell.cuh"
 
 namespace gt {
@@ -1242,6 +1243,102 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
   }
 }
 
+// The FP64-valued P1 kernel in double-float arithmetic (gt_dfloat.cuh):
+// the same formulas and summation order as k_elements_p1<FORM, double>, with
+// J's nine differences taken in FP64 (x_i - x_0 loses nothing there) and
+// everything after them -- cofactors, det J, its reciprocal, the entries,
+// the load vector -- in pairs of FP32 numbers (48 significant bits) on the
+// FP32 pipes, rounded to FP64 at the end.  About 9 FP64 instructions per
+// cell instead of ~75, so the kernel is no longer bound by GB300's FP64
+// rate; the values agree with the FP64 kernel's (and the FP64 oracle's) to
+// a few units of 2^-48 relative to the largest entry, far inside the 1e-12
+// parity tolerance.
+template <int FORM>
+__global__ void __launch_bounds__(256) k_elements_p1_df(const double* __restrict__ coords,
+                                                        const int32_t* __restrict__ cell_nodes,
+                                                        const double* __restrict__ coef,
+                                                        const double* __restrict__ consts, int64_t c_begin,
+                                                        int64_t ncells, double* __restrict__ Ke,
+                                                        double* __restrict__ be, const double* __restrict__ fsrc,
+                                                        const double* __restrict__ scoef, int want_matrix,
+                                                        uint32_t* err) {
+  const dfl wsum = df_from_double(__ldg(consts));
+  const bool load_equal = __double_as_longlong(__ldg(consts + 21)) != 0;
+  const dfl f0 = df_from_double(fsrc ? __ldg(fsrc) : 0.0);
+  dfl sload[4], smass[10];
+#pragma unroll
+  for (int n = 0; n < 4; n++) sload[n] = df_from_double(__ldg(consts + 1 + n));
+  if (FORM == GT_MASS) {
+    int e = 0;
+#pragma unroll
+    for (int n = 0; n < 4; n++)
+#pragma unroll
+      for (int m = n; m < 4; m++) smass[e++] = df_from_double(__ldg(consts + 5 + n * 4 + m));
+  }
+  const dfl one = {1.0f, 0.0f};
+  for (int64_t c = c_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    int4 nd = *reinterpret_cast<const int4*>(cell_nodes + 4 * c);
+    const double* p0 = coords + 3 * (int64_t)nd.x;
+    const double* p1 = coords + 3 * (int64_t)nd.y;
+    const double* p2 = coords + 3 * (int64_t)nd.z;
+    const double* p3 = coords + 3 * (int64_t)nd.w;
+    const double x0 = p0[0], y0 = p0[1], z0 = p0[2];
+    // J columns a, b, d (FP64 differences), then double-float
+    const dfl a[3] = {df_from_double(p1[0] - x0), df_from_double(p1[1] - y0), df_from_double(p1[2] - z0)};
+    const dfl b[3] = {df_from_double(p2[0] - x0), df_from_double(p2[1] - y0), df_from_double(p2[2] - z0)};
+    const dfl d[3] = {df_from_double(p3[0] - x0), df_from_double(p3[1] - y0), df_from_double(p3[2] - z0)};
+    // cofactor columns c_1, c_2, c_3 (the physical gradients times det J)
+    const dfl g1[3] = {df_mul_sub(b[1], d[2], b[2], d[1]), df_mul_sub(b[2], d[0], b[0], d[2]),
+                       df_mul_sub(b[0], d[1], b[1], d[0])};
+    const dfl det = df_dot3(a, g1);
+    if (det.hi == 0.0f) atomicOr(err, DEV_ERR_DEGENERATE);
+    const dfl adet = df_abs(det);
+    const dfl cf = coef ? df_from_double(coef[c]) : one;
+    if (want_matrix) {
+      dfl k[10];
+      if (FORM == GT_LAPLACE) {
+        const dfl g2[3] = {df_mul_sub(d[1], a[2], d[2], a[1]), df_mul_sub(d[2], a[0], d[0], a[2]),
+                           df_mul_sub(d[0], a[1], d[1], a[0])};
+        const dfl g3[3] = {df_mul_sub(a[1], b[2], a[2], b[1]), df_mul_sub(a[2], b[0], a[0], b[2]),
+                           df_mul_sub(a[0], b[1], a[1], b[0])};
+        const dfl s = df_mul(df_mul(cf, wsum), df_recip(adet));
+        const dfl k11 = df_mul(s, df_dot3(g1, g1)), k12 = df_mul(s, df_dot3(g1, g2)), k13 = df_mul(s, df_dot3(g1, g3));
+        const dfl k22 = df_mul(s, df_dot3(g2, g2)), k23 = df_mul(s, df_dot3(g2, g3));
+        const dfl k33 = df_mul(s, df_dot3(g3, g3));
+        // vertex 0 from the zero row sums, as in the FP64 kernel
+        const dfl k01 = df_neg(df_add(df_add(k11, k12), k13));
+        const dfl k02 = df_neg(df_add(df_add(k12, k22), k23));
+        const dfl k03 = df_neg(df_add(df_add(k13, k23), k33));
+        const dfl k00 = df_neg(df_add(df_add(k01, k02), k03));
+        k[0] = k00; k[1] = k01; k[2] = k02; k[3] = k03;
+        k[4] = k11; k[5] = k12; k[6] = k13;
+        k[7] = k22; k[8] = k23;
+        k[9] = k33;
+      } else {
+        const dfl s = df_mul(cf, adet);
+#pragma unroll
+        for (int e = 0; e < 10; e++) k[e] = df_mul(s, smass[e]);
+      }
+      double* K = Ke + 10 * c;
+#pragma unroll
+      for (int e = 0; e < 10; e++) K[e] = df_to_double(k[e]);
+    }
+    if (be) {
+      const dfl sc = df_mul(scoef ? df_mul(df_from_double(scoef[c]), f0) : f0, adet);
+      if (load_equal) {
+        const double v = df_to_double(df_mul(sc, sload[0]));
+        double2* b2 = reinterpret_cast<double2*>(be + 4 * c);  // 32-byte records of a pool block
+        b2[0] = make_double2(v, v);
+        b2[1] = make_double2(v, v);
+      } else {
+#pragma unroll
+        for (int n = 0; n < 4; n++) be[4 * c + n] = df_to_double(df_mul(sc, sload[n]));
+      }
+    }
+  }
+}
+
 // element kernels per cell type / order; returns GT_OK or an error
 template <class T>
 static int elements_T(const Space* sp, int form, const double* coef, double nu, const double* tab, const TabLayout& L,
@@ -1259,12 +1356,24 @@ static int elements_T(const Space* sp, int form, const double* coef, double nu, 
     for (int i = 0; i < nch; i++) {
       const int64_t c0 = nc * i / nch, c1 = nc * (i + 1) / nch;
       const int grid = grid_for(c1 - c0 > 0 ? c1 - c0 : 1, 256);
-      if (form == GT_LAPLACE)
+      bool df = false;
+      if constexpr (std::is_same<T, double>::value) df = ctx->p1_dfloat;
+      if (df) {
+        if constexpr (std::is_same<T, double>::value) {
+          if (form == GT_LAPLACE)
+            k_elements_p1_df<GT_LAPLACE><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
+                sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, c0, c1, Ke, be, f, scoef, want_matrix, ctx->d_err);
+          else
+            k_elements_p1_df<GT_MASS><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
+                sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, c0, c1, Ke, be, f, scoef, want_matrix, ctx->d_err);
+        }
+      } else if (form == GT_LAPLACE) {
         k_elements_p1<GT_LAPLACE, T><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
             sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, c0, c1, Ke, be, f, scoef, want_matrix, ctx->d_err);
-      else
+      } else {
         k_elements_p1<GT_MASS, T><<<GT_KC(ctx, grid), 256, 0, ctx->stream>>>(
             sp->mesh->coords, sp->mesh->cell_nodes, coef, consts, c0, c1, Ke, be, f, scoef, want_matrix, ctx->d_err);
+      }
       GT_LAUNCH(ctx, "k_elements_p1");
       if (chunks) {
         chunks->end[i] = c1;

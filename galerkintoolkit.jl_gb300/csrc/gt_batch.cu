@@ -235,12 +235,20 @@ __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, co
           block_sum<2>(v, s_red[buf]);
           buf ^= 1;
           beta = rzold != 0.0 ? v[0] / rzold : 0.0;
+          // the recurrence lost track of the true residual: restart the directions
+          if (v[0] > kRestartRatio * rz) beta = 0.0;
           const double prev = rmax2;
           rz = v[0];
           rr = v[1];
           rmax2 = v[1];
           nupd++;
           done = rr <= tol2 || iters >= maxit || !(rr == rr);
+          if (sizeof(X) == sizeof(double) && !done) {
+            // FP64: checks that do not halve ||r||, kStagnation times running:
+            // the tolerance lies below the attainable accuracy
+            stall = rr > 0.25 * prev ? stall + 1 : 0;
+            if (stall >= kStagnation) done = true;
+          }
           if (sizeof(X) < sizeof(double) && !done) {
             stall = rr > stall_ratio * prev ? stall + 1 : 0;
             if (stall >= stall_count || slow) {

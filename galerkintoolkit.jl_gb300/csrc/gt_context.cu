@@ -324,6 +324,8 @@ int gt_ctx_create(int device, gt_ctx** out) {
   c->overlap = !(ov && strcmp(ov, "0") == 0);
   const char* pt = getenv("GTGPU_PATTERN");
   c->pattern_rows = !(pt && strcmp(pt, "warps") == 0);
+  const char* p1 = getenv("GTGPU_P1");
+  c->p1_dfloat = !(p1 && strcmp(p1, "fp64") == 0);
   const char* un = getenv("GTGPU_UNIFORM");
   c->uniform_geom = !(un && strcmp(un, "0") == 0);
   const char* irs = getenv("GTGPU_IR_STALL");

@@ -114,6 +114,9 @@ struct Ctx {
   // measured: Q2 elasticity 64^3 5244 FP32 iterations (0.1: 7049), the P1
   // Poisson 96^3 x 6 solve 2% slower (20 updates instead of 11)
   double ir_delta = 0.3;
+  // FP64-valued P1 element matrices computed in double-float on the FP32
+  // pipes (GTGPU_P1=fp64 at context creation: the FP64-pipe kernel)
+  bool p1_dfloat = true;
   // lanes per row of the CSR row kernels: 0 = from the mean row length,
   // else 1, 2, 4 or 8 (GTGPU_SPMV_LANES at context creation)
   int spmv_lanes = 0;
@@ -314,6 +317,14 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
 // residual.  (Measured: problems at 300-450 FP32 iterations per decade still
 // gain from FP32; one at ~2500 per decade needed 4x the FP64 count.)
 constexpr int kSlowCycle = 1000;
+// A true-residual check whose r.z exceeds the recurrence's by this factor
+// restarts the CG directions from the true residual (beta = 0): the
+// recurrence has drifted (FP64 past its attainable accuracy, or FP32).
+constexpr double kRestartRatio = 100.0;
+// FP64 CG ends (not converged) after this many true-residual checks in a row
+// that did not halve the residual norm: the tolerance is below what
+// eps64 * cond(A) allows.
+constexpr int kStagnation = 3;
 
 // persistent cooperative Jacobi-PCG (gt_pcg.cu); x holds the start value
 int pcg_persistent(Matrix* A, int mode, const double* b, double* x, double rtol, int maxit, int32_t* iters,

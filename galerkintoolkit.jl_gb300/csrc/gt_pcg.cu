@@ -368,12 +368,24 @@ __global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
         if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
         grid_total<2>(slot2, nb, s_red, s_tot);
         beta = S.rzold != 0.0 ? s_tot[0] / S.rzold : 0.0;
+        // the recurrence lost track of the true residual (an FP64 run past
+        // its attainable accuracy, or FP32 drift): the next direction
+        // restarts from the true residual instead of scaling the old one by
+        // the true/recurrence mismatch
+        if (s_tot[0] > kRestartRatio * S.rz) beta = 0.0;
         const double prev = S.rmax2;
         S.rz = s_tot[0];
         S.rr = s_tot[1];
         S.rmax2 = s_tot[1];
         S.nupd += 1;
         S.done = s_tot[1] <= S.tol2 || S.iters >= a.maxit || !(s_tot[1] == s_tot[1]);
+        if (sizeof(X) == sizeof(double) && !S.done) {
+          // FP64: true-residual checks that do not halve ||r||, kStagnation
+          // times running -- the tolerance lies below the attainable accuracy
+          // (eps64 * cond(A)); the solve ends, not converged
+          S.stall = s_tot[1] > 0.25 * prev ? S.stall + 1 : 0;
+          if (S.stall >= kStagnation) S.done = 1;
+        }
         if (sizeof(X) < sizeof(double) && !S.done) {
           // the recurrence fell by delta but the true residual did not halve:
           // the FP32 operator no longer resolves the error (eps32 * cond ~ 1)

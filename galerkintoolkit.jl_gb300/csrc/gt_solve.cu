@@ -962,11 +962,19 @@ __global__ void __launch_bounds__(RED_T) k_rl_resid(const int64_t* __restrict__ 
   if (reduce_last<2, double, G>(v, rb) && threadIdx.x == 0) {
     // the next direction is built from the true residual
     st->beta = st->rzold != 0.0 ? v[0] / st->rzold : 0.0;
+    // the recurrence lost track of the true residual: restart the directions
+    if (st->nupd > 0 && v[0] > kRestartRatio * st->rz) st->beta = 0.0;
     const double prev = st->rmax2;
     st->rz = v[0];
     st->rr = v[1];
     st->nupd += 1;
     if (v[1] <= st->tol2 || st->iters >= st->maxit || !(v[1] == v[1])) st->done = 1;
+    if (sizeof(X) == sizeof(double) && !st->done && st->nupd > 1) {
+      // FP64: checks that do not halve ||r||, kStagnation times running: the
+      // tolerance lies below the attainable accuracy; ends not converged
+      st->stall = v[1] > 0.25 * prev ? st->stall + 1 : 0;
+      if (st->stall >= kStagnation) st->done = 1;
+    }
     if (sizeof(X) < sizeof(double) && !st->done && st->nupd > 1) {
       // the recurrence fell by delta but the true residual did not halve,
       // three times running, or the cycle slowed down: continue in FP64

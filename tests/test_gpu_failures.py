@@ -121,3 +121,26 @@ def test_grid_barrier_times_out():
     assert info["converged"]
     n = C.c_int64()
     assert lib.gt_ctx_launch_count(ctx.h, C.byref(n)) == 0 and n.value > 0
+
+
+@pytest.mark.parametrize("n", [6, 72])
+def test_unattainable_tolerance_stops_without_diverging(n):
+    """A tolerance below FP64's attainable accuracy: the CG (persistent kernel
+    for the small system, one launch per phase for the 357k-row one) ends as
+    not converged after a few true-residual checks without progress, with
+    the residual at the attainable level -- it neither runs to maxit nor
+    diverges (the directions restart when the recurrence has drifted from
+    the true residual)."""
+    m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (n, n, n), simplexify=True)
+    V = GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m))
+    A, b = GT.assemble_matrix_and_vector(GT.laplacian(), GT.source(1.0), "mixed", V)
+    _, ok = GT.solve(A, b, rtol=1e-10, mode="fp64")
+    for mode in ("fp64", "ir"):
+        x, info = GT.solve(A, b, rtol=1e-19, maxit=200000, mode=mode, raise_on_fail=False)
+        assert not info["converged"]
+        assert info["iterations"] < 20 * ok["iterations"] + 200
+        assert info["rel_residual"] < 1e-12
+    B = GB.Batch([A]) if n == 6 else None
+    if B is not None:
+        xb, infos = B.solve([b], rtol=1e-19, maxit=200000, mode="fp64", raise_on_fail=False)
+        assert infos[0]["iterations"] < 20 * ok["iterations"] + 200 and infos[0]["rel_residual"] < 1e-12

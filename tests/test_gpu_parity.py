@@ -350,3 +350,37 @@ def test_uniform_geometry_path_matches_per_cell_records(case, monkeypatch):
     del B, V2
     m._device.pop(id(ctx2), None)
     ctx2.close()
+
+
+@pytest.mark.parametrize("form", [O.LAPLACE, O.MASS])
+def test_p1_double_float_kernel_matches_fp64_kernel(form, monkeypatch):
+    """FP64-valued P1 element matrices are computed in double-float (pairs of
+    FP32) by default; a context created with GTGPU_P1=fp64 takes the FP64
+    kernel.  Matrices and load vectors agree with each other to 1e-13 and
+    with the oracle to 1e-12 (of the largest entry)."""
+    m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (20, 18, 16), simplexify=True)
+    GT.jitter_interior_nodes(m, 0.2, 31)
+    kappa = GT.lognormal_cells(m.num_cells, 1.0, 32)
+    a = GT.laplacian(kappa) if form == O.LAPLACE else GT.mass(kappa)
+    l = GT.source(1.0, kappa)
+    V = GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m))
+    A, b = GT.assemble_matrix_and_vector(a, l, np.float64, V)
+    monkeypatch.setenv("GTGPU_P1", "fp64")
+    ctx2 = GT.Context(0)
+    monkeypatch.delenv("GTGPU_P1")
+    V2 = GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m), ctx=ctx2)
+    A2, b2 = GT.assemble_matrix_and_vector(a, l, np.float64, V2)
+    _, _, v = A.csr()
+    _, _, v2 = A2.csr()
+    scale = np.abs(v2).max()
+    assert np.abs(v - v2).max() <= 1e-13 * scale
+    assert np.abs(b - b2).max() <= 1e-13 * np.abs(b2).max()
+    ref, _ = _oracle_space(m, 1, 1, "boundary")
+    cp, rv, nz = O.assemble_matrix(ref, form, 2, coef=kappa)
+    _, _, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
+    assert np.abs(v - ov).max() <= TOL64 * np.abs(ov).max()
+    ob = O.assemble_vector(ref, 2, 1.0, coef=kappa)
+    assert np.abs(b - ob).max() <= TOL64 * np.abs(ob).max()
+    del A2, V2
+    m._device.pop(id(ctx2), None)
+    ctx2.close()
