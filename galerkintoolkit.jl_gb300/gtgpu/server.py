@@ -23,6 +23,14 @@ request's latency.  Every kernel reduces in a fixed order per request, and a
 refill gives bitwise the values of a fresh assembly, so a request's result
 is bitwise the same alone, in any mix, hit or miss.
 
+Continuous batching: a slot that takes a small scalar request (a Poisson
+request of at most ``batch_rows`` rows) also takes the other small scalar
+requests pending at that moment (up to ``batch_max``, within the budget) and
+solves them together in one persistent launch (``gt_batch``: one CTA per
+request, each running its whole CG alone), so a stream of small requests is
+not served one grid-wide solve at a time.  Small scalar requests always take
+this path, even alone, so a request's result never depends on its batch.
+
 ``request_stream`` draws the seeded request mix of the serving benchmark:
 Poisson arrivals, each request Poisson or linear elasticity on Q1 or Q2
 hexahedra, cell count log-uniform in a range, seeded per-cell coefficients.
@@ -80,6 +88,12 @@ class Request:
         per = {"mixed": 16, "fp64": 12, "fp32": 8}[precision]
         return int(nnz * per + nodes * ncomp * 120 + self.cells * (24 + 8 + 4 * 27 * 3))
 
+    @property
+    def rows(self):
+        """free block rows (the homogeneous Dirichlet boundary removed)"""
+        m = self.order * self.cells_per_dir - 1
+        return m ** 3 if self.form == "poisson" else (self.order * self.cells_per_dir) * m * m
+
     def est_work(self):
         """Relative cost of the solve: matrix entries x a CG iteration count
         growing with the nodes per direction (x4 for elasticity's ratio of
@@ -129,8 +143,10 @@ class _Entry:
 
 
 class GeometryCache:
-    """One slot's resident geometries: key -> (space, matrix), least recently
-    used out first when the cached bytes pass the capacity."""
+    """One slot's resident geometries: key -> the instances (space, matrix)
+    kept for it -- several when requests of one geometry run in one batch,
+    each taking its own -- least recently used keys out first when the
+    cached bytes pass the capacity."""
 
     def __init__(self, ctx, capacity_bytes):
         self.ctx = ctx
@@ -140,20 +156,27 @@ class GeometryCache:
         self.hits = 0
         self.misses = 0
 
-    def get(self, key):
-        e = self.entries.get(key)
-        if e is not None:
-            self.entries.move_to_end(key)
-            self.hits += 1
-        return e
+    def acquire(self, key, taken):
+        """a cached instance of key not in taken (ids), or None"""
+        lst = self.entries.get(key)
+        if lst:
+            for e in lst:
+                if id(e) not in taken:
+                    self.entries.move_to_end(key)
+                    self.hits += 1
+                    taken.add(id(e))
+                    return e
+        return None
 
-    def put(self, key, V, A, nbytes, library):
+    def put(self, key, V, A, nbytes, library, taken):
         self.misses += 1
         if nbytes > self.capacity:
             return False
         while self.entries and self.bytes + nbytes > self.capacity:
             self._evict(library)
-        self.entries[key] = _Entry(V, A, nbytes)
+        e = _Entry(V, A, nbytes)
+        self.entries.setdefault(key, []).append(e)
+        taken.add(id(e))
         self.bytes += nbytes
         return True
 
@@ -161,9 +184,9 @@ class GeometryCache:
         return any(key[2] == k for key in self.entries)
 
     def _evict(self, library):
-        key, e = self.entries.popitem(last=False)
-        self.bytes -= e.bytes
-        del e
+        key, lst = self.entries.popitem(last=False)
+        self.bytes -= sum(e.bytes for e in lst)
+        del lst
         if not self.uses_mesh(key[2]):  # the mesh's device copy goes with its last entry
             library.get(key[2])._device.pop(id(self.ctx), None)
 
@@ -178,17 +201,17 @@ def _forms(req, coef):
     return elasticity(coef, 0.3), source([0.0, 0.0, -1.0])
 
 
-def run_request(req: Request, ctx: Context, precision="mixed", rtol=1e-8, keep_solution=True, cache=None,
-                library=None):
-    """Assemble and solve one request on ctx: from the slot's cache when its
-    geometry is resident (values and load vector refilled), else mesh upload,
-    space and assembly (then cached when it fits the slot's share)."""
-    library = library or MeshLibrary()
+def _assemble(req: Request, ctx, precision, cache, library, taken=None):
+    """The request's matrix and load vector on ctx: refilled in the slot's
+    cache when its geometry is resident, else mesh upload, space and
+    assembly (then cached when it fits the slot's share).  Returns (A, b,
+    release) with release() dropping what nothing resident keeps."""
     m = library.get(req.cells_per_dir)
     coef = lognormal_cells(m.num_cells, 0.5, req.seed)
     a, l = _forms(req, coef)
     T = "mixed" if precision == "mixed" else np.float64
-    e = cache.get(req.key) if cache is not None else None
+    taken = set() if taken is None else taken
+    e = cache.acquire(req.key, taken) if cache is not None else None
     if e is not None:
         A, b = update_matrix_and_vector(e.A, a, l)
         req.cache_hit = True
@@ -199,24 +222,59 @@ def run_request(req: Request, ctx: Context, precision="mixed", rtol=1e-8, keep_s
             V = lagrange_space(interior(m), req.order, tensor_size=(3,), dirichlet_boundary=boundary(m, ["2-face-5"]),
                                ctx=ctx)
         A, b = assemble_matrix_and_vector(a, l, T, V)
-        if cache is None or not cache.put(req.key, V, A, req.est_bytes(precision), library):
+        if cache is None or not cache.put(req.key, V, A, req.est_bytes(precision), library, taken):
             del V
-    x, info = solve(A, b, rtol=rtol, maxit=200000, mode="ir" if precision == "mixed" else "fp64",
-                    raise_on_fail=False)
+
+    def release():
+        if cache is None or (e is None and not cache.uses_mesh(req.cells_per_dir)):
+            m._device.pop(id(ctx), None)  # nothing resident keeps this mesh's device copy
+    return A, b, release
+
+
+def _record(req, x, info, rtol, keep_solution):
     req.iterations = info["iterations"]
     req.rel_residual = info["rel_residual"]
-    req.status = 0 if info["converged"] else _lib.GT_ERR_NOT_CONVERGED
+    req.status = 0 if info["rel_residual"] <= rtol else _lib.GT_ERR_NOT_CONVERGED
     if keep_solution:
         req.solution = x
+
+
+def run_request(req: Request, ctx: Context, precision="mixed", rtol=1e-8, keep_solution=True, cache=None,
+                library=None):
+    """Assemble (or refill) and solve one request on ctx."""
+    A, b, release = _assemble(req, ctx, precision, cache, library or MeshLibrary())
+    x, info = solve(A, b, rtol=rtol, maxit=200000, mode="ir" if precision == "mixed" else "fp64",
+                    raise_on_fail=False)
+    _record(req, x, info, rtol, keep_solution)
     del A
-    if cache is None or (e is None and not cache.uses_mesh(req.cells_per_dir)):
-        m._device.pop(id(ctx), None)  # nothing resident keeps this mesh's device copy
+    release()
     return req
+
+
+def run_batch_requests(reqs, ctx: Context, precision="mixed", rtol=1e-8, keep_solution=True, cache=None,
+                       library=None):
+    """Assemble (or refill) several small scalar requests on ctx and solve
+    them in one persistent launch (gt_batch, one CTA per request)."""
+    from .batch import Batch
+    library = library or MeshLibrary()
+    taken = set()  # cached instances handed to this batch: one per request
+    built = [_assemble(r, ctx, precision, cache, library, taken) for r in reqs]
+    B = Batch([A for A, _, _ in built], ctx=ctx)
+    x, infos = B.solve([b for _, b, _ in built], rtol=rtol, maxit=200000,
+                       mode="ir" if precision == "mixed" else "fp64", raise_on_fail=False)
+    for r, xi, info in zip(reqs, B.split(x), infos):
+        _record(r, xi.copy() if keep_solution else None, info, rtol, keep_solution)
+    del B
+    for A, b, release in built:
+        del A
+        release()
+    return reqs
 
 
 class Server:
     def __init__(self, slots=4, budget_bytes=150e9, precision="mixed", rtol=1e-8, device=0, keep_solutions=True,
-                 ctx_factory=None, runner=None, policy="sjf", cache_fraction=0.1, library=None):
+                 ctx_factory=None, runner=None, policy="sjf", cache_fraction=0.1, library=None, batch_max=64,
+                 batch_rows=32768):
         self.slots = slots
         self.runner = runner or run_request
         self.budget = float(budget_bytes)
@@ -224,6 +282,8 @@ class Server:
         self.rtol = rtol
         self.keep = keep_solutions
         self.policy = policy
+        self.batch_max = batch_max if runner is None else 1
+        self.batch_rows = batch_rows
         self.library = library or MeshLibrary()
         self.ctxs = [(ctx_factory or (lambda: Context(device)))() for _ in range(slots)]
         # each slot caches geometries up to its share of cache_fraction of the
@@ -260,27 +320,45 @@ class Server:
                 self.pending.append(req)
             self.lock.notify_all()
 
+    def _batchable(self, r):
+        return self.batch_max > 1 and r.form == "poisson" and r.rows <= self.batch_rows
+
+    def _pop_next(self):
+        """the next request by the policy if the budget has room for it"""
+        if not self.pending:
+            return None
+        r = self.pending[0][3] if self.policy == "sjf" else self.pending[0]
+        if self.in_use + self.reserved + r.est_bytes(self.precision) > self.budget:
+            return None
+        if self.policy == "sjf":
+            heapq.heappop(self.pending)
+        else:
+            self.pending.popleft()
+        self.in_use += r.est_bytes(self.precision)
+        r.admitted = self._now()
+        return r
+
     def _take(self):
+        """a list of requests to run together (one, or a batch of small
+        scalar ones) and their budget bytes"""
         with self.lock:
             while True:
                 if self.deadline is not None and self._now() >= self.deadline:
                     return None, 0
-                # the next request by the policy, admitted once the budget has
-                # room for it (else wait for running requests to finish)
-                r = None
-                if self.pending:
-                    r = self.pending[0][3] if self.policy == "sjf" else self.pending[0]
-                    if self.in_use + self.reserved + r.est_bytes(self.precision) > self.budget:
-                        r = None
+                r = self._pop_next()
                 if r is not None:
-                    if self.policy == "sjf":
-                        heapq.heappop(self.pending)
-                    else:
-                        self.pending.popleft()
-                    need = r.est_bytes(self.precision)
-                    self.in_use += need
-                    r.admitted = self._now()
-                    return r, need
+                    got = [r]
+                    if self._batchable(r):
+                        # the small scalar requests at the head of the queue join it
+                        while len(got) < self.batch_max and self.pending:
+                            nxt = self.pending[0][3] if self.policy == "sjf" else self.pending[0]
+                            if not self._batchable(nxt):
+                                break
+                            q = self._pop_next()
+                            if q is None:
+                                break
+                            got.append(q)
+                    return got, sum(q.est_bytes(self.precision) for q in got)
                 if self.closed and not self.pending:
                     return None, 0
                 self.lock.wait(0.01)
@@ -289,25 +367,31 @@ class Server:
         ctx = self.ctxs[slot]
         cache = self.caches[slot]
         while True:
-            req, need = self._take()
-            if req is None:
+            reqs, need = self._take()
+            if reqs is None:
                 return
             try:
-                if cache is not None:
-                    self.runner(req, ctx, self.precision, self.rtol, self.keep, cache=cache, library=self.library)
+                if self._batchable(reqs[0]):  # a batch of one too: the result never depends on the batch
+                    run_batch_requests(reqs, ctx, self.precision, self.rtol, self.keep, cache=cache,
+                                       library=self.library)
+                elif cache is not None:
+                    self.runner(reqs[0], ctx, self.precision, self.rtol, self.keep, cache=cache, library=self.library)
                 else:
-                    self.runner(req, ctx, self.precision, self.rtol, self.keep)
+                    self.runner(reqs[0], ctx, self.precision, self.rtol, self.keep)
             except Exception as e:  # a failed request is reported, the server continues
-                req.status = getattr(e, "code", _lib.GT_ERR_CUDA)
-                self.errors.append((req.rid, repr(e)))
-            req.finished = self._now()
+                for req in reqs:
+                    req.status = getattr(e, "code", _lib.GT_ERR_CUDA)
+                self.errors.append((reqs[0].rid, repr(e)))
+            now = self._now()
+            for req in reqs:
+                req.finished = now
             # pooled blocks of a finished request are not counted against the
             # budget, so hand large pools back to the driver
             if ctx is not None and hasattr(ctx, "memory") and ctx.memory()[1] > self.budget / (4 * self.slots):
                 ctx.trim()
             with self.lock:
                 self.in_use -= need
-                self.done.append(req)
+                self.done.extend(reqs)
                 self.lock.notify_all()
 
     def serve(self, requests, realtime=True, duration=None):

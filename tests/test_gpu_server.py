@@ -52,3 +52,24 @@ def test_serving_window_reports_pending():
     fed = sum(1 for r in reqs if r.arrival < 0.05)
     assert rep["completed"] + rep["pending_at_end"] + rep["failed"] + rep["refused_budget"] == fed
     assert rep["pending_at_end"] > 0
+
+
+def test_batched_small_requests_with_shared_geometry():
+    """Small Poisson requests pending together are solved in one persistent
+    launch; requests on the same geometry in one batch each take their own
+    resident instance.  Every result is bitwise that of the request served
+    alone, and within 1e-10 in residual."""
+    from gtgpu.server import Request
+    def reqs():
+        return [Request(i, 0.0, "poisson", 1 + (i % 2), 9 if i % 2 == 0 else 5, 300 + i) for i in range(8)]
+    together, alone = reqs(), reqs()
+    s1 = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo")
+    rep = s1.serve(together, realtime=False)
+    s2 = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo", batch_max=1)
+    s2.serve(alone, realtime=False)
+    assert rep["completed"] == 8
+    for a, b in zip(together, alone):
+        assert a.rel_residual <= 1e-10
+        assert np.array_equal(a.solution, b.solution)
+    s1.close()
+    s2.close()
