@@ -110,6 +110,10 @@ def run_elasticity(args):
     _, _, v64 = A.csr()
     res["fp32_values_rel_err_vs_fp64"] = float(np.abs(v32 - v64).max() / np.abs(v64).max())
     del A32, v32
+    if args.no_solve:
+        out.update({"assembly": res, "nnz": int(nnz)})
+        print(json.dumps(out), flush=True)
+        return
     sol = {}
     xs = {}
     for mode in ("fp64", "ir"):

@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, co
           buf ^= 1;
           beta = rzold != 0.0 ? v[0] / rzold : 0.0;
           // the recurrence lost track of the true residual: restart the directions
-          if (v[0] > kRestartRatio * rz) beta = 0.0;
+          if (v[0] > (sizeof(X) == sizeof(double) ? kRestartRatio64 : kRestartRatio) * rz) beta = 0.0;
           const double prev = rmax2;
           rz = v[0];
           rr = v[1];

@@ -319,8 +319,13 @@ int solve(Matrix* A, const double* b, double* x, double rtol, int maxit, int mod
 constexpr int kSlowCycle = 1000;
 // A true-residual check whose r.z exceeds the recurrence's by this factor
 // restarts the CG directions from the true residual (beta = 0): the
-// recurrence has drifted (FP64 past its attainable accuracy, or FP32).
+// recurrence has drifted.  kRestartRatio64 for the FP64 iteration, whose
+// checks come only when the recurrence claims convergence (a mismatch there
+// means the recurrence ran past the attainable accuracy, and scaling the
+// old direction by it corrupts the iteration), kRestartRatio for the
+// periodic reliable updates of the FP32 iteration.
 constexpr double kRestartRatio = 100.0;
+constexpr double kRestartRatio64 = 4.0;
 // FP64 CG ends (not converged) after this many true-residual checks in a row
 // that did not halve the residual norm: the tolerance is below what
 // eps64 * cond(A) allows.

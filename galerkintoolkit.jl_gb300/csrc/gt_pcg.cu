@@ -372,7 +372,7 @@ __global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
         // its attainable accuracy, or FP32 drift): the next direction
         // restarts from the true residual instead of scaling the old one by
         // the true/recurrence mismatch
-        if (s_tot[0] > kRestartRatio * S.rz) beta = 0.0;
+        if (s_tot[0] > (sizeof(X) == sizeof(double) ? kRestartRatio64 : kRestartRatio) * S.rz) beta = 0.0;
         const double prev = S.rmax2;
         S.rz = s_tot[0];
         S.rr = s_tot[1];

@@ -963,7 +963,8 @@ __global__ void __launch_bounds__(RED_T) k_rl_resid(const int64_t* __restrict__ 
     // the next direction is built from the true residual
     st->beta = st->rzold != 0.0 ? v[0] / st->rzold : 0.0;
     // the recurrence lost track of the true residual: restart the directions
-    if (st->nupd > 0 && v[0] > kRestartRatio * st->rz) st->beta = 0.0;
+    if (st->nupd > 0 && v[0] > (sizeof(X) == sizeof(double) ? kRestartRatio64 : kRestartRatio) * st->rz)
+      st->beta = 0.0;
     const double prev = st->rmax2;
     st->rz = v[0];
     st->rr = v[1];
