@@ -219,7 +219,10 @@ __global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
     cta_sum<2>(v, s_red, slot2 + (size_t)blk * PSLOT);
     if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
     grid_total<2>(slot2, nb, s_red, s_tot);
-    const X bx = (X)(S.rzold != 0.0 ? s_tot[0] / S.rzold : 0.0);
+    // the FP32 direction is kept unless the FP32 recurrence has drifted from
+    // the true residual (then the FP64 iteration restarts from it)
+    const bool drifted = s_tot[0] > kRestartRatio64 * S.rz;
+    const X bx = (X)(S.rzold != 0.0 && !drifted ? s_tot[0] / S.rzold : 0.0);
     for (int64_t i = e0 + tid; i < e1; i += PT) p[i] = z[i] + bx * (X)a.pcont[i];
     S.rz = s_tot[0];
     S.rr = s_tot[1];
