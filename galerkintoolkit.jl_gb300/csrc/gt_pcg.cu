@@ -192,9 +192,9 @@ __global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
   __syncthreads();
 
   if (init == 2) {
-    // continuation of an FP32 run in FP64: x holds the FP64 solution, pcont
-    // the FP32 direction; r = b - A x, z = Dinv r, p = z + beta pcont with
-    // beta = r.z / rzold, so the Krylov direction carries over
+    // continuation of a stalled FP32 run in FP64: x holds the FP64
+    // solution; r = b - A x, z = Dinv r, p = z (the iteration count and
+    // ||b|| carry over)
     double v[2] = {0.0, 0.0};
     for (int64_t base = r0; base < r1; base += NG) {
       int64_t row = base + grp;
@@ -219,11 +219,11 @@ __global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
     cta_sum<2>(v, s_red, slot2 + (size_t)blk * PSLOT);
     if (!grid_sync(a.bar, (++nbar) * nb, a.err, &s_abort)) return;
     grid_total<2>(slot2, nb, s_red, s_tot);
-    // the FP32 direction is kept unless the FP32 recurrence has drifted from
-    // the true residual (then the FP64 iteration restarts from it)
-    const bool drifted = s_tot[0] > kRestartRatio64 * S.rz;
-    const X bx = (X)(S.rzold != 0.0 && !drifted ? s_tot[0] / S.rzold : 0.0);
-    for (int64_t i = e0 + tid; i < e1; i += PT) p[i] = z[i] + bx * (X)a.pcont[i];
+    // the FP64 iteration restarts from the true residual (p = z): the FP32
+    // run stalled, so its direction no longer fits the true residual, and
+    // continuing it made the FP64 recurrence stagnate or diverge at
+    // tolerances near the attainable accuracy (measured)
+    for (int64_t i = e0 + tid; i < e1; i += PT) p[i] = z[i];
     S.rz = s_tot[0];
     S.rr = s_tot[1];
     S.rmax2 = S.rr;
