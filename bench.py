@@ -241,7 +241,7 @@ def run_serving(args):
     lib = MeshLibrary(r.cells_per_dir for r in reqs0)  # untimed: the pre-built meshes
     res = {}
     arms = (("mixed", args.slots, "mixed", {}), ("fp64", args.slots, "fp64", {}),
-            ("plain_fp64", 1, "fp64", {"cache_fraction": 1e-12, "batch_max": 1}))
+            ("plain_fp64", 1, "fp64", {"cache_fraction": 1e-12, "batching": False}))
     for name, slots, prec, kw in arms:
         reqs = request_stream(n, rate=rate, seed=505)
         srv = Server(slots=slots, budget_bytes=args.budget_gb * 1e9, precision=prec, rtol=1e-10,

@@ -273,8 +273,8 @@ def run_batch_requests(reqs, ctx: Context, precision="mixed", rtol=1e-8, keep_so
 
 class Server:
     def __init__(self, slots=4, budget_bytes=150e9, precision="mixed", rtol=1e-8, device=0, keep_solutions=True,
-                 ctx_factory=None, runner=None, policy="sjf", cache_fraction=0.1, library=None, batch_max=64,
-                 batch_rows=32768):
+                 ctx_factory=None, runner=None, policy="sjf", cache_fraction=0.1, library=None, batching=True,
+                 batch_max=64, batch_rows=32768):
         self.slots = slots
         self.runner = runner or run_request
         self.budget = float(budget_bytes)
@@ -282,7 +282,11 @@ class Server:
         self.rtol = rtol
         self.keep = keep_solutions
         self.policy = policy
-        self.batch_max = batch_max if runner is None else 1
+        # small scalar requests go through the batched kernel (alone or
+        # with others, up to batch_max); batching=False: one grid-wide solve
+        # per request
+        self.batching = batching and runner is None
+        self.batch_max = max(1, batch_max)
         self.batch_rows = batch_rows
         self.library = library or MeshLibrary()
         self.ctxs = [(ctx_factory or (lambda: Context(device)))() for _ in range(slots)]
@@ -321,7 +325,7 @@ class Server:
             self.lock.notify_all()
 
     def _batchable(self, r):
-        return self.batch_max > 1 and r.form == "poisson" and r.rows <= self.batch_rows
+        return self.batching and r.form == "poisson" and r.rows <= self.batch_rows
 
     def _pop_next(self):
         """the next request by the policy if the budget has room for it"""
