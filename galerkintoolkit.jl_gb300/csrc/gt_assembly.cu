@@ -2312,6 +2312,10 @@ __global__ void k_scatter_uniform(const int64_t* __restrict__ rowptr, const int3
     // load; later incidences (a node in more than PF cells) load in the loop
     const int nin = (int)(ie - ib);
     const int32_t my_cb = gl < nin ? __ldg(inc + ib + gl) : 0;
+    // each incidence's scale |det J| coef_c computed by one lane and handed
+    // to the group by shuffles (a conversion per lane would load the FP64
+    // pipe, which also converts FP64 to FP32)
+    const T my_sc = (T)(adet * ((coef && gl < nin) ? __ldg(coef + my_cb / NN) : 1.0));
     int32_t cbk[PF], jk[PF], pk[PF];
     T sck[PF];
 #pragma unroll
@@ -2319,7 +2323,7 @@ __global__ void k_scatter_uniform(const int64_t* __restrict__ rowptr, const int3
       cbk[k] = __shfl_sync(gmask, my_cb, k, G);
       const int32_t c = cbk[k] / NN;
       jk[k] = (k < nin && b < NN) ? __ldg(cnd + (int64_t)c * NN + b) : 0;
-      sck[k] = (T)(adet * ((coef && k < nin) ? __ldg(coef + c) : 1.0));
+      sck[k] = __shfl_sync(gmask, my_sc, k, G);
     }
 #pragma unroll
     for (int k = 0; k < PF; k++) pk[k] = jk[k] > 0 ? find_col(cols, L, jk[k] - 1) : -1;
