@@ -40,7 +40,7 @@ static inline Ctx* ctx_of(const Space* sp) { return sp->mesh->ctx; }
 struct TabLayout {
   int D, nlv, nn, nq;
   int off_w, off_gg, off_sv, off_sg;
-  int off_k;  // 32 doubles of per-reference-cell quadrature sums (P1 path)
+  int off_k;  // 48 doubles of per-reference-cell quadrature sums (P1 path): 22 FP64 sums, then FP32-pair splits
   int off_gv;  // geometry shape values at the points (nq x nlv), past the kernels' staged part
   int total;
 };
@@ -57,7 +57,7 @@ inline TabLayout tab_layout(int ctype, int order) {
   L.off_sv = L.off_gg + L.nq * L.nlv * L.D;
   L.off_sg = L.off_sv + L.nq * L.nn;
   L.off_k = L.off_sg + L.nq * L.nn * L.D;
-  L.off_gv = L.off_k + 32;
+  L.off_gv = L.off_k + 48;
   L.total = L.off_gv + L.nq * L.nlv;
   return L;
 }
@@ -1152,6 +1152,23 @@ __global__ void k_p1_consts(const double* __restrict__ tab, TabLayout L, double*
 #pragma unroll
   for (int n = 0; n < 4; n++) b[n] = __double_as_longlong(__shfl_sync(0xffffffffu, s, n + 1));
   if (t == 21) k[t] = (b[0] == b[1] && b[0] == b[2] && b[0] == b[3]) ? 1.0 : 0.0;
+  // the sums as FP32 pairs for the double-float kernel (from k[24] on, as
+  // floats): [0,1] sum w, [2..9] the four load sums, [10..29] the ten
+  // upper-triangle mass sums in the packed order
+  float* kf = reinterpret_cast<float*>(k + 24);
+  if (t < 5) {
+    const dfl v = df_from_double(s);
+    kf[2 * t] = v.hi;
+    kf[2 * t + 1] = v.lo;
+  } else if (t < 21) {
+    const int n = (t - 5) >> 2, m = (t - 5) & 3;
+    if (n <= m) {
+      const int e = n * 4 - ((n * (n - 1)) >> 1) + (m - n);
+      const dfl v = df_from_double(s);
+      kf[10 + 2 * e] = v.hi;
+      kf[11 + 2 * e] = v.lo;
+    }
+  }
 }
 
 template <int FORM, class T>
@@ -1262,18 +1279,16 @@ __global__ void __launch_bounds__(256) k_elements_p1_df(const double* __restrict
                                                         double* __restrict__ be, const double* __restrict__ fsrc,
                                                         const double* __restrict__ scoef, int want_matrix,
                                                         uint32_t* err) {
-  const dfl wsum = df_from_double(__ldg(consts));
+  // the reference-cell sums as FP32 pairs, split once by k_p1_consts
+  const float* kf = reinterpret_cast<const float*>(consts + 24);
+  const dfl wsum = {__ldg(kf), __ldg(kf + 1)};
   const bool load_equal = __double_as_longlong(__ldg(consts + 21)) != 0;
-  const dfl f0 = df_from_double(fsrc ? __ldg(fsrc) : 0.0);
   dfl sload[4], smass[10];
 #pragma unroll
-  for (int n = 0; n < 4; n++) sload[n] = df_from_double(__ldg(consts + 1 + n));
+  for (int n = 0; n < 4; n++) sload[n] = {__ldg(kf + 2 + 2 * n), __ldg(kf + 3 + 2 * n)};
   if (FORM == GT_MASS) {
-    int e = 0;
 #pragma unroll
-    for (int n = 0; n < 4; n++)
-#pragma unroll
-      for (int m = n; m < 4; m++) smass[e++] = df_from_double(__ldg(consts + 5 + n * 4 + m));
+    for (int e = 0; e < 10; e++) smass[e] = {__ldg(kf + 10 + 2 * e), __ldg(kf + 11 + 2 * e)};
   }
   const dfl one = {1.0f, 0.0f};
   for (int64_t c = c_begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells;
@@ -1325,6 +1340,7 @@ __global__ void __launch_bounds__(256) k_elements_p1_df(const double* __restrict
       for (int e = 0; e < 10; e++) K[e] = df_to_double(k[e]);
     }
     if (be) {
+      const dfl f0 = fsrc ? df_from_double(__ldg(fsrc)) : dfl{0.0f, 0.0f};  // only with a load vector
       const dfl sc = df_mul(scoef ? df_mul(df_from_double(scoef[c]), f0) : f0, adet);
       if (load_equal) {
         const double v = df_to_double(df_mul(sc, sload[0]));
