@@ -52,7 +52,8 @@ extern "C" {
 /* precision of the assembled values */
 #define GT_FP64 0  /* FP64 integration, FP64 values */
 #define GT_FP32 1  /* FP64 Jacobian inverse/determinant, FP32 element matrix and values */
-#define GT_MIXED 2 /* FP64 integration, FP64 values plus an FP32 copy sharing the index arrays */
+#define GT_MIXED 2 /* FP64-integrated FP64 values (the outer residual) plus FP32-integrated
+                      FP32 values (the inner CG), sharing the index arrays */
 
 /* solve modes */
 /* Convergence of GT_SOLVE_FP64 and GT_SOLVE_IR is decided on the FP64 true
@@ -198,8 +199,10 @@ int gt_update_matrix(gt_matrix* matrix, int form, const double* cell_coef, doubl
  * process whose device memory is budgeted up front by its own admission
  * control or memory pool, or a latency-critical refill loop where
  * cudaMalloc/cudaFree can synchronise the device).  Refills the values of an
- * assembled matrix using one static 128 MiB device array as scratch;
- * cell_coef must be device memory or NULL; a refill needing more scratch
+ * assembled matrix using one static 128 MiB device array as scratch (a
+ * GT_MIXED matrix gets its FP32 values as the rounded FP64 values, in the
+ * same pass); cell_coef must be device memory of the matrix's device or
+ * NULL; a refill needing more scratch
  * than 128 MiB (tabulation + ncells*nloc^2 values) returns GT_ERR_INVALID.
  * The first call on a device looks up the array's address (make it before
  * any stream capture); every call waits for the context's stream before it
