@@ -43,12 +43,11 @@ SOLVE_RTOL = 1e-10   # relative residual of the headline solves (FP64 and mixed)
 SOLVE_SAMPLES = 100  # timed solves per mode (p50 / p99 latency)
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # DRAM bytes (read + write) per launch on the default workload (96^3 x 6 P1
-# tets), from ncu captures (summaries under profiles/): the element and
-# scatter kernels captured on 64^3 x 6 tets (1,572,864 cells) and scaled by
-# the cell ratio 3.375 (their traffic is proportional to the cells); the FP64
-# SpMV (sliced-ELL copy) captured on the full workload
-TRAFFIC: dict = {"elements": (44.357120e6 + 114.737920e6) * 3.375,
-                 "scatter": (244.073472e6 + 24.874752e6) * 3.375,
+# tets), from one-pass ncu captures of the full workload (summaries under
+# profiles/): the double-float element kernel, the scatter and the FP64 SpMV
+# (sliced-ELL copy)
+TRAFFIC: dict = {"elements": 155.32e6 + 537.38e6,
+                 "scatter": 826.07e6 + 96.52e6,
                  "spmv": 159.938048e6 + 5.819904e6}
 
 
@@ -595,16 +594,18 @@ def main():
                                               "frac": g / peaks["hbm_gbs"]}
     p1_dfloat = os.environ.get("GTGPU_P1") != "fp64"
     if dom == "elements" and p1_dfloat:
-        # double-float element arithmetic on the FP32 pipes: bounded by the
-        # kernel's HBM traffic (coordinates, cells, coefficient in; packed
-        # blocks and element vectors out) and by FP32 issue
+        # double-float element arithmetic on the FP32 pipes: the HBM roofline
+        # of the kernel's traffic (coordinates, cells, coefficient in; packed
+        # blocks and element vectors out); ncu shows it issue-bound
         achieved = alg["elements"] / (ph[dom] * 1e-3) / 1e9
         roof = {"bound": "hbm", "kernel": "k_elements_p1_df<Laplacian>", "achieved": achieved, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks_kind,
                 "algorithmic_bytes": alg["elements"], "traffic": TRAFFIC.get("elements"),
                 "arithmetic": "double-float (FP32 pairs, 48-bit) after FP64 differences x_i - x_0; "
                               f"{flops_el / (ph[dom] * 1e-3) / 1e12:.3f} TFLOP/s of FP64-equivalent work "
-                              f"(93 flops/cell) against the FP64 FMA rate {fp64_tf:.3f}"}
+                              f"(93 flops/cell) against the FP64 FMA rate {fp64_tf:.3f}",
+                "limiter": "instruction issue (ncu, 64^3 x 6: issue 71% active, FP64 pipe 33%, ALU 57%, "
+                           "DRAM 13%; profiles/k_elements_p1_df_p1tet64.md)"}
     elif dom == "elements":
         achieved = flops_el / (ph[dom] * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": "k_elements_p1<Laplacian, double>", "achieved": achieved,

@@ -82,6 +82,17 @@ __device__ __forceinline__ dfl df_recip(dfl x) {
   return r;
 }
 
+// The rare cases of the two conversions below, in FP64 arithmetic.  Out of
+// line on purpose: inlined, the compiler may if-convert them into the common
+// path, and their FP64 instructions would then issue (predicated off) for
+// every value converted.
+__device__ __noinline__ dfl df_from_double_rare(double x) {
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+
+__device__ __noinline__ double df_to_double_rare(float hi, float lo) { return (double)hi + (double)lo; }
+
 // FP64 -> double-float with integer instructions: hi takes the top 24
 // significand bits of x (exact), lo the remaining 29 bits rounded to FP32.
 // Zeros stay integer too; other values outside |x| in [2^-74, 2^127) take
@@ -92,10 +103,7 @@ __device__ __forceinline__ dfl df_from_double(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   if ((b << 1) == 0) return {__uint_as_float((unsigned)(b >> 32) & 0x80000000u), 0.0f};  // +-0
   const int e = (int)((b >> 52) & 0x7ff);
-  if (e < 949 || e > 1149) {
-    const float h = __double2float_rn(x);
-    return {h, __double2float_rn(x - (double)h)};
-  }
+  if (e < 949 || e > 1149) return df_from_double_rare(x);
   const unsigned sign = (unsigned)(b >> 63) << 31;
   const float hi = __uint_as_float(sign | ((unsigned)(e - 896) << 23) | (unsigned)((b >> 29) & 0x7fffffu));
   // remainder: (b & (2^29 - 1)) * 2^(e - 1075); the scale is a normal FP32 power of two
@@ -113,7 +121,7 @@ __device__ __forceinline__ double df_to_double(dfl v) {
   if ((hb << 1) == 0 && (lb << 1) == 0) return __longlong_as_double((long long)(hb >> 31) << 63);  // +-0
   const int eh = (int)((hb >> 23) & 0xff), el = (int)((lb >> 23) & 0xff);
   if (eh == 0 || eh == 255 || (el == 0 && (lb & 0x7fffffffu) != 0))
-    return (double)v.hi + (double)v.lo;  // zero, subnormal or non-finite parts: FP64 arithmetic
+    return df_to_double_rare(v.hi, v.lo);  // zero, subnormal or non-finite parts: FP64 arithmetic
   // hi = mh * 2^(eh - 150), unit of the sum: 2^(eh - 179)
   long long H = (long long)((hb & 0x7fffffu) | 0x800000u) << 29;
   if (hb >> 31) H = -H;
