@@ -228,10 +228,10 @@ def run_serving(args):
     load is far above what one GPU completes, so the window, not a request
     count, bounds the run).  Arms: the served path in mixed precision and
     in FP64 (--slots slots, geometries kept resident and values refilled on
-    a repeat, small Poisson requests solved in batches of up to 64 in one
-    persistent launch), and the plain FP64 path (one slot, no resident
-    state, one solve per request).  Host meshes come from a library built
-    before the stream.
+    a repeat, requests of up to 2048 scalar rows solved in batches of up to
+    16 in one persistent launch, coefficients generated on the device), and
+    the plain FP64 path (one slot, no resident state, one solve per
+    request).  Host meshes come from a library built before the stream.
     p50/p99 latency = arrival -> result, over the completed requests."""
     from gtgpu.server import MeshLibrary, Server, request_stream
     rate, dur = 2000.0, args.serve_seconds

@@ -1702,10 +1702,8 @@ __device__ __forceinline__ void row_load_sum(const int64_t ib, int64_t ie, const
 // With be != nullptr the group also sums the element vectors of the row's
 // incidences (row_load_sum), then lane 0 subtracts the Dirichlet lift of
 // each incidence in ascending order (when xd), and writes bvec.
-// PK: element matrices stored packed (the upper triangle of a symmetric
-// 4 x 4 block per cell, scalar P1 tetrahedra); entry (a, b) is read from
-// (min, max) of the pair.
-template <int BS, int G, class TK, class TA, bool PK>
+// (Scalar P1 tetrahedra, whose blocks are stored packed, take k_scatter_p1.)
+template <int BS, int G, class TK, class TA>
 __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                           const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                           const int32_t* __restrict__ cnd, int nn_arg, int64_t row_begin, int64_t row_end,
@@ -1714,9 +1712,7 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
                           const double* __restrict__ xd) {
   extern __shared__ __align__(16) unsigned char s_raw[];
   constexpr int RPW = 32 / G;  // rows per warp
-  // packed blocks are P1 tetrahedra: 4 nodes per cell, known at compile time
-  // (the incidence decode cell = e / nn, node = e % nn is then a shift)
-  const int nn = PK ? 4 : nn_arg;
+  const int nn = nn_arg;
   const int nloc = nn * BS;
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int sub = lane / G, gl = lane - sub * G;
@@ -1762,13 +1758,7 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
           int32_t cb = __ldg(inc + k);
           int32_t c = cb / nn, a = cb - c * nn;
           jj[u] = __ldg(cnd + (int64_t)c * nn + b);
-          const TK* Krow;
-          if constexpr (PK) {
-            const int lo = a < b ? a : b, hi = a ^ b ^ lo;
-            Krow = Ke + (int64_t)c * 10 + (lo * 4 - ((lo * (lo - 1)) >> 1)) + (hi - lo);
-          } else {
-            Krow = Ke + (int64_t)c * nloc * nloc + (int64_t)(a * BS) * nloc + b * BS;
-          }
+          const TK* Krow = Ke + (int64_t)c * nloc * nloc + (int64_t)(a * BS) * nloc + b * BS;
 #pragma unroll
           for (int cc = 0; cc < BS; cc++)
 #pragma unroll
@@ -1816,6 +1806,101 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
   }
 }
 
+// Scalar P1 tetrahedra (packed blocks: the upper triangle of the symmetric
+// 4 x 4 block, 10 entries per cell): the row-owner scatter of k_scatter,
+// specialised.  Four lanes own a row, lane b the local column node b of
+// every incidence.  Incidences are taken U at a time: their loads are
+// issued together; their column positions come from branchless binary
+// searches advanced in lock step (the row's length fixes the number of
+// steps, so the U searches overlap instead of running one after the other);
+// then the U contributions are added in ascending incidence order with a
+// group barrier between them -- the summation order of k_scatter, so the
+// values are bitwise those of the generic kernel.  LIFT (the Dirichlet lift
+// b -= Ad xd) is a compile-time choice, so the common case carries none of
+// its FP64 code.
+template <class TK, class TA, bool LIFT>
+__global__ void __launch_bounds__(128) k_scatter_p1(const int64_t* __restrict__ rowptr,
+                                                    const int32_t* __restrict__ colind,
+                                                    const int64_t* __restrict__ inc_ptr,
+                                                    const int32_t* __restrict__ inc, const int32_t* __restrict__ cnd,
+                                                    int /* nodes per cell: 4 */, int64_t row_begin, int64_t row_end,
+                                                    int lmax,
+                                                    const TK* __restrict__ Ke, double* __restrict__ v64,
+                                                    float* __restrict__ v32, const double* __restrict__ be,
+                                                    double* __restrict__ bvec, const double* __restrict__ xd) {
+  extern __shared__ __align__(16) unsigned char s_raw[];
+  constexpr int G = 4, RPW = 8, U = 8;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int sub = lane >> 2, b = lane & 3;
+  const int slot = w * RPW + sub;
+  TA* acc = (TA*)s_raw + (size_t)slot * lmax;
+  int32_t* cols = (int32_t*)((TA*)s_raw + (size_t)(blockDim.x / G) * lmax) + (size_t)slot * lmax;
+  const int64_t r = row_begin + ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * RPW + sub;
+  if (r >= row_end) return;  // the group's four lanes leave together
+  const unsigned gmask = 0xfu << (sub * G);
+  // packed offset of entry (a, b) for this lane's b, one nibble per a:
+  // (min, max) of the pair in the row-by-row upper triangle
+  unsigned offs = 0;
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const int lo = a < b ? a : b, hi = a ^ b ^ lo;
+    offs |= (unsigned)(lo * 4 - ((lo * (lo - 1)) >> 1) + (hi - lo)) << (4 * a);
+  }
+  const int64_t rb = rowptr[r];
+  const int L = (int)(rowptr[r + 1] - rb);
+  for (int i = b; i < L; i += G) {
+    cols[i] = colind[rb + i];
+    acc[i] = (TA)0;
+  }
+  __syncwarp(gmask);
+  const int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
+  double bsum = 0.0;
+  if (be != nullptr) row_load_sum<1>(ib, ie, inc, 4, be, b, gmask, &bsum);
+  for (int64_t k0 = ib; k0 < ie; k0 += U) {
+    int32_t jj[U], key[U];
+    int pos[U];
+    TA kv[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      jj[u] = 0;
+      kv[u] = (TA)0;
+      if (k0 + u < ie) {
+        const int32_t cb = __ldg(inc + k0 + u);
+        const int32_t c = cb >> 2, a = cb & 3;
+        jj[u] = __ldg(cnd + (int64_t)c * 4 + b);
+        kv[u] = (TA)__ldg(Ke + (int64_t)c * 10 + ((offs >> (4 * a)) & 15u));
+      }
+      key[u] = jj[u] > 0 ? jj[u] - 1 : INT_MIN;  // INT_MIN: stays at position 0, unused
+      pos[u] = 0;
+    }
+    // last position whose column is <= key: the column's own position
+    for (int n = L; n > 1;) {
+      const int half = n >> 1;
+#pragma unroll
+      for (int u = 0; u < U; u++) pos[u] = cols[pos[u] + half] <= key[u] ? pos[u] + half : pos[u];
+      n -= half;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      if (jj[u] > 0) acc[pos[u]] += kv[u];
+      if constexpr (LIFT) {
+        double lv = 0.0;
+        if (jj[u] < 0) lv += (double)kv[u] * __ldg(xd - jj[u] - 1);
+        lv += __shfl_xor_sync(gmask, lv, 2);
+        lv += __shfl_xor_sync(gmask, lv, 1);
+        if (b == 0) bsum -= lv;
+      }
+      __syncwarp(gmask);
+    }
+  }
+  for (int i = b; i < L; i += G) {
+    const TA v = acc[i];
+    if (v64) v64[rb + i] = (double)v;
+    if (v32) v32[rb + i] = (float)v;
+  }
+  if (be != nullptr && b == 0) bvec[r] = bsum;
+}
+
 template <int BS, class TK, class TA>
 static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, const double* be, double* bvec,
                           const double* xd, int64_t r0, int64_t r1) {
@@ -1841,11 +1926,14 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
     bool done = false;
     if constexpr (BS == 1 && G == 4) {
       if (ke_packed(sp)) {
-        launch(k_scatter<1, 4, TK, TA, true>);
+        if (xd != nullptr && be != nullptr)
+          launch(k_scatter_p1<TK, TA, true>);
+        else
+          launch(k_scatter_p1<TK, TA, false>);
         done = true;
       }
     }
-    if (!done) launch(k_scatter<BS, G, TK, TA, false>);
+    if (!done) launch(k_scatter<BS, G, TK, TA>);
     GT_LAUNCH(ctx, "k_scatter");
     return GT_OK;
   };
@@ -2275,7 +2363,7 @@ __global__ void k_kref(const double* __restrict__ gref, T lamf, T muf, T* __rest
     for (int dd = 0; dd < BS; dd++) kref[(size_t)ab * BS * BS + cc * BS + dd] = blk[cc][dd];
 }
 
-template <int D, int ORDER, int BS, int G, class T>
+template <int D, int ORDER, int BS, int G, class T, bool LIFT>
 __global__ void k_scatter_uniform(const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colind,
                                   const int64_t* __restrict__ inc_ptr, const int32_t* __restrict__ inc,
                                   const int32_t* __restrict__ cnd, int64_t nrows, int lmax,
@@ -2302,7 +2390,6 @@ __global__ void k_scatter_uniform(const int64_t* __restrict__ rowptr, const int3
   int32_t* cols = (int32_t*)((T*)(s_raw + KREF_BYTES) + (size_t)(blockDim.x / G) * lmax * KB) + (size_t)slot * lmax;
   const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (sub * G));
   const bool vec = be != nullptr && gl == 0;
-  const bool lift = be != nullptr && xd != nullptr;
   const int b = gl;
   const int64_t nblk = (nrows + (int64_t)nw * RPW - 1) / ((int64_t)nw * RPW);
   for (int64_t blk = blockIdx.x; blk < nblk; blk += gridDim.x) {
@@ -2343,51 +2430,50 @@ __global__ void k_scatter_uniform(const int64_t* __restrict__ rowptr, const int3
     }
 #pragma unroll
     for (int k = 0; k < PF; k++) pk[k] = jk[k] > 0 ? find_col(cols, L, jk[k] - 1) : -1;
-    for (int k = 0; k < nin; k++) {
-      int32_t cb, j, p;
-      T sc;
-      if (k < PF) {
-        cb = cbk[0];
-        j = jk[0];
-        p = pk[0];
-        sc = sck[0];
-#pragma unroll
-        for (int u = 1; u < PF; u++)
-          if (k == u) { cb = cbk[u]; j = jk[u]; p = pk[u]; sc = sck[u]; }
-      } else {
-        cb = __ldg(inc + ib + k);
-        const int32_t c = cb / NN;
-        j = b < NN ? __ldg(cnd + (int64_t)c * NN + b) : 0;
-        p = j > 0 ? find_col(cols, L, j - 1) : -1;
-        sc = (T)(adet * (coef ? __ldg(coef + c) : 1.0));
-      }
+    // incidence cb's block: row node a, this lane's column node b (column
+    // DOF j, position p), scale sc; then the group barrier that keeps the
+    // summation order
+    auto contribute = [&](int32_t cb, int32_t j, int p, T sc) {
       const int32_t a = cb - (cb / NN) * NN;
       double lv[BS];
 #pragma unroll
       for (int cc = 0; cc < BS; cc++) lv[cc] = 0.0;
       if (b < NN) {
-        if (j > 0 || (j < 0 && lift)) {
-          const T* kr = s_ref + (size_t)(a * NN + b) * KB;
-          if (j > 0) {
+        const T* kr = s_ref + (size_t)(a * NN + b) * KB;
+        if (j > 0) {
 #pragma unroll
-            for (int e = 0; e < KB; e++) acc[p * KB + e] += sc * kr[e];
-          } else {
+          for (int e = 0; e < KB; e++) acc[p * KB + e] += sc * kr[e];
+        } else if (LIFT && j < 0) {
 #pragma unroll
-            for (int cc = 0; cc < BS; cc++)
+          for (int cc = 0; cc < BS; cc++)
 #pragma unroll
-              for (int dd = 0; dd < BS; dd++)
-                lv[cc] += (double)(sc * kr[cc * BS + dd]) * __ldg(xd + (int64_t)(-j - 1) * BS + dd);
-          }
+            for (int dd = 0; dd < BS; dd++)
+              lv[cc] += (double)(sc * kr[cc * BS + dd]) * __ldg(xd + (int64_t)(-j - 1) * BS + dd);
         }
       }
-      if (lift)
+      if constexpr (LIFT) {
 #pragma unroll
         for (int cc = 0; cc < BS; cc++) {
 #pragma unroll
           for (int o = G >> 1; o; o >>= 1) lv[cc] += __shfl_xor_sync(gmask, lv[cc], o);
           if (gl == 0) bsum[cc] -= lv[cc];
         }
+      }
       __syncwarp(gmask);
+    };
+    // the prefetched incidences (indices known at compile time), then the
+    // rest -- a node in more than PF cells, none on a structured mesh -- in
+    // a loop of their own, so that their FP64 scale computation stays out
+    // of the common path
+#pragma unroll
+    for (int k = 0; k < PF; k++)
+      if (k < nin) contribute(cbk[k], jk[k], pk[k], sck[k]);
+    for (int k = PF; k < nin; k++) {
+      const int32_t cb = __ldg(inc + ib + k);
+      const int32_t c = cb / NN;
+      const int32_t j = b < NN ? __ldg(cnd + (int64_t)c * NN + b) : 0;
+      const int p = j > 0 ? find_col(cols, L, j - 1) : -1;
+      contribute(cb, j, p, (T)(adet * (coef ? __ldg(coef + c) : 1.0)));
     }
     const int64_t ob = rb * KB;
     for (int i = gl; i < L * KB; i += G) {
@@ -2426,7 +2512,8 @@ static int launch_uniform(Matrix* A, const double* gref, const double* coef, dou
   while (warps > 1 && KREF_BYTES + (size_t)warps * RPW * per_row > 210 * 1024) warps >>= 1;
   size_t smem = KREF_BYTES + (size_t)warps * RPW * per_row;
   if (smem > 210 * 1024) return GT_ERR_UNSUPPORTED;
-  auto kern = k_scatter_uniform<D, ORDER, BS, G, T>;
+  auto kern = (be != nullptr && xd != nullptr) ? k_scatter_uniform<D, ORDER, BS, G, T, true>
+                                               : k_scatter_uniform<D, ORDER, BS, G, T, false>;
   GT_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   GT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem));

@@ -1,7 +1,7 @@
 // gt_batch.cu -- many independent solves of uneven size in few launches.
 //
-// A batch holds n assembled scalar matrices (block size 1).  Instances are
-// split by size:
+// A batch holds n assembled matrices of block size 1 (scalar problems) or
+// 3 (3-D linear elasticity).  Instances are split by size (scalar rows):
 //
 //  * small instances (rows <= kSmallRows) are solved by ONE persistent
 //    launch: each CTA takes the next instance from a queue (largest first)
@@ -36,9 +36,10 @@ struct BInst {
   const int32_t* colind;
   const double* v64;
   const float* v32;
-  const int32_t* diag;  // position of the diagonal in each row
-  int64_t nrows;
-  int64_t off;          // offset of the instance in the concatenated vectors
+  const int32_t* diag;  // position of the diagonal block in each block row
+  int64_t nrows;        // block rows
+  int64_t off;          // offset of the instance in the concatenated vectors (scalar entries)
+  int32_t bs, pad;
 };
 
 // per-instance outcome of the batched kernel
@@ -88,10 +89,12 @@ __device__ __forceinline__ const V* inst_vals(const BInst& in) {
   else return (const V*)in.v32;
 }
 
-// One CTA per instance, instances from a queue.  V: values of the iteration,
-// X: vector type; REL: FP64 reliable updates (needs v64).  from_x: start
-// from the given x (else x = 0).
-template <int G, class V, class X, bool REL>
+// One CTA per instance, instances from a queue.  BS: block size of the
+// instances of the launch (G lanes per block row); V: values of the
+// iteration, X: vector type; REL: FP64 reliable updates (needs v64).
+// from_x: start from the given x (else x = 0).  Jacobi on the scalar
+// diagonal, as the single-system solver.
+template <int BS, int G, class V, class X, bool REL>
 __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, const int32_t* __restrict__ queue,
                                              int nq, int32_t* head, const double* __restrict__ b, double* x, X* xs,
                                              X* r, X* z, X* p, X* q, X* dinv, BRes* res, double rtol2, double delta2,
@@ -109,13 +112,15 @@ __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, co
     if (k >= nq) return;
     const int ii = queue[k];
     const BInst in = insts[ii];
-    const int64_t n = in.nrows, off = in.off;
+    const int64_t nb = in.nrows, n = nb * BS, off = in.off;
     const V* val = inst_vals<V>(in);
     const double* bi = b + off;
     double* xi = x + off;
     X *xsi = xs + off, *ri = r + off, *zi = z + off, *pi = p + off, *qi = q + off, *di = dinv + off;
     for (int64_t i = tid; i < n; i += BT) {
-      const int64_t pos = in.rowptr[i] + in.diag[i];
+      const int64_t br = i / BS;
+      const int c = (int)(i - br * BS);
+      const int64_t pos = (in.rowptr[br] + in.diag[br]) * BS * BS + c * BS + c;
       const double d = in.v64 ? in.v64[pos] : (double)in.v32[pos];
       di[i] = (X)(1.0 / d);
       if (!from_x) xi[i] = 0.0;
@@ -125,23 +130,27 @@ __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, co
     double rz, rr, bb;
     {
       double v[3] = {0.0, 0.0, 0.0};
-      for (int64_t base = 0; base < n; base += NG) {
+      for (int64_t base = 0; base < nb; base += NG) {
         int64_t row = base + grp;
-        const bool valid = row < n;
-        if (!valid) row = n - 1;
-        double o[1];
-        if constexpr (REL) row_dot<1, G, double, double, double, false>(in.rowptr, in.colind, in.v64, xi, row, gl, o);
-        else row_dot<1, G, V, double, double, false>(in.rowptr, in.colind, val, xi, row, gl, o);
+        const bool valid = row < nb;
+        if (!valid) row = nb - 1;
+        double o[BS];
+        if constexpr (REL) row_dot<BS, G, double, double, double, false>(in.rowptr, in.colind, in.v64, xi, row, gl, o);
+        else row_dot<BS, G, V, double, double, false>(in.rowptr, in.colind, val, xi, row, gl, o);
         if (gl == 0 && valid) {
-          const double bv = bi[row], rv = bv - o[0];
-          const X rx = (X)rv, zx = di[row] * rx;
-          ri[row] = rx;
-          zi[row] = zx;
-          pi[row] = zx;
-          xsi[row] = (X)0;
-          v[0] += (double)rx * (double)zx;
-          v[1] += rv * rv;
-          v[2] += bv * bv;
+#pragma unroll
+          for (int c = 0; c < BS; c++) {
+            const int64_t i = row * BS + c;
+            const double bv = bi[i], rv = bv - o[c];
+            const X rx = (X)rv, zx = di[i] * rx;
+            ri[i] = rx;
+            zi[i] = zx;
+            pi[i] = zx;
+            xsi[i] = (X)0;
+            v[0] += (double)rx * (double)zx;
+            v[1] += rv * rv;
+            v[2] += bv * bv;
+          }
         }
       }
       block_sum<3>(v, s_red[buf]);
@@ -159,23 +168,27 @@ __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, co
       double pq;
       {
         X acc = (X)0;
-        for (int64_t base = 0; base < n; base += 2 * NG) {
+        for (int64_t base = 0; base < nb; base += 2 * NG) {
           int64_t ra = base + grp, rb = base + NG + grp;
-          const bool va = ra < n, vb = rb < n;
-          if (!va) ra = n - 1;
-          if (!vb) rb = n - 1;
-          X oa[1], ob[1];
-          row_dot<1, G, V, X, X, false>(in.rowptr, in.colind, val, pi, ra, gl, oa);
-          row_dot<1, G, V, X, X, false>(in.rowptr, in.colind, val, pi, rb, gl, ob);
+          const bool va = ra < nb, vb = rb < nb;
+          if (!va) ra = nb - 1;
+          if (!vb) rb = nb - 1;
+          X oa[BS], ob[BS];
+          row_dot<BS, G, V, X, X, false>(in.rowptr, in.colind, val, pi, ra, gl, oa);
+          row_dot<BS, G, V, X, X, false>(in.rowptr, in.colind, val, pi, rb, gl, ob);
           if (gl == 0) {
-            if (va) {
-              qi[ra] = oa[0];
-              acc += oa[0] * pi[ra];
-            }
-            if (vb) {
-              qi[rb] = ob[0];
-              acc += ob[0] * pi[rb];
-            }
+            if (va)
+#pragma unroll
+              for (int c = 0; c < BS; c++) {
+                qi[ra * BS + c] = oa[c];
+                acc += oa[c] * pi[ra * BS + c];
+              }
+            if (vb)
+#pragma unroll
+              for (int c = 0; c < BS; c++) {
+                qi[rb * BS + c] = ob[c];
+                acc += ob[c] * pi[rb * BS + c];
+              }
           }
         }
         double v[1] = {(double)acc};
@@ -217,19 +230,23 @@ __global__ void __launch_bounds__(BT) k_bpcg(const BInst* __restrict__ insts, co
           }
           __syncthreads();
           double v[2] = {0.0, 0.0};
-          for (int64_t base = 0; base < n; base += NG) {
+          for (int64_t base = 0; base < nb; base += NG) {
             int64_t row = base + grp;
-            const bool valid = row < n;
-            if (!valid) row = n - 1;
-            double o[1];
-            row_dot<1, G, double, double, double, false>(in.rowptr, in.colind, in.v64, xi, row, gl, o);
+            const bool valid = row < nb;
+            if (!valid) row = nb - 1;
+            double o[BS];
+            row_dot<BS, G, double, double, double, false>(in.rowptr, in.colind, in.v64, xi, row, gl, o);
             if (gl == 0 && valid) {
-              const double rv = bi[row] - o[0];
-              const X rx = (X)rv, zx = di[row] * rx;
-              ri[row] = rx;
-              zi[row] = zx;
-              v[0] += (double)rx * (double)zx;
-              v[1] += rv * rv;
+#pragma unroll
+              for (int c = 0; c < BS; c++) {
+                const int64_t i = row * BS + c;
+                const double rv = bi[i] - o[c];
+                const X rx = (X)rv, zx = di[i] * rx;
+                ri[i] = rx;
+                zi[i] = zx;
+                v[0] += (double)rx * (double)zx;
+                v[1] += rv * rv;
+              }
             }
           }
           block_sum<2>(v, s_red[buf]);
@@ -293,7 +310,7 @@ struct gt_batch : gt::BatchImpl {};
 namespace gt {
 
 template <class V, class X, bool REL>
-static int launch_small_g(gt_batch* B, int G, const std::vector<int>& ids, const double* b, double* x, double rtol,
+static int launch_small_g(gt_batch* B, int bs, int G, const std::vector<int>& ids, const double* b, double* x, double rtol,
                           int maxit, double delta, int from_x, std::vector<BRes>& hres) {
   Ctx* ctx = B->ctx;
   cudaStream_t s = ctx->stream;
@@ -325,11 +342,16 @@ static int launch_small_g(gt_batch* B, int G, const std::vector<int>& ids, const
     return GT_OK;
   };
   int st;
-  switch (G) {
-    case 1: st = launch(k_bpcg<1, V, X, REL>); break;
-    case 2: st = launch(k_bpcg<2, V, X, REL>); break;
-    case 8: st = launch(k_bpcg<8, V, X, REL>); break;
-    default: st = launch(k_bpcg<4, V, X, REL>); break;
+  if (bs == 3) {
+    // block rows of 3-D elasticity: 2 or 4 lanes (inst_lanes)
+    st = G == 2 ? launch(k_bpcg<3, 2, V, X, REL>) : launch(k_bpcg<3, 4, V, X, REL>);
+  } else {
+    switch (G) {
+      case 1: st = launch(k_bpcg<1, 1, V, X, REL>); break;
+      case 2: st = launch(k_bpcg<1, 2, V, X, REL>); break;
+      case 8: st = launch(k_bpcg<1, 8, V, X, REL>); break;
+      default: st = launch(k_bpcg<1, 4, V, X, REL>); break;
+    }
   }
   if (st == GT_OK) {
     std::vector<BRes> all(B->n);
@@ -350,23 +372,27 @@ static int launch_small_g(gt_batch* B, int G, const std::vector<int>& ids, const
 }
 
 // lanes of instance i in the one-CTA solves: fixed by set_lanes, else from
-// the instance's own mean row length (so the result depends on nothing else)
+// the instance's own mean row length (so the result depends on nothing
+// else); block rows of 3 take 2 or 4
 static int inst_lanes(const gt_batch* B, int i) {
-  if (B->G) return B->G;
   const Matrix* A = B->mats[i];
-  return row_lanes(A->nbrows > 0 ? (double)A->bnnz / (double)A->nbrows : 1.0);
+  int g = B->G ? B->G : row_lanes(A->nbrows > 0 ? (double)A->bnnz / (double)A->nbrows : 1.0);
+  if (A->bs == 3) g = g <= 2 ? 2 : 4;
+  return g;
 }
 
-// one launch per lane count (instances keep their largest-first order)
+// one launch per block size and lane count (instances keep their
+// largest-first order)
 template <class V, class X, bool REL>
 static int launch_small(gt_batch* B, const std::vector<int>& ids, const double* b, double* x, double rtol, int maxit,
                         double delta, int from_x, std::vector<BRes>& hres) {
-  for (int g : {1, 2, 4, 8}) {
-    std::vector<int> sub;
-    for (int i : ids)
-      if (inst_lanes(B, i) == g) sub.push_back(i);
-    if (!sub.empty()) GT_TRY((launch_small_g<V, X, REL>(B, g, sub, b, x, rtol, maxit, delta, from_x, hres)));
-  }
+  for (int bs : {1, 3})
+    for (int g : {1, 2, 4, 8}) {
+      std::vector<int> sub;
+      for (int i : ids)
+        if (B->mats[i]->bs == bs && inst_lanes(B, i) == g) sub.push_back(i);
+      if (!sub.empty()) GT_TRY((launch_small_g<V, X, REL>(B, bs, g, sub, b, x, rtol, maxit, delta, from_x, hres)));
+    }
   return GT_OK;
 }
 
@@ -420,7 +446,7 @@ static int batch_solve(gt_batch* B, const double* b, double* x, double rtol, int
   for (int i : B->large) {
     Matrix* A = B->mats[i];
     const int64_t off = B->h_inst[i].off;
-    GT_CUDA(ctx, cudaMemsetAsync(x + off, 0, sizeof(double) * A->nbrows, ctx->stream));
+    GT_CUDA(ctx, cudaMemsetAsync(x + off, 0, sizeof(double) * A->nbrows * A->bs, ctx->stream));
     // a matrix of another context solves on that context's stream: b and x
     // (written on this one) are complete first; solve() returns synchronised
     if (A->ctx != ctx) GT_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -451,9 +477,10 @@ int gt_batch_create(gt_ctx* ctx, int n, gt_matrix* const* mats, gt_batch** out) 
   int64_t off = 0;
   for (int i = 0; i < n; i++) {
     Matrix* A = mats[i];
-    if (!A || A->ctx->device != ctx->device || A->bs != 1) {
+    if (!A || A->ctx->device != ctx->device || (A->bs != 1 && A->bs != 3)) {
       delete B;
-      return set_error(ctx, GT_ERR_INVALID, "batch: matrices must be scalar (block size 1) and on this context's device");
+      return set_error(ctx, GT_ERR_INVALID,
+                       "batch: matrices must have block size 1 or 3 and be on this context's device");
     }
     int s = find_diag(A);
     // a matrix of another context (assembled on another stream): its
@@ -472,15 +499,17 @@ int gt_batch_create(gt_ctx* ctx, int n, gt_matrix* const* mats, gt_batch** out) 
     in.diag = A->diag_pos;
     in.nrows = A->nbrows;
     in.off = off;
-    off += A->nbrows;
+    in.bs = A->bs;
+    off += A->nbrows * A->bs;
     B->h_inst.push_back(in);
     B->mats.push_back(A);
-    if (A->nbrows <= kSmallRows) B->small.push_back(i);
+    if (A->nbrows * A->bs <= kSmallRows) B->small.push_back(i);
     else B->large.push_back(i);
   }
   // largest small instances first: the queue then balances the CTAs
-  std::stable_sort(B->small.begin(), B->small.end(),
-                   [&](int a, int c) { return B->h_inst[a].nrows > B->h_inst[c].nrows; });
+  std::stable_sort(B->small.begin(), B->small.end(), [&](int a, int c) {
+    return B->h_inst[a].nrows * B->h_inst[a].bs > B->h_inst[c].nrows * B->h_inst[c].bs;
+  });
   B->ntot = off;
   int s = dalloc(ctx, &B->d_inst, n);
   if (s == GT_OK) s = copy_in(ctx, B->d_inst, B->h_inst.data(), n);

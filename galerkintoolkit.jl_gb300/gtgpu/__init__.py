@@ -2,7 +2,8 @@
 GalerkinToolkit.jl problem-level API (assemble_matrix / assemble_vector /
 linear problem + solve) over hand-written sm_103a CUDA kernels."""
 from ._lib import GTError, load  # noqa: F401
-from .api import (Context, DiscreteField, Domain, Form, LinearProblem, Matrix, Polynomial, Source, Space,  # noqa: F401
+from .api import (Context, DeviceArray, DiscreteField, Domain, Form, LinearProblem, Matrix, Polynomial, Source,  # noqa: F401
+                  Space, lognormal_cells_device,
                   assemble_boundary_vector, assemble_matrix, assemble_matrix_and_vector, assemble_vector, boundary,
                   default_context, device_mesh, elasticity, h1_error, integrate, interior, interpolate_dirichlet,
                   l2_error, lagrange_space, laplacian, linear_problem, mass, num_dirichlet_dofs, num_free_dofs, solve,

@@ -91,6 +91,10 @@ SIGNATURES = [
     ("gt_batch_info", I32, [P, P]),
     ("gt_batch_solve", I32, [P, P, P, DBL, I32, I32, P]),
     ("gt_batch_destroy", I32, [P]),
+    ("gt_device_alloc", I32, [P, I64, C.POINTER(P)]),
+    ("gt_device_free", I32, [P, P]),
+    ("gt_device_copy", I32, [P, P, P, I64]),
+    ("gt_lognormal_cells", I32, [P, I64, DBL, C.c_uint64, P]),
 ]
 
 _lock = threading.Lock()

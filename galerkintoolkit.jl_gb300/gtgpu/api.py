@@ -139,6 +139,46 @@ class DeviceMesh:
             pass
 
 
+class DeviceArray:
+    """float64 device array from a context's buffer pool (gt_device_alloc):
+    a per-cell coefficient or load data that stays on the device.  Passed to
+    the forms like a host array; numpy() copies it back."""
+
+    def __init__(self, ctx: Context, n: int):
+        self.ctx, self.n = ctx, int(n)
+        h = C.c_void_p()
+        check(ctx.h, ctx.lib.gt_device_alloc(ctx.h, 8 * self.n, C.byref(h)))
+        self.h = h
+
+    def data_ptr(self):
+        return self.h.value
+
+    def __len__(self):
+        return self.n
+
+    def numpy(self):
+        out = np.empty(self.n, np.float64)
+        check(self.ctx.h, self.ctx.lib.gt_device_copy(self.ctx.h, _ptr(out), self.h, 8 * self.n))
+        return out
+
+    def __del__(self):
+        try:
+            if self.h and self.ctx.h:
+                self.ctx.lib.gt_device_free(self.ctx.h, self.h)
+        except Exception:
+            pass
+
+
+def lognormal_cells_device(ncells: int, sigma: float, seed: int, ctx: Context | None = None) -> DeviceArray:
+    """The seeded per-cell coefficient of gtgpu.lognormal_cells generated on
+    the device (gt_lognormal_cells): same keyed uniforms and Box-Muller
+    transform, values equal up to the last bits of log, cos and exp."""
+    ctx = ctx or default_context()
+    a = DeviceArray(ctx, ncells)
+    check(ctx.h, ctx.lib.gt_lognormal_cells(ctx.h, int(ncells), float(sigma), int(seed) & 0xFFFFFFFFFFFFFFFF, a.h))
+    return a
+
+
 def device_mesh(mesh: Mesh, ctx: Context | None = None) -> DeviceMesh:
     ctx = ctx or default_context()
     dm = mesh._device.get(id(ctx))

@@ -1,6 +1,7 @@
 """Batched assembly + solve of many independent problems.
 
-``Batch`` wraps ``gt_batch_*``: the small instances (up to 32768 rows) are
+``Batch`` wraps ``gt_batch_*`` (scalar matrices, or block size 3 for 3-D
+elasticity): the small instances (up to 32768 scalar rows) are
 solved by one persistent launch in which every CTA takes instances from a
 queue (largest first) and runs each one's whole Jacobi-PCG alone; the large
 instances run through the single-system solver.  Each instance keeps its own
@@ -39,8 +40,9 @@ _MODES = {"fp64": _lib.GT_SOLVE_FP64, "ir": _lib.GT_SOLVE_IR, "mixed": _lib.GT_S
 
 
 class Batch:
-    """gt_batch over assembled scalar matrices of one device (they may come
-    from several contexts); solved on ``ctx`` (default: the first matrix's)."""
+    """gt_batch over assembled matrices of one device, block size 1 or 3
+    (they may come from several contexts); solved on ``ctx`` (default: the
+    first matrix's)."""
 
     def __init__(self, matrices, lanes: int | None = None, ctx=None):
         if not matrices:

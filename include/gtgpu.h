@@ -273,27 +273,44 @@ int gt_spmv(gt_matrix* matrix, const double* x, double* y);
 
 /* ---- batched solves ----------------------------------------------------- */
 /* No counterpart in the reference (which solves one problem per call).
- * A batch of n assembled scalar matrices (block size 1) on the device of
- * ctx (they may come from other contexts of that device, e.g. assembled
- * concurrently on several streams), solved together on ctx's stream: instances of up to 32768 rows in one persistent launch
- * in which each CTA takes instances from a queue (largest first) and runs
- * each one's whole PCG alone; larger instances one after the other through
- * the single-system solver.  An instance's result does not depend on the
- * rest of the batch.  b and x are the instances' vectors
- * concatenated in batch order (num_free_dofs each, FP64); x is the output
- * (every solve starts from 0).  infos: n entries.  GT_SOLVE_IR needs
- * GT_MIXED matrices. */
+ * A batch of n assembled matrices of block size 1 (scalar problems) or 3
+ * (3-D elasticity) on the device of ctx (they may come from other contexts
+ * of that device, e.g. assembled concurrently on several streams), solved
+ * together on ctx's stream: instances of up to 32768 scalar rows in one
+ * persistent launch per block size in which each CTA takes instances from a
+ * queue (largest first) and runs each one's whole Jacobi-PCG alone; larger
+ * instances one after the other through the single-system solver.  An
+ * instance's result does not depend on the rest of the batch.  b and x are
+ * the instances' vectors concatenated in batch order (num_free_dofs each,
+ * FP64); x is the output (every solve starts from 0).  infos: n entries.
+ * GT_SOLVE_IR needs GT_MIXED matrices.  Other block sizes: GT_ERR_INVALID. */
 typedef struct gt_batch gt_batch;
 int gt_batch_create(gt_ctx* ctx, int n, gt_matrix* const* matrices, gt_batch** batch);
 /* lanes per matrix row in the SpMV of the one-CTA-per-instance solves (1, 2,
- * 4 or 8; 0, the default: each instance's own, from its mean row length) */
+ * 4 or 8; 0, the default: each instance's own, from its mean row length;
+ * block rows of 3 take 2 or 4: 1 -> 2, 8 -> 4) */
 int gt_batch_set_lanes(gt_batch* batch, int lanes);
-/* info[0]=instances info[1]=total rows info[2]=instances solved one per CTA
+/* info[0]=instances info[1]=total scalar rows info[2]=instances solved one per CTA
  * info[3]=lanes */
 int gt_batch_info(const gt_batch* batch, int64_t* info);
 int gt_batch_solve(gt_batch* batch, const double* b, double* x, double rtol, int maxit, int mode,
                    gt_solve_info* infos);
 int gt_batch_destroy(gt_batch* batch);
+
+/* ---- device buffers and served-request inputs --------------------------- */
+/* No counterpart in the reference.  Device memory from ctx's buffer pool
+ * (bytes >= 0; freed back to the pool, ordered after the work already
+ * queued on ctx); a synchronous copy in any direction on ctx's stream. */
+int gt_device_alloc(gt_ctx* ctx, int64_t bytes, void** out);
+int gt_device_free(gt_ctx* ctx, void* ptr);
+int gt_device_copy(gt_ctx* ctx, void* dst, const void* src, int64_t bytes);
+/* The seeded per-cell coefficient of a served request, generated on the
+ * device on ctx's stream: out[c] = exp(sigma z_c), z_c =
+ * sqrt(-2 log(1 - u(2c))) cos(2 pi u(2c + 1)), u(k) = (splitmix64(s ^ k)
+ * >> 11) 2^-53 with s = seed ^ 0xC0EFF1C1E47 -- the host generator of the
+ * Python package (gtgpu.lognormal_cells) up to the last bits of log, cos and
+ * exp.  out: device memory of ctx's device, ncells doubles. */
+int gt_lognormal_cells(gt_ctx* ctx, int64_t ncells, double sigma, uint64_t seed, double* out);
 
 #ifdef __cplusplus
 }

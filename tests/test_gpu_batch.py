@@ -41,6 +41,41 @@ def test_batch_result_independent_of_batch_mix():
         assert np.array_equal(alone, xs_full[k])
 
 
+def _elasticity_instances(T="mixed"):
+    """3-D linear elasticity (block size 3) on Q1 and Q2 hexahedra, clamped
+    at x = 0, lognormal(0, 0.5) Young's modulus per cell"""
+    out = []
+    for k, (order, n) in enumerate([(1, 4), (2, 3), (1, 6), (2, 2)]):
+        m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (n, n, n))
+        coef = GT.lognormal_cells(m.num_cells, 0.5, 900 + k)
+        V = GT.lagrange_space(GT.interior(m), order, tensor_size=(3,), dirichlet_boundary=GT.boundary(m, ["2-face-5"]))
+        A, b = GT.assemble_matrix_and_vector(GT.elasticity(coef, 0.3), GT.source([0.0, 0.0, -1.0]), T, V)
+        out.append((m, V, A, b))
+    return out
+
+
+@pytest.mark.parametrize("mode", ["fp64", "ir"])
+def test_batch_of_block_matrices(mode):
+    """Elasticity (3 x 3 blocks) and scalar instances in one batch: one launch
+    per block size; every solution within 1e-8 of its stand-alone FP64 solve
+    and bitwise the same alone and in the mix."""
+    el = _elasticity_instances()
+    sc = _instances()[:3]
+    mats = [A for _, _, A, _ in el] + [A for _, _, A, _ in sc]
+    bs = [b for _, _, _, b in el] + [b for _, _, _, b in sc]
+    B = GB.Batch(mats)
+    assert B.info()["small_instances"] == len(mats)
+    x, infos = B.solve(bs, rtol=1e-10, mode=mode)
+    parts = B.split(x)
+    for k, (A, b) in enumerate(zip(mats, bs)):
+        xs, _ = GT.solve(A, b, rtol=1e-12, mode="fp64")
+        assert infos[k]["rel_residual"] <= 1e-10
+        assert np.abs(parts[k] - xs).max() <= 1e-8 * np.abs(xs).max()
+    for k in (0, 1, 4):
+        alone, _ = GB.Batch([mats[k]]).solve([bs[k]], rtol=1e-10, mode=mode)
+        assert np.array_equal(alone, parts[k])
+
+
 def test_autotune_picks_a_candidate(tmp_path):
     inst = _instances()
     B = GB.Batch([A for _, _, A, _ in inst])

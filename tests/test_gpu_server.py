@@ -30,11 +30,12 @@ def test_cached_geometry_refill_is_bitwise_a_fresh_assembly():
     from gtgpu.server import Request
     reqs = [Request(0, 0.0, "poisson", 2, 7, 101), Request(1, 0.0, "elasticity", 1, 6, 102),
             Request(2, 0.0, "poisson", 2, 7, 103), Request(3, 0.0, "elasticity", 1, 6, 104)]
-    warm = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo")
+    # batches of two: requests 2 and 3 come after the batch that cached their geometries
+    warm = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo", batch_max=2)
     warm.serve(reqs, realtime=False)
     assert [r.cache_hit for r in sorted(reqs, key=lambda r: r.rid)] == [False, False, True, True]
     fresh = [Request(r.rid, 0.0, r.form, r.order, r.cells_per_dir, r.seed) for r in reqs[2:]]
-    cold = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo", cache_fraction=1e-9)
+    cold = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo", cache_fraction=1e-9, batch_max=2)
     cold.serve(fresh, realtime=False)
     for a, b in zip(sorted(reqs[2:], key=lambda r: r.rid), sorted(fresh, key=lambda r: r.rid)):
         assert not b.cache_hit and a.rel_residual <= 1e-10
@@ -55,13 +56,14 @@ def test_serving_window_reports_pending():
 
 
 def test_batched_small_requests_with_shared_geometry():
-    """Small Poisson requests pending together are solved in one persistent
-    launch; requests on the same geometry in one batch each take their own
-    resident instance.  Every result is bitwise that of the request served
-    alone, and within 1e-10 in residual."""
+    """Small Poisson and elasticity requests pending together are solved in
+    one persistent launch per block size; requests on the same geometry in
+    one batch each take their own resident instance.  Every result is
+    bitwise that of the request served alone, and within 1e-10 in residual."""
     from gtgpu.server import Request
     def reqs():
-        return [Request(i, 0.0, "poisson", 1 + (i % 2), 9 if i % 2 == 0 else 5, 300 + i) for i in range(8)]
+        return [Request(i, 0.0, "elasticity" if i % 4 == 3 else "poisson", 1 + (i % 2),
+                        4 if i % 4 == 3 else (9 if i % 2 == 0 else 5), 300 + i) for i in range(8)]
     together, alone = reqs(), reqs()
     s1 = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo")
     rep = s1.serve(together, realtime=False)
@@ -73,3 +75,13 @@ def test_batched_small_requests_with_shared_geometry():
         assert np.array_equal(a.solution, b.solution)
     s1.close()
     s2.close()
+
+
+def test_device_coefficients_match_host_generator():
+    """gt_lognormal_cells: the served requests' coefficients generated on the
+    device equal the host generator's up to the last bits of log/cos/exp."""
+    import gtgpu as GT
+    for n, seed in ((1, 7), (1000, 505000003), (123457, 2 ** 40 + 3)):
+        d = GT.lognormal_cells_device(n, 0.5, seed).numpy()
+        h = GT.lognormal_cells(n, 0.5, seed)
+        assert np.all(d > 0) and np.abs(d - h).max() <= 1e-14 * np.abs(h).max()
