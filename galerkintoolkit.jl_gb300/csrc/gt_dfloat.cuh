@@ -86,12 +86,12 @@ __device__ __forceinline__ dfl df_recip(dfl x) {
 // line on purpose: inlined, the compiler may if-convert them into the common
 // path, and their FP64 instructions would then issue (predicated off) for
 // every value converted.
-__device__ __noinline__ dfl df_from_double_rare(double x) {
+static __device__ __noinline__ dfl df_from_double_rare(double x) {
   const float h = __double2float_rn(x);
   return {h, __double2float_rn(x - (double)h)};
 }
 
-__device__ __noinline__ double df_to_double_rare(float hi, float lo) { return (double)hi + (double)lo; }
+static __device__ __noinline__ double df_to_double_rare(float hi, float lo) { return (double)hi + (double)lo; }
 
 // FP64 -> double-float with integer instructions: hi takes the top 24
 // significand bits of x (exact), lo the remaining 29 bits rounded to FP32.
