@@ -1335,9 +1335,11 @@ __global__ void __launch_bounds__(256) k_elements_p1_df(const double* __restrict
 #pragma unroll
         for (int e = 0; e < 10; e++) k[e] = df_mul(s, smass[e]);
       }
-      double* K = Ke + 10 * c;
+      // the entries stay double-float pairs: the scatter sums them as such
+      // and rounds each CSR value to FP64 once
+      float2* K = reinterpret_cast<float2*>(Ke + 10 * c);
 #pragma unroll
-      for (int e = 0; e < 10; e++) K[e] = df_to_double(k[e]);
+      for (int e = 0; e < 10; e++) K[e] = make_float2(k[e].hi, k[e].lo);
     }
     if (be) {
       const dfl f0 = fsrc ? df_from_double(__ldg(fsrc)) : dfl{0.0f, 0.0f};  // only with a load vector
@@ -1806,6 +1808,27 @@ __global__ void k_scatter(const int64_t* __restrict__ rowptr, const int32_t* __r
   }
 }
 
+// Element-block entries and row accumulators of the P1 scatter: FP64 or
+// FP32 numbers, or double-float pairs (the double-float element kernel's
+// entries, summed as pairs on the FP32 pipes and rounded to FP64 once per
+// CSR value).
+template <class T>
+__device__ __forceinline__ T ke_load(const T* p) { return __ldg(p); }
+template <>
+__device__ __forceinline__ dfl ke_load<dfl>(const dfl* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return {v.x, v.y};
+}
+__device__ __forceinline__ void acc_add(double& a, double v) { a += v; }
+__device__ __forceinline__ void acc_add(float& a, float v) { a += v; }
+__device__ __forceinline__ void acc_add(dfl& a, dfl v) { a = df_add_sloppy(a, v); }
+__device__ __forceinline__ double to_f64(double v) { return v; }
+__device__ __forceinline__ double to_f64(float v) { return (double)v; }
+__device__ __forceinline__ double to_f64(dfl v) { return df_to_double(v); }
+__device__ __forceinline__ float to_f32(double v) { return (float)v; }
+__device__ __forceinline__ float to_f32(float v) { return v; }
+__device__ __forceinline__ float to_f32(dfl v) { return (float)df_to_double(v); }
+
 // Scalar P1 tetrahedra (packed blocks: the upper triangle of the symmetric
 // 4 x 4 block, 10 entries per cell): the row-owner scatter of k_scatter,
 // specialised.  Four lanes own a row, lane b the local column node b of
@@ -1850,7 +1873,7 @@ __global__ void __launch_bounds__(128) k_scatter_p1(const int64_t* __restrict__ 
   const int L = (int)(rowptr[r + 1] - rb);
   for (int i = b; i < L; i += G) {
     cols[i] = colind[rb + i];
-    acc[i] = (TA)0;
+    acc[i] = TA{};
   }
   __syncwarp(gmask);
   const int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
@@ -1863,12 +1886,12 @@ __global__ void __launch_bounds__(128) k_scatter_p1(const int64_t* __restrict__ 
 #pragma unroll
     for (int u = 0; u < U; u++) {
       jj[u] = 0;
-      kv[u] = (TA)0;
+      kv[u] = TA{};
       if (k0 + u < ie) {
         const int32_t cb = __ldg(inc + k0 + u);
         const int32_t c = cb >> 2, a = cb & 3;
         jj[u] = __ldg(cnd + (int64_t)c * 4 + b);
-        kv[u] = (TA)__ldg(Ke + (int64_t)c * 10 + ((offs >> (4 * a)) & 15u));
+        kv[u] = (TA)ke_load(Ke + (int64_t)c * 10 + ((offs >> (4 * a)) & 15u));
       }
       key[u] = jj[u] > 0 ? jj[u] - 1 : INT_MIN;  // INT_MIN: stays at position 0, unused
       pos[u] = 0;
@@ -1882,10 +1905,10 @@ __global__ void __launch_bounds__(128) k_scatter_p1(const int64_t* __restrict__ 
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
-      if (jj[u] > 0) acc[pos[u]] += kv[u];
+      if (jj[u] > 0) acc_add(acc[pos[u]], kv[u]);
       if constexpr (LIFT) {
         double lv = 0.0;
-        if (jj[u] < 0) lv += (double)kv[u] * __ldg(xd - jj[u] - 1);
+        if (jj[u] < 0) lv += to_f64(kv[u]) * __ldg(xd - jj[u] - 1);
         lv += __shfl_xor_sync(gmask, lv, 2);
         lv += __shfl_xor_sync(gmask, lv, 1);
         if (b == 0) bsum -= lv;
@@ -1895,8 +1918,8 @@ __global__ void __launch_bounds__(128) k_scatter_p1(const int64_t* __restrict__ 
   }
   for (int i = b; i < L; i += G) {
     const TA v = acc[i];
-    if (v64) v64[rb + i] = (double)v;
-    if (v32) v32[rb + i] = (float)v;
+    if (v64) v64[rb + i] = to_f64(v);
+    if (v32) v32[rb + i] = to_f32(v);
   }
   if (be != nullptr && b == 0) bvec[r] = bsum;
 }
@@ -1933,7 +1956,9 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
         done = true;
       }
     }
-    if (!done) launch(k_scatter<BS, G, TK, TA>);
+    if constexpr (!std::is_same<TK, dfl>::value) {
+      if (!done) launch(k_scatter<BS, G, TK, TA>);
+    }
     GT_LAUNCH(ctx, "k_scatter");
     return GT_OK;
   };
@@ -1956,6 +1981,10 @@ int scatter_matrix(Matrix* A, const void* Ke, int ke_precision, int out_precisio
     if (bs == 2) return launch_scatter<2, float, float>(A, K, v64, v32, be, bvec, xd, r0, r1);
     return launch_scatter<3, float, float>(A, K, v64, v32, be, bvec, xd, r0, r1);
   }
+  // FP64-valued packed P1 blocks from the double-float element kernel are
+  // double-float pairs
+  if (bs == 1 && ke_packed(A->space) && ctx_of(A->space)->p1_dfloat)
+    return launch_scatter<1, dfl, dfl>(A, (const dfl*)Ke, v64, v32, be, bvec, xd, r0, r1);
   const double* K = (const double*)Ke;
   if (bs == 1) return launch_scatter<1, double, double>(A, K, v64, v32, be, bvec, xd, r0, r1);
   if (bs == 2) return launch_scatter<2, double, double>(A, K, v64, v32, be, bvec, xd, r0, r1);

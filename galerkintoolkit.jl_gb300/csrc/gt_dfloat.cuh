@@ -23,7 +23,7 @@
 
 namespace gt {
 
-struct dfl {
+struct alignas(8) dfl {
   float hi, lo;
 };
 
@@ -48,6 +48,15 @@ __device__ __forceinline__ dfl df_add(dfl x, dfl y) {
   const dfl t = df_two_sum(x.lo, y.lo);
   const dfl u = df_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
   return df_fast_two_sum(u.hi, __fadd_rn(u.lo, t.lo));
+}
+
+// x + y with one two-sum of the high parts and the low parts added in FP32
+// (Dekker's / Bailey's "sloppy" sum: absolute error about 2^-47 of the
+// larger operand, not of the result -- enough for sums whose terms are all
+// of the size of the result, such as a matrix entry over its cells)
+__device__ __forceinline__ dfl df_add_sloppy(dfl x, dfl y) {
+  const dfl s = df_two_sum(x.hi, y.hi);
+  return df_fast_two_sum(s.hi, __fadd_rn(__fadd_rn(x.lo, y.lo), s.lo));
 }
 
 __device__ __forceinline__ dfl df_neg(dfl x) { return {-x.hi, -x.lo}; }
