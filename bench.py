@@ -46,8 +46,8 @@ PEAKS_FALLBACK = {"hbm_gbs": 6800.0}
 # tets), from one-pass ncu captures of the full workload (summaries under
 # profiles/): the double-float element kernel, the scatter and the FP64 SpMV
 # (sliced-ELL copy)
-TRAFFIC: dict = {"elements": 155.32e6 + 537.38e6,
-                 "scatter": 826.07e6 + 96.52e6,
+TRAFFIC: dict = {"elements": 149.65e6 + 532.88e6,
+                 "scatter": 826.09e6 + 97.81e6,
                  "spmv": 159.938048e6 + 5.819904e6}
 
 
@@ -604,8 +604,8 @@ def main():
                 "arithmetic": "double-float (FP32 pairs, 48-bit) after FP64 differences x_i - x_0; "
                               f"{flops_el / (ph[dom] * 1e-3) / 1e12:.3f} TFLOP/s of FP64-equivalent work "
                               f"(93 flops/cell) against the FP64 FMA rate {fp64_tf:.3f}",
-                "limiter": "instruction issue (ncu, 64^3 x 6: issue 71% active, FP64 pipe 33%, ALU 57%, "
-                           "DRAM 13%; profiles/k_elements_p1_df_p1tet64.md)"}
+                "limiter": "instruction issue (ncu, 64^3 x 6: issue 68% active, FP64 pipe 45% -- the nine FP64 "
+                           "differences per cell --, DRAM 17%; profiles/k_elements_p1_df_p1tet64.md)"}
     elif dom == "elements":
         achieved = flops_el / (ph[dom] * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": "k_elements_p1<Laplacian, double>", "achieved": achieved,
@@ -614,6 +614,14 @@ def main():
                 "peak_method": "gt_ctx_fma_rate: 8 CTAs/SM x 256 threads, 8 independent FMA chains per thread, "
                                "2048 iterations, CUDA events after a warm-up launch (FMA = 2 flops)",
                 "algorithmic_flops": flops_el, "traffic": TRAFFIC.get("elements")}
+    elif dom == "scatter":
+        achieved = alg["scatter"] / (ph[dom] * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": "k_scatter_p1<dfl, dfl>" if p1_dfloat else "k_scatter_p1<double, double>",
+                "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                "peak_source": peaks_kind, "algorithmic_bytes": alg["scatter"], "traffic": TRAFFIC.get("scatter"),
+                "b_asm": hbm["scatter"]["b_asm"],
+                "limiter": "gather latency (ncu, 64^3 x 6: long_scoreboard first, 40% of the warp slots, issue 58%, "
+                           "DRAM 29%; profiles/k_scatter_p1_p1tet64.md)"}
     else:
         bytes_dom = alg.get(dom, nnz * 12)
         achieved = bytes_dom / (ph[dom] * 1e-3) / 1e9
