@@ -141,8 +141,8 @@ def run_batched(args):
       fp64_batched   the same runner in plain FP64
       plain_fp64     one instance at a time on one context, FP64 assembly and
                      FP64 CG
-    The worker count and the small tier's SpMV lanes come from
-    autotune_batch (untimed, cached).  Solutions of a seeded sample of the
+    The worker count, the one-CTA tier's row limit and the small tier's SpMV
+    lanes come from autotune_batch (untimed, cached).  Solutions of a seeded sample of the
     instances are compared with the oracle's FP64 solve."""
     import gtgpu as GT
     from gtgpu import batch as GB
@@ -156,7 +156,7 @@ def run_batched(args):
     runs = {}
     for name, prec in (("mixed_batched", "mixed"), ("fp64_batched", "fp64")):
         r = GB.run_batch(specs, host, prec, rtol=rtol, workers=tune["workers"], lanes=tune["lanes"],
-                         budget_bytes=budget)
+                         small_rows=tune["small_rows"], budget_bytes=budget)
         its = [i["iterations"] for i in r.infos.values()]
         runs[name] = {"solves_per_s": len(specs) / r.seconds, "seconds": r.seconds, "waves": r.waves,
                       "small_tier": r.small, "large_tier": r.large,

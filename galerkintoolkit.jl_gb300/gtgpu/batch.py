@@ -313,16 +313,19 @@ def run_batch(specs, inputs, precision="mixed", rtol=1e-10, maxit=100000, worker
 
 
 def autotune_batch(specs, inputs, precision="mixed", rtol=1e-10, workers=(1, 2, 4, 8), sample=48, max_rows=2_000_000,
-                   cache=None, use_cache=True, seed=0):
-    """Pick run_batch's concurrency (worker contexts) and the small tier's
-    SpMV lanes for a workload: run_batch is timed on a seeded sample of the
-    instances (at most ``sample``, each under ``max_rows`` rows, spread over
-    the size range) once per worker count, then autotune_lanes times the
-    lane candidates on the sample's small tier.  The choice is cached in the
-    autotune JSON file under the workload's signature."""
+                   cache=None, use_cache=True, seed=0, small_rows=(4096, 16384, 32768)):
+    """Pick run_batch's concurrency (worker contexts), the row limit of its
+    one-CTA-per-instance tier (the tile of the batched kernel: an instance
+    up to it is solved by one CTA, a larger one by the whole device) and
+    the small tier's SpMV lanes for a workload: run_batch is timed on a
+    seeded sample of the instances (at most ``sample``, each under
+    ``max_rows`` rows, spread over the size range) once per worker count,
+    then once per row limit with the best worker count, then autotune_lanes
+    times the lane candidates on the sample's small tier.  The choice is
+    cached in the autotune JSON file under the workload's signature."""
     path = _cache_path(cache)
     sig = hashlib.sha1(repr(sorted((s.dim, s.order, s.cells_per_dir) for s in specs)).encode()).hexdigest()[:16]
-    key = f"batch:{precision}:{sig}"
+    key = f"batch2:{precision}:{sig}"
     table = {}
     if use_cache and os.path.exists(path):
         try:
@@ -342,17 +345,23 @@ def autotune_batch(specs, inputs, precision="mixed", rtol=1e-10, workers=(1, 2, 
     for w in workers:
         times[w] = run_batch(pool, sub, precision, rtol=rtol, workers=w, keep_solutions=False).seconds
     best_w = min(times, key=times.get)
+    tiers = {}
+    for sr in small_rows:
+        tiers[sr] = run_batch(pool, sub, precision, rtol=rtol, workers=best_w, small_rows=sr,
+                              keep_solutions=False).seconds
+    best_sr = min(tiers, key=tiers.get)
     ctx = default_context()
     T = "mixed" if precision == "mixed" else np.float64
-    small = [s for s in pool if rows[s.index] <= 32768]
+    small = [s for s in pool if rows[s.index] <= best_sr]
     lanes = 0
     if small:
         inst = [assemble_instance(s, T=T, ctx=ctx, inputs=sub[s.index]) for s in small]
         B = Batch([A for _, _, A, _ in inst])
         lanes = autotune_lanes(B, np.concatenate([b for *_, b in inst]), iters=32, cache=cache, use_cache=use_cache)["lanes"]
         del B, inst
-    entry = {"workers": int(best_w), "lanes": int(lanes), "seconds": {str(k): v for k, v in times.items()},
-             "sample": len(pool)}
+    entry = {"workers": int(best_w), "small_rows": int(best_sr), "lanes": int(lanes),
+             "seconds": {str(k): v for k, v in times.items()},
+             "small_rows_seconds": {str(k): v for k, v in tiers.items()}, "sample": len(pool)}
     table = {}
     if os.path.exists(path):
         try:

@@ -87,6 +87,21 @@ def test_autotune_picks_a_candidate(tmp_path):
     assert again["lanes"] == entry["lanes"]
 
 
+def test_autotune_batch_picks_workers_tier_and_lanes(tmp_path):
+    """autotune_batch times run_batch per worker count and per row limit of
+    the one-CTA tier on a sample, tunes the lanes, and caches the choice."""
+    specs = [GB.InstanceSpec(i, 2 + (i % 2), 1 + (i // 2) % 2, n) for i, n in enumerate((9, 5, 40, 7, 70, 4, 24, 6))]
+    inputs = {s.index: GB.instance_inputs(s, seed=5) for s in specs}
+    cache = str(tmp_path / "tune.json")
+    e = GB.autotune_batch(specs, inputs, "mixed", rtol=1e-8, workers=(1, 2), small_rows=(1024, 32768), cache=cache)
+    assert e["workers"] in (1, 2) and e["small_rows"] in (1024, 32768) and e["lanes"] in (0, 1, 2, 4, 8)
+    assert set(e["small_rows_seconds"]) == {"1024", "32768"}
+    assert GB.autotune_batch(specs, inputs, "mixed", rtol=1e-8, cache=cache) == e
+    r = GB.run_batch(specs, inputs, "mixed", rtol=1e-8, workers=e["workers"], small_rows=e["small_rows"],
+                     lanes=e["lanes"] or None)
+    assert all(i["rel_residual"] <= 1e-8 for i in r.infos.values())
+
+
 def test_batch_with_large_instance_matches_alone():
     """A batch mixing one-CTA instances with one above the size limit (solved
     by the persistent grid solver): every result equals its solve alone."""
