@@ -27,8 +27,7 @@
 //     them;
 //   * the first call on a device looks up the array's device address
 //     (cudaGetSymbolAddress with that device current, the caller's current
-//     device restored afterwards); make that first call before any stream
-//     capture;
+//     device restored afterwards);
 //   * every call waits for the context's stream before it returns (it reads
 //     the kernels' error word).
 #include <mutex>

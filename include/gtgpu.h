@@ -204,9 +204,8 @@ int gt_update_matrix(gt_matrix* matrix, int form, const double* cell_coef, doubl
  * same pass); cell_coef must be device memory of the matrix's device or
  * NULL; a refill needing more scratch
  * than 128 MiB (tabulation + ncells*nloc^2 values) returns GT_ERR_INVALID.
- * The first call on a device looks up the array's address (make it before
- * any stream capture); every call waits for the context's stream before it
- * returns.  All calls on a device share the one array, which keeps the last
+ * The first call on a device looks up the array's address; every call
+ * waits for the context's stream before it returns.  All calls on a device share the one array, which keeps the last
  * call's contents: calls that overlap on the GPU (two streams, contexts or
  * threads at once) race on it, so callers serialise them. */
 int gt_update_matrix_noalloc(gt_matrix* matrix, int form, const double* cell_coef, double nu);
