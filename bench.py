@@ -612,7 +612,7 @@ def main():
                               f"{flops_el / (ph[dom] * 1e-3) / 1e12:.3f} TFLOP/s of FP64-equivalent work "
                               f"(93 flops/cell) against the FP64 FMA rate {fp64_tf:.3f}",
                 "limiter": "instruction issue (ncu, 64^3 x 6: issue 68% active, FP64 pipe 45% -- the nine FP64 "
-                           "differences per cell --, DRAM 17%; profiles/k_elements_p1_df_p1tet64.md)"}
+                           "differences per cell --, DRAM 17%)"}
     elif dom == "elements":
         achieved = flops_el / (ph[dom] * 1e-3) / 1e12
         roof = {"bound": "fp64", "kernel": "k_elements_p1<Laplacian, double>", "achieved": achieved,
@@ -628,7 +628,7 @@ def main():
                 "peak_source": peaks_kind, "algorithmic_bytes": alg["scatter"], "traffic": TRAFFIC.get("scatter"),
                 "b_asm": hbm["scatter"]["b_asm"],
                 "limiter": "gather latency (ncu, 64^3 x 6: long_scoreboard first, 40% of the warp slots, issue 58%, "
-                           "DRAM 29%; profiles/k_scatter_p1_p1tet64.md)"}
+                           "DRAM 29%)"}
     else:
         bytes_dom = alg.get(dom, nnz * 12)
         achieved = bytes_dom / (ph[dom] * 1e-3) / 1e9
