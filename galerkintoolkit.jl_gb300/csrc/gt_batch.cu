@@ -8,6 +8,10 @@
 //    and runs its whole Jacobi-PCG alone -- SpMV with G lanes per row, CTA
 //    reductions through shared memory, no inter-CTA synchronisation -- then
 //    takes the next one, so the device stays full however uneven the sizes;
+//  * medium instances (up to the persistent solver's 262,144 rows, matrices
+//    of the batch's own context, FP64 or mixed mode) share cooperative
+//    launches of the persistent solver: each one on the CTAs its own solve
+//    would use, with its own bounded barrier, so many run at once;
 //  * large instances, which fill the device by themselves, run one after
 //    the other through the single-system solver of gt_solve.cu.
 //
@@ -58,8 +62,22 @@ struct BatchImpl {
   std::vector<Matrix*> mats;
   std::vector<BInst> h_inst;
   BInst* d_inst = nullptr;
+  int64_t small_rows = kSmallRows;  // scalar rows up to which an instance runs on one CTA
   std::vector<int> small, large;   // instance ids by class (small: largest first)
 };
+
+// the one-CTA tier: instances up to B->small_rows scalar rows, largest first
+static void classify(BatchImpl* B) {
+  B->small.clear();
+  B->large.clear();
+  for (int i = 0; i < B->n; i++) {
+    if (B->h_inst[i].nrows * B->h_inst[i].bs <= B->small_rows) B->small.push_back(i);
+    else B->large.push_back(i);
+  }
+  std::stable_sort(B->small.begin(), B->small.end(), [&](int a, int c) {
+    return B->h_inst[a].nrows * B->h_inst[a].bs > B->h_inst[c].nrows * B->h_inst[c].bs;
+  });
+}
 
 // CTA sum of K values, identical in every thread (fixed order); sr is one of
 // two alternating shared buffers of K * BNW doubles
@@ -441,9 +459,42 @@ static int batch_solve(gt_batch* B, const double* b, double* x, double rtol, int
     if (hres[i].status != 0) status = GT_ERR_NOT_CONVERGED;
   }
   mark(ctx, "batch_small");
+  // medium instances of this context: grouped persistent launches
+  std::vector<int> rest;
+  {
+    std::vector<int> grouped;
+    for (int i : B->large) {
+      Matrix* A = B->mats[i];
+      if ((mode == GT_SOLVE_FP64 || mode == GT_SOLVE_IR) && A->ctx == ctx && A->nbrows * A->bs <= kPersistentMaxRows)
+        grouped.push_back(i);
+      else
+        rest.push_back(i);
+    }
+    if (!grouped.empty()) {
+      std::vector<Matrix*> As;
+      std::vector<const double*> bs;
+      std::vector<double*> xs;
+      for (int i : grouped) {
+        const int64_t off = B->h_inst[i].off;
+        As.push_back(B->mats[i]);
+        bs.push_back(b + off);
+        xs.push_back(x + off);
+        GT_CUDA(ctx, cudaMemsetAsync(x + off, 0, sizeof(double) * B->mats[i]->nbrows * B->mats[i]->bs, ctx->stream));
+      }
+      std::vector<gt_solve_info> ginf;
+      std::vector<int> gst;
+      GT_TRY(pcg_persistent_groups(ctx, As, mode, bs, xs, rtol, maxit, ginf, gst));
+      for (size_t k = 0; k < grouped.size(); k++) {
+        info[grouped[k]] = ginf[k];
+        if (gst[k] != GT_OK && gst[k] != GT_ERR_NOT_CONVERGED) return gst[k];
+        if (gst[k] == GT_ERR_NOT_CONVERGED) status = gst[k];
+      }
+    }
+  }
+  mark(ctx, "batch_grouped");
   // large instances: the single-system solver, one after the other (each
   // fills the device by itself)
-  for (int i : B->large) {
+  for (int i : rest) {
     Matrix* A = B->mats[i];
     const int64_t off = B->h_inst[i].off;
     GT_CUDA(ctx, cudaMemsetAsync(x + off, 0, sizeof(double) * A->nbrows * A->bs, ctx->stream));
@@ -503,13 +554,8 @@ int gt_batch_create(gt_ctx* ctx, int n, gt_matrix* const* mats, gt_batch** out) 
     off += A->nbrows * A->bs;
     B->h_inst.push_back(in);
     B->mats.push_back(A);
-    if (A->nbrows * A->bs <= kSmallRows) B->small.push_back(i);
-    else B->large.push_back(i);
   }
-  // largest small instances first: the queue then balances the CTAs
-  std::stable_sort(B->small.begin(), B->small.end(), [&](int a, int c) {
-    return B->h_inst[a].nrows * B->h_inst[a].bs > B->h_inst[c].nrows * B->h_inst[c].bs;
-  });
+  classify(B);  // largest small instances first: the queue then balances the CTAs
   B->ntot = off;
   int s = dalloc(ctx, &B->d_inst, n);
   if (s == GT_OK) s = copy_in(ctx, B->d_inst, B->h_inst.data(), n);
@@ -525,6 +571,13 @@ int gt_batch_create(gt_ctx* ctx, int n, gt_matrix* const* mats, gt_batch** out) 
 int gt_batch_set_lanes(gt_batch* B, int lanes) {
   if (!B || (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8)) return GT_ERR_INVALID;
   B->G = lanes;
+  return GT_OK;
+}
+
+int gt_batch_set_small_rows(gt_batch* B, int64_t rows) {
+  if (!B || rows < 0 || rows > kSmallRows) return GT_ERR_INVALID;
+  B->small_rows = rows;
+  classify(B);
   return GT_OK;
 }
 

@@ -334,6 +334,14 @@ constexpr int kStagnation = 3;
 // persistent cooperative Jacobi-PCG (gt_pcg.cu); x holds the start value
 int pcg_persistent(Matrix* A, int mode, const double* b, double* x, double rtol, int maxit, int32_t* iters,
                    int32_t* nupd, int32_t* iters64, double* relres);
+// scalar rows up to which a system is solved by the persistent kernel
+constexpr int64_t kPersistentMaxRows = 262144;
+// pcg_persistent for several systems of ctx at once (GT_SOLVE_FP64 or
+// GT_SOLVE_IR), in shared cooperative launches; results bitwise those of
+// pcg_persistent on each system alone
+int pcg_persistent_groups(Ctx* ctx, const std::vector<Matrix*>& As, int mode, const std::vector<const double*>& b,
+                          const std::vector<double*>& x, double rtol, int maxit, std::vector<gt_solve_info>& infos,
+                          std::vector<int>& status);
 int spmv64(Matrix* A, const double* x, double* y);
 // the persistent solver's grid barrier run alone (gt_pcg.cu): ctas CTAs wait
 // for ctas + missing arrivals with the given time limit

@@ -60,6 +60,7 @@ struct PArgs {
   const void* val;       // iteration values (V)
   const double* val64;   // FP64 values (true residual), may be null without reliable updates
   int64_t nrows;         // block rows
+  int nb;                // CTAs that solve this system (the grouped launch)
   const double* b;
   double* x;
   void *xs, *r, *z, *p, *q;
@@ -165,14 +166,15 @@ __device__ __forceinline__ void grid_total(const double* slot, int nb, double* s
   __syncthreads();
 }
 
+// The solve of one system by nb CTAs, this CTA being number blk of them
+// (k_pcg: the whole grid; k_pcg_groups: one group of a grouped launch).
+// The shared arrays are the caller's.
 template <int BS, int G, class V, class X, bool RELIABLE>
-__global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
-  __shared__ double s_red[3 * NW];
-  __shared__ double s_tot[4];
-  __shared__ int s_abort;
+__device__ __forceinline__ void pcg_body(const PArgs& a, int nb, int blk, int init, int it_end, double* s_red,
+                                         double* s_tot, int& s_abort) {
   constexpr int NG = PT / G;  // row groups per CTA
   if (threadIdx.x == 0) s_abort = 0;
-  const int nb = gridDim.x, blk = blockIdx.x, tid = threadIdx.x;
+  const int tid = threadIdx.x;
   const int gl = tid % G, grp = tid / G;
   const int64_t rows_per = (a.nrows + nb - 1) / nb;
   const int64_t r0 = min(a.nrows, (int64_t)blk * rows_per), r1 = min(a.nrows, r0 + rows_per);
@@ -417,6 +419,31 @@ __global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
   if (blk == 0 && tid == 0) *a.st = S;
 }
 
+template <int BS, int G, class V, class X, bool RELIABLE>
+__global__ void __launch_bounds__(PT) k_pcg(PArgs a, int init, int it_end) {
+  __shared__ double s_red[3 * NW];
+  __shared__ double s_tot[4];
+  __shared__ int s_abort;
+  pcg_body<BS, G, V, X, RELIABLE>(a, gridDim.x, blockIdx.x, init, it_end, s_red, s_tot, s_abort);
+}
+
+// Several systems in one cooperative launch: CTA c is CTA map[c].y of the
+// args[map[c].x].nb CTAs that solve system map[c].x, exactly as that
+// system's own launch would (its barrier, its partial slots), for `chunk`
+// more iterations than its count at entry.
+template <int BS, int G, class V, class X, bool RELIABLE>
+__global__ void __launch_bounds__(PT) k_pcg_groups(const PArgs* __restrict__ args, const int2* __restrict__ map,
+                                                   int init, int chunk) {
+  __shared__ double s_red[3 * NW];
+  __shared__ double s_tot[4];
+  __shared__ int s_abort;
+  const int2 m = map[blockIdx.x];
+  const PArgs a = args[m.x];
+  int it_end = a.st->iters + chunk;
+  if (it_end > a.maxit || it_end < 0) it_end = a.maxit;
+  pcg_body<BS, G, V, X, RELIABLE>(a, a.nb, m.y, init, it_end, s_red, s_tot, s_abort);
+}
+
 template <int BS, class V, class X>
 __global__ void k_pdinv(const int64_t* rowptr, const int32_t* diag_pos, const V* val, int64_t nbrows, X* dinv) {
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -437,124 +464,281 @@ struct PRun {
   float* p32 = nullptr;
 };
 
+// One system's persistent solve: its CTA count (as many as give two row
+// passes per CTA, at most the co-resident CTAs of k_pcg), its buffers and
+// its kernel arguments.
 template <int BS, int G, class V, class X, bool REL>
-int run_typed(Matrix* A, const V* val, const double* b, double* x, double rtol, int maxit, double delta,
-              const PRun* from, PRun* out) {
-  Ctx* ctx = A->ctx;
-  cudaStream_t s = ctx->stream;
-  const int64_t n = A->nbrows * BS;
-  auto kern = k_pcg<BS, G, V, X, REL>;
+struct PSolve {
+  Matrix* A = nullptr;
+  int nb = 0;
+  X *xs = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
+  double* part = nullptr;
+  uint32_t* bar = nullptr;  // own (stand-alone) or a slot of a grouped launch's array
+  int32_t* err = nullptr;
+  PState* st = nullptr;
+  bool own_sync = true;     // bar, err and st allocated here
+  PArgs args{};
+};
+
+template <int BS, int G, class V, class X, bool REL>
+static int pcg_ctas(Ctx* ctx, const Matrix* A, int* nb) {
   int per_sm = 0;
-  GT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PT, 0));
+  GT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg<BS, G, V, X, REL>, PT, 0));
   if (per_sm < 1) return set_error(ctx, GT_ERR_CUDA, "persistent PCG kernel does not fit on an SM");
   constexpr int NG = PT / G;
   int64_t want = (A->nbrows + 2 * NG - 1) / (2 * NG);  // at least two row passes per CTA
   int64_t cap = (int64_t)per_sm * ctx->num_sms;
-  int nb = (int)(want < cap ? (want > 0 ? want : 1) : cap);
-  X *xs = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr;
-  double* part = nullptr;
-  uint32_t* bar = nullptr;
-  int32_t* err = nullptr;
-  PState* st = nullptr;
-  GT_TRY(dalloc(ctx, &xs, n));
-  GT_TRY(dalloc(ctx, &r, n));
-  GT_TRY(dalloc(ctx, &z, n));
-  GT_TRY(dalloc(ctx, &p, n));
-  GT_TRY(dalloc(ctx, &q, n));
-  GT_TRY(dalloc(ctx, &dinv, n));
-  GT_TRY(dalloc(ctx, &part, (int64_t)3 * nb * PSLOT));
-  GT_TRY(dalloc(ctx, &bar, 2));
-  GT_TRY(dalloc(ctx, &err, 2));
-  GT_TRY(dalloc(ctx, (unsigned char**)&st, sizeof(PState)));
-  GT_CUDA(ctx, cudaMemsetAsync(err, 0, 2 * sizeof(int32_t), s));
+  *nb = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+  return GT_OK;
+}
+
+// buffers, the start state (zero, or a continuation's) and the Jacobi
+// diagonal of one system; bar / err / st come from the caller when given
+template <int BS, int G, class V, class X, bool REL>
+static int pcg_prepare(PSolve<BS, G, V, X, REL>& P, Matrix* A, const V* val, const double* b, double* x,
+                       double rtol, int maxit, double delta, const PRun* from, uint32_t* bar = nullptr,
+                       int32_t* err = nullptr, PState* st = nullptr) {
+  Ctx* ctx = A->ctx;
+  cudaStream_t s = ctx->stream;
+  const int64_t n = A->nbrows * BS;
+  P.A = A;
+  GT_TRY((pcg_ctas<BS, G, V, X, REL>(ctx, A, &P.nb)));
+  GT_TRY(dalloc(ctx, &P.xs, n));
+  GT_TRY(dalloc(ctx, &P.r, n));
+  GT_TRY(dalloc(ctx, &P.z, n));
+  GT_TRY(dalloc(ctx, &P.p, n));
+  GT_TRY(dalloc(ctx, &P.q, n));
+  GT_TRY(dalloc(ctx, &P.dinv, n));
+  GT_TRY(dalloc(ctx, &P.part, (int64_t)3 * P.nb * PSLOT));
+  P.own_sync = bar == nullptr;
+  if (P.own_sync) {
+    GT_TRY(dalloc(ctx, &P.bar, 2));
+    GT_TRY(dalloc(ctx, &P.err, 2));
+    GT_TRY(dalloc(ctx, (unsigned char**)&P.st, sizeof(PState)));
+    GT_CUDA(ctx, cudaMemsetAsync(P.err, 0, 2 * sizeof(int32_t), s));
+  } else {
+    P.bar = bar;
+    P.err = err;
+    P.st = st;
+  }
   if (from) {
     // continuation: scalars of the FP32 run (iteration count, ||b||, rzold)
     PState* h0 = reinterpret_cast<PState*>(ctx->h_dscratch);
     *h0 = from->st;
     h0->done = 0;
-    GT_CUDA(ctx, cudaMemcpyAsync(st, h0, sizeof(PState), cudaMemcpyHostToDevice, s));
+    GT_CUDA(ctx, cudaMemcpyAsync(P.st, h0, sizeof(PState), cudaMemcpyHostToDevice, s));
     GT_CUDA(ctx, cudaStreamSynchronize(s));
   } else {
-    GT_CUDA(ctx, cudaMemsetAsync(st, 0, sizeof(PState), s));
+    GT_CUDA(ctx, cudaMemsetAsync(P.st, 0, sizeof(PState), s));
   }
   GT_TRY(find_diag(A));
   const double* dval = REL ? A->val64 : (const double*)nullptr;
   if (REL || A->val64)
-    k_pdinv<BS, double, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, A->val64, A->nbrows, dinv);
+    k_pdinv<BS, double, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, A->val64, A->nbrows,
+                                                                         P.dinv);
   else
-    k_pdinv<BS, V, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, dinv);
+    k_pdinv<BS, V, X><<<GT_KC(ctx, grid_for(n, 256)), 256, 0, s>>>(A->rowptr, A->diag_pos, val, A->nbrows, P.dinv);
   GT_LAUNCH(ctx, "k_pdinv");
-  PArgs args{};
+  PArgs& args = P.args;
   args.rowptr = A->rowptr;
   args.colind = A->colind;
   args.val = val;
   args.val64 = dval;
   args.nrows = A->nbrows;
+  args.nb = P.nb;
   args.b = b;
   args.x = x;
-  args.xs = xs;
-  args.r = r;
-  args.z = z;
-  args.p = p;
-  args.q = q;
-  args.dinv = dinv;
+  args.xs = P.xs;
+  args.r = P.r;
+  args.z = P.z;
+  args.p = P.p;
+  args.q = P.q;
+  args.dinv = P.dinv;
   args.pcont = from ? from->p32 : nullptr;
-  args.part = part;
-  args.bar = bar;
-  args.err = err;
-  args.st = st;
+  args.part = P.part;
+  args.bar = P.bar;
+  args.err = P.err;
+  args.st = P.st;
   args.rtol2 = rtol * rtol;
   args.delta2 = delta * delta;
   args.maxit = maxit;
   args.stall_ratio = ctx->ir_stall_ratio;
   args.stall_count = ctx->ir_stall_count;
-  PState h{};
+  return GT_OK;
+}
+
+// the outcome of a finished system (h: its final state; err: a barrier timed
+// out) and the release of its buffers (a stalled FP32 run keeps p for the
+// FP64 continuation)
+template <int BS, int G, class V, class X, bool REL>
+static int pcg_finish(PSolve<BS, G, V, X, REL>& P, const PState& h, bool err, PRun* out) {
+  Ctx* ctx = P.A->ctx;
   int status = GT_OK;
+  if (err) status = set_error(ctx, GT_ERR_TIMEOUT, "persistent PCG: a grid barrier timed out");
+  out->st = h;
+  if (status == GT_OK && h.done == 2) {
+    status = PCG_STALLED;
+    out->stalled = true;
+    if constexpr (sizeof(X) == sizeof(float)) {
+      out->p32 = reinterpret_cast<float*>(P.p);
+      P.p = nullptr;
+    }
+  } else if (status == GT_OK && !(h.rr <= h.tol2)) {
+    status = GT_ERR_NOT_CONVERGED;
+  }
+  dfree(ctx, P.xs);
+  dfree(ctx, P.r);
+  dfree(ctx, P.z);
+  dfree(ctx, P.p);
+  dfree(ctx, P.q);
+  dfree(ctx, P.dinv);
+  dfree(ctx, P.part);
+  if (P.own_sync) {
+    dfree(ctx, P.bar);
+    dfree(ctx, P.err);
+    pool_free(ctx, P.st);
+  }
+  return status;
+}
+
+template <int BS, int G, class V, class X, bool REL>
+int run_typed(Matrix* A, const V* val, const double* b, double* x, double rtol, int maxit, double delta,
+              const PRun* from, PRun* out) {
+  Ctx* ctx = A->ctx;
+  cudaStream_t s = ctx->stream;
+  auto kern = k_pcg<BS, G, V, X, REL>;
+  PSolve<BS, G, V, X, REL> P;
+  GT_TRY((pcg_prepare<BS, G, V, X, REL>(P, A, val, b, x, rtol, maxit, delta, from)));
+  PArgs& args = P.args;
+  PState h{};
+  bool err = false;
   int chunk = 32, done_iters = from ? from->st.iters : 0;
   for (int launch = 0;; launch++) {
     int init = launch == 0 ? (from ? 2 : 1) : 0;
     int it_end = done_iters + chunk;
     if (it_end > maxit || it_end < 0) it_end = maxit;
-    GT_CUDA(ctx, cudaMemsetAsync(bar, 0, sizeof(uint32_t), s));
+    GT_CUDA(ctx, cudaMemsetAsync(P.bar, 0, sizeof(uint32_t), s));
     void* kargs[] = {&args, &init, &it_end};
     ctx->launches++;
-    GT_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(nb), dim3(PT), kargs, 0, s));
-    GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, st, sizeof(PState), cudaMemcpyDeviceToHost, s));
-    GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_scratch, err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    GT_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3(P.nb), dim3(PT), kargs, 0, s));
+    GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_dscratch, P.st, sizeof(PState), cudaMemcpyDeviceToHost, s));
+    GT_CUDA(ctx, cudaMemcpyAsync(ctx->h_scratch, P.err, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     GT_CUDA(ctx, cudaStreamSynchronize(s));
     memcpy(&h, ctx->h_dscratch, sizeof(PState));
     int32_t e = 0;
     memcpy(&e, ctx->h_scratch, sizeof(int32_t));
     if (e) {
-      status = set_error(ctx, GT_ERR_TIMEOUT, "persistent PCG: a grid barrier timed out");
+      err = true;
       break;
     }
     done_iters = h.iters;
     if (h.done || h.iters >= maxit) break;
     if (chunk < 2048) chunk *= 2;
   }
-  out->st = h;
-  if (status == GT_OK && h.done == 2) {
-    status = PCG_STALLED;
-    out->stalled = true;
-    if constexpr (sizeof(X) == sizeof(float)) {
-      out->p32 = reinterpret_cast<float*>(p);
-      p = nullptr;
+  return pcg_finish<BS, G, V, X, REL>(P, h, err, out);
+}
+
+// Grouped persistent solves: systems of one block size and lane count, each
+// on the CTAs its stand-alone solve would use (so its partition, its
+// reductions and its result are bitwise that solve's), packed in order into
+// cooperative launches whose CTAs are co-resident; every system waits only
+// on its own bounded barrier.  All systems of one call start alike (froms
+// all null, or all continuations).  A system larger than one launch holds
+// is solved stand-alone.
+template <int BS, int G, class V, class X, bool REL>
+static int run_groups_typed(Ctx* ctx, const std::vector<Matrix*>& As, const std::vector<const V*>& vals,
+                            const std::vector<const double*>& bs, const std::vector<double*>& xs, double rtol,
+                            int maxit, double delta, const std::vector<const PRun*>& froms, std::vector<PRun>& outs,
+                            std::vector<int>& status) {
+  cudaStream_t s = ctx->stream;
+  const int n = (int)As.size();
+  auto kern = k_pcg_groups<BS, G, V, X, REL>;
+  int per_sm = 0;
+  GT_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, PT, 0));
+  const int64_t cap = (int64_t)(per_sm > 0 ? per_sm : 0) * ctx->num_sms;
+  std::vector<int> nbs(n);
+  for (int i = 0; i < n; i++) GT_TRY((pcg_ctas<BS, G, V, X, REL>(ctx, As[i], &nbs[i])));
+  int i0 = 0;
+  while (i0 < n) {
+    int i1 = i0;
+    int64_t tot = 0;
+    while (i1 < n && tot + nbs[i1] <= cap) tot += nbs[i1++];
+    if (i1 == i0) {
+      status[i0] = run_typed<BS, G, V, X, REL>(As[i0], vals[i0], bs[i0], xs[i0], rtol, maxit, delta, froms[i0],
+                                               &outs[i0]);
+      i0++;
+      continue;
     }
-  } else if (status == GT_OK && !(h.rr <= h.tol2)) {
-    status = GT_ERR_NOT_CONVERGED;
+    const int m = i1 - i0;
+    uint32_t* bars = nullptr;
+    int32_t* errs = nullptr;
+    PState* sts = nullptr;
+    PArgs* dargs = nullptr;
+    int2* dmap = nullptr;
+    GT_TRY(dalloc(ctx, &bars, 2 * (int64_t)m));
+    GT_TRY(dalloc(ctx, &errs, 2 * (int64_t)m));
+    GT_TRY(dalloc(ctx, (unsigned char**)&sts, (int64_t)sizeof(PState) * m));
+    GT_TRY(dalloc(ctx, (unsigned char**)&dargs, (int64_t)sizeof(PArgs) * m));
+    GT_TRY(dalloc(ctx, (unsigned char**)&dmap, (int64_t)sizeof(int2) * tot));
+    GT_CUDA(ctx, cudaMemsetAsync(errs, 0, sizeof(int32_t) * 2 * m, s));
+    std::vector<PSolve<BS, G, V, X, REL>> P(m);
+    std::vector<PArgs> hargs(m);
+    std::vector<int2> hmap;
+    hmap.reserve(tot);
+    for (int k = 0; k < m; k++) {
+      const int i = i0 + k;
+      GT_TRY((pcg_prepare<BS, G, V, X, REL>(P[k], As[i], vals[i], bs[i], xs[i], rtol, maxit, delta, froms[i],
+                                            bars + 2 * k, errs + 2 * k, sts + k)));
+      hargs[k] = P[k].args;
+      for (int j = 0; j < P[k].nb; j++) hmap.push_back(make_int2(k, j));
+    }
+    GT_TRY(copy_in(ctx, (unsigned char*)dargs, (const unsigned char*)hargs.data(), (int64_t)sizeof(PArgs) * m));
+    GT_TRY(copy_in(ctx, (unsigned char*)dmap, (const unsigned char*)hmap.data(), (int64_t)sizeof(int2) * tot));
+    std::vector<PState> h(m);
+    std::vector<int32_t> e(2 * m, 0);
+    bool err = false;
+    int chunk = 32;
+    for (int launch = 0;; launch++) {
+      int init = launch == 0 ? (froms[i0] ? 2 : 1) : 0;
+      GT_CUDA(ctx, cudaMemsetAsync(bars, 0, sizeof(uint32_t) * 2 * m, s));
+      void* kargs[] = {&dargs, &dmap, &init, &chunk};
+      ctx->launches++;
+      GT_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3((unsigned)tot), dim3(PT), kargs, 0, s));
+      GT_CUDA(ctx, cudaMemcpyAsync(h.data(), sts, sizeof(PState) * m, cudaMemcpyDeviceToHost, s));
+      GT_CUDA(ctx, cudaMemcpyAsync(e.data(), errs, sizeof(int32_t) * 2 * m, cudaMemcpyDeviceToHost, s));
+      GT_CUDA(ctx, cudaStreamSynchronize(s));
+      bool all = true;
+      for (int k = 0; k < m; k++) {
+        err |= e[2 * k] != 0;
+        all &= h[k].done != 0 || h[k].iters >= maxit;
+      }
+      if (err || all) break;
+      if (chunk < 2048) chunk *= 2;
+    }
+    for (int k = 0; k < m; k++) status[i0 + k] = pcg_finish<BS, G, V, X, REL>(P[k], h[k], err, &outs[i0 + k]);
+    dfree(ctx, bars);
+    dfree(ctx, errs);
+    pool_free(ctx, sts);
+    pool_free(ctx, dargs);
+    pool_free(ctx, dmap);
+    i0 = i1;
   }
-  dfree(ctx, xs);
-  dfree(ctx, r);
-  dfree(ctx, z);
-  dfree(ctx, p);
-  dfree(ctx, q);
-  dfree(ctx, dinv);
-  dfree(ctx, part);
-  dfree(ctx, bar);
-  dfree(ctx, err);
-  pool_free(ctx, st);
-  return status;
+  return GT_OK;
+}
+
+template <class V, class X, bool REL>
+static int run_groups_dispatch(Ctx* ctx, int bs, int G, const std::vector<Matrix*>& As,
+                               const std::vector<const V*>& vals, const std::vector<const double*>& b,
+                               const std::vector<double*>& x, double rtol, int maxit, double delta,
+                               const std::vector<const PRun*>& froms, std::vector<PRun>& outs,
+                               std::vector<int>& status) {
+#define GT_PCGG_CASE(BS_, G_)                                                                                  \
+  if (bs == BS_ && G == G_)                                                                                    \
+    return run_groups_typed<BS_, G_, V, X, REL>(ctx, As, vals, b, x, rtol, maxit, delta, froms, outs, status);
+  GT_PCGG_CASE(1, 1) GT_PCGG_CASE(1, 2) GT_PCGG_CASE(1, 4) GT_PCGG_CASE(1, 8)
+  GT_PCGG_CASE(3, 1) GT_PCGG_CASE(3, 2) GT_PCGG_CASE(3, 4) GT_PCGG_CASE(3, 8)
+#undef GT_PCGG_CASE
+  return set_error(ctx, GT_ERR_UNSUPPORTED, "grouped persistent PCG: unsupported block size");
 }
 
 template <class V, class X, bool REL>
@@ -609,6 +793,86 @@ int barrier_probe(Ctx* ctx, int ctas, int missing, int64_t timeout_ns) {
   dfree(ctx, bar);
   dfree(ctx, err);
   return e ? set_error(ctx, GT_ERR_TIMEOUT, "barrier probe: the grid barrier timed out") : GT_OK;
+}
+
+// pcg_persistent for several systems of ctx (FP64 or FP32 with reliable
+// updates), grouped into shared cooperative launches by block size and
+// lane count; x: start values; per-system infos and statuses.  Each system's
+// result is bitwise that of pcg_persistent on it alone.
+int pcg_persistent_groups(Ctx* ctx, const std::vector<Matrix*>& As, int mode, const std::vector<const double*>& b,
+                          const std::vector<double*>& x, double rtol, int maxit, std::vector<gt_solve_info>& infos,
+                          std::vector<int>& status) {
+  const int n = (int)As.size();
+  infos.assign(n, gt_solve_info{});
+  status.assign(n, GT_OK);
+  if (mode != GT_SOLVE_FP64 && mode != GT_SOLVE_IR)
+    return set_error(ctx, GT_ERR_INVALID, "grouped persistent PCG: FP64 or mixed mode");
+  std::vector<PRun> runs(n);
+  for (int bs : {1, 3})
+    for (int g : {1, 2, 4, 8}) {
+      std::vector<int> ids;
+      for (int i = 0; i < n; i++)
+        if (As[i]->bs == bs && lanes_for(As[i]) == g) ids.push_back(i);
+      if (ids.empty()) continue;
+      std::vector<Matrix*> A;
+      std::vector<const double*> bb;
+      std::vector<double*> xx;
+      std::vector<const PRun*> none(ids.size(), nullptr);
+      std::vector<PRun> out(ids.size());
+      std::vector<int> st(ids.size(), GT_OK);
+      for (int i : ids) {
+        A.push_back(As[i]);
+        bb.push_back(b[i]);
+        xx.push_back(x[i]);
+      }
+      if (mode == GT_SOLVE_FP64) {
+        std::vector<const double*> v;
+        for (Matrix* M : A) v.push_back(M->val64);
+        GT_TRY((run_groups_dispatch<double, double, true>(ctx, bs, g, A, v, bb, xx, rtol, maxit, 0.0, none, out, st)));
+        for (size_t k = 0; k < ids.size(); k++) infos[ids[k]].fp64_iterations = out[k].st.iters;
+      } else {
+        std::vector<const float*> v;
+        for (Matrix* M : A) v.push_back(M->val32);
+        GT_TRY((run_groups_dispatch<float, float, true>(ctx, bs, g, A, v, bb, xx, rtol, maxit, ctx->ir_delta, none,
+                                                        out, st)));
+        // stalled FP32 runs go on in FP64 from their FP64 solutions, as alone
+        std::vector<size_t> sk;
+        for (size_t k = 0; k < ids.size(); k++)
+          if (st[k] == PCG_STALLED) sk.push_back(k);
+        if (!sk.empty()) {
+          std::vector<Matrix*> A2;
+          std::vector<const double*> v2, b2;
+          std::vector<double*> x2;
+          std::vector<const PRun*> f2;
+          for (size_t k : sk) {
+            A2.push_back(A[k]);
+            v2.push_back(A[k]->val64);
+            b2.push_back(bb[k]);
+            x2.push_back(xx[k]);
+            f2.push_back(&out[k]);
+          }
+          std::vector<PRun> o2(sk.size());
+          std::vector<int> s2(sk.size(), GT_OK);
+          int e = run_groups_dispatch<double, double, true>(ctx, bs, g, A2, v2, b2, x2, rtol, maxit, 0.0, f2, o2, s2);
+          for (size_t k : sk)
+            if (out[k].p32) pool_free(ctx, out[k].p32);
+          GT_TRY(e);
+          for (size_t j = 0; j < sk.size(); j++) {
+            infos[ids[sk[j]]].fp64_iterations = o2[j].st.iters - out[sk[j]].st.iters;
+            out[sk[j]] = o2[j];
+            st[sk[j]] = s2[j];
+          }
+        }
+      }
+      for (size_t k = 0; k < ids.size(); k++) {
+        gt_solve_info& inf = infos[ids[k]];
+        inf.iterations = out[k].st.iters;
+        inf.outer_iterations = out[k].st.nupd;
+        inf.rel_residual = out[k].st.bb > 0 ? sqrt(out[k].st.rr / out[k].st.bb) : 0.0;
+        status[ids[k]] = st[k];
+      }
+    }
+  return GT_OK;
 }
 
 int pcg_persistent(Matrix* A, int mode, const double* b, double* x, double rtol, int maxit, int32_t* iters,

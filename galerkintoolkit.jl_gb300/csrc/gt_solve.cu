@@ -28,7 +28,6 @@ constexpr unsigned kOneLevel = 2048;  // grids up to this size reduce in one lev
 constexpr int64_t kLoopUpdate = int64_t(1) << 22;  // vector length of the looping update kernels
 constexpr int CHUNK = 16;   // CG iterations between host polls
 constexpr int CG_STALLED = 1;  // internal status: the FP32 iteration stalled
-constexpr int64_t kPersistentMaxRows = 262144;  // scalar rows solved by the persistent kernel
 
 // Programmatic dependent launch (sm_90 and later) for the kernels of a CG
 // iteration: each is launched with programmatic stream serialisation, so its

@@ -88,6 +88,7 @@ SIGNATURES = [
     ("gt_spmv", I32, [P, P, P]),
     ("gt_batch_create", I32, [P, I32, P, C.POINTER(P)]),
     ("gt_batch_set_lanes", I32, [P, I32]),
+    ("gt_batch_set_small_rows", I32, [P, I64]),
     ("gt_batch_info", I32, [P, P]),
     ("gt_batch_solve", I32, [P, P, P, DBL, I32, I32, P]),
     ("gt_batch_destroy", I32, [P]),

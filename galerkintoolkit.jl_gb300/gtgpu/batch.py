@@ -44,7 +44,7 @@ class Batch:
     (they may come from several contexts); solved on ``ctx`` (default: the
     first matrix's)."""
 
-    def __init__(self, matrices, lanes: int | None = None, ctx=None):
+    def __init__(self, matrices, lanes: int | None = None, ctx=None, small_rows: int | None = None):
         if not matrices:
             raise ValueError("empty batch")
         self.mats = list(matrices)
@@ -57,9 +57,17 @@ class Batch:
         self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
         if lanes:
             self.set_lanes(lanes)
+        if small_rows is not None:
+            self.set_small_rows(small_rows)
 
     def set_lanes(self, lanes: int):
         check(self.ctx.h, self.ctx.lib.gt_batch_set_lanes(self.h, int(lanes)))
+
+    def set_small_rows(self, rows: int):
+        """scalar rows up to which an instance is solved by one CTA (at most
+        32768); larger instances of the batch's own context, up to 262,144
+        rows, share grouped persistent launches (FP64 and mixed modes)"""
+        check(self.ctx.h, self.ctx.lib.gt_batch_set_small_rows(self.h, int(rows)))
 
     def info(self):
         a = np.zeros(4, np.int64)

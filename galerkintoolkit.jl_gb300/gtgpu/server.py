@@ -23,14 +23,16 @@ request's latency.  Every kernel reduces in a fixed order per request, and a
 refill gives bitwise the values of a fresh assembly, so a request's result
 is bitwise the same alone, in any mix, hit or miss.
 
-Continuous batching: a slot that takes a small request (Poisson or
-elasticity, at most ``batch_rows`` scalar rows) also takes the other small
-requests pending at that moment (up to ``batch_max``, within the budget) and
-solves them together (``gt_batch``: one persistent launch per block size,
-one CTA per request, each running its whole CG alone), so a stream of small
-requests is not served one grid-wide solve at a time.  Small requests always
-take this path, even alone, so a request's result never depends on its
-batch.
+Continuous batching: a slot that takes a request of at most ``batch_rows``
+scalar rows (Poisson or elasticity; by default 2,048) also takes the other
+such requests pending at that moment (up to ``batch_max``, within the
+budget) and solves them together with ``gt_batch``: those up to
+``small_rows`` rows one CTA each in one persistent launch per block size,
+larger ones (when ``batch_rows`` admits them) in shared grouped persistent
+launches, each on the CTAs its own solve would use.  So a stream of small
+requests is not served one grid-wide solve at a time, and a request's result
+never depends on its batch: the one-CTA tier's depends on the request alone,
+the grouped tier's is bitwise that of the request's own solve.
 
 ``request_stream`` draws the seeded request mix of the serving benchmark:
 Poisson arrivals, each request Poisson or linear elasticity on Q1 or Q2
@@ -259,14 +261,16 @@ def run_request(req: Request, ctx: Context, precision="mixed", rtol=1e-8, keep_s
 
 
 def run_batch_requests(reqs, ctx: Context, precision="mixed", rtol=1e-8, keep_solution=True, cache=None,
-                       library=None):
-    """Assemble (or refill) several small requests on ctx and solve them in
-    one persistent launch per block size (gt_batch, one CTA per request)."""
+                       library=None, small_rows=2048):
+    """Assemble (or refill) several requests on ctx and solve them together
+    (gt_batch): those up to small_rows scalar rows one CTA each in one
+    persistent launch per block size, the larger ones in grouped persistent
+    launches (each on the CTAs its own solve would use)."""
     from .batch import Batch
     library = library or MeshLibrary()
     taken = set()  # cached instances handed to this batch: one per request
     built = [_assemble(r, ctx, precision, cache, library, taken) for r in reqs]
-    B = Batch([A for A, _, _ in built], ctx=ctx)
+    B = Batch([A for A, _, _ in built], ctx=ctx, small_rows=small_rows)
     x, infos = B.solve([b for _, b, _ in built], rtol=rtol, maxit=200000,
                        mode="ir" if precision == "mixed" else "fp64", raise_on_fail=False)
     for r, xi, info in zip(reqs, B.split(x), infos):
@@ -281,7 +285,7 @@ def run_batch_requests(reqs, ctx: Context, precision="mixed", rtol=1e-8, keep_so
 class Server:
     def __init__(self, slots=4, budget_bytes=150e9, precision="mixed", rtol=1e-8, device=0, keep_solutions=True,
                  ctx_factory=None, runner=None, policy="sjf", cache_fraction=0.1, library=None, batching=True,
-                 batch_max=16, batch_rows=2048):
+                 batch_max=16, batch_rows=2048, small_rows=2048):
         self.slots = slots
         self.runner = runner or run_request
         self.budget = float(budget_bytes)
@@ -289,16 +293,23 @@ class Server:
         self.rtol = rtol
         self.keep = keep_solutions
         self.policy = policy
-        # small requests go through the batched kernel (alone or with
-        # others, up to batch_max); batching=False: one grid-wide solve per
-        # request.  One CTA solves a batched request, so a batch lasts as
-        # long as its largest member: the row limit keeps batches short (on
-        # GB300, under the 2000 req/s stream, 2048 scalar rows and batches
-        # of 16 completed 1.8x the requests of 32768 and 64 at a p50 of
-        # 10 ms instead of 0.4 s)
+        # requests up to batch_rows scalar rows go through gt_batch (alone
+        # or with others, up to batch_max); batching=False: one grid-wide
+        # solve per request.  In a batch, requests up to small_rows are
+        # solved by one CTA each, so that tier lasts as long as its largest
+        # member: the limit keeps it short (on GB300, under the 2000 req/s
+        # stream, 2048 scalar rows and batches of 16 completed 1.8x the
+        # requests of 32768 and 64 at a p50 of 10 ms instead of 0.4 s); the
+        # larger ones, when batch_rows lets them in, share grouped persistent
+        # launches, each bitwise its own solve.  Measured with batch_rows
+        # 262,144: 588 requests/s at a p50 of 138 ms against 604 at 9.3 ms
+        # (a batch then waits for its grouped launches, and requests of one
+        # geometry in one batch each need their own resident instance), so
+        # by default only the one-CTA requests are batched
         self.batching = batching and runner is None
         self.batch_max = max(1, batch_max)
         self.batch_rows = batch_rows
+        self.small_rows = small_rows
         self.library = library or MeshLibrary()
         self.ctxs = [(ctx_factory or (lambda: Context(device)))() for _ in range(slots)]
         # each slot caches geometries up to its share of cache_fraction of the
@@ -388,7 +399,7 @@ class Server:
             try:
                 if self._batchable(reqs[0]):  # a batch of one too: the result never depends on the batch
                     run_batch_requests(reqs, ctx, self.precision, self.rtol, self.keep, cache=cache,
-                                       library=self.library)
+                                       library=self.library, small_rows=self.small_rows)
                 elif cache is not None:
                     self.runner(reqs[0], ctx, self.precision, self.rtol, self.keep, cache=cache, library=self.library)
                 else:

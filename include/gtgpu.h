@@ -275,10 +275,11 @@ int gt_spmv(gt_matrix* matrix, const double* x, double* y);
  * A batch of n assembled matrices of block size 1 (scalar problems) or 3
  * (3-D elasticity) on the device of ctx (they may come from other contexts
  * of that device, e.g. assembled concurrently on several streams), solved
- * together on ctx's stream: instances of up to 32768 scalar rows in one
- * persistent launch per block size in which each CTA takes instances from a
- * queue (largest first) and runs each one's whole Jacobi-PCG alone; larger
- * instances one after the other through the single-system solver.  An
+ * together on ctx's stream: instances of up to 32768 scalar rows (see
+ * gt_batch_set_small_rows) in one persistent launch per block size in which
+ * each CTA takes instances from a queue (largest first) and runs each one's
+ * whole Jacobi-PCG alone; medium ones in grouped persistent launches (below);
+ * larger ones one after the other through the single-system solver.  An
  * instance's result does not depend on the rest of the batch.  b and x are
  * the instances' vectors concatenated in batch order (num_free_dofs each,
  * FP64); x is the output (every solve starts from 0).  infos: n entries.
@@ -289,6 +290,11 @@ int gt_batch_create(gt_ctx* ctx, int n, gt_matrix* const* matrices, gt_batch** b
  * 4 or 8; 0, the default: each instance's own, from its mean row length;
  * block rows of 3 take 2 or 4: 1 -> 2, 8 -> 4) */
 int gt_batch_set_lanes(gt_batch* batch, int lanes);
+/* scalar rows up to which an instance is solved by one CTA (0 .. 32768; the
+ * default 32768); larger ones up to 262,144 rows, of ctx's own matrices,
+ * share grouped persistent launches in GT_SOLVE_FP64 / GT_SOLVE_IR mode,
+ * each bitwise as its own gt_solve would give */
+int gt_batch_set_small_rows(gt_batch* batch, int64_t rows);
 /* info[0]=instances info[1]=total scalar rows info[2]=instances solved one per CTA
  * info[3]=lanes */
 int gt_batch_info(const gt_batch* batch, int64_t* info);

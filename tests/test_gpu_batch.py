@@ -76,6 +76,32 @@ def test_batch_of_block_matrices(mode):
         assert np.array_equal(alone, parts[k])
 
 
+@pytest.mark.parametrize("mode", ["fp64", "ir"])
+def test_grouped_tier_is_bitwise_the_single_solves(mode):
+    """Medium instances (above the one-CTA limit, up to 262,144 rows) share
+    grouped persistent launches, each on the CTAs of its own solve: every
+    solution is bitwise what gt_solve gives for the instance alone, scalar
+    and 3 x 3 block matrices alike."""
+    specs = [GB.InstanceSpec(0, 2, 1, 150), GB.InstanceSpec(1, 3, 1, 30), GB.InstanceSpec(2, 2, 2, 60),
+             GB.InstanceSpec(3, 2, 1, 9), GB.InstanceSpec(4, 3, 2, 12)]
+    inst = [GB.assemble_instance(s, seed=8, T="mixed") for s in specs]
+    m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (12, 12, 12))
+    V = GT.lagrange_space(GT.interior(m), 1, tensor_size=(3,), dirichlet_boundary=GT.boundary(m, ["2-face-5"]))
+    Ae, be = GT.assemble_matrix_and_vector(GT.elasticity(GT.lognormal_cells(m.num_cells, 0.5, 77), 0.3),
+                                           GT.source([0.0, 0.0, -1.0]), "mixed", V)
+    mats = [A for _, _, A, _ in inst] + [Ae]
+    bs = [b for _, _, _, b in inst] + [be]
+    B = GB.Batch(mats, small_rows=1024)
+    assert B.info()["small_instances"] == 1
+    x, infos = B.solve(bs, rtol=1e-10, mode=mode)
+    for k, (A, b, xb) in enumerate(zip(mats, bs, B.split(x))):
+        xs, info = GT.solve(A, b, rtol=1e-10, mode=mode)
+        assert infos[k]["rel_residual"] <= 1e-10
+        if A.shape[0] > 1024:
+            assert np.array_equal(xb, xs), k
+            assert infos[k]["iterations"] == info["iterations"]
+
+
 def test_autotune_picks_a_candidate(tmp_path):
     inst = _instances()
     B = GB.Batch([A for _, _, A, _ in inst])

@@ -85,3 +85,29 @@ def test_device_coefficients_match_host_generator():
         d = GT.lognormal_cells_device(n, 0.5, seed).numpy()
         h = GT.lognormal_cells(n, 0.5, seed)
         assert np.all(d > 0) and np.abs(d - h).max() <= 1e-14 * np.abs(h).max()
+
+
+def test_batched_medium_requests_are_bitwise_their_own_solves():
+    """Requests above the one-CTA limit are batched into grouped persistent
+    launches; each result is bitwise that of the same request served with
+    batching off (one persistent solve per request).  Those up to the limit
+    (one CTA each) agree within the tolerance."""
+    from gtgpu.server import Request
+    def reqs():
+        return [Request(i, 0.0, "elasticity" if i % 3 == 2 else "poisson", 1 + (i % 2), (14, 10, 8, 12, 16, 7)[i],
+                        700 + i) for i in range(6)]
+    a, b = reqs(), reqs()
+    s1 = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo", batch_rows=262144)
+    rep = s1.serve(a, realtime=False)
+    s2 = Server(slots=1, budget_bytes=150e9, rtol=1e-10, policy="fifo", batching=False)
+    s2.serve(b, realtime=False)
+    s1.close()
+    s2.close()
+    assert rep["completed"] == 6
+    assert any(r.scalar_rows > 2048 for r in a)
+    for ra, rb in zip(a, b):
+        assert ra.rel_residual <= 1e-10
+        if ra.scalar_rows > 2048:
+            assert np.array_equal(ra.solution, rb.solution), (ra.form, ra.order, ra.cells_per_dir)
+        else:
+            assert np.abs(ra.solution - rb.solution).max() <= 1e-8 * np.abs(rb.solution).max()
