@@ -675,52 +675,63 @@ static int run_groups_typed(Ctx* ctx, const std::vector<Matrix*>& As, const std:
     PState* sts = nullptr;
     PArgs* dargs = nullptr;
     int2* dmap = nullptr;
-    GT_TRY(dalloc(ctx, &bars, 2 * (int64_t)m));
-    GT_TRY(dalloc(ctx, &errs, 2 * (int64_t)m));
-    GT_TRY(dalloc(ctx, (unsigned char**)&sts, (int64_t)sizeof(PState) * m));
-    GT_TRY(dalloc(ctx, (unsigned char**)&dargs, (int64_t)sizeof(PArgs) * m));
-    GT_TRY(dalloc(ctx, (unsigned char**)&dmap, (int64_t)sizeof(int2) * tot));
-    GT_CUDA(ctx, cudaMemsetAsync(errs, 0, sizeof(int32_t) * 2 * m, s));
     std::vector<PSolve<BS, G, V, X, REL>> P(m);
-    std::vector<PArgs> hargs(m);
-    std::vector<int2> hmap;
-    hmap.reserve(tot);
-    for (int k = 0; k < m; k++) {
-      const int i = i0 + k;
-      GT_TRY((pcg_prepare<BS, G, V, X, REL>(P[k], As[i], vals[i], bs[i], xs[i], rtol, maxit, delta, froms[i],
-                                            bars + 2 * k, errs + 2 * k, sts + k)));
-      hargs[k] = P[k].args;
-      for (int j = 0; j < P[k].nb; j++) hmap.push_back(make_int2(k, j));
-    }
-    GT_TRY(copy_in(ctx, (unsigned char*)dargs, (const unsigned char*)hargs.data(), (int64_t)sizeof(PArgs) * m));
-    GT_TRY(copy_in(ctx, (unsigned char*)dmap, (const unsigned char*)hmap.data(), (int64_t)sizeof(int2) * tot));
+    int prepared = 0;
     std::vector<PState> h(m);
-    std::vector<int32_t> e(2 * m, 0);
     bool err = false;
-    int chunk = 32;
-    for (int launch = 0;; launch++) {
-      int init = launch == 0 ? (froms[i0] ? 2 : 1) : 0;
-      GT_CUDA(ctx, cudaMemsetAsync(bars, 0, sizeof(uint32_t) * 2 * m, s));
-      void* kargs[] = {&dargs, &dmap, &init, &chunk};
-      ctx->launches++;
-      GT_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3((unsigned)tot), dim3(PT), kargs, 0, s));
-      GT_CUDA(ctx, cudaMemcpyAsync(h.data(), sts, sizeof(PState) * m, cudaMemcpyDeviceToHost, s));
-      GT_CUDA(ctx, cudaMemcpyAsync(e.data(), errs, sizeof(int32_t) * 2 * m, cudaMemcpyDeviceToHost, s));
-      GT_CUDA(ctx, cudaStreamSynchronize(s));
-      bool all = true;
-      for (int k = 0; k < m; k++) {
-        err |= e[2 * k] != 0;
-        all &= h[k].done != 0 || h[k].iters >= maxit;
+    // one wave; every exit below goes through the release of its blocks
+    auto wave = [&]() -> int {
+      GT_TRY(dalloc(ctx, &bars, 2 * (int64_t)m));
+      GT_TRY(dalloc(ctx, &errs, 2 * (int64_t)m));
+      GT_TRY(dalloc(ctx, (unsigned char**)&sts, (int64_t)sizeof(PState) * m));
+      GT_TRY(dalloc(ctx, (unsigned char**)&dargs, (int64_t)sizeof(PArgs) * m));
+      GT_TRY(dalloc(ctx, (unsigned char**)&dmap, (int64_t)sizeof(int2) * tot));
+      GT_CUDA(ctx, cudaMemsetAsync(errs, 0, sizeof(int32_t) * 2 * m, s));
+      std::vector<PArgs> hargs(m);
+      std::vector<int2> hmap;
+      hmap.reserve(tot);
+      for (int k = 0; k < m; k++, prepared++) {
+        const int i = i0 + k;
+        GT_TRY((pcg_prepare<BS, G, V, X, REL>(P[k], As[i], vals[i], bs[i], xs[i], rtol, maxit, delta, froms[i],
+                                              bars + 2 * k, errs + 2 * k, sts + k)));
+        hargs[k] = P[k].args;
+        for (int j = 0; j < P[k].nb; j++) hmap.push_back(make_int2(k, j));
       }
-      if (err || all) break;
-      if (chunk < 2048) chunk *= 2;
+      GT_TRY(copy_in(ctx, (unsigned char*)dargs, (const unsigned char*)hargs.data(), (int64_t)sizeof(PArgs) * m));
+      GT_TRY(copy_in(ctx, (unsigned char*)dmap, (const unsigned char*)hmap.data(), (int64_t)sizeof(int2) * tot));
+      std::vector<int32_t> e(2 * m, 0);
+      int chunk = 32;
+      for (int launch = 0;; launch++) {
+        int init = launch == 0 ? (froms[i0] ? 2 : 1) : 0;
+        GT_CUDA(ctx, cudaMemsetAsync(bars, 0, sizeof(uint32_t) * 2 * m, s));
+        void* kargs[] = {&dargs, &dmap, &init, &chunk};
+        ctx->launches++;
+        GT_CUDA(ctx, cudaLaunchCooperativeKernel((const void*)kern, dim3((unsigned)tot), dim3(PT), kargs, 0, s));
+        GT_CUDA(ctx, cudaMemcpyAsync(h.data(), sts, sizeof(PState) * m, cudaMemcpyDeviceToHost, s));
+        GT_CUDA(ctx, cudaMemcpyAsync(e.data(), errs, sizeof(int32_t) * 2 * m, cudaMemcpyDeviceToHost, s));
+        GT_CUDA(ctx, cudaStreamSynchronize(s));
+        bool all = true;
+        for (int k = 0; k < m; k++) {
+          err |= e[2 * k] != 0;
+          all &= h[k].done != 0 || h[k].iters >= maxit;
+        }
+        if (err || all) break;
+        if (chunk < 2048) chunk *= 2;
+      }
+      return GT_OK;
+    };
+    const int ws = wave();
+    if (ws != GT_OK) cudaStreamSynchronize(s);  // nothing of the wave may be reused before the stream drains
+    for (int k = 0; k < prepared; k++) {
+      const int st = pcg_finish<BS, G, V, X, REL>(P[k], h[k], err, &outs[i0 + k]);
+      status[i0 + k] = ws == GT_OK ? st : ws;
     }
-    for (int k = 0; k < m; k++) status[i0 + k] = pcg_finish<BS, G, V, X, REL>(P[k], h[k], err, &outs[i0 + k]);
     dfree(ctx, bars);
     dfree(ctx, errs);
     pool_free(ctx, sts);
     pool_free(ctx, dargs);
     pool_free(ctx, dmap);
+    if (ws != GT_OK) return ws;
     i0 = i1;
   }
   return GT_OK;
