@@ -26,6 +26,12 @@ def _space(kind):
         m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (24, 24, 24), simplexify=True)
         GT.jitter_interior_nodes(m, 0.2, 4)
         return m, GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m)), GT.laplacian, 1.0
+    if kind == "p2tet":
+        # tetrahedra whose elements run in one launch: it waits for the whole
+        # (chunked) coefficient upload
+        m = GT.cartesian_mesh((0, 1, 0, 1, 0, 1), (12, 10, 9), simplexify=True)
+        GT.jitter_interior_nodes(m, 0.2, 5)
+        return m, GT.lagrange_space(GT.interior(m), 2, dirichlet_boundary=GT.boundary(m)), GT.laplacian, 1.0
     if kind == "q1quad":
         m = GT.cartesian_mesh((0, 1, 0, 1), (9, 7))
         return m, GT.lagrange_space(GT.interior(m), 1, dirichlet_boundary=GT.boundary(m)), GT.laplacian, 1.0
@@ -34,7 +40,7 @@ def _space(kind):
     return m, V, (lambda k: GT.elasticity(k, 0.3)), [0.0, 0.0, -1.0]
 
 
-@pytest.mark.parametrize("kind", ["p1tet", "p1tet_large", "q1quad", "q2hex_elast"])
+@pytest.mark.parametrize("kind", ["p1tet", "p1tet_large", "p2tet", "q1quad", "q2hex_elast"])
 @pytest.mark.parametrize("pinned", [True, False])
 def test_assemble_csr_matches_separate_calls(kind, pinned):
     m, V, form, f = _space(kind)
