@@ -19,7 +19,7 @@ const LIB = get(ENV, "GTGPU_LIB", joinpath(@__DIR__, "..", "_build", "libgtgpu.s
 const GT_QUAD4, GT_HEX8, GT_TET4 = Cint(1), Cint(2), Cint(3)
 const GT_LAPLACE, GT_MASS, GT_ELASTICITY = Cint(1), Cint(2), Cint(3)
 const GT_FP64, GT_FP32, GT_MIXED = Cint(0), Cint(1), Cint(2)
-const GT_SOLVE_FP64, GT_SOLVE_IR = Cint(0), Cint(1)
+const GT_SOLVE_FP64, GT_SOLVE_IR, GT_SOLVE_FP32 = Cint(0), Cint(1), Cint(2)
 
 struct SolveInfo
     iterations::Int32
@@ -137,6 +137,62 @@ function download(dm::DeviceMatrix, ::Type{T}) where {T}
                                 (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int32}, Ptr{Float64}, Ptr{Float32}), dm.h, rowptr, colind, v64, v32))
     # symmetric pattern and values: CSR rows are CSC columns
     SparseMatrixCSC{T,Int32}(n, n, Int32.(rowptr .+ 1), colind .+ Int32(1), T === Float64 ? v64 : v32)
+end
+
+_dmatrix(V::Space, h) = (dm = DeviceMatrix(V, h);
+                          finalizer(m -> ccall((:gt_matrix_destroy, LIB), Cint, (Ptr{Cvoid},), m.h), dm); dm)
+_ptr_or_null(a) = a === nothing ? C_NULL : a
+
+"""
+    assemble_matrix_and_vector(a::Form, f (ncomp), T, V; source_coef=nothing) -> A, b, dm
+
+GT.assemble_matrix_and_vector(a, l, T, U, V) for l(v) = ∫ source_coef f⋅v:
+matrix and load vector in one pass (gt_assemble_matrix_and_vector).
+"""
+function assemble_matrix_and_vector(a::Form, f::AbstractVector, ::Type{T}, V::Space; source_coef=nothing) where {T}
+    b = zeros(Float64, V.num_free_dofs)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(V.ctx.h, ccall((:gt_assemble_matrix_and_vector, LIB), Cint,
+                         (Ptr{Cvoid}, Cint, Ptr{Float64}, Float64, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                          Ptr{Ptr{Cvoid}}),
+                         V.h, a.kind, _coef(a), a.nu, _prec(T), collect(Float64, f), _ptr_or_null(source_coef), b, r))
+    dm = _dmatrix(V, r[])
+    download(dm, T), b, dm
+end
+
+"""
+    linear_problem(dirichlet_values, a::Form, f (ncomp), T, V; source_coef=nothing) -> A, b, dm
+
+GT.PartitionedSolvers_linear_problem(uhd, a, l): A and b with the Dirichlet
+lift b -= Ad * dirichlet_values (values in the Dirichlet numbering) in the
+same pass (gt_linear_problem).
+"""
+function linear_problem(dirichlet_values::AbstractVector, a::Form, f::AbstractVector, ::Type{T}, V::Space;
+                        source_coef=nothing) where {T}
+    b = zeros(Float64, V.num_free_dofs)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(V.ctx.h, ccall((:gt_linear_problem, LIB), Cint,
+                         (Ptr{Cvoid}, Cint, Ptr{Float64}, Float64, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                          Ptr{Float64}, Ptr{Ptr{Cvoid}}),
+                         V.h, a.kind, _coef(a), a.nu, _prec(T), collect(Float64, f), _ptr_or_null(source_coef),
+                         collect(Float64, dirichlet_values), b, r))
+    dm = _dmatrix(V, r[])
+    download(dm, T), b, dm
+end
+
+"""
+    update_matrix_and_vector!(A, b, dm::DeviceMatrix, a::Form, f; source_coef=nothing)
+
+GT.update_matrix_and_vector!: new values and load vector on the assembled
+pattern (gt_update_matrix_and_vector).
+"""
+function update_matrix_and_vector!(A::SparseMatrixCSC{T}, b::Vector{Float64}, dm::DeviceMatrix, a::Form,
+                                   f::AbstractVector; source_coef=nothing) where {T}
+    check(dm.space.ctx.h, ccall((:gt_update_matrix_and_vector, LIB), Cint,
+                                (Ptr{Cvoid}, Cint, Ptr{Float64}, Float64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                                dm.h, a.kind, _coef(a), a.nu, collect(Float64, f), _ptr_or_null(source_coef), b))
+    copyto!(A.nzval, download(dm, T).nzval)
+    A, b
 end
 
 """
