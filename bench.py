@@ -72,11 +72,38 @@ def parse():
 # ---------------------------------------------------------------------------
 # other configurations (one JSON line each; not the driver's headline)
 # ---------------------------------------------------------------------------
+def cpu_elasticity(n):
+    """The oracle's FP64 assembly (counting pass, COO append, COO -> CSC, and
+    the load vector) of the elasticity problem on a bounded n^3 sample, on
+    all host cores and on one (the reference is single-threaded), in nnz/s:
+    the per-nonzero rate carries over to the full size (its COO, ~60 GB at
+    64^3, does not fit the host)."""
+    O = _oracle()
+    from gtgpu.mesh import cartesian_mesh
+    m = cartesian_mesh((0, 1, 0, 1, 0, 1), (n, n, n))
+    om = dict(D=3, ctype=m.cell_type, coords=m.coords, cell_nodes=m.cell_nodes, pf0=m.corners, pf1=m.bedges,
+              pf2=m.bfaces, pf2g=m.bface_group, cells=m.cells_per_dir, box=m.domain)
+    ref = O.lagrange_space(om, 2, ncomp=3, dirichlet=["2-face-5"])
+    out = {"unit": "nnz/s", "kind": "port", "sample": f"{n}^3 HEX8 Q2 elasticity, FP64, one repetition"}
+    for key, th in (("value", os.cpu_count()), ("single_thread", 1)):
+        O.set_threads(th)
+        t0 = time.perf_counter()
+        _, rv, _ = O.assemble_matrix(ref, O.ELASTICITY, 4, coef=None, nu=0.3)
+        O.assemble_vector(ref, 4, [0.0, 0.0, -1.0])
+        dt = time.perf_counter() - t0
+        if key == "value":
+            out.update({"value": rv.size / dt, "cores": O.num_threads(), "nnz": int(rv.size), "seconds": dt})
+        else:
+            out["single_thread"] = {"value": rv.size / dt, "cores": 1, "seconds": dt}
+    return out
+
+
 def run_elasticity(args):
     """3-D linear elasticity, 64^3 HEX8 cells, Q2 vector space (6.39M free
     DOFs), E=1, nu=0.3, body force (0,0,-1), clamped at x=0, 3x3x3 Gauss.
     Assembly in FP64, FP32 and mixed; solves: plain FP64 PCG and FP64
-    refinement around FP32 PCG to 1e-10."""
+    refinement around FP32 PCG to 1e-10; the CPU baseline (the oracle) on a
+    12^3 sample, per nonzero."""
     import torch
     import gtgpu as GT
     n = args.cells if args.cells != 96 else 64
@@ -109,6 +136,8 @@ def run_elasticity(args):
     _, _, v64 = A.csr()
     res["fp32_values_rel_err_vs_fp64"] = float(np.abs(v32 - v64).max() / np.abs(v64).max())
     del A32, v32
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_elasticity(12)
     if args.no_solve:
         out.update({"assembly": res, "nnz": int(nnz)})
         print(json.dumps(out), flush=True)
