@@ -1265,11 +1265,13 @@ __global__ void __launch_bounds__(256) k_elements_p1(const double* __restrict__ 
 // J's nine differences taken in FP64 (x_i - x_0 loses nothing there) and
 // everything after them -- cofactors, det J, its reciprocal, the entries,
 // the load vector -- in pairs of FP32 numbers (48 significant bits) on the
-// FP32 pipes, rounded to FP64 at the end.  About 9 FP64 instructions per
-// cell instead of ~75, so the kernel is no longer bound by GB300's FP64
-// rate; the values agree with the FP64 kernel's (and the FP64 oracle's) to
-// a few units of 2^-48 relative to the largest entry, far inside the 1e-12
-// parity tolerance.
+// FP32 pipes; the matrix entries leave as pairs (the scatter rounds each CSR
+// value to FP64 once).  About 9 FP64 instructions per cell instead of ~75,
+// so the kernel is no longer bound by GB300's FP64 rate.  Its sums are the
+// sloppy double-float sum (error ~2^-47 of the terms, which are of the size
+// of the element matrix's entries): the values agree with the FP64 kernel's
+// (and the FP64 oracle's) to a few units of 2^-47 relative to the largest
+// entry, far inside the 1e-12 parity tolerance.
 template <int FORM>
 __global__ void __launch_bounds__(256) k_elements_p1_df(const double* __restrict__ coords,
                                                         const int32_t* __restrict__ cell_nodes,
@@ -1304,28 +1306,28 @@ __global__ void __launch_bounds__(256) k_elements_p1_df(const double* __restrict
     const dfl b[3] = {df_from_double(p2[0] - x0), df_from_double(p2[1] - y0), df_from_double(p2[2] - z0)};
     const dfl d[3] = {df_from_double(p3[0] - x0), df_from_double(p3[1] - y0), df_from_double(p3[2] - z0)};
     // cofactor columns c_1, c_2, c_3 (the physical gradients times det J)
-    const dfl g1[3] = {df_mul_sub(b[1], d[2], b[2], d[1]), df_mul_sub(b[2], d[0], b[0], d[2]),
-                       df_mul_sub(b[0], d[1], b[1], d[0])};
-    const dfl det = df_dot3(a, g1);
+    const dfl g1[3] = {df_mul_sub_s(b[1], d[2], b[2], d[1]), df_mul_sub_s(b[2], d[0], b[0], d[2]),
+                       df_mul_sub_s(b[0], d[1], b[1], d[0])};
+    const dfl det = df_dot3_s(a, g1);
     if (det.hi == 0.0f) atomicOr(err, DEV_ERR_DEGENERATE);
     const dfl adet = df_abs(det);
     const dfl cf = coef ? df_from_double(coef[c]) : one;
     if (want_matrix) {
       dfl k[10];
       if (FORM == GT_LAPLACE) {
-        const dfl g2[3] = {df_mul_sub(d[1], a[2], d[2], a[1]), df_mul_sub(d[2], a[0], d[0], a[2]),
-                           df_mul_sub(d[0], a[1], d[1], a[0])};
-        const dfl g3[3] = {df_mul_sub(a[1], b[2], a[2], b[1]), df_mul_sub(a[2], b[0], a[0], b[2]),
-                           df_mul_sub(a[0], b[1], a[1], b[0])};
-        const dfl s = df_mul(df_mul(cf, wsum), df_recip(adet));
-        const dfl k11 = df_mul(s, df_dot3(g1, g1)), k12 = df_mul(s, df_dot3(g1, g2)), k13 = df_mul(s, df_dot3(g1, g3));
-        const dfl k22 = df_mul(s, df_dot3(g2, g2)), k23 = df_mul(s, df_dot3(g2, g3));
-        const dfl k33 = df_mul(s, df_dot3(g3, g3));
+        const dfl g2[3] = {df_mul_sub_s(d[1], a[2], d[2], a[1]), df_mul_sub_s(d[2], a[0], d[0], a[2]),
+                           df_mul_sub_s(d[0], a[1], d[1], a[0])};
+        const dfl g3[3] = {df_mul_sub_s(a[1], b[2], a[2], b[1]), df_mul_sub_s(a[2], b[0], a[0], b[2]),
+                           df_mul_sub_s(a[0], b[1], a[1], b[0])};
+        const dfl s = df_mul(df_mul(cf, wsum), df_recip_s(adet));
+        const dfl k11 = df_mul(s, df_dot3_s(g1, g1)), k12 = df_mul(s, df_dot3_s(g1, g2)), k13 = df_mul(s, df_dot3_s(g1, g3));
+        const dfl k22 = df_mul(s, df_dot3_s(g2, g2)), k23 = df_mul(s, df_dot3_s(g2, g3));
+        const dfl k33 = df_mul(s, df_dot3_s(g3, g3));
         // vertex 0 from the zero row sums, as in the FP64 kernel
-        const dfl k01 = df_neg(df_add(df_add(k11, k12), k13));
-        const dfl k02 = df_neg(df_add(df_add(k12, k22), k23));
-        const dfl k03 = df_neg(df_add(df_add(k13, k23), k33));
-        const dfl k00 = df_neg(df_add(df_add(k01, k02), k03));
+        const dfl k01 = df_neg(df_add_sloppy(df_add_sloppy(k11, k12), k13));
+        const dfl k02 = df_neg(df_add_sloppy(df_add_sloppy(k12, k22), k23));
+        const dfl k03 = df_neg(df_add_sloppy(df_add_sloppy(k13, k23), k33));
+        const dfl k00 = df_neg(df_add_sloppy(df_add_sloppy(k01, k02), k03));
         k[0] = k00; k[1] = k01; k[2] = k02; k[3] = k03;
         k[4] = k11; k[5] = k12; k[6] = k13;
         k[7] = k22; k[8] = k23;

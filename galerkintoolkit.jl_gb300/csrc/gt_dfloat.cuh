@@ -102,6 +102,24 @@ static __device__ __noinline__ dfl df_from_double_rare(double x) {
 
 static __device__ __noinline__ double df_to_double_rare(float hi, float lo) { return (double)hi + (double)lo; }
 
+// The same operations with the sloppy sum (df_add_sloppy): absolute error
+// about 2^-47 of the operands rather than of the result -- for formulas
+// whose accuracy is measured against their largest terms (an element
+// matrix against its largest entry), at about half the instructions of the
+// accurate sum
+__device__ __forceinline__ dfl df_sub_s(dfl x, dfl y) { return df_add_sloppy(x, df_neg(y)); }
+__device__ __forceinline__ dfl df_mul_sub_s(dfl a, dfl b, dfl c, dfl d) { return df_sub_s(df_mul(a, b), df_mul(c, d)); }
+__device__ __forceinline__ dfl df_dot3_s(const dfl* x, const dfl* y) {
+  return df_add_sloppy(df_add_sloppy(df_mul(x[0], y[0]), df_mul(x[1], y[1])), df_mul(x[2], y[2]));
+}
+__device__ __forceinline__ dfl df_recip_s(dfl x) {
+  dfl r = {__frcp_rn(x.hi), 0.0f};
+  const dfl one = {1.0f, 0.0f};
+#pragma unroll
+  for (int it = 0; it < 2; it++) r = df_add_sloppy(r, df_mul(r, df_sub_s(one, df_mul(x, r))));
+  return r;
+}
+
 // FP64 -> double-float with integer instructions: hi takes the top 24
 // significand bits of x (exact), lo the remaining 29 bits rounded to FP32.
 // Zeros stay integer too; other values outside |x| in [2^-74, 2^127) take
