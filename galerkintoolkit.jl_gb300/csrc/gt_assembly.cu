@@ -1842,8 +1842,17 @@ __device__ __forceinline__ float to_f32(dfl v) { return (float)df_to_double(v); 
 // group barrier between them -- the summation order of k_scatter, so the
 // values are bitwise those of the generic kernel.  LIFT (the Dirichlet lift
 // b -= Ad xd) is a compile-time choice, so the common case carries none of
-// its FP64 code.
-template <class TK, class TA, bool LIFT>
+// its FP64 code.  NB > 0: every row has at most 2^NB columns, the slot
+// holds 2^NB of them (the tail padded with INT_MAX; slots 2^NB + 1 apart,
+// an odd stride, so the eight groups of a warp spread over the banks) and
+// the search takes NB steps of fixed width 2^(NB-1), ..., 1 -- unrolled,
+// constant offsets -- instead of the row-length loop (NB = 0); same
+// positions, same values.  Its first two steps compare with three columns
+// held in registers (the only ones they can read), so each search reads
+// shared memory NB - 2 times: the kernel is bound by the L1 data pipe
+// (shared-memory wavefronts of the searches and accumulators plus the
+// gathers' wavefronts), not by DRAM.
+template <class TK, class TA, bool LIFT, int NB>
 __global__ void __launch_bounds__(128) k_scatter_p1(const int64_t* __restrict__ rowptr,
                                                     const int32_t* __restrict__ colind,
                                                     const int64_t* __restrict__ inc_ptr,
@@ -1877,7 +1886,17 @@ __global__ void __launch_bounds__(128) k_scatter_p1(const int64_t* __restrict__ 
     cols[i] = colind[rb + i];
     acc[i] = TA{};
   }
+  if constexpr (NB > 0)
+    for (int i = L + b; i < (1 << NB); i += G) cols[i] = INT_MAX;  // above every key
   __syncwarp(gmask);
+  // the columns of the first two search steps: H1, then H1 - H2 or H1 + H2
+  constexpr int H1 = NB > 0 ? 1 << (NB - 1) : 1, H2 = NB > 1 ? 1 << (NB - 2) : 1;
+  int32_t c_mid = 0, c_lo = 0, c_hi = 0;
+  if constexpr (NB > 1) {
+    c_mid = cols[H1];
+    c_lo = cols[H1 - H2];
+    c_hi = cols[H1 + H2];
+  }
   const int64_t ib = inc_ptr[r], ie = inc_ptr[r + 1];
   double bsum = 0.0;
   if (be != nullptr) row_load_sum<1>(ib, ie, inc, 4, be, b, gmask, &bsum);
@@ -1899,11 +1918,29 @@ __global__ void __launch_bounds__(128) k_scatter_p1(const int64_t* __restrict__ 
       pos[u] = 0;
     }
     // last position whose column is <= key: the column's own position
-    for (int n = L; n > 1;) {
-      const int half = n >> 1;
+    if constexpr (NB > 1) {
 #pragma unroll
-      for (int u = 0; u < U; u++) pos[u] = cols[pos[u] + half] <= key[u] ? pos[u] + half : pos[u];
-      n -= half;
+      for (int u = 0; u < U; u++) {
+        const bool up = c_mid <= key[u];
+        pos[u] = up ? H1 : 0;
+        if ((up ? c_hi : c_lo) <= key[u]) pos[u] += H2;
+      }
+#pragma unroll
+      for (int half = H2 >> 1; half > 0; half >>= 1)
+#pragma unroll
+        for (int u = 0; u < U; u++) pos[u] = cols[pos[u] + half] <= key[u] ? pos[u] + half : pos[u];
+    } else if constexpr (NB > 0) {
+#pragma unroll
+      for (int half = 1 << (NB - 1); half > 0; half >>= 1)
+#pragma unroll
+        for (int u = 0; u < U; u++) pos[u] = cols[pos[u] + half] <= key[u] ? pos[u] + half : pos[u];
+    } else {
+      for (int n = L; n > 1;) {
+        const int half = n >> 1;
+#pragma unroll
+        for (int u = 0; u < U; u++) pos[u] = cols[pos[u] + half] <= key[u] ? pos[u] + half : pos[u];
+        n -= half;
+      }
     }
 #pragma unroll
     for (int u = 0; u < U; u++) {
@@ -1932,7 +1969,12 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
   const Space* sp = A->space;
   Ctx* ctx = ctx_of(sp);
   int nn = sp->nn;
-  int lmax = A->max_row > 0 ? A->max_row : 1;
+  // row slots an odd number of entries apart: the groups of a warp, all at
+  // the same step of their rows, then read different banks
+  int lmax = (A->max_row > 0 ? A->max_row : 1) | 1;
+  // the P1 kernel's fixed-step search: slots of 16 or 32 columns
+  const int p1_nb = (BS == 1 && ke_packed(sp)) ? (A->max_row <= 16 ? 4 : (A->max_row <= 32 ? 5 : 0)) : 0;
+  if (p1_nb > 0) lmax = (1 << p1_nb) + 1;
   auto go = [&](auto Gtag) -> int {
     constexpr int G = decltype(Gtag)::value;
     constexpr int RPW = 32 / G;
@@ -1951,10 +1993,13 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
     bool done = false;
     if constexpr (BS == 1 && G == 4) {
       if (ke_packed(sp)) {
-        if (xd != nullptr && be != nullptr)
-          launch(k_scatter_p1<TK, TA, true>);
+        const bool lift = xd != nullptr && be != nullptr;
+        if (p1_nb == 4)
+          lift ? launch(k_scatter_p1<TK, TA, true, 4>) : launch(k_scatter_p1<TK, TA, false, 4>);
+        else if (p1_nb == 5)
+          lift ? launch(k_scatter_p1<TK, TA, true, 5>) : launch(k_scatter_p1<TK, TA, false, 5>);
         else
-          launch(k_scatter_p1<TK, TA, false>);
+          lift ? launch(k_scatter_p1<TK, TA, true, 0>) : launch(k_scatter_p1<TK, TA, false, 0>);
         done = true;
       }
     }
@@ -2533,7 +2578,7 @@ static int launch_uniform(Matrix* A, const double* gref, const double* coef, dou
   constexpr int RPW = 32 / G;
   constexpr int KREF_N = NN * NN * BS * BS;
   constexpr size_t KREF_BYTES = ((size_t)KREF_N * sizeof(T) + 15) & ~size_t(15);
-  int lmax = A->max_row > 0 ? A->max_row : 1;
+  int lmax = (A->max_row > 0 ? A->max_row : 1) | 1;  // odd slot stride (banks)
   double* v64 = A->precision != GT_FP32 ? A->val64 : nullptr;
   float* v32 = A->precision != GT_FP64 ? A->val32 : nullptr;
   // up to 16 warps per CTA where the row slots fit beside the reference
@@ -2589,7 +2634,7 @@ static int launch_kron(Matrix* A, const T* Gc, double nu, const double* be, doub
   constexpr int NN = D == 2 ? M1 * M1 : M1 * M1 * M1;
   constexpr int G = NN <= 4 ? 4 : (NN <= 8 ? 8 : (NN <= 16 ? 16 : 32));
   constexpr int RPW = 32 / G;
-  int lmax = A->max_row > 0 ? A->max_row : 1;
+  int lmax = (A->max_row > 0 ? A->max_row : 1) | 1;  // odd slot stride (banks)
   matrix_values_changed(A);
   double* v64 = A->precision != GT_FP32 ? A->val64 : nullptr;
   float* v32 = A->precision != GT_FP64 ? A->val32 : nullptr;
