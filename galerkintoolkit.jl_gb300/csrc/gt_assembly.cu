@@ -1843,11 +1843,17 @@ __device__ __forceinline__ float to_f32(dfl v) { return (float)df_to_double(v); 
 // values are bitwise those of the generic kernel.  LIFT (the Dirichlet lift
 // b -= Ad xd) is a compile-time choice, so the common case carries none of
 // its FP64 code.  NB > 0: every row has at most 2^NB columns, the slot
-// holds 2^NB of them (the tail padded with INT_MAX; slots 2^NB + 1 apart,
-// an odd stride, so the eight groups of a warp spread over the banks) and
-// the search takes NB steps of fixed width 2^(NB-1), ..., 1 -- unrolled,
-// constant offsets -- instead of the row-length loop (NB = 0); same
-// positions, same values.  Its first two steps compare with three columns
+// holds 2^NB of them (the tail padded with INT_MAX) and the search takes NB
+// steps of fixed width 2^(NB-1), ..., 1 -- unrolled, constant offsets --
+// instead of the row-length loop (NB = 0); same positions, same values.
+// The slot strides set the shared-memory bank conflicts: the eight rows of a
+// warp are consecutive DOFs, whose incidences on a structured mesh hit the
+// same column positions at the same step, so the row slots must not map
+// those positions onto one bank.  Column slots 2^NB + 5 words apart and
+// accumulator slots 2^NB + 4 entries apart (8-byte entries: the four rows of
+// a half warp start 0, 4, 8, 12 bank pairs apart) take, on the P1 Kuhn-cube
+// pattern, 1.53 wavefronts per search load and 3.9 per accumulator access,
+// against 2.5 and 5.2 with both 2^NB + 1 apart and 4.0 and 7.5 with 2^NB.  Its first two steps compare with three columns
 // held in registers (the only ones they can read), so each search reads
 // shared memory NB - 2 times: the kernel is bound by the L1 data pipe
 // (shared-memory wavefronts of the searches and accumulators plus the
@@ -1867,8 +1873,10 @@ __global__ void __launch_bounds__(128) k_scatter_p1(const int64_t* __restrict__ 
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int sub = lane >> 2, b = lane & 3;
   const int slot = w * RPW + sub;
+  // accumulator slots lmax entries apart, column slots one more (NB > 0)
+  const int cstride = NB > 0 ? lmax + 1 : lmax;
   TA* acc = (TA*)s_raw + (size_t)slot * lmax;
-  int32_t* cols = (int32_t*)((TA*)s_raw + (size_t)(blockDim.x / G) * lmax) + (size_t)slot * lmax;
+  int32_t* cols = (int32_t*)((TA*)s_raw + (size_t)(blockDim.x / G) * lmax) + (size_t)slot * cstride;
   const int64_t r = row_begin + ((int64_t)blockIdx.x * (blockDim.x >> 5) + w) * RPW + sub;
   if (r >= row_end) return;  // the group's four lanes leave together
   const unsigned gmask = 0xfu << (sub * G);
@@ -1972,14 +1980,15 @@ static int launch_scatter(Matrix* A, const TK* Ke, double* v64, float* v32, cons
   // row slots an odd number of entries apart: the groups of a warp, all at
   // the same step of their rows, then read different banks
   int lmax = (A->max_row > 0 ? A->max_row : 1) | 1;
-  // the P1 kernel's fixed-step search: slots of 16 or 32 columns
+  // the P1 kernel's fixed-step search: slots of 16 or 32 columns, the
+  // accumulator slots 2^NB + 4 entries apart (the column slots one more)
   const int p1_nb = (BS == 1 && ke_packed(sp)) ? (A->max_row <= 16 ? 4 : (A->max_row <= 32 ? 5 : 0)) : 0;
-  if (p1_nb > 0) lmax = (1 << p1_nb) + 1;
+  if (p1_nb > 0) lmax = (1 << p1_nb) + 4;
   auto go = [&](auto Gtag) -> int {
     constexpr int G = decltype(Gtag)::value;
     constexpr int RPW = 32 / G;
     int warps = 4;
-    size_t per_row = (size_t)lmax * (BS * BS * sizeof(TA) + sizeof(int32_t));
+    size_t per_row = (size_t)lmax * (BS * BS * sizeof(TA) + sizeof(int32_t)) + (p1_nb > 0 ? sizeof(int32_t) : 0);
     while (warps > 1 && (size_t)warps * RPW * per_row > 96 * 1024) warps >>= 1;
     size_t smem = (size_t)warps * RPW * per_row;
     if (smem > 200 * 1024) return set_error(ctx, GT_ERR_UNSUPPORTED, "sparsity row too wide for the scatter kernel");

@@ -278,6 +278,32 @@ def test_pattern_rows_beyond_the_thread_pass(dirichlet):
     assert np.abs(v - ov).max() <= TOL64 * np.abs(ov).max()
 
 
+@pytest.mark.parametrize("n", [12, 20, 40])
+def test_p1_scatter_row_lengths(n):
+    """The centre row of a fan over an n-gon holds n + 3 columns: 15 (the
+    scatter's 16-column slots), 23 (32-column slots) and 43 (the search over
+    the row's length) -- FP64, FP32 values and the load vector against the
+    oracle"""
+    m = _fan_mesh(n)
+    V = GT.lagrange_space(GT.interior(m), 1)
+    coef = GT.lognormal_cells(m.num_cells, 0.5, 7)
+    a = GT.laplacian(coef)
+    A, b = GT.assemble_matrix_and_vector(a, GT.source(1.0, coef), np.float64, V)
+    rp, ci, v = A.csr()
+    assert np.diff(rp).max() == n + 3
+    om = dict(D=3, ctype=m.cell_type, coords=m.coords, cell_nodes=m.cell_nodes, pf0=m.corners, pf1=m.bedges,
+              pf1g=None, pf2=m.bfaces, pf2g=m.bface_group, cells=(), box=())
+    ref = O.lagrange_space(om, 1)
+    cp, rv, nz = O.assemble_matrix(ref, O.LAPLACE, 2, coef=coef)
+    orp, oci, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    assert np.abs(v - ov).max() <= TOL64 * np.abs(ov).max()
+    ob = O.assemble_vector(ref, 2, 1.0, coef=coef)
+    assert np.abs(b - ob).max() <= TOL64 * np.abs(ob).max()
+    v32 = GT.assemble_matrix(a, np.float32, V).values32()
+    assert np.abs(v32 - ov).max() <= TOL32 * np.abs(ov).max()
+
+
 def _graded(cells, order, ncomp, groups, form, sig):
     """A Cartesian mesh with x -> x^2 (and y -> y^1.5): every cell stays an
     axis-aligned box (affine), but cell sizes differ, so the sum-factorised
