@@ -508,19 +508,25 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
 // sorts, rounds and compaction are per-warp costs).  Same results: the
 // row's incidences ascending, its distinct free columns ascending.  After a
 // *redo the warp kernel recounts every row.
+// C16: the space's DOF spread is below 2^15, so every column differs from
+// its row by less than 2^15 and the list holds column - row in 16 bits:
+// 192 instead of 256 bytes of shared memory per thread, 8 instead of 6
+// blocks per SM (the pass is bound by shared-memory latency, not bandwidth).
 constexpr int kRowsMI = 32, kRowsS = 32;
 static_assert(kIncBucket == kRowsMI, "a bucket holds the incidences the row-per-thread pass takes");
-template <int NN>
+template <int NN, bool C16>
 __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict__ inc_ptr, int32_t* __restrict__ inc,
                                                       const int32_t* __restrict__ cnd, int64_t nrows,
                                                       int32_t* __restrict__ rowcnt, int32_t* __restrict__ slots,
                                                       uint8_t* __restrict__ small, int32_t* maxrow, int32_t* redo,
                                                       const int32_t* __restrict__ bucket) {
   extern __shared__ int32_t s_rows[];
+  using CT = typename std::conditional<C16, int16_t, int32_t>::type;
   const int T = blockDim.x, tid = threadIdx.x;
-  int32_t* I = s_rows + tid;                 // incidences, I[k * T]
-  int32_t* Cl = s_rows + kRowsMI * T + tid;  // columns, Cl[k * T]
+  int32_t* I = s_rows + tid;                                      // incidences, I[k * T]
+  CT* Cl = reinterpret_cast<CT*>(s_rows + kRowsMI * T) + tid;     // columns (- row with C16), Cl[k * T]
   const int64_t r = blockIdx.x * (int64_t)T + tid;
+  const int32_t cbase = C16 ? (int32_t)r : 0;
   if (r >= nrows) return;
   const int64_t ib = inc_ptr[r];
   const int ninc = (int)(inc_ptr[r + 1] - ib);
@@ -571,7 +577,7 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
   int n = 0;
   bool over = false;
   if (ninc > 0) {
-    Cl[0] = (int32_t)r;  // the row's own DOF (block row r is node r + 1)
+    Cl[0] = (CT)((int32_t)r - cbase);  // the row's own DOF (block row r is node r + 1)
     n = 1;
   }
   // the next incidence's node DOFs are loaded while the current ones are
@@ -614,7 +620,7 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
 #pragma unroll
         for (int q = 0; q < NN; q++) known |= prev[u][q] == d[b];
       if (known) continue;
-      const int32_t key = d[b] - 1;
+      const int32_t key = d[b] - 1 - cbase;
       int lo = 0, hi = n;
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
@@ -627,7 +633,7 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
         continue;
       }
       for (int j = n; j > lo; j--) Cl[j * T] = Cl[(j - 1) * T];
-      Cl[lo * T] = key;
+      Cl[lo * T] = (CT)key;
       n++;
     }
     if constexpr (PV > 0) {
@@ -647,7 +653,7 @@ __global__ void __launch_bounds__(128) k_pattern_rows(const int64_t* __restrict_
   }
   rowcnt[r] = n;
   small[r] = 1;
-  for (int k = 0; k < n; k++) slots[r * kRowsS + k] = Cl[k * T];
+  for (int k = 0; k < n; k++) slots[r * kRowsS + k] = (int32_t)Cl[k * T] + cbase;
   if (n > __ldcg(maxrow)) atomicMax(maxrow, n);
 }
 
@@ -784,9 +790,15 @@ static int launch_pattern(Matrix* A, int32_t maxinc, const int32_t* bucket, bool
     GT_CUDA(ctx, cudaMemsetAsync(dmax, 0, sizeof(int32_t), st));
     GT_CUDA(ctx, cudaMemsetAsync(dredo, 0, sizeof(int32_t), st));
     if (nrows > 0 && rows_pass) {
-      const size_t rsm = (size_t)128 * (kRowsMI + kRowsS) * sizeof(int32_t);
-      k_pattern_rows<NN><<<GT_KC(ctx, grid_for(nrows, 128)), 128, rsm, st>>>(
-          A->inc_ptr, A->inc, sp->cell_ndofs, nrows, rowcnt, slots, small, dmax, dredo, bucket);
+      // 16-bit column offsets when every column is within 2^15 of its row
+      const bool c16 = sp->dof_spread >= 0 && sp->dof_spread < 32768;
+      const size_t rsm = (size_t)128 * (kRowsMI * sizeof(int32_t) + kRowsS * (c16 ? sizeof(int16_t) : sizeof(int32_t)));
+      if (c16)
+        k_pattern_rows<NN, true><<<GT_KC(ctx, grid_for(nrows, 128)), 128, rsm, st>>>(
+            A->inc_ptr, A->inc, sp->cell_ndofs, nrows, rowcnt, slots, small, dmax, dredo, bucket);
+      else
+        k_pattern_rows<NN, false><<<GT_KC(ctx, grid_for(nrows, 128)), 128, rsm, st>>>(
+            A->inc_ptr, A->inc, sp->cell_ndofs, nrows, rowcnt, slots, small, dmax, dredo, bucket);
     } else if (nrows > 0) {
       k_pattern<NN, S, false><<<GT_KC(ctx, grid), warps * 32, smem, st>>>(A->inc_ptr, A->inc, sp->cell_ndofs, nrows,
                                                                           hcap, icap, rowcnt, nullptr, nullptr, slots,

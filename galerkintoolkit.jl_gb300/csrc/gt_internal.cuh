@@ -213,6 +213,9 @@ struct Space {
   int order = 1, ncomp = 1, nn = 0, nloc = 0;
   int64_t nfree_nodes = 0, ndiri_nodes = 0;
   int32_t* cell_ndofs = nullptr;  // ncells * nn: node-level dof, >0 free (1-based), <0 Dirichlet
+  // largest difference of two free node DOFs of one cell (-1: not known): a
+  // bound on |column - row| in every row of the space's matrices
+  int32_t dof_spread = -1;
   // incidence cache used by stand-alone vector assembly
   int64_t* inc_ptr = nullptr;
   int32_t* inc = nullptr;

@@ -373,6 +373,26 @@ static int device_error_status(Ctx* ctx, const char* where) {
   return set_error(ctx, GT_ERR_INVALID, m);
 }
 
+// largest difference of two free node DOFs of one cell: per cell max - min,
+// a warp maximum, one atomicMax per warp
+__global__ void k_dof_spread(const int32_t* __restrict__ cnd, int64_t nc, int nn, int32_t* out) {
+  const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int32_t v = 0;
+  if (c < nc) {
+    int32_t lo = INT_MAX, hi = 0;
+    for (int a = 0; a < nn; a++) {
+      const int32_t d = cnd[c * nn + a];
+      if (d > 0) {
+        lo = min(lo, d);
+        hi = max(hi, d);
+      }
+    }
+    if (hi > 0) v = hi - lo;
+  }
+  for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((threadIdx.x & 31) == 0 && v > 0) atomicMax(out, v);
+}
+
 int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
   Mesh* M = sp->mesh;
   Ctx* ctx = M->ctx;
@@ -535,12 +555,22 @@ int number_dofs(Space* sp, int ngroups, const int32_t* groups_host) {
   GT_LAUNCH(ctx, "k_renumber");
   GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[0], fpos + nnodes_sp, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[1], dpos + nnodes_sp, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  GT_TRY(device_error_status(ctx, "lagrange_space"));  // synchronises
-  int32_t nf = 0, ndr = 0;
+  int32_t* dspread = nullptr;
+  GT_TRY(dalloc(ctx, &dspread, 1));
+  GT_CUDA(ctx, cudaMemsetAsync(dspread, 0, sizeof(int32_t), st));
+  if (nc > 0) k_dof_spread<<<GT_KC(ctx, grid_for(nc, 256)), 256, 0, st>>>(sp->cell_ndofs, nc, t.nn, dspread);
+  GT_LAUNCH(ctx, "k_dof_spread");
+  GT_CUDA(ctx, cudaMemcpyAsync(&ctx->h_scratch[2], dspread, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  const int ds = device_error_status(ctx, "lagrange_space");  // synchronises
+  dfree(ctx, dspread);
+  GT_TRY(ds);
+  int32_t nf = 0, ndr = 0, spread = 0;
   memcpy(&nf, &ctx->h_scratch[0], sizeof(int32_t));
   memcpy(&ndr, &ctx->h_scratch[1], sizeof(int32_t));
+  memcpy(&spread, &ctx->h_scratch[2], sizeof(int32_t));
   sp->nfree_nodes = nf;
   sp->ndiri_nodes = ndr;
+  sp->dof_spread = spread;
   dfree(ctx, tag);
   dfree(ctx, freef);
   dfree(ctx, fpos);

@@ -304,6 +304,23 @@ def test_p1_scatter_row_lengths(n):
     assert np.abs(v32 - ov).max() <= TOL32 * np.abs(ov).max()
 
 
+def test_pattern_rows_wide_dof_spread():
+    """Two layers of 180 x 180 cubes: the DOFs of a cell lie up to 181^2 + 182
+    apart, beyond the count pass's 16-bit column offsets (it keeps 32-bit
+    column ids there) -- pattern and values against the oracle"""
+    m = GT.cartesian_mesh((0, 1, 0, 1, 0, 0.02), (180, 180, 2), simplexify=True)
+    V = GT.lagrange_space(GT.interior(m), 1)
+    cd = V.face_dofs()
+    assert (cd.max(axis=1) - cd.min(axis=1)).max() >= 32768
+    A = GT.assemble_matrix(GT.laplacian(), np.float64, V, V)
+    rp, ci, v = A.csr()
+    ref, om = _oracle_space(m, 1, 1, None)
+    cp, rv, nz = O.assemble_matrix(ref, O.LAPLACE, 2)
+    orp, oci, ov = O.csc_to_csr(cp, rv, nz, ref["nfree"])
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    assert np.abs(v - ov).max() <= TOL64 * np.abs(ov).max()
+
+
 def _graded(cells, order, ncomp, groups, form, sig):
     """A Cartesian mesh with x -> x^2 (and y -> y^1.5): every cell stays an
     axis-aligned box (affine), but cell sizes differ, so the sum-factorised
