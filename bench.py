@@ -658,8 +658,9 @@ def main():
                 "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                 "peak_source": peaks_kind, "algorithmic_bytes": alg["scatter"], "traffic": traffic.get("scatter"),
                 "b_asm": hbm["scatter"]["b_asm"],
-                "limiter": "the L1 data pipe (ncu, 64^3 x 6: LSU wavefronts 81% of peak -- the column searches and "
-                           "row accumulators in shared memory, the gathers --, issue 56%, DRAM 30%)"}
+                "limiter": "gathers and the L1 data pipe (ncu, 64^3 x 6: LSU wavefronts 70% of peak -- the column "
+                           "searches and row accumulators in shared memory, the gathers --, issue 58%, long_scoreboard "
+                           "stalls first, DRAM 32%)"}
     else:
         bytes_dom = alg.get(dom, nnz * 12)
         achieved = bytes_dom / (ph[dom] * 1e-3) / 1e9
