@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(256) k_pattern(const int64_t* __restrict__ inc
 // *redo the warp kernel recounts every row.
 // C16: the space's DOF spread is below 2^15, so every column differs from
 // its row by less than 2^15 and the list holds column - row in 16 bits:
-// 192 instead of 256 bytes of shared memory per thread, 8 instead of 6
+// 192 instead of 256 bytes of shared memory per thread, 9 instead of 6
 // blocks per SM (the pass is bound by shared-memory latency, not bandwidth).
 constexpr int kRowsMI = 32, kRowsS = 32;
 static_assert(kIncBucket == kRowsMI, "a bucket holds the incidences the row-per-thread pass takes");
